@@ -1,0 +1,168 @@
+/*
+ * gblu.h -- C ABI of libgblu, the GB300 (sm_103a) dense LU library.
+ *
+ * libgblu is the device side of LinearSolve.jl's dense LU path: getrf
+ * (partial-pivot LU) and getrs (the back-solve), plus mixed-precision
+ * factorization with FP64 iterative refinement.  A host binding calls it the
+ * way LinearSolve.jl calls OpenBLAS: symbols resolved once, plain pointers and
+ * sizes, LAPACK conventions (column-major, leading dimensions, 1-based int64
+ * ipiv, int64 info).  No torch, CUDA or C++ types cross this boundary; the
+ * stream getter returns an opaque pointer.
+ *
+ * Conventions shared by every entry point
+ *   - Return value: int32 status, GBLU_OK (0) on success.  A failed call leaves
+ *     a message readable with gblu_last_error(ctx).
+ *   - `info` follows LAPACK getrf: 0 = success, k > 0 = U(k,k) is exactly zero
+ *     (the first such column, 1-based).  A singular matrix is a *successful*
+ *     call with info > 0, as in the reference (src/factorization.jl:716-722).
+ *   - Every call is synchronous on return unless its name ends in _async.
+ *   - Threading: a context serialises its own calls with an internal mutex;
+ *     use one context per host thread for concurrency.
+ *   - Device waits inside kernels are bounded; an expired wait returns
+ *     GBLU_ETIMEOUT instead of hanging.
+ */
+#ifndef GBLU_H
+#define GBLU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+#define GBLU_OK 0
+#define GBLU_EINVAL 1        /* bad argument (LAPACK info < 0 / chkargsok)   */
+#define GBLU_ECUDA 2         /* CUDA runtime error                          */
+#define GBLU_ENOMEM 3        /* device allocation failed or budget exceeded */
+#define GBLU_ETIMEOUT 4      /* a bounded device-side wait expired          */
+#define GBLU_ENOTFACTORED 5  /* getrs before a successful getrf            */
+#define GBLU_ESTALL 6        /* refinement stalled and fallback disabled    */
+#define GBLU_EUNSUPPORTED 7  /* size/precision outside what is implemented */
+#define GBLU_ENODEVICE 8     /* no usable CUDA device                       */
+
+/* ---- factor precisions ---------------------------------------------------- */
+#define GBLU_FP64 0 /* plain FP64 LU, FP64 getrs                              */
+#define GBLU_FP32 1 /* FP32 LU, FP64 iterative refinement                      */
+
+/* ---- buffer locations ---------------------------------------------------- */
+#define GBLU_HOST 0
+#define GBLU_DEVICE 1
+
+typedef struct gblu_ctx gblu_ctx;
+typedef struct gblu_factor gblu_factor;
+
+/* Library version, (major << 16) | minor. */
+int32_t gblu_version(void);
+
+/* ---- context --------------------------------------------------------------
+ * A context binds one CUDA device, one CUDA stream and an HBM budget for all
+ * device memory it allocates (0 = no budget beyond the device's free memory).
+ * Replaces: the per-process BLAS handle of src/openblas.jl:48-72 (dlopen +
+ * dlsym once, then fixed pointers). */
+int32_t gblu_create(gblu_ctx** out, int32_t device, uint64_t hbm_budget_bytes);
+int32_t gblu_destroy(gblu_ctx* ctx);
+/* Message of the last failed call on this context ("" if none).  With ctx ==
+ * NULL: the last failure of gblu_create or of the LAPACK-shaped entries. */
+const char* gblu_last_error(const gblu_ctx* ctx);
+/* The context's cudaStream_t, for callers that time or order work around it. */
+int32_t gblu_ctx_stream(gblu_ctx* ctx, void** stream_out);
+/* Device bytes currently held by the context's objects, and its budget. */
+int32_t gblu_ctx_memory(gblu_ctx* ctx, uint64_t* in_use, uint64_t* budget);
+
+/* ---- factorization objects -------------------------------------------------
+ * A factor owns, in HBM, everything getrf/getrs need for an m x n matrix:
+ * the factors, ipiv, the row permutation, and all scratch.  It is the
+ * device-resident counterpart of LinearCache.cacheval (src/common.jl:281-306;
+ * the OpenBLASLUCache of src/openblas.jl:318-360).  Refactoring reuses it
+ * without allocating, as src/factorization.jl:630-641 does with ipiv.
+ * precision: GBLU_FP64 or GBLU_FP32 (mixed: FP32 factors, FP64 refinement;
+ * the FP64 copy of A is kept on the device for residuals). */
+int32_t gblu_factor_create(gblu_ctx* ctx, int64_t m, int64_t n, int32_t precision,
+                           gblu_factor** out);
+int32_t gblu_factor_destroy(gblu_ctx* ctx, gblu_factor* f);
+
+/* getrf: factor A (m x n, leading dimension lda) into f.  A is read, never
+ * written; a_loc = GBLU_HOST copies it to the device first.
+ * Replaces: LAPACK.getrf! reached from solve!(cache, ::LUFactorization)
+ * (src/factorization.jl:643-736, do_factorization :738-751) and the
+ * dgetrf_ ccall of src/openblas.jl:131-154. */
+int32_t gblu_getrf(gblu_ctx* ctx, gblu_factor* f, const double* A, int64_t lda,
+                   int32_t a_loc, int64_t* info);
+
+/* getrs: solve op(A) X = B in place for nrhs columns of B (ldb), with
+ * trans = 'N' or 'T'.  For a GBLU_FP32 factor this is the refined solve
+ * (gblu_solve_refined with default options), so the result is FP64-accurate.
+ * Replaces: _smart_lu_ldiv! / ldiv! -> getrs (src/factorization.jl:603-611,
+ * :727-728) and the dgetrs_ ccall of src/openblas.jl:247-278. */
+int32_t gblu_getrs(gblu_ctx* ctx, gblu_factor* f, char trans, int64_t nrhs, double* B,
+                   int64_t ldb, int32_t b_loc);
+
+/* Copies of the factorization result, for parity checks against LAPACK. */
+int32_t gblu_get_ipiv(gblu_ctx* ctx, gblu_factor* f, int64_t* ipiv_host);
+/* The packed L\U factors (FP64; low-precision factors are widened). */
+int32_t gblu_get_factors(gblu_ctx* ctx, gblu_factor* f, double* host, int64_t ld);
+/* info of the last getrf on f. */
+int32_t gblu_get_info(gblu_ctx* ctx, gblu_factor* f, int64_t* info);
+
+/* ---- mixed precision and iterative refinement --------------------------------
+ * A GBLU_FP32 factor holds FP32 L\U factors; solves reach FP64 accuracy by
+ * refinement: r = b - A x in FP64 (A kept in FP64 on the device), a
+ * correction solved with the FP32 factors, x += d in FP64.  mode
+ * GBLU_REFINE_IR is classic iterative refinement; GBLU_REFINE_GMRES is
+ * GMRES-IR (the correction equation solved by FP64 GMRES left-preconditioned
+ * by the FP32 LU).  When the backward error stops decreasing, or after
+ * max_iter iterations, the library factors A in FP64 and solves with that
+ * (fallback != 0), or returns GBLU_ESTALL (fallback == 0).
+ * No counterpart in the reference: its *32Mixed* types stop after the FP32
+ * solve (src/openblas.jl:487-543, ext/LinearSolveCUDAExt.jl:211-242). */
+#define GBLU_REFINE_IR 0
+#define GBLU_REFINE_GMRES 1
+
+typedef struct gblu_refine_opts {
+  int32_t mode;          /* GBLU_REFINE_IR or GBLU_REFINE_GMRES              */
+  int32_t max_iter;      /* outer refinement iterations                      */
+  double tol;            /* stop when backward error <= tol (<= 0: n * eps)  */
+  int32_t fallback;      /* nonzero: FP64 LU when refinement stalls          */
+  int32_t gmres_restart; /* GMRES basis size (<= 30)                          */
+  double gmres_tol;      /* relative residual target of each GMRES solve     */
+} gblu_refine_opts;
+
+typedef struct gblu_refine_stats {
+  int32_t iterations;       /* outer iterations taken (max over columns)     */
+  int32_t inner_iterations; /* total GMRES iterations                        */
+  int32_t converged;        /* 1 if every column met tol                     */
+  int32_t fell_back;        /* 1 if the FP64 fallback produced the answer    */
+  double backward_error;    /* final max_j ||b-Ax||/(||A|| ||x|| + ||b||), inf-norms */
+} gblu_refine_stats;
+
+int32_t gblu_refine_opts_default(gblu_refine_opts* opts);
+/* Solve op(A) X = B (in place) to FP64 accuracy with the factor f.  For a
+ * GBLU_FP64 factor this is the plain getrs followed by one residual that
+ * fills stats.  opts may be NULL (defaults); stats may be NULL. */
+int32_t gblu_solve_refined(gblu_ctx* ctx, gblu_factor* f, char trans, int64_t nrhs, double* B,
+                           int64_t ldb, int32_t b_loc, const gblu_refine_opts* opts,
+                           gblu_refine_stats* stats);
+
+/* ---- LAPACK-shaped entries ---------------------------------------------------
+ * Same argument lists as LAPACK dgetrf_/dgetrs_/sgetrf_/sgetrs_ with 64-bit
+ * integers (the ILP64 BlasInt of src/LinearSolve.jl:52-63), so a binding can
+ * swap the symbol in the ccall of src/openblas.jl:144-153,267-276.  Host
+ * buffers; each call copies to and from a process-wide default context on
+ * the current device.  info < 0 reports a bad argument as LAPACK does;
+ * info = -1000 - status reports a library failure (see gblu_last_error(NULL)). */
+void gblu_dgetrf_(const int64_t* m, const int64_t* n, double* A, const int64_t* lda,
+                  int64_t* ipiv, int64_t* info);
+void gblu_dgetrs_(const char* trans, const int64_t* n, const int64_t* nrhs,
+                  const double* A, const int64_t* lda, const int64_t* ipiv, double* B,
+                  const int64_t* ldb, int64_t* info, long trans_len);
+void gblu_sgetrf_(const int64_t* m, const int64_t* n, float* A, const int64_t* lda,
+                  int64_t* ipiv, int64_t* info);
+void gblu_sgetrs_(const char* trans, const int64_t* n, const int64_t* nrhs,
+                  const float* A, const int64_t* lda, const int64_t* ipiv, float* B,
+                  const int64_t* ldb, int64_t* info, long trans_len);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBLU_H */

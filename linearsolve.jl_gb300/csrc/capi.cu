@@ -1,0 +1,798 @@
+// The C ABI of libgblu (include/gblu.h): contexts, factor objects, getrf /
+// getrs entry points and the LAPACK-shaped host entries.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "gblu_internal.h"
+#include "objects.h"
+#include "refine.h"
+
+using namespace gblu;
+
+namespace gblu {
+
+const DeviceInfo& device_info(int device) {
+  static std::mutex mu;
+  static DeviceInfo cache[64];
+  static bool have[64] = {false};
+  if (device < 0 || device >= 64) device = 0;
+  std::lock_guard<std::mutex> g(mu);
+  if (!have[device]) {
+    DeviceInfo d;
+    d.device = device;
+    cudaDeviceGetAttribute(&d.num_sms, cudaDevAttrMultiProcessorCount, device);
+    int optin = 0;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+    d.smem_optin = (size_t)optin;
+    cudaDeviceGetAttribute(&d.cc_major, cudaDevAttrComputeCapabilityMajor, device);
+    cudaDeviceGetAttribute(&d.cc_minor, cudaDevAttrComputeCapabilityMinor, device);
+    if (d.num_sms <= 0) d.num_sms = 1;
+    cache[device] = d;
+    have[device] = true;
+  }
+  return cache[device];
+}
+
+}  // namespace gblu
+
+namespace {
+std::mutex g_err_mu;
+std::string g_err;  // errors with no context
+}  // namespace
+
+namespace gblu {
+
+int32_t fail(gblu_ctx* ctx, int32_t code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (ctx) ctx->last_error = buf;
+  else {
+    std::lock_guard<std::mutex> g(g_err_mu);
+    g_err = buf;
+  }
+  return code;
+}
+
+int32_t cuda_fail(gblu_ctx* ctx, cudaError_t e, const char* what) {
+  return fail(ctx, GBLU_ECUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CK GBLU_CK
+
+int32_t ctx_alloc(gblu_ctx* ctx, size_t bytes, void** out) {
+  if (ctx->budget && ctx->in_use + bytes > ctx->budget)
+    return fail(ctx, GBLU_ENOMEM, "HBM budget exceeded: %llu in use + %llu requested > %llu",
+                (unsigned long long)ctx->in_use, (unsigned long long)bytes,
+                (unsigned long long)ctx->budget);
+  cudaError_t e = cudaMalloc(out, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(ctx, GBLU_ENOMEM, "cudaMalloc(%llu): %s", (unsigned long long)bytes,
+                cudaGetErrorString(e));
+  }
+  ctx->in_use += bytes;
+  return GBLU_OK;
+}
+
+void ctx_free(gblu_ctx* ctx, void* p, size_t bytes) {
+  if (!p) return;
+  cudaFree(p);
+  ctx->in_use -= std::min<uint64_t>(ctx->in_use, bytes);
+}
+
+// Reads back the sticky device error words of the plans a call used.
+int32_t check_device_errors(gblu_ctx* ctx, std::initializer_list<DevScratch*> scr) {
+  for (DevScratch* s : scr) {
+    if (!s) continue;
+    int32_t err = 0;
+    cudaError_t e = cudaMemcpyAsync(&err, &s->error, sizeof(err), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "reading device error word");
+    if (err != DEV_OK) {
+      int32_t zero = 0;
+      cudaMemcpyAsync(&s->error, &zero, sizeof(zero), cudaMemcpyHostToDevice, ctx->stream);
+      cudaStreamSynchronize(ctx->stream);
+      if (err == DEV_TIMEOUT_PANEL || err == DEV_TIMEOUT_SOLVE)
+        return fail(ctx, GBLU_ETIMEOUT, "device wait timed out (code %d)", err);
+      return fail(ctx, GBLU_EINVAL, "device detected invalid pivot data (code %d)", err);
+    }
+  }
+  return GBLU_OK;
+}
+
+// Bytes and carving of one factorization set (factors, ipiv, perm, info,
+// getrf and getrs scratch) for an m x n matrix with leading dimension ld.
+template <typename T>
+size_t set_bytes(int64_t m, int64_t n, int64_t ld, int device, int64_t work_cols) {
+  size_t b = align256((size_t)ld * n * sizeof(T));
+  b += align256(std::max<int64_t>(1, std::min(m, n)) * sizeof(int64_t));
+  b += align256(std::max<int64_t>(1, m) * sizeof(int32_t));
+  b += align256(sizeof(int64_t));
+  b += align256(getrf_scratch_bytes(m, n, sizeof(T), 32, device));
+  b += align256(getrs_scratch_bytes(std::max<int64_t>(m, 1), sizeof(T), work_cols));
+  return b;
+}
+
+template <typename T>
+char* carve_set(char* c, int64_t m, int64_t n, int64_t ld, int device, int64_t work_cols,
+                T** lu, int64_t** ipiv, int32_t** perm, int64_t** info, GetrfPlan<T>& rf,
+                GetrsPlan<T>& rs) {
+  auto take = [&](size_t b) { char* r = c; c += align256(b); return r; };
+  *lu = reinterpret_cast<T*>(take((size_t)ld * n * sizeof(T)));
+  *ipiv = reinterpret_cast<int64_t*>(take(std::max<int64_t>(1, std::min(m, n)) * sizeof(int64_t)));
+  *perm = reinterpret_cast<int32_t*>(take(std::max<int64_t>(1, m) * sizeof(int32_t)));
+  *info = reinterpret_cast<int64_t*>(take(sizeof(int64_t)));
+  size_t fb = getrf_scratch_bytes(m, n, sizeof(T), 32, device);
+  getrf_carve(rf, take(fb), fb, device);
+  size_t sb = getrs_scratch_bytes(std::max<int64_t>(m, 1), sizeof(T), work_cols);
+  rs.n = m;  // getrs plans are only used for square factors
+  getrs_carve(rs, take(sb), sb, work_cols);
+  rf.m = m;
+  rf.n = n;
+  rf.lda = ld;
+  rf.A = *lu;
+  rf.ipiv = *ipiv;
+  rf.info = *info;
+  rf.perm = *perm;
+  rs.lda = ld;
+  rs.LU = *lu;
+  rs.perm = *perm;
+  rs.ipiv = *ipiv;
+  return c;
+}
+
+constexpr int64_t kWorkCols = 8;
+constexpr int64_t kWorkColsFb = 8;
+
+int32_t ensure_rhs(gblu_ctx* ctx, gblu_factor* f, int64_t cols) {
+  if (f->rhs_cols >= cols) return GBLU_OK;
+  if (f->rhs) ctx_free(ctx, f->rhs, (size_t)f->ld * f->rhs_cols * sizeof(double));
+  f->rhs = nullptr;
+  f->rhs_cols = 0;
+  void* p = nullptr;
+  int32_t st = ctx_alloc(ctx, (size_t)f->ld * cols * sizeof(double), &p);
+  if (st) return st;
+  f->rhs = reinterpret_cast<double*>(p);
+  f->rhs_cols = cols;
+  return GBLU_OK;
+}
+
+}  // namespace gblu
+
+
+extern "C" {
+
+int32_t gblu_version(void) { return (1 << 16) | 0; }
+
+int32_t gblu_create(gblu_ctx** out, int32_t device, uint64_t hbm_budget_bytes) {
+  if (!out) return fail(nullptr, GBLU_EINVAL, "gblu_create: out is NULL");
+  *out = nullptr;
+  int count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess || count == 0) {
+    cudaGetLastError();
+    return fail(nullptr, GBLU_ENODEVICE, "no CUDA device: %s", cudaGetErrorString(e));
+  }
+  if (device < 0 || device >= count)
+    return fail(nullptr, GBLU_EINVAL, "gblu_create: device %d out of range [0,%d)", device, count);
+  DeviceGuard g(device);
+  const DeviceInfo& di = device_info(device);
+  if (di.cc_major < 10)
+    return fail(nullptr, GBLU_EUNSUPPORTED, "device %d is sm_%d%d; libgblu is built for sm_103a",
+                device, di.cc_major, di.cc_minor);
+  {
+    static std::mutex cfg_mu;
+    static bool configured[64] = {false};
+    std::lock_guard<std::mutex> lk(cfg_mu);
+    if (device < 64 && !configured[device]) {
+      getrf_configure(device);
+      configured[device] = true;
+    }
+  }
+  gblu_ctx* c = new (std::nothrow) gblu_ctx();
+  if (!c) return fail(nullptr, GBLU_ENOMEM, "host allocation failed");
+  c->device = device;
+  c->budget = hbm_budget_bytes;
+  e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete c;
+    return fail(nullptr, GBLU_ECUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
+  }
+  *out = c;
+  return GBLU_OK;
+}
+
+int32_t gblu_destroy(gblu_ctx* ctx) {
+  if (!ctx) return GBLU_OK;
+  {
+    DeviceGuard g(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    cudaStreamDestroy(ctx->stream);
+  }
+  delete ctx;
+  return GBLU_OK;
+}
+
+const char* gblu_last_error(const gblu_ctx* ctx) {
+  if (ctx) return ctx->last_error.c_str();
+  thread_local std::string copy;
+  std::lock_guard<std::mutex> g(g_err_mu);
+  copy = g_err;
+  return copy.c_str();
+}
+
+int32_t gblu_ctx_stream(gblu_ctx* ctx, void** stream_out) {
+  if (!ctx || !stream_out) return fail(ctx, GBLU_EINVAL, "gblu_ctx_stream: NULL argument");
+  *stream_out = reinterpret_cast<void*>(ctx->stream);
+  return GBLU_OK;
+}
+
+int32_t gblu_ctx_memory(gblu_ctx* ctx, uint64_t* in_use, uint64_t* budget) {
+  if (!ctx) return fail(ctx, GBLU_EINVAL, "gblu_ctx_memory: NULL ctx");
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  if (in_use) *in_use = ctx->in_use;
+  if (budget) *budget = ctx->budget;
+  return GBLU_OK;
+}
+
+int32_t gblu_factor_create(gblu_ctx* ctx, int64_t m, int64_t n, int32_t precision,
+                           gblu_factor** out) {
+  if (!ctx || !out) return fail(ctx, GBLU_EINVAL, "gblu_factor_create: NULL argument");
+  *out = nullptr;
+  if (m < 0 || n < 0) return fail(ctx, GBLU_EINVAL, "gblu_factor_create: negative size %lld x %lld",
+                                  (long long)m, (long long)n);
+  if (precision != GBLU_FP64 && precision != GBLU_FP32)
+    return fail(ctx, GBLU_EUNSUPPORTED, "gblu_factor_create: unknown precision %d", precision);
+  if (m > (int64_t)INT32_MAX || n > (int64_t)INT32_MAX)
+    return fail(ctx, GBLU_EUNSUPPORTED, "gblu_factor_create: dimension too large");
+  if (precision != GBLU_FP64 && m != n)
+    return fail(ctx, GBLU_EUNSUPPORTED, "mixed-precision factors must be square");
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  DeviceGuard g(ctx->device);
+  gblu_factor* f = new (std::nothrow) gblu_factor();
+  if (!f) return fail(ctx, GBLU_ENOMEM, "host allocation failed");
+  f->m = m;
+  f->n = n;
+  f->precision = precision;
+  f->ld = std::max<int64_t>(32, ((m + 31) / 32) * 32);
+  size_t bytes;
+  if (precision == GBLU_FP64) {
+    bytes = set_bytes<double>(m, n, f->ld, ctx->device, kWorkCols);
+  } else {
+    bytes = set_bytes<float>(m, n, f->ld, ctx->device, kWorkCols);
+    bytes += align256((size_t)f->ld * n * sizeof(double));  // FP64 copy of A
+    bytes += refine_bytes(m, kWorkCols);
+  }
+  int32_t st = ctx_alloc(ctx, bytes, &f->arena);
+  if (st) {
+    delete f;
+    return st;
+  }
+  f->bytes = bytes;
+  char* c = reinterpret_cast<char*>(f->arena);
+  if (precision == GBLU_FP64) {
+    c = carve_set<double>(c, m, n, f->ld, ctx->device, kWorkCols, &f->lu64, &f->ipiv, &f->perm,
+                          &f->info_dev, f->rf64, f->rs64);
+  } else {
+    c = carve_set<float>(c, m, n, f->ld, ctx->device, kWorkCols, &f->lu32, &f->ipiv, &f->perm,
+                         &f->info_dev, f->rf32, f->rs32);
+    f->lu64 = reinterpret_cast<double*>(c);
+    c += align256((size_t)f->ld * n * sizeof(double));
+    refine_carve(f->refine, c, m, kWorkCols);
+  }
+  cudaError_t e = cudaMemsetAsync(f->arena, 0, bytes, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) {
+    ctx_free(ctx, f->arena, bytes);
+    delete f;
+    return cuda_fail(ctx, e, "clearing factor arena");
+  }
+  *out = f;
+  return GBLU_OK;
+}
+
+int32_t gblu_factor_destroy(gblu_ctx* ctx, gblu_factor* f) {
+  if (!f) return GBLU_OK;
+  if (!ctx) return fail(ctx, GBLU_EINVAL, "gblu_factor_destroy: NULL ctx");
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  DeviceGuard g(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  ctx_free(ctx, f->arena, f->bytes);
+  if (f->rhs) ctx_free(ctx, f->rhs, (size_t)f->ld * f->rhs_cols * sizeof(double));
+  if (f->fb_arena) ctx_free(ctx, f->fb_arena, f->fb_bytes);
+  delete f;
+  return GBLU_OK;
+}
+
+}  // extern "C"
+
+namespace gblu {
+
+// Copy a host or device FP64 matrix (rows x cols, ld_src) into dst (ld_dst).
+int32_t upload_matrix(gblu_ctx* ctx, double* dst, int64_t ld_dst, const double* src, int64_t ld_src,
+                      int64_t rows, int64_t cols, int32_t loc) {
+  if (rows == 0 || cols == 0) return GBLU_OK;
+  cudaMemcpyKind kind = loc == GBLU_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  CK(ctx, cudaMemcpy2DAsync(dst, ld_dst * sizeof(double), src, ld_src * sizeof(double),
+                            rows * sizeof(double), cols, kind, ctx->stream),
+     "copying matrix to device");
+  return GBLU_OK;
+}
+
+int32_t factor_getrf(gblu_ctx* ctx, gblu_factor* f, const double* A, int64_t lda, int32_t a_loc,
+                     int64_t* info) {
+  f->factored = false;
+  f->fb_valid = false;
+  int32_t st;
+  if (f->precision == GBLU_FP64) {
+    st = upload_matrix(ctx, f->lu64, f->ld, A, lda, f->m, f->n, a_loc);
+    if (st) return st;
+    CK(ctx, getrf_launch<double>(f->rf64, ctx->stream), "launching getrf");
+  } else {
+    st = upload_matrix(ctx, f->lu64, f->ld, A, lda, f->m, f->n, a_loc);
+    if (st) return st;
+    CK(ctx, refine_prepare(f->refine, f->n, f->lu64, f->ld, f->lu32, f->ld, ctx->stream),
+       "preparing mixed-precision factorization");
+    CK(ctx, getrf_launch<float>(f->rf32, ctx->stream), "launching getrf");
+  }
+  int64_t hinfo = 0;
+  CK(ctx, cudaMemcpyAsync(&hinfo, f->info_dev, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream),
+     "reading info");
+  CK(ctx, cudaStreamSynchronize(ctx->stream), "getrf");
+  st = check_device_errors(ctx, {f->precision == GBLU_FP64 ? f->rf64.scratch : f->rf32.scratch});
+  if (st) return st;
+  f->info = hinfo;
+  f->use_fb = false;
+  if (f->precision != GBLU_FP64 && hinfo != 0) {
+    // An exactly zero pivot in the low-precision factors: decide singularity
+    // with the FP64 factorization, which then serves every solve.
+    int64_t info64 = 0;
+    st = factor_fp64_fallback(ctx, f, &info64);
+    if (st) return st;
+    f->info = info64;
+    f->use_fb = f->fb_valid;
+  }
+  f->factored = true;
+  if (info) *info = f->info;
+  return GBLU_OK;
+}
+
+int32_t factor_fp64_fallback(gblu_ctx* ctx, gblu_factor* f, int64_t* info_out) {
+  if (!f->fb_arena) {
+    size_t bytes = set_bytes<double>(f->m, f->n, f->ld, ctx->device, kWorkColsFb);
+    int32_t st = ctx_alloc(ctx, bytes, &f->fb_arena);
+    if (st) return st;
+    f->fb_bytes = bytes;
+    CK(ctx, cudaMemsetAsync(f->fb_arena, 0, bytes, ctx->stream), "clearing fallback arena");
+    carve_set<double>(reinterpret_cast<char*>(f->fb_arena), f->m, f->n, f->ld, ctx->device,
+                      kWorkColsFb, &f->fb_lu, &f->fb_ipiv, &f->fb_perm, &f->fb_info, f->fb_rf,
+                      f->fb_rs);
+  }
+  CK(ctx, cudaMemcpyAsync(f->fb_lu, f->lu64, (size_t)f->ld * f->n * sizeof(double),
+                          cudaMemcpyDeviceToDevice, ctx->stream),
+     "copying A for the FP64 fallback");
+  CK(ctx, getrf_launch<double>(f->fb_rf, ctx->stream), "launching fallback getrf");
+  int64_t hinfo = 0;
+  CK(ctx, cudaMemcpyAsync(&hinfo, f->fb_info, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream),
+     "reading fallback info");
+  CK(ctx, cudaStreamSynchronize(ctx->stream), "fallback getrf");
+  int32_t st = check_device_errors(ctx, {f->fb_rf.scratch});
+  if (st) return st;
+  f->fb_valid = (hinfo == 0);
+  if (info_out) *info_out = hinfo;
+  return GBLU_OK;
+}
+
+int32_t factor_getrs_plain(gblu_ctx* ctx, gblu_factor* f, char trans, int64_t nrhs, double* dB,
+                           int64_t ldb) {
+  CK(ctx, getrs_launch<double>(f->rs64, trans, nrhs, dB, ldb, nullptr, ctx->stream),
+     "launching getrs");
+  return GBLU_OK;
+}
+
+}  // namespace gblu
+
+extern "C" {
+
+int32_t gblu_getrf(gblu_ctx* ctx, gblu_factor* f, const double* A, int64_t lda, int32_t a_loc,
+                   int64_t* info) {
+  if (!ctx || !f) return fail(ctx, GBLU_EINVAL, "gblu_getrf: NULL argument");
+  if (!A && f->m * f->n > 0) return fail(ctx, GBLU_EINVAL, "gblu_getrf: A is NULL");
+  if (lda < std::max<int64_t>(1, f->m)) return fail(ctx, GBLU_EINVAL, "gblu_getrf: lda %lld < m %lld",
+                                                   (long long)lda, (long long)f->m);
+  if (a_loc != GBLU_HOST && a_loc != GBLU_DEVICE) return fail(ctx, GBLU_EINVAL, "gblu_getrf: bad a_loc");
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  DeviceGuard g(ctx->device);
+  return factor_getrf(ctx, f, A, lda, a_loc, info);
+}
+
+int32_t gblu_getrs(gblu_ctx* ctx, gblu_factor* f, char trans, int64_t nrhs, double* B, int64_t ldb,
+                   int32_t b_loc) {
+  if (!ctx || !f) return fail(ctx, GBLU_EINVAL, "gblu_getrs: NULL argument");
+  if (!(trans == 'N' || trans == 'n' || trans == 'T' || trans == 't' || trans == 'C' || trans == 'c'))
+    return fail(ctx, GBLU_EINVAL, "gblu_getrs: trans must be 'N' or 'T'");
+  if (f->m != f->n) return fail(ctx, GBLU_EINVAL, "gblu_getrs: factor is not square");
+  if (nrhs < 0) return fail(ctx, GBLU_EINVAL, "gblu_getrs: nrhs < 0");
+  if (ldb < std::max<int64_t>(1, f->n)) return fail(ctx, GBLU_EINVAL, "gblu_getrs: ldb < n");
+  if (b_loc != GBLU_HOST && b_loc != GBLU_DEVICE) return fail(ctx, GBLU_EINVAL, "gblu_getrs: bad b_loc");
+  if (!f->factored) return fail(ctx, GBLU_ENOTFACTORED, "gblu_getrs: no factorization");
+  if (f->info != 0)
+    return fail(ctx, GBLU_EINVAL, "gblu_getrs: factorization is singular (info = %lld)",
+                (long long)f->info);
+  if (nrhs == 0 || f->n == 0) return GBLU_OK;
+  if (!B) return fail(ctx, GBLU_EINVAL, "gblu_getrs: B is NULL");
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  DeviceGuard g(ctx->device);
+  if (f->precision != GBLU_FP64) {
+    gblu_refine_opts o = refine_default_opts();
+    return refine_solve(ctx, f, trans, nrhs, B, ldb, b_loc, &o, nullptr);
+  }
+  double* dB = B;
+  int64_t lddb = ldb;
+  int32_t st;
+  if (b_loc == GBLU_HOST) {
+    st = ensure_rhs(ctx, f, std::max<int64_t>(nrhs, 1));
+    if (st) return st;
+    dB = f->rhs;
+    lddb = f->ld;
+    st = upload_matrix(ctx, dB, lddb, B, ldb, f->n, nrhs, GBLU_HOST);
+    if (st) return st;
+  }
+  st = factor_getrs_plain(ctx, f, trans, nrhs, dB, lddb);
+  if (st) return st;
+  if (b_loc == GBLU_HOST)
+    CK(ctx, cudaMemcpy2DAsync(B, ldb * sizeof(double), dB, lddb * sizeof(double),
+                              f->n * sizeof(double), nrhs, cudaMemcpyDeviceToHost, ctx->stream),
+       "copying solution to host");
+  CK(ctx, cudaStreamSynchronize(ctx->stream), "getrs");
+  return check_device_errors(ctx, {f->rs64.scratch});
+}
+
+int32_t gblu_solve_refined(gblu_ctx* ctx, gblu_factor* f, char trans, int64_t nrhs, double* B,
+                           int64_t ldb, int32_t b_loc, const gblu_refine_opts* opts,
+                           gblu_refine_stats* stats) {
+  if (!ctx || !f) return fail(ctx, GBLU_EINVAL, "gblu_solve_refined: NULL argument");
+  if (opts && (opts->mode != GBLU_REFINE_IR && opts->mode != GBLU_REFINE_GMRES))
+    return fail(ctx, GBLU_EINVAL, "gblu_solve_refined: unknown mode %d", opts->mode);
+  if (opts && (opts->max_iter < 0 || opts->gmres_restart < 1))
+    return fail(ctx, GBLU_EINVAL, "gblu_solve_refined: bad iteration limits");
+  if (f->precision == GBLU_FP64) {
+    int32_t st = gblu_getrs(ctx, f, trans, nrhs, B, ldb, b_loc);
+    if (st) return st;
+    if (stats) {
+      *stats = gblu_refine_stats{};
+      stats->converged = 1;
+      stats->backward_error = -1.0;  // A is not kept for FP64 factors
+    }
+    return GBLU_OK;
+  }
+  if (!(trans == 'N' || trans == 'n' || trans == 'T' || trans == 't' || trans == 'C' || trans == 'c'))
+    return fail(ctx, GBLU_EINVAL, "gblu_solve_refined: trans must be 'N' or 'T'");
+  if (nrhs < 0) return fail(ctx, GBLU_EINVAL, "gblu_solve_refined: nrhs < 0");
+  if (ldb < std::max<int64_t>(1, f->n)) return fail(ctx, GBLU_EINVAL, "gblu_solve_refined: ldb < n");
+  if (b_loc != GBLU_HOST && b_loc != GBLU_DEVICE)
+    return fail(ctx, GBLU_EINVAL, "gblu_solve_refined: bad b_loc");
+  if (!f->factored) return fail(ctx, GBLU_ENOTFACTORED, "gblu_solve_refined: no factorization");
+  if (f->info != 0)
+    return fail(ctx, GBLU_EINVAL, "gblu_solve_refined: factorization is singular (info = %lld)",
+                (long long)f->info);
+  if (nrhs == 0 || f->n == 0) {
+    if (stats) { *stats = gblu_refine_stats{}; stats->converged = 1; }
+    return GBLU_OK;
+  }
+  if (!B) return fail(ctx, GBLU_EINVAL, "gblu_solve_refined: B is NULL");
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  DeviceGuard g(ctx->device);
+  return refine_solve(ctx, f, trans, nrhs, B, ldb, b_loc, opts, stats);
+}
+
+int32_t gblu_get_ipiv(gblu_ctx* ctx, gblu_factor* f, int64_t* ipiv_host) {
+  if (!ctx || !f || !ipiv_host) return fail(ctx, GBLU_EINVAL, "gblu_get_ipiv: NULL argument");
+  if (!f->factored) return fail(ctx, GBLU_ENOTFACTORED, "gblu_get_ipiv: no factorization");
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  DeviceGuard g(ctx->device);
+  int64_t k = std::min(f->m, f->n);
+  if (k == 0) return GBLU_OK;
+  CK(ctx, cudaMemcpyAsync(ipiv_host, f->ipiv, k * sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream),
+     "copying ipiv");
+  CK(ctx, cudaStreamSynchronize(ctx->stream), "copying ipiv");
+  return GBLU_OK;
+}
+
+int32_t gblu_get_factors(gblu_ctx* ctx, gblu_factor* f, double* host, int64_t ld) {
+  if (!ctx || !f || (!host && f->m * f->n > 0))
+    return fail(ctx, GBLU_EINVAL, "gblu_get_factors: NULL argument");
+  if (ld < std::max<int64_t>(1, f->m)) return fail(ctx, GBLU_EINVAL, "gblu_get_factors: ld < m");
+  if (!f->factored) return fail(ctx, GBLU_ENOTFACTORED, "gblu_get_factors: no factorization");
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  DeviceGuard g(ctx->device);
+  if (f->m * f->n == 0) return GBLU_OK;
+  if (f->precision == GBLU_FP64) {
+    CK(ctx, cudaMemcpy2DAsync(host, ld * sizeof(double), f->lu64, f->ld * sizeof(double),
+                              f->m * sizeof(double), f->n, cudaMemcpyDeviceToHost, ctx->stream),
+       "copying factors");
+    CK(ctx, cudaStreamSynchronize(ctx->stream), "copying factors");
+  } else {
+    std::vector<float> tmp((size_t)f->ld * f->n);
+    CK(ctx, cudaMemcpyAsync(tmp.data(), f->lu32, tmp.size() * sizeof(float), cudaMemcpyDeviceToHost,
+                            ctx->stream),
+       "copying factors");
+    CK(ctx, cudaStreamSynchronize(ctx->stream), "copying factors");
+    for (int64_t j = 0; j < f->n; ++j)
+      for (int64_t i = 0; i < f->m; ++i) host[i + j * ld] = (double)tmp[i + j * f->ld];
+  }
+  return GBLU_OK;
+}
+
+int32_t gblu_get_info(gblu_ctx* ctx, gblu_factor* f, int64_t* info) {
+  if (!ctx || !f || !info) return fail(ctx, GBLU_EINVAL, "gblu_get_info: NULL argument");
+  if (!f->factored) return fail(ctx, GBLU_ENOTFACTORED, "gblu_get_info: no factorization");
+  *info = f->info;
+  return GBLU_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// LAPACK-shaped host entries on a process-wide default context.
+
+namespace {
+
+std::mutex g_lapack_mu;
+gblu_ctx* g_lapack_ctx = nullptr;
+gblu_factor* g_lapack_f64 = nullptr;
+
+gblu_ctx* lapack_ctx(int32_t* st) {
+  if (!g_lapack_ctx) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    *st = gblu_create(&g_lapack_ctx, dev, 0);
+    if (*st) g_lapack_ctx = nullptr;
+  }
+  return g_lapack_ctx;
+}
+
+gblu_factor* lapack_factor(gblu_ctx* ctx, gblu_factor** slot, int64_t m, int64_t n, int32_t* st) {
+  if (*slot && ((*slot)->m != m || (*slot)->n != n)) {
+    gblu_factor_destroy(ctx, *slot);
+    *slot = nullptr;
+  }
+  if (!*slot) *st = gblu_factor_create(ctx, m, n, GBLU_FP64, slot);
+  return *slot;
+}
+
+int64_t lapack_err(int32_t st, gblu_ctx* ctx) {
+  if (ctx) fail(nullptr, st, "%s", ctx->last_error.c_str());
+  return -1000 - (int64_t)st;
+}
+
+}  // namespace
+
+namespace gblu {
+int32_t factor_getrf_f32_host(gblu_ctx* ctx, int64_t m, int64_t n, float* A, int64_t lda,
+                              int64_t* ipiv, int64_t* info);
+int32_t factor_getrs_f32_host(gblu_ctx* ctx, char trans, int64_t n, int64_t nrhs, const float* A,
+                              int64_t lda, const int64_t* ipiv, float* B, int64_t ldb);
+int32_t factor_getrs_f64_host(gblu_ctx* ctx, gblu_factor* f, char trans, int64_t nrhs,
+                              const double* A, int64_t lda, const int64_t* ipiv, double* B,
+                              int64_t ldb);
+}  // namespace gblu
+
+extern "C" {
+
+void gblu_dgetrf_(const int64_t* m, const int64_t* n, double* A, const int64_t* lda, int64_t* ipiv,
+                  int64_t* info) {
+  if (!m || !n || !lda || !info) return;
+  if (*m < 0) { *info = -1; return; }
+  if (*n < 0) { *info = -2; return; }
+  if (*lda < std::max<int64_t>(1, *m)) { *info = -4; return; }
+  *info = 0;
+  if (*m == 0 || *n == 0) return;
+  std::lock_guard<std::mutex> g(g_lapack_mu);
+  int32_t st = GBLU_OK;
+  gblu_ctx* ctx = lapack_ctx(&st);
+  if (!ctx) { *info = lapack_err(st, nullptr); return; }
+  gblu_factor* f = lapack_factor(ctx, &g_lapack_f64, *m, *n, &st);
+  if (!f) { *info = lapack_err(st, ctx); return; }
+  int64_t inf = 0;
+  st = gblu_getrf(ctx, f, A, *lda, GBLU_HOST, &inf);
+  if (st) { *info = lapack_err(st, ctx); return; }
+  st = gblu_get_factors(ctx, f, A, *lda);
+  if (!st) st = gblu_get_ipiv(ctx, f, ipiv);
+  if (st) { *info = lapack_err(st, ctx); return; }
+  *info = inf;
+}
+
+void gblu_dgetrs_(const char* trans, const int64_t* n, const int64_t* nrhs, const double* A,
+                  const int64_t* lda, const int64_t* ipiv, double* B, const int64_t* ldb,
+                  int64_t* info, long trans_len) {
+  (void)trans_len;
+  if (!trans || !n || !nrhs || !lda || !ldb || !info) return;
+  char t = *trans;
+  if (!(t == 'N' || t == 'n' || t == 'T' || t == 't' || t == 'C' || t == 'c')) { *info = -1; return; }
+  if (*n < 0) { *info = -2; return; }
+  if (*nrhs < 0) { *info = -3; return; }
+  if (*lda < std::max<int64_t>(1, *n)) { *info = -5; return; }
+  if (*ldb < std::max<int64_t>(1, *n)) { *info = -8; return; }
+  *info = 0;
+  if (*n == 0 || *nrhs == 0) return;
+  std::lock_guard<std::mutex> g(g_lapack_mu);
+  int32_t st = GBLU_OK;
+  gblu_ctx* ctx = lapack_ctx(&st);
+  if (!ctx) { *info = lapack_err(st, nullptr); return; }
+  gblu_factor* f = lapack_factor(ctx, &g_lapack_f64, *n, *n, &st);
+  if (!f) { *info = lapack_err(st, ctx); return; }
+  st = factor_getrs_f64_host(ctx, f, t, *nrhs, A, *lda, ipiv, B, *ldb);
+  if (st) *info = lapack_err(st, ctx);
+}
+
+void gblu_sgetrf_(const int64_t* m, const int64_t* n, float* A, const int64_t* lda, int64_t* ipiv,
+                  int64_t* info) {
+  if (!m || !n || !lda || !info) return;
+  if (*m < 0) { *info = -1; return; }
+  if (*n < 0) { *info = -2; return; }
+  if (*lda < std::max<int64_t>(1, *m)) { *info = -4; return; }
+  *info = 0;
+  if (*m == 0 || *n == 0) return;
+  std::lock_guard<std::mutex> g(g_lapack_mu);
+  int32_t st = GBLU_OK;
+  gblu_ctx* ctx = lapack_ctx(&st);
+  if (!ctx) { *info = lapack_err(st, nullptr); return; }
+  int64_t inf = 0;
+  st = factor_getrf_f32_host(ctx, *m, *n, A, *lda, ipiv, &inf);
+  *info = st ? lapack_err(st, ctx) : inf;
+}
+
+void gblu_sgetrs_(const char* trans, const int64_t* n, const int64_t* nrhs, const float* A,
+                  const int64_t* lda, const int64_t* ipiv, float* B, const int64_t* ldb,
+                  int64_t* info, long trans_len) {
+  (void)trans_len;
+  if (!trans || !n || !nrhs || !lda || !ldb || !info) return;
+  char t = *trans;
+  if (!(t == 'N' || t == 'n' || t == 'T' || t == 't' || t == 'C' || t == 'c')) { *info = -1; return; }
+  if (*n < 0) { *info = -2; return; }
+  if (*nrhs < 0) { *info = -3; return; }
+  if (*lda < std::max<int64_t>(1, *n)) { *info = -5; return; }
+  if (*ldb < std::max<int64_t>(1, *n)) { *info = -8; return; }
+  *info = 0;
+  if (*n == 0 || *nrhs == 0) return;
+  std::lock_guard<std::mutex> g(g_lapack_mu);
+  int32_t st = GBLU_OK;
+  gblu_ctx* ctx = lapack_ctx(&st);
+  if (!ctx) { *info = lapack_err(st, nullptr); return; }
+  st = factor_getrs_f32_host(ctx, t, *n, *nrhs, A, *lda, ipiv, B, *ldb);
+  if (st) *info = lapack_err(st, ctx);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Host-factor paths of the LAPACK-shaped entries.
+
+namespace gblu {
+
+namespace {
+__global__ void upload_ipiv_check_kernel(const int64_t* ipiv, int64_t n, DevScratch* scr) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    int64_t t = ipiv[k] - 1;
+    if (t < k || t >= n) atomicCAS(&scr->error, 0, (int)DEV_BAD_PIVOT_INDEX);
+  }
+}
+}  // namespace
+
+int32_t factor_getrs_f64_host(gblu_ctx* ctx, gblu_factor* f, char trans, int64_t nrhs,
+                              const double* A, int64_t lda, const int64_t* ipiv, double* B,
+                              int64_t ldb) {
+  DeviceGuard g(ctx->device);
+  const int64_t n = f->n;
+  int32_t st = upload_matrix(ctx, f->lu64, f->ld, A, lda, n, n, GBLU_HOST);
+  if (st) return st;
+  CK(ctx, cudaMemcpyAsync(f->ipiv, ipiv, n * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream),
+     "copying ipiv");
+  upload_ipiv_check_kernel<<<std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 1024)), 256, 0,
+                             ctx->stream>>>(f->ipiv, n, f->rf64.scratch);
+  CK(ctx, cudaGetLastError(), "checking ipiv");
+  st = check_device_errors(ctx, {f->rf64.scratch});
+  if (st) return st;
+  CK(ctx, perm_build_launch(f->ipiv, n, n, f->perm, f->rf64.scratch, ctx->stream), "building perm");
+  f->factored = true;
+  f->info = 0;
+  f->fb_valid = false;
+  return gblu_getrs(ctx, f, trans, nrhs, B, ldb, GBLU_HOST);
+}
+
+int32_t factor_getrf_f32_host(gblu_ctx* ctx, int64_t m, int64_t n, float* A, int64_t lda,
+                              int64_t* ipiv, int64_t* info) {
+  DeviceGuard g(ctx->device);
+  const int64_t ld = std::max<int64_t>(32, ((m + 31) / 32) * 32);
+  size_t bytes = set_bytes<float>(m, n, ld, ctx->device, kWorkCols);
+  void* arena = nullptr;
+  int32_t st = ctx_alloc(ctx, bytes, &arena);
+  if (st) return st;
+  GetrfPlan<float> rf;
+  GetrsPlan<float> rs;
+  float* lu;
+  int64_t *dipiv, *dinfo;
+  int32_t* perm;
+  CK(ctx, cudaMemsetAsync(arena, 0, bytes, ctx->stream), "clearing arena");
+  carve_set<float>(reinterpret_cast<char*>(arena), m, n, ld, ctx->device, kWorkCols, &lu, &dipiv,
+                   &perm, &dinfo, rf, rs);
+  cudaError_t e = cudaMemcpy2DAsync(lu, ld * sizeof(float), A, lda * sizeof(float), m * sizeof(float),
+                                    n, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) e = getrf_launch<float>(rf, ctx->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpy2DAsync(A, lda * sizeof(float), lu, ld * sizeof(float), m * sizeof(float), n,
+                          cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(ipiv, dipiv, std::min(m, n) * sizeof(int64_t), cudaMemcpyDeviceToHost,
+                        ctx->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(info, dinfo, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e == cudaSuccess) st = check_device_errors(ctx, {rf.scratch});
+  ctx_free(ctx, arena, bytes);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "sgetrf");
+  return st;
+}
+
+int32_t factor_getrs_f32_host(gblu_ctx* ctx, char trans, int64_t n, int64_t nrhs, const float* A,
+                              int64_t lda, const int64_t* ipiv, float* B, int64_t ldb) {
+  DeviceGuard g(ctx->device);
+  const int64_t ld = std::max<int64_t>(32, ((n + 31) / 32) * 32);
+  size_t bytes = set_bytes<float>(n, n, ld, ctx->device, kWorkCols) + align256((size_t)ld * nrhs * 4);
+  void* arena = nullptr;
+  int32_t st = ctx_alloc(ctx, bytes, &arena);
+  if (st) return st;
+  GetrfPlan<float> rf;
+  GetrsPlan<float> rs;
+  float* lu;
+  int64_t *dipiv, *dinfo;
+  int32_t* perm;
+  char* end = carve_set<float>(reinterpret_cast<char*>(arena), n, n, ld, ctx->device, kWorkCols, &lu,
+                               &dipiv, &perm, &dinfo, rf, rs);
+  float* dB = reinterpret_cast<float*>(end);
+  cudaError_t e = cudaMemsetAsync(arena, 0, bytes, ctx->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpy2DAsync(lu, ld * sizeof(float), A, lda * sizeof(float), n * sizeof(float), n,
+                          cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(dipiv, ipiv, n * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) {
+    upload_ipiv_check_kernel<<<std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 1024)), 256, 0,
+                               ctx->stream>>>(dipiv, n, rf.scratch);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) {
+    e = cudaStreamSynchronize(ctx->stream);
+    if (e == cudaSuccess) st = check_device_errors(ctx, {rf.scratch});
+  }
+  if (e == cudaSuccess && st == GBLU_OK) {
+    e = perm_build_launch(dipiv, n, n, perm, rf.scratch, ctx->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpy2DAsync(dB, ld * sizeof(float), B, ldb * sizeof(float), n * sizeof(float), nrhs,
+                            cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = getrs_launch<float>(rs, trans, nrhs, dB, ld, nullptr, ctx->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpy2DAsync(B, ldb * sizeof(float), dB, ld * sizeof(float), n * sizeof(float), nrhs,
+                            cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e == cudaSuccess) st = check_device_errors(ctx, {rs.scratch});
+  }
+  ctx_free(ctx, arena, bytes);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "sgetrs");
+  return st;
+}
+
+}  // namespace gblu

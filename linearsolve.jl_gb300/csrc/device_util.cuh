@@ -1,0 +1,77 @@
+// Device helpers shared by the kernels: bounded waits, coherent loads.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gblu_internal.h"
+
+namespace gblu {
+
+// Every spin-wait in this library gives up after this many nanoseconds of
+// %globaltimer and records an error word instead of hanging the GPU.
+constexpr unsigned long long kSpinTimeoutNs = 2000000000ull;  // 2 s
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ int ld_acquire_i32(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void st_release_i32(int* p, int v) {
+  asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ int ld_volatile_i32(const int* p) {
+  return *(volatile const int*)p;
+}
+
+// Grid-wide barrier for cooperative launches.  Arrival counter is
+// s->barrier (zeroed before the launch); `target` = (#barriers so far) * G.
+// Returns false (on every thread of the CTA) when the wait timed out or another
+// CTA already recorded an error; the caller then leaves the kernel.
+__device__ __forceinline__ bool grid_barrier(DevScratch* s, unsigned target) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(&s->barrier, 1u);
+    int res = 1;
+    unsigned long long t0 = 0;
+    for (unsigned it = 0;; ++it) {
+      if (ld_acquire_u32(&s->barrier) >= target) break;
+      if (ld_volatile_i32(&s->error) != 0) { res = 0; break; }
+      if ((it & 63u) == 0) {
+        unsigned long long now = global_ns();
+        if (t0 == 0) t0 = now;
+        else if (now - t0 > kSpinTimeoutNs) {
+          atomicCAS(&s->error, 0, (int)DEV_TIMEOUT_PANEL);
+          res = 0;
+          break;
+        }
+      }
+    }
+    __threadfence();
+    ok = res;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+template <typename T>
+__device__ __forceinline__ T ldcg(const T* p) { return __ldcg(p); }
+template <typename T>
+__device__ __forceinline__ void stcg(T* p, T v) { __stcg(p, v); }
+
+}  // namespace gblu

@@ -1,0 +1,112 @@
+// Internal declarations shared by the gblu translation units.
+//
+// Layout conventions (identical to LAPACK, which is what LinearSolve.jl's
+// LUFactorization hands to getrf/getrs, src/openblas.jl:131-154,247-278):
+//   * matrices are column-major with a leading dimension `ld` >= rows;
+//   * ipiv is int64, 1-based, the row-interchange sequence of getrf;
+//   * info is int64: 0 ok, k > 0 first exactly-zero pivot (1-based).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <mutex>
+#include <string>
+
+#include "../../include/gblu.h"
+
+namespace gblu {
+
+// ---------------------------------------------------------------------------
+// Device-side error words.  Every bounded wait in a kernel writes one of these
+// into the scratch error word instead of spinning forever.
+enum : int32_t {
+  DEV_OK = 0,
+  DEV_TIMEOUT_PANEL = 1,    // grid barrier in the panel kernel gave up
+  DEV_TIMEOUT_SOLVE = 2,    // a getrs block row waited too long for a predecessor
+  DEV_BAD_PIVOT_INDEX = 3,  // ipiv entry out of range (corrupt input)
+};
+
+// Scratch words used by the cooperative panel kernel and the wavefront solve.
+struct DevScratch {
+  unsigned int barrier;  // grid-barrier arrival counter (zeroed per launch)
+  int32_t error;         // DEV_* code, sticky
+  unsigned int ticket;   // wavefront block-row ticket (zeroed per launch)
+  int32_t pad;
+};
+
+// Panel-kernel exchange slots: per CTA one pivot candidate and its panel row.
+template <typename T>
+struct PanelSlots {
+  T* cand_val;       // [2][G]       |candidate|
+  int64_t* cand_row; // [2][G]       global row index of candidate (-1: none)
+  T* cand_rowvals;   // [2][G][W]    candidate's panel row
+  T* diag_rowvals;   // [2][W]       current diagonal row
+};
+
+// ---------------------------------------------------------------------------
+// Host-side helpers
+
+// Per-device launch facts, queried once.
+struct DeviceInfo {
+  int device = 0;
+  int num_sms = 0;
+  size_t smem_optin = 0;
+  int cc_major = 0, cc_minor = 0;
+};
+
+const DeviceInfo& device_info(int device);
+
+// ---------------------------------------------------------------------------
+// Kernel launch wrappers (implemented in getrf.cu / getrs.cu / refine.cu).
+// All are asynchronous on `stream` and return a cudaError_t from the launch.
+
+template <typename T>
+struct GetrfPlan {
+  int64_t m = 0, n = 0, lda = 0;
+  T* A = nullptr;            // device matrix, factored in place
+  int64_t* ipiv = nullptr;   // device, length min(m,n), 1-based
+  int64_t* info = nullptr;   // device scalar
+  int32_t* perm = nullptr;   // device, length m: (P A)[i] = A[perm[i]]
+  DevScratch* scratch = nullptr;
+  PanelSlots<T> slots{};
+  int panel_width = 32;      // leaf width of the recursion
+  int panel_ctas = 0;        // CTAs of the cooperative panel kernel (0: auto)
+  int trsm_base = 64;        // base size of the recursive TRSM
+};
+
+template <typename T>
+cudaError_t getrf_launch(const GetrfPlan<T>& p, cudaStream_t stream);
+
+// Per-device kernel attributes (shared-memory opt-in); once per device, outside capture.
+void getrf_configure(int device);
+cudaError_t perm_build_launch(const int64_t* ipiv, int64_t kmax, int64_t m, int32_t* perm,
+                              DevScratch* scr, cudaStream_t s);
+
+// Bytes of device scratch getrf needs for an m x n matrix (slots + scratch).
+size_t getrf_scratch_bytes(int64_t m, int64_t n, int elem_size, int panel_width,
+                           int device);
+template <typename T>
+void getrf_carve(GetrfPlan<T>& p, void* base, size_t bytes, int device);
+
+template <typename T>
+struct GetrsPlan {
+  int64_t n = 0, lda = 0;
+  const T* LU = nullptr;
+  const int32_t* perm = nullptr;
+  const int64_t* ipiv = nullptr;
+  DevScratch* scratch = nullptr;
+  int32_t* flags = nullptr;  // 2 * nblocks
+  T* work = nullptr;         // n * nrhs_chunk
+  int64_t work_cols = 0;
+};
+
+// In-place solve op(A) X = B for nrhs columns of B (ldb), trans 'N' or 'T'.
+template <typename T>
+cudaError_t getrs_launch(const GetrsPlan<T>& p, char trans, int64_t nrhs, T* B,
+                         int64_t ldb, uint32_t* epoch, cudaStream_t stream);
+
+size_t getrs_scratch_bytes(int64_t n, int elem_size, int64_t work_cols);
+template <typename T>
+void getrs_carve(GetrsPlan<T>& p, void* base, size_t bytes, int64_t work_cols);
+
+}  // namespace gblu

@@ -1,0 +1,571 @@
+// getrf on the device: recursive right-looking LU with partial pivoting.
+//
+// Structure (the LAPACK getrf structure the reference states in
+// src/blocked_lufact.jl:658-679, arranged recursively as in
+// RFLUFactorization's RecursiveFactorization, ext/LinearSolveRecursiveFactorizationExt.jl:15-42):
+//
+//   rec(c0, w):  if w <= panel width:  panel_kernel   (getf2 on the leaf,
+//                                       blocked_lufact.jl:93-122)
+//                                       laswp_kernel   (interchanges on every
+//                                       other column, :126-141)
+//                else  rec(c0, w1)
+//                      trsm  U12 := L11 \ A12       (:146-178)
+//                      gemm  A22 -= L21 * U12       (:186-656)
+//                      rec(c0 + w1, w - w1)
+//
+// Floating point: each element A[i,j] receives fma(-l_ik, u_kj, a_ij) for
+// k ascending, exactly as the reference's muladd loops, and the multipliers
+// are a_ik * (1 / u_kk).  Every kernel below keeps that per-element order
+// (C is loaded first, then updated k = 0, 1, ...), so the factors and ipiv
+// are bit-identical to the reference's blocked LU for any blocking.
+#include <algorithm>
+#include <cstdio>
+
+#include "device_util.cuh"
+#include "gblu_internal.h"
+
+namespace gblu {
+
+constexpr int kPanelThreads = 256;
+constexpr int kPanelMaxW = 32;
+constexpr int kPanelRowsTarget = 64;
+
+// ---------------------------------------------------------------------------
+// Pivot-candidate ordering: larger |a| wins; ties go to the smaller row;
+// row -1 means "no candidate" (|a| == 0 or NaN everywhere, blocked_lufact.jl:38-54).
+template <typename T>
+__device__ __forceinline__ bool cand_better(T v, int64_t g, T bv, int64_t bg) {
+  if (g < 0) return false;
+  if (bg < 0) return true;
+  return (v > bv) || (v == bv && g < bg);
+}
+
+template <typename T>
+__device__ __forceinline__ T absval(T x) { return x < T(0) ? -x : (x == T(0) ? T(0) : x); }
+template <>
+__device__ __forceinline__ double absval<double>(double x) { return fabs(x); }
+template <>
+__device__ __forceinline__ float absval<float>(float x) { return fabsf(x); }
+
+// ---------------------------------------------------------------------------
+// Cooperative panel kernel: getf2 on rows [c0, m) x columns [c0, c0+w).
+// Each CTA holds a contiguous slice of R rows of the panel in shared memory;
+// one grid barrier per column exchanges the pivot candidates.
+template <typename T>
+__global__ void __launch_bounds__(kPanelThreads)
+panel_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w,
+             int64_t* __restrict__ ipiv, int64_t* __restrict__ info_out,
+             DevScratch* __restrict__ scr, PanelSlots<T> slots, int R) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* tile = reinterpret_cast<T*>(smem_raw);  // column j at tile + j*R
+  __shared__ T pivrow[kPanelMaxW];
+  __shared__ T diagrow[kPanelMaxW];
+  __shared__ T red_v[kPanelThreads / 32];
+  __shared__ int64_t red_g[kPanelThreads / 32];
+  __shared__ int red_c[kPanelThreads / 32];
+  __shared__ int64_t s_best_g;
+  __shared__ int s_best_c;
+
+  const int G = gridDim.x;
+  const int cta = blockIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t base = c0 + (int64_t)cta * R;
+  const int nloc = (int)max((int64_t)0, min((int64_t)R, m - base));
+
+  for (int idx = tid; idx < w * R; idx += blockDim.x) {
+    int j = idx / R, i = idx - j * R;
+    tile[idx] = (i < nloc) ? A[(base + i) + (c0 + j) * lda] : T(0);
+  }
+  int64_t info_local = 0;
+  __syncthreads();
+
+  for (int k = 0; k < w; ++k) {
+    const int64_t d = c0 + k;
+    const int buf = k & 1;
+    const T* colk = tile + (size_t)k * R;
+
+    // 1. local candidate: first row of max |a| among rows >= d (NaN ignored)
+    T bv = T(0);
+    int64_t bg = -1;
+    for (int i = tid; i < nloc; i += blockDim.x) {
+      int64_t g = base + i;
+      T v = absval(colk[i]);
+      if (g >= d && v > bv) { bv = v; bg = g; }
+    }
+    for (int off = 16; off; off >>= 1) {
+      T ov = __shfl_down_sync(0xffffffffu, bv, off);
+      int64_t og = __shfl_down_sync(0xffffffffu, bg, off);
+      if (cand_better(ov, og, bv, bg)) { bv = ov; bg = og; }
+    }
+    if (lane == 0) { red_v[warp] = bv; red_g[warp] = bg; }
+    __syncthreads();
+    if (warp == 0) {
+      bv = lane < (kPanelThreads / 32) ? red_v[lane] : T(0);
+      bg = lane < (kPanelThreads / 32) ? red_g[lane] : -1;
+      for (int off = 16; off; off >>= 1) {
+        T ov = __shfl_down_sync(0xffffffffu, bv, off);
+        int64_t og = __shfl_down_sync(0xffffffffu, bg, off);
+        if (cand_better(ov, og, bv, bg)) { bv = ov; bg = og; }
+      }
+      if (lane == 0) {
+        stcg(&slots.cand_val[buf * G + cta], bv);
+        stcg(&slots.cand_row[buf * G + cta], bg);
+        s_best_g = bg;
+      }
+    }
+    __syncthreads();
+    // 2. publish the candidate's panel row and, if owned here, the diagonal row
+    if (tid < w) {
+      if (s_best_g >= 0)
+        stcg(&slots.cand_rowvals[((size_t)buf * G + cta) * kPanelMaxW + tid],
+             tile[(size_t)tid * R + (s_best_g - base)]);
+      if (d >= base && d < base + nloc)
+        stcg(&slots.diag_rowvals[buf * kPanelMaxW + tid], tile[(size_t)tid * R + (d - base)]);
+    }
+    if (!grid_barrier(scr, (unsigned)(k + 1) * (unsigned)G)) return;
+
+    // 3. global winner over the G candidates (same reduction on every CTA)
+    bv = T(0);
+    bg = -1;
+    int bc = -1;
+    for (int c = tid; c < G; c += blockDim.x) {
+      T v = ldcg(&slots.cand_val[buf * G + c]);
+      int64_t g = ldcg(&slots.cand_row[buf * G + c]);
+      if (cand_better(v, g, bv, bg)) { bv = v; bg = g; bc = c; }
+    }
+    for (int off = 16; off; off >>= 1) {
+      T ov = __shfl_down_sync(0xffffffffu, bv, off);
+      int64_t og = __shfl_down_sync(0xffffffffu, bg, off);
+      int oc = __shfl_down_sync(0xffffffffu, bc, off);
+      if (cand_better(ov, og, bv, bg)) { bv = ov; bg = og; bc = oc; }
+    }
+    if (lane == 0) { red_v[warp] = bv; red_g[warp] = bg; red_c[warp] = bc; }
+    __syncthreads();
+    if (warp == 0) {
+      bv = lane < (kPanelThreads / 32) ? red_v[lane] : T(0);
+      bg = lane < (kPanelThreads / 32) ? red_g[lane] : -1;
+      bc = lane < (kPanelThreads / 32) ? red_c[lane] : -1;
+      for (int off = 16; off; off >>= 1) {
+        T ov = __shfl_down_sync(0xffffffffu, bv, off);
+        int64_t og = __shfl_down_sync(0xffffffffu, bg, off);
+        int oc = __shfl_down_sync(0xffffffffu, bc, off);
+        if (cand_better(ov, og, bv, bg)) { bv = ov; bg = og; bc = oc; }
+      }
+      if (lane == 0) { s_best_g = bg; s_best_c = bc; }
+    }
+    __syncthreads();
+    const int64_t p = s_best_g < 0 ? d : s_best_g;  // kp = k when amax == 0
+    const int pc = s_best_c;
+    if (tid < w) {
+      T dv = ldcg(&slots.diag_rowvals[buf * kPanelMaxW + tid]);
+      diagrow[tid] = dv;
+      pivrow[tid] = (p == d) ? dv : ldcg(&slots.cand_rowvals[((size_t)buf * G + pc) * kPanelMaxW + tid]);
+    }
+    if (cta == 0 && tid == 0) ipiv[d] = p + 1;
+    __syncthreads();
+    const T piv = pivrow[k];
+
+    // 4. interchange (only when the pivot is nonzero), scale, rank-1 update
+    if (piv != T(0)) {
+      if (p != d) {
+        if (tid < w) {
+          if (d >= base && d < base + nloc) tile[(size_t)tid * R + (d - base)] = pivrow[tid];
+          if (p >= base && p < base + nloc) tile[(size_t)tid * R + (p - base)] = diagrow[tid];
+        }
+        __syncthreads();
+      }
+      const T inv = T(1) / piv;
+      for (int i = tid; i < nloc; i += blockDim.x)
+        if (base + i > d) tile[(size_t)k * R + i] *= inv;
+    } else if (info_local == 0) {
+      info_local = d + 1;
+    }
+    __syncthreads();
+    const int ncols = w - k - 1;
+    for (int idx = tid; idx < ncols * nloc; idx += blockDim.x) {
+      int jj = idx / nloc, i = idx - jj * nloc;
+      int j = k + 1 + jj;
+      if (base + i > d) {
+        T l = tile[(size_t)k * R + i];
+        tile[(size_t)j * R + i] = fma(-l, pivrow[j], tile[(size_t)j * R + i]);
+      }
+    }
+    __syncthreads();
+  }
+
+  for (int idx = tid; idx < w * R; idx += blockDim.x) {
+    int j = idx / R, i = idx - j * R;
+    if (i < nloc) A[(base + i) + (c0 + j) * lda] = tile[idx];
+  }
+  if (cta == 0 && tid == 0 && info_local != 0 && *info_out == 0) *info_out = info_local;
+}
+
+// ---------------------------------------------------------------------------
+// laswp for one leaf: interchanges ipiv[c0, c0+w) applied to every column
+// outside [c0, c0+w) (blocked_lufact.jl:126-141 applies them to [1, j0) and
+// (j1, n]).  Warp 0 of every CTA composes the w swaps into at most 2w moves
+// "row r receives old row src(r)"; then each warp moves one column at a time.
+template <typename T>
+__global__ void __launch_bounds__(256)
+laswp_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t ncols_total,
+                  int64_t c0, int w, const int64_t* __restrict__ ipiv,
+                  DevScratch* __restrict__ scr) {
+  __shared__ int64_t mv_dst[2 * kPanelMaxW];
+  __shared__ int64_t mv_src[2 * kPanelMaxW];
+  __shared__ int s_nmv;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (warp == 0) {
+    // entry 0 of lane k tracks row c0+k; entry 1 tracks target t_k when it lies
+    // below the leaf and no earlier lane already tracks it.
+    int64_t t = (lane < w) ? ipiv[c0 + lane] - 1 : -1;
+    if (lane < w && (t < c0 + lane || t >= m)) atomicCAS(&scr->error, 0, (int)DEV_BAD_PIVOT_INDEX);
+    int64_t row0 = (lane < w) ? c0 + lane : -1;
+    int64_t src0 = row0;
+    bool dup = false;
+    for (int j = 0; j < 32; ++j) {
+      int64_t tj = __shfl_sync(0xffffffffu, t, j);
+      if (j < lane && tj == t) dup = true;
+    }
+    int64_t row1 = (lane < w && t >= c0 + w && t < m && !dup) ? t : -1;
+    int64_t src1 = row1;
+    for (int k = 0; k < w; ++k) {
+      int64_t a = c0 + k;
+      int64_t b = __shfl_sync(0xffffffffu, t, k);
+      if (b == a || b < 0) continue;
+      unsigned ha0 = __ballot_sync(0xffffffffu, row0 == a), ha1 = __ballot_sync(0xffffffffu, row1 == a);
+      unsigned hb0 = __ballot_sync(0xffffffffu, row0 == b), hb1 = __ballot_sync(0xffffffffu, row1 == b);
+      if ((ha0 | ha1) == 0 || (hb0 | hb1) == 0) continue;  // corrupt ipiv: flagged above
+      int la = ha0 ? __ffs(ha0) - 1 : __ffs(ha1) - 1;
+      int lb = hb0 ? __ffs(hb0) - 1 : __ffs(hb1) - 1;
+      int64_t sa = ha0 ? __shfl_sync(0xffffffffu, src0, la) : __shfl_sync(0xffffffffu, src1, la);
+      int64_t sb = hb0 ? __shfl_sync(0xffffffffu, src0, lb) : __shfl_sync(0xffffffffu, src1, lb);
+      if (ha0) { if (lane == la) src0 = sb; } else { if (lane == la) src1 = sb; }
+      if (hb0) { if (lane == lb) src0 = sa; } else { if (lane == lb) src1 = sa; }
+    }
+    bool m0 = row0 >= 0 && src0 != row0, m1 = row1 >= 0 && src1 != row1;
+    unsigned b0 = __ballot_sync(0xffffffffu, m0), b1 = __ballot_sync(0xffffffffu, m1);
+    int n0 = __popc(b0);
+    if (m0) { int pos = __popc(b0 & ((1u << lane) - 1)); mv_dst[pos] = row0; mv_src[pos] = src0; }
+    if (m1) { int pos = n0 + __popc(b1 & ((1u << lane) - 1)); mv_dst[pos] = row1; mv_src[pos] = src1; }
+    if (lane == 0) s_nmv = n0 + __popc(b1);
+  }
+  __syncthreads();
+  const int nmv = s_nmv;
+  if (nmv == 0) return;
+  const int64_t nother = ncols_total - w;
+  const int warps = blockDim.x >> 5;
+  for (int64_t q = (int64_t)blockIdx.x * warps + warp; q < nother; q += (int64_t)gridDim.x * warps) {
+    const int64_t col = q < c0 ? q : q + w;
+    T* a = A + col * lda;
+    T v0 = T(0), v1 = T(0);
+    if (lane < nmv) v0 = a[mv_src[lane]];
+    if (lane + 32 < nmv) v1 = a[mv_src[lane + 32]];
+    __syncwarp();
+    if (lane < nmv) a[mv_dst[lane]] = v0;
+    if (lane + 32 < nmv) a[mv_dst[lane + 32]] = v1;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Unit-lower TRSM base case: B[0:k, cols] := L \ B with L = k x k (k <= 64)
+// held in shared memory; one thread per right-hand-side column, forward
+// substitution k ascending (blocked_lufact.jl:146-178 order).
+constexpr int kTrsmMax = 64;
+constexpr int kTrsmCols = 128;
+
+template <typename T>
+__global__ void __launch_bounds__(kTrsmCols)
+trsm_lunit_kernel(const T* __restrict__ L, int64_t ldl, int k, T* __restrict__ B,
+                  int64_t ldb, int64_t ncols) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* sL = reinterpret_cast<T*>(smem_raw);       // [k][k], column c at sL + c*k
+  T* sB = sL + kTrsmMax * kTrsmMax;             // [k][kTrsmCols], row i at sB + i*kTrsmCols
+  const int tid = threadIdx.x;
+  const int64_t col0 = (int64_t)blockIdx.x * kTrsmCols;
+  const int nc = (int)min((int64_t)kTrsmCols, ncols - col0);
+  for (int idx = tid; idx < k * k; idx += blockDim.x) {
+    int c = idx / k, r = idx - c * k;
+    sL[idx] = L[r + (int64_t)c * ldl];
+  }
+  for (int idx = tid; idx < k * nc; idx += blockDim.x) {
+    int c = idx / k, r = idx - c * k;
+    sB[r * kTrsmCols + c] = B[r + (col0 + c) * ldb];
+  }
+  __syncthreads();
+  if (tid < nc) {
+    for (int kk = 0; kk < k; ++kk) {
+      const T bk = sB[kk * kTrsmCols + tid];
+      const T* lc = sL + kk * k;
+      for (int i = kk + 1; i < k; ++i)
+        sB[i * kTrsmCols + tid] = fma(-lc[i], bk, sB[i * kTrsmCols + tid]);
+    }
+  }
+  __syncthreads();
+  for (int idx = tid; idx < k * nc; idx += blockDim.x) {
+    int c = idx / k, r = idx - c * k;
+    B[r + (col0 + c) * ldb] = sB[r * kTrsmCols + c];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// SIMT GEMM update C -= A * B (column-major), every C element updated by
+// fma(-a_k, b_k, c) for k ascending.  64 x 64 tile, 16-deep k slices,
+// 256 threads with a 4 x 4 register tile each.
+constexpr int kGBM = 64, kGBN = 64, kGBK = 16;
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+gemm_sub_kernel(int64_t M, int64_t N, int64_t K, const T* __restrict__ A, int64_t lda,
+                const T* __restrict__ B, int64_t ldb, T* __restrict__ C, int64_t ldc) {
+  __shared__ T sA[kGBK][kGBM];
+  __shared__ T sB[kGBK][kGBN + 1];
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const int64_t m0 = (int64_t)blockIdx.x * kGBM, n0 = (int64_t)blockIdx.y * kGBN;
+  T c[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      int64_t r = m0 + tx + 16 * i, cc = n0 + ty + 16 * j;
+      c[i][j] = (r < M && cc < N) ? C[r + cc * ldc] : T(0);
+    }
+  for (int64_t k0 = 0; k0 < K; k0 += kGBK) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      int idx = tid + 256 * q;
+      int kk = idx >> 6, i = idx & 63;
+      int64_t r = m0 + i, kc = k0 + kk;
+      sA[kk][i] = (r < M && kc < K) ? A[r + kc * lda] : T(0);
+      int kb = idx & 15, j = idx >> 4;
+      int64_t kr = k0 + kb, cc = n0 + j;
+      sB[kb][j] = (kr < K && cc < N) ? B[kr + cc * ldb] : T(0);
+    }
+    __syncthreads();
+    const int kmax = (int)min((int64_t)kGBK, K - k0);
+    for (int kk = 0; kk < kmax; ++kk) {
+      T a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = sA[kk][tx + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = sB[kk][ty + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) c[i][j] = fma(-a[i], b[j], c[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      int64_t r = m0 + tx + 16 * i, cc = n0 + ty + 16 * j;
+      if (r < M && cc < N) C[r + cc * ldc] = c[i][j];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// perm from ipiv: (P A)[i] = A[perm[i]].  One CTA; the interchanges are
+// inherently sequential, the rest is parallel.
+constexpr int kPermSmemMax = 48 * 1024;  // rows held in shared memory
+
+__global__ void __launch_bounds__(1024)
+perm_from_ipiv_kernel(const int64_t* __restrict__ ipiv, int64_t kmax, int64_t m,
+                      int32_t* __restrict__ perm, DevScratch* __restrict__ scr) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  int32_t* sp = reinterpret_cast<int32_t*>(smem_raw);
+  const bool in_smem = m <= kPermSmemMax;
+  int32_t* p = in_smem ? sp : perm;
+  for (int64_t i = threadIdx.x; i < m; i += blockDim.x) p[i] = (int32_t)i;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int64_t k = 0; k < kmax; ++k) {
+      int64_t t = ipiv[k] - 1;
+      if (t < k || t >= m) { atomicCAS(&scr->error, 0, (int)DEV_BAD_PIVOT_INDEX); break; }
+      int32_t x = p[k]; p[k] = p[t]; p[t] = x;
+    }
+  }
+  __syncthreads();
+  if (in_smem)
+    for (int64_t i = threadIdx.x; i < m; i += blockDim.x) perm[i] = sp[i];
+}
+
+// ---------------------------------------------------------------------------
+// Host driver
+
+size_t getrf_scratch_bytes(int64_t m, int64_t n, int elem_size, int panel_width,
+                           int device) {
+  const DeviceInfo& di = device_info(device);
+  size_t G = (size_t)di.num_sms * 8;  // upper bound on panel CTAs
+  size_t b = 256;                     // DevScratch, aligned
+  b += 2 * G * elem_size + 2 * G * sizeof(int64_t);
+  b += 2 * G * kPanelMaxW * elem_size + 2 * kPanelMaxW * elem_size;
+  return b + 1024;
+}
+
+template <typename T>
+void getrf_carve(GetrfPlan<T>& p, void* base, size_t bytes, int device) {
+  const DeviceInfo& di = device_info(device);
+  size_t G = (size_t)di.num_sms * 8;
+  char* c = reinterpret_cast<char*>(base);
+  auto take = [&](size_t n) { char* r = c; c += (n + 255) & ~size_t(255); return r; };
+  p.scratch = reinterpret_cast<DevScratch*>(take(sizeof(DevScratch)));
+  p.slots.cand_val = reinterpret_cast<T*>(take(2 * G * sizeof(T)));
+  p.slots.cand_row = reinterpret_cast<int64_t*>(take(2 * G * sizeof(int64_t)));
+  p.slots.cand_rowvals = reinterpret_cast<T*>(take(2 * G * kPanelMaxW * sizeof(T)));
+  p.slots.diag_rowvals = reinterpret_cast<T*>(take(2 * kPanelMaxW * sizeof(T)));
+  (void)bytes;
+}
+
+namespace {
+
+template <typename T>
+int panel_max_blocks(size_t smem, int /*device*/) {
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, panel_kernel<T>, kPanelThreads, smem) !=
+      cudaSuccess)
+    return 0;
+  return nb;
+}
+
+template <typename T>
+struct Driver {
+  const GetrfPlan<T>& p;
+  cudaStream_t s;
+  int device;
+  cudaError_t err = cudaSuccess;
+
+  T* at(int64_t r, int64_t c) const { return p.A + r + c * p.lda; }
+
+  void check(cudaError_t e) {
+    if (err == cudaSuccess && e != cudaSuccess) err = e;
+  }
+
+  void panel(int64_t c0, int w) {
+    const int64_t M = p.m - c0;
+    const DeviceInfo& di = device_info(device);
+    int G = p.panel_ctas > 0 ? p.panel_ctas
+                             : (int)std::max<int64_t>(1, (M + kPanelRowsTarget - 1) / kPanelRowsTarget);
+    int R = (int)((M + G - 1) / G);
+    size_t smem = (size_t)R * w * sizeof(T);
+    const size_t smem_cap = std::min<size_t>(di.smem_optin, 200 * 1024);
+    if (smem > smem_cap) {  // need more CTAs for this height
+      int64_t rmax = (int64_t)(smem_cap / ((size_t)w * sizeof(T)));
+      G = (int)((M + rmax - 1) / rmax);
+      R = (int)((M + G - 1) / G);
+      smem = (size_t)R * w * sizeof(T);
+    }
+    int per_sm = panel_max_blocks<T>(smem, device);
+    int gmax = std::min(per_sm * di.num_sms, di.num_sms * 8);
+    if (G > gmax) {
+      G = gmax;
+      R = (int)((M + G - 1) / G);
+      smem = (size_t)R * w * sizeof(T);
+      if (smem > smem_cap || G <= 0) { check(cudaErrorInvalidConfiguration); return; }
+    }
+    check(cudaMemsetAsync(&p.scratch->barrier, 0, sizeof(unsigned), s));
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(G);
+    cfg.blockDim = dim3(kPanelThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    check(cudaLaunchKernelEx(&cfg, panel_kernel<T>, p.A, p.lda, p.m, c0, w, p.ipiv, p.info,
+                             p.scratch, p.slots, R));
+    // interchanges on every other column
+    const int64_t nother = p.n - w;
+    if (nother > 0) {
+      int64_t warps_needed = nother;
+      int blocks = (int)std::min<int64_t>((warps_needed + 7) / 8, (int64_t)di.num_sms * 16);
+      laswp_leaf_kernel<T><<<blocks, 256, 0, s>>>(p.A, p.lda, p.m, p.n, c0, w, p.ipiv, p.scratch);
+      check(cudaGetLastError());
+    }
+  }
+
+  void gemm(int64_t M, int64_t N, int64_t K, const T* A, int64_t lda, const T* B, int64_t ldb,
+            T* C, int64_t ldc) {
+    if (M <= 0 || N <= 0 || K <= 0) return;
+    dim3 grid((unsigned)((M + kGBM - 1) / kGBM), (unsigned)((N + kGBN - 1) / kGBN));
+    gemm_sub_kernel<T><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc);
+    check(cudaGetLastError());
+  }
+
+  // B (k x ncols at (r0, bc0)) := L \ B, L unit lower at (r0, r0) of size k.
+  void trsm(int64_t r0, int64_t k, int64_t bc0, int64_t ncols) {
+    if (k <= 0 || ncols <= 0) return;
+    if (k <= p.trsm_base && k <= kTrsmMax) {
+      size_t smem = (size_t)(kTrsmMax * kTrsmMax + kTrsmMax * kTrsmCols) * sizeof(T);
+      unsigned blocks = (unsigned)((ncols + kTrsmCols - 1) / kTrsmCols);
+      trsm_lunit_kernel<T><<<blocks, kTrsmCols, smem, s>>>(at(r0, r0), p.lda, (int)k,
+                                                           at(r0, bc0), p.lda, ncols);
+      check(cudaGetLastError());
+      return;
+    }
+    int64_t k1 = k / 2;
+    trsm(r0, k1, bc0, ncols);
+    gemm(k - k1, ncols, k1, at(r0 + k1, r0), p.lda, at(r0, bc0), p.lda, at(r0 + k1, bc0), p.lda);
+    trsm(r0 + k1, k - k1, bc0, ncols);
+  }
+
+  void rec(int64_t c0, int64_t w) {
+    const int wb = p.panel_width;
+    if (w <= wb) {
+      panel(c0, (int)w);
+      return;
+    }
+    int64_t w1 = ((w / 2 + wb - 1) / wb) * wb;
+    if (w1 >= w) w1 = w - wb;
+    rec(c0, w1);
+    const int64_t c1 = c0 + w1, w2 = w - w1;
+    trsm(c0, w1, c1, w2);
+    gemm(p.m - c1, w2, w1, at(c1, c0), p.lda, at(c0, c1), p.lda, at(c1, c1), p.lda);
+    rec(c1, w2);
+  }
+};
+
+}  // namespace
+
+cudaError_t perm_build_launch(const int64_t* ipiv, int64_t kmax, int64_t m, int32_t* perm,
+                              DevScratch* scr, cudaStream_t s) {
+  size_t smem = m <= kPermSmemMax ? (size_t)m * sizeof(int32_t) : 0;
+  perm_from_ipiv_kernel<<<1, 1024, smem, s>>>(ipiv, kmax, m, perm, scr);
+  return cudaGetLastError();
+}
+
+void getrf_configure(int device) {
+  const DeviceInfo& di = device_info(device);
+  const int cap = (int)std::min<size_t>(di.smem_optin, 200 * 1024);
+  cudaFuncSetAttribute(panel_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  cudaFuncSetAttribute(panel_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  const int tsm = (kTrsmMax * kTrsmMax + kTrsmMax * kTrsmCols) * (int)sizeof(double);
+  cudaFuncSetAttribute(trsm_lunit_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsm);
+  cudaFuncSetAttribute(trsm_lunit_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsm / 2);
+  cudaFuncSetAttribute(perm_from_ipiv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       kPermSmemMax * (int)sizeof(int32_t));
+}
+
+template <typename T>
+cudaError_t getrf_launch(const GetrfPlan<T>& p, cudaStream_t stream) {
+  int device = 0;
+  cudaGetDevice(&device);
+  Driver<T> d{p, stream, device};
+  const int64_t minmn = std::min(p.m, p.n);
+  d.check(cudaMemsetAsync(p.info, 0, sizeof(int64_t), stream));
+  if (minmn > 0) {
+    d.rec(0, minmn);
+    if (p.n > p.m) d.trsm(0, p.m, p.m, p.n - p.m);  // wide: U12 := L11 \ A12
+    d.check(perm_build_launch(p.ipiv, minmn, p.m, p.perm, p.scratch, stream));
+  }
+  return d.err;
+}
+
+template cudaError_t getrf_launch<double>(const GetrfPlan<double>&, cudaStream_t);
+template cudaError_t getrf_launch<float>(const GetrfPlan<float>&, cudaStream_t);
+template void getrf_carve<double>(GetrfPlan<double>&, void*, size_t, int);
+template void getrf_carve<float>(GetrfPlan<float>&, void*, size_t, int);
+
+}  // namespace gblu

@@ -1,0 +1,89 @@
+// Host objects behind the opaque handles of gblu.h, and the helpers the
+// translation units share.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <initializer_list>
+#include <mutex>
+#include <string>
+
+#include "gblu_internal.h"
+#include "refine.h"
+
+struct gblu_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  uint64_t budget = 0;
+  uint64_t in_use = 0;
+  std::recursive_mutex mu;
+  std::string last_error;
+};
+
+struct gblu_factor {
+  int64_t m = 0, n = 0, ld = 0;
+  int32_t precision = GBLU_FP64;
+  bool factored = false;
+  int64_t info = 0;
+  uint64_t bytes = 0;
+  void* arena = nullptr;
+  // views into the arena
+  double* lu64 = nullptr;  // FP64 factors (FP64) or FP64 copy of A (mixed)
+  float* lu32 = nullptr;   // FP32 factors (mixed)
+  int64_t* ipiv = nullptr;
+  int32_t* perm = nullptr;
+  int64_t* info_dev = nullptr;
+  gblu::GetrfPlan<double> rf64;
+  gblu::GetrfPlan<float> rf32;
+  gblu::GetrsPlan<double> rs64;
+  gblu::GetrsPlan<float> rs32;
+  double* rhs = nullptr;  // device RHS staging, rhs_cols columns of length ld
+  int64_t rhs_cols = 0;
+  gblu::RefineWork refine;  // mixed-precision refinement buffers
+  // FP64 fallback factorization of a mixed factor (allocated on first use)
+  void* fb_arena = nullptr;
+  uint64_t fb_bytes = 0;
+  double* fb_lu = nullptr;
+  int64_t* fb_ipiv = nullptr;
+  int32_t* fb_perm = nullptr;
+  int64_t* fb_info = nullptr;
+  gblu::GetrfPlan<double> fb_rf;
+  gblu::GetrsPlan<double> fb_rs;
+  bool fb_valid = false;   // fallback factors hold the current A
+  bool use_fb = false;     // solves go straight to the fallback factors
+};
+
+namespace gblu {
+
+int32_t fail(gblu_ctx* ctx, int32_t code, const char* fmt, ...);
+int32_t cuda_fail(gblu_ctx* ctx, cudaError_t e, const char* what);
+int32_t ctx_alloc(gblu_ctx* ctx, size_t bytes, void** out);
+void ctx_free(gblu_ctx* ctx, void* p, size_t bytes);
+int32_t check_device_errors(gblu_ctx* ctx, std::initializer_list<DevScratch*> scr);
+int32_t upload_matrix(gblu_ctx* ctx, double* dst, int64_t ld_dst, const double* src,
+                      int64_t ld_src, int64_t rows, int64_t cols, int32_t loc);
+int32_t ensure_rhs(gblu_ctx* ctx, gblu_factor* f, int64_t cols);
+// FP64 factorization of the FP64 copy of A of a mixed factor (fb_* fields).
+int32_t factor_fp64_fallback(gblu_ctx* ctx, gblu_factor* f, int64_t* info_out);
+
+inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    cudaGetDevice(&prev);
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    cudaGetDevice(&cur);
+    if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+#define GBLU_CK(ctx, expr, what)                                   \
+  do {                                                             \
+    cudaError_t e_ = (expr);                                       \
+    if (e_ != cudaSuccess) return ::gblu::cuda_fail(ctx, e_, what); \
+  } while (0)
+
+}  // namespace gblu

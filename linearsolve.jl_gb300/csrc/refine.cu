@@ -1,0 +1,579 @@
+// Mixed-precision solve: FP32 factors + FP64 iterative refinement / GMRES-IR.
+//
+// No counterpart in the reference: LinearSolve.jl's *32Mixed* algorithms
+// (src/openblas.jl:461-543, ext/LinearSolveCUDAExt.jl:211-242) factor and
+// solve in FP32 and stop.  Here only the residual r = b - A x, the update
+// x += d and the convergence test run in FP64; the correction is solved with
+// the FP32 factors (IR) or by FP64 GMRES preconditioned by them (GMRES-IR,
+// Carson & Higham, SIAM J. Sci. Comput. 40(2), 2018).  Every reduction has a
+// fixed order, so a solve's result does not depend on what else runs on the
+// device.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "device_util.cuh"
+#include "gblu_internal.h"
+#include "objects.h"
+#include "refine.h"
+
+namespace gblu {
+
+constexpr int kRowsPerCta = 256;
+constexpr int kXTile = 128;  // columns of X staged in shared memory at a time
+constexpr int kMaxW = 8;
+
+// ---------------------------------------------------------------------------
+// kernels
+
+__global__ void convert_f64_f32_kernel(int64_t rows, int64_t cols, const double* __restrict__ A,
+                                       int64_t lda, float* __restrict__ B, int64_t ldb) {
+  const int64_t total = rows * cols;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    int64_t j = idx / rows, i = idx - j * rows;
+    B[i + j * ldb] = (float)A[i + j * lda];
+  }
+}
+
+__device__ __forceinline__ void atomic_max_nonneg(unsigned long long* p, double v) {
+  // non-negative doubles order like their bit patterns; NaN maps above +inf
+  unsigned long long bits = isnan(v) ? 0x7ff8000000000000ull : (unsigned long long)__double_as_longlong(v);
+  atomicMax(p, bits);
+}
+
+// P[s][q][i] = sum_{j in chunk s} op(A)[i, j] * X[j, q]
+//   'N': op(A)[i,j] = A[i + j*lda], A is rows x cols, i < rows
+//   'T': op(A)[i,j] = A[j + i*lda], i < cols (one warp per output row)
+// Chunks are fixed by (cols or rows) and kSplit, so the sum order is fixed.
+__global__ void __launch_bounds__(kRowsPerCta)
+gemv_n_partial_kernel(int64_t rows, int64_t cols, const double* __restrict__ A, int64_t lda,
+                      const double* __restrict__ X, int64_t ldx, int W, double* __restrict__ P,
+                      int absval) {
+  __shared__ double sx[kXTile][kMaxW];
+  const int s = blockIdx.y;
+  const int64_t cs = (cols + kSplit - 1) / kSplit;
+  const int64_t j0 = s * cs, j1 = min(cols, j0 + cs);
+  const int64_t i = (int64_t)blockIdx.x * kRowsPerCta + threadIdx.x;
+  double acc[kMaxW];
+#pragma unroll
+  for (int q = 0; q < kMaxW; ++q) acc[q] = 0.0;
+  for (int64_t jt = j0; jt < j1; jt += kXTile) {
+    const int nt = (int)min((int64_t)kXTile, j1 - jt);
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < nt * W; idx += blockDim.x) {
+      int jj = idx / W, q = idx - jj * W;
+      sx[jj][q] = X ? X[(jt + jj) + q * ldx] : 1.0;
+    }
+    __syncthreads();
+    if (i < rows) {
+      const double* a = A + i + jt * lda;
+#pragma unroll 4
+      for (int jj = 0; jj < nt; ++jj) {
+        double v = a[jj * lda];
+        if (absval) v = fabs(v);
+        for (int q = 0; q < W; ++q) acc[q] = fma(v, sx[jj][q], acc[q]);
+      }
+    }
+  }
+  if (i < rows)
+    for (int q = 0; q < W; ++q) P[((size_t)s * W + q) * rows + i] = acc[q];
+}
+
+__global__ void __launch_bounds__(256)
+gemv_t_partial_kernel(int64_t rows, int64_t cols, const double* __restrict__ A, int64_t lda,
+                      const double* __restrict__ X, int64_t ldx, int W, double* __restrict__ P) {
+  const int s = blockIdx.y;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t i = (int64_t)blockIdx.x * 8 + warp;  // output index = column of A
+  const int64_t cs = (rows + kSplit - 1) / kSplit;
+  const int64_t j0 = s * cs, j1 = min(rows, j0 + cs);
+  if (i >= cols) return;
+  double acc[kMaxW];
+#pragma unroll
+  for (int q = 0; q < kMaxW; ++q) acc[q] = 0.0;
+  const double* a = A + i * lda;
+  for (int64_t j = j0 + lane; j < j1; j += 32) {
+    double v = a[j];
+    for (int q = 0; q < W; ++q) acc[q] = fma(v, X[j + q * ldx], acc[q]);
+  }
+  for (int q = 0; q < W; ++q) {
+    double v = acc[q];
+    for (int off = 16; off; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if (lane == 0) P[((size_t)s * W + q) * cols + i] = v;
+  }
+}
+
+// out[i,q] = beta*C[i,q] + alpha*sum_s P[s][q][i]; optional column max of |out|.
+__global__ void gemv_reduce_kernel(int64_t len, int W, const double* __restrict__ P, double alpha,
+                                   const double* __restrict__ C, int64_t ldc, double beta,
+                                   double* __restrict__ out, int64_t ldo,
+                                   unsigned long long* __restrict__ colmax) {
+  __shared__ double red[256 / 32];
+  for (int q = 0; q < W; ++q) {
+    double mx = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len;
+         i += (int64_t)gridDim.x * blockDim.x) {
+      double sum = 0.0;
+      for (int s = 0; s < kSplit; ++s) sum += P[((size_t)s * W + q) * len + i];
+      double v = alpha * sum;
+      if (beta != 0.0) v = fma(beta, C[i + q * ldc], v);
+      out[i + q * ldo] = v;
+      double av = fabs(v);
+      mx = (av > mx || isnan(av)) ? av : mx;
+    }
+    if (colmax) {
+      for (int off = 16; off; off >>= 1) {
+        double o = __shfl_down_sync(0xffffffffu, mx, off);
+        mx = (o > mx || isnan(o)) ? o : mx;
+      }
+      if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        double m = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = (red[w] > m || isnan(red[w])) ? red[w] : m;
+        atomic_max_nonneg(colmax + q, m);
+      }
+      __syncthreads();
+    }
+  }
+}
+
+__global__ void colmax_kernel(int64_t n, int W, const double* __restrict__ X, int64_t ldx,
+                              unsigned long long* __restrict__ colmax) {
+  __shared__ double red[256 / 32];
+  for (int q = 0; q < W; ++q) {
+    double mx = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+      double av = fabs(X[i + q * ldx]);
+      mx = (av > mx || isnan(av)) ? av : mx;
+    }
+    for (int off = 16; off; off >>= 1) {
+      double o = __shfl_down_sync(0xffffffffu, mx, off);
+      mx = (o > mx || isnan(o)) ? o : mx;
+    }
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double m = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = (red[w] > m || isnan(red[w])) ? red[w] : m;
+      atomic_max_nonneg(colmax + q, m);
+    }
+    __syncthreads();
+  }
+}
+
+// D[:,q] = float(R[:,q] * inv_scale[q])
+__global__ void scale_to_f32_kernel(int64_t n, int W, const double* __restrict__ R, int64_t ldr,
+                                    const double* __restrict__ inv_scale, float* __restrict__ D,
+                                    int64_t ldd) {
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < n * W;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    int q = (int)(idx / n);
+    int64_t i = idx - (int64_t)q * n;
+    D[i + q * ldd] = (float)(R[i + q * ldr] * inv_scale[q]);
+  }
+}
+
+// X[:,q] = beta*X[:,q] + scale[q] * double(D[:,q])
+__global__ void update_from_f32_kernel(int64_t n, int W, double* __restrict__ X, int64_t ldx,
+                                       const float* __restrict__ D, int64_t ldd,
+                                       const double* __restrict__ scale, double beta) {
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < n * W;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    int q = (int)(idx / n);
+    int64_t i = idx - (int64_t)q * n;
+    double d = scale[q] * (double)D[i + q * ldd];
+    X[i + q * ldx] = beta == 0.0 ? d : fma(beta, X[i + q * ldx], d);
+  }
+}
+
+// Y = a*X + b*Y
+__global__ void axpby_kernel(int64_t n, double a, const double* __restrict__ X, double b,
+                             double* __restrict__ Y) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    Y[i] = b == 0.0 ? a * X[i] : fma(a, X[i], b * Y[i]);
+}
+
+// ---------------------------------------------------------------------------
+// buffers
+
+size_t refine_bytes(int64_t n, int64_t W) {
+  size_t b = 0;
+  b += 3 * align256((size_t)n * W * sizeof(double));       // x, r, b
+  b += align256((size_t)n * W * sizeof(float));            // d32
+  size_t pe = (size_t)kSplit * std::max<int64_t>(n, kGmresRestart + 1) * W;
+  b += align256(pe * sizeof(double));                      // partial
+  b += align256((size_t)n * (kGmresRestart + 1) * sizeof(double));  // V
+  b += align256((size_t)n * sizeof(double));               // w
+  b += align256((kGmresRestart + 1) * sizeof(double));     // h
+  b += align256(4 * W * sizeof(unsigned long long));       // colmax
+  b += align256((size_t)kDotBlocks * (kGmresRestart + 1) * sizeof(double));
+  b += align256(4 * sizeof(double) * W);                   // scales
+  b += align256(sizeof(double));                           // anorm
+  return b + 256;
+}
+
+void refine_carve(RefineWork& w, char* base, int64_t n, int64_t W) {
+  char* c = base;
+  auto take = [&](size_t b) { char* r = c; c += align256(b); return r; };
+  w.n = n;
+  w.W = W;
+  w.restart = kGmresRestart;
+  w.x = reinterpret_cast<double*>(take((size_t)n * W * sizeof(double)));
+  w.r = reinterpret_cast<double*>(take((size_t)n * W * sizeof(double)));
+  w.b = reinterpret_cast<double*>(take((size_t)n * W * sizeof(double)));
+  w.d32 = reinterpret_cast<float*>(take((size_t)n * W * sizeof(float)));
+  size_t pe = (size_t)kSplit * std::max<int64_t>(n, kGmresRestart + 1) * W;
+  w.partial = reinterpret_cast<double*>(take(pe * sizeof(double)));
+  w.V = reinterpret_cast<double*>(take((size_t)n * (kGmresRestart + 1) * sizeof(double)));
+  w.w = reinterpret_cast<double*>(take((size_t)n * sizeof(double)));
+  w.h = reinterpret_cast<double*>(take((kGmresRestart + 1) * sizeof(double)));
+  w.colmax = reinterpret_cast<unsigned long long*>(take(4 * W * sizeof(unsigned long long)));
+  w.dots = reinterpret_cast<double*>(take((size_t)kDotBlocks * (kGmresRestart + 1) * sizeof(double)));
+  w.anorm_dev = reinterpret_cast<double*>(take(4 * sizeof(double) * W));
+}
+
+namespace {
+
+unsigned grid_for(int64_t n, int threads = 256) {
+  int64_t b = (n + threads - 1) / threads;
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>(b, 152 * 8));
+}
+
+// out = beta*C + alpha*op(A) X   (op(A): len x k; A stored rows x cols)
+cudaError_t gemv(char op, int64_t rows, int64_t cols, const double* A, int64_t lda, const double* X,
+                 int64_t ldx, int W, double alpha, const double* C, int64_t ldc, double beta,
+                 double* out, int64_t ldo, double* P, unsigned long long* colmax, cudaStream_t s,
+                 bool absval = false) {
+  int64_t len;
+  if (op == 'N') {
+    len = rows;
+    dim3 grid((unsigned)((rows + kRowsPerCta - 1) / kRowsPerCta), kSplit);
+    gemv_n_partial_kernel<<<grid, kRowsPerCta, 0, s>>>(rows, cols, A, lda, X, ldx, W, P, absval ? 1 : 0);
+  } else {
+    len = cols;
+    dim3 grid((unsigned)((cols + 7) / 8), kSplit);
+    gemv_t_partial_kernel<<<grid, 256, 0, s>>>(rows, cols, A, lda, X, ldx, W, P);
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  gemv_reduce_kernel<<<grid_for(len), 256, 0, s>>>(len, W, P, alpha, C, ldc, beta, out, ldo, colmax);
+  return cudaGetLastError();
+}
+
+double bits_to_double(unsigned long long b) {
+  double d;
+  std::memcpy(&d, &b, sizeof(d));
+  return d;
+}
+
+}  // namespace
+
+cudaError_t refine_prepare(RefineWork& w, int64_t n, const double* A, int64_t lda, float* A32,
+                           int64_t ld32, cudaStream_t s) {
+  if (n == 0) { w.anorm = 0; return cudaSuccess; }
+  convert_f64_f32_kernel<<<grid_for(n * n), 256, 0, s>>>(n, n, A, lda, A32, ld32);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  // ||A||_inf = max_i sum_j |A[i,j]|
+  e = cudaMemsetAsync(w.colmax, 0, sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return e;
+  e = gemv('N', n, n, A, lda, nullptr, 1, 1, 1.0, nullptr, 1, 0.0, w.w, n, w.partial, w.colmax, s, true);
+  if (e != cudaSuccess) return e;
+  unsigned long long bits = 0;
+  e = cudaMemcpyAsync(&bits, w.colmax, sizeof(bits), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  w.anorm = bits_to_double(bits);
+  return e;
+}
+
+gblu_refine_opts refine_default_opts() {
+  gblu_refine_opts o;
+  o.mode = GBLU_REFINE_IR;
+  o.max_iter = 30;
+  o.tol = 0.0;
+  o.fallback = 1;
+  o.gmres_restart = kGmresRestart;
+  o.gmres_tol = 1e-10;
+  return o;
+}
+
+namespace {
+
+struct Solver {
+  gblu_ctx* ctx;
+  gblu_factor* f;
+  RefineWork& w;
+  char trans;
+  cudaStream_t s;
+  int64_t n;
+
+  // x (len n, W cols) <- M^{-1} v using the FP32 factors with a per-column
+  // power-of-two scale so the FP32 right-hand side is O(1).
+  int32_t precond(const double* v, int64_t ldv, double* out, int64_t ldo, int W) {
+    std::vector<unsigned long long> bits(W);
+    GBLU_CK(ctx, cudaMemsetAsync(w.colmax + 3 * w.W, 0, W * sizeof(unsigned long long), s), "memset");
+    colmax_kernel<<<grid_for(n), 256, 0, s>>>(n, W, v, ldv, w.colmax + 3 * w.W);
+    GBLU_CK(ctx, cudaGetLastError(), "colmax");
+    GBLU_CK(ctx, cudaMemcpyAsync(bits.data(), w.colmax + 3 * w.W, W * sizeof(unsigned long long),
+                                 cudaMemcpyDeviceToHost, s), "colmax readback");
+    GBLU_CK(ctx, cudaStreamSynchronize(s), "precond");
+    double sc[2 * kMaxW];
+    for (int q = 0; q < W; ++q) {
+      double m = bits_to_double(bits[q]);
+      double scale = 1.0;
+      if (m > 0 && std::isfinite(m)) scale = std::ldexp(1.0, std::ilogb(m));
+      sc[q] = 1.0 / scale;
+      sc[kMaxW + q] = scale;
+    }
+    double* dsc = w.anorm_dev;  // 4*W doubles of scale storage
+    GBLU_CK(ctx, cudaMemcpyAsync(dsc, sc, 2 * kMaxW * sizeof(double), cudaMemcpyHostToDevice, s),
+            "scales");
+    scale_to_f32_kernel<<<grid_for(n * W), 256, 0, s>>>(n, W, v, ldv, dsc, w.d32, n);
+    GBLU_CK(ctx, cudaGetLastError(), "scale");
+    GBLU_CK(ctx, getrs_launch<float>(f->rs32, trans, W, w.d32, n, nullptr, s), "FP32 getrs");
+    update_from_f32_kernel<<<grid_for(n * W), 256, 0, s>>>(n, W, out, ldo, w.d32, n, dsc + kMaxW, 0.0);
+    GBLU_CK(ctx, cudaGetLastError(), "update");
+    return GBLU_OK;
+  }
+
+  // r = b - op(A) x for W columns; returns |r|_inf and |x|_inf per column.
+  int32_t residual(int W, double* rnorm, double* xnorm) {
+    GBLU_CK(ctx, cudaMemsetAsync(w.colmax, 0, 2 * w.W * sizeof(unsigned long long), s), "memset");
+    GBLU_CK(ctx, gemv(trans == 'N' ? 'N' : 'T', n, n, f->lu64, f->ld, w.x, n, W, -1.0, w.b, n, 1.0,
+                      w.r, n, w.partial, w.colmax, s),
+            "residual");
+    colmax_kernel<<<grid_for(n), 256, 0, s>>>(n, W, w.x, n, w.colmax + w.W);
+    GBLU_CK(ctx, cudaGetLastError(), "colmax");
+    std::vector<unsigned long long> bits(2 * w.W);
+    GBLU_CK(ctx, cudaMemcpyAsync(bits.data(), w.colmax, 2 * w.W * sizeof(unsigned long long),
+                                 cudaMemcpyDeviceToHost, s), "readback");
+    GBLU_CK(ctx, cudaStreamSynchronize(s), "residual");
+    for (int q = 0; q < W; ++q) {
+      rnorm[q] = bits_to_double(bits[q]);
+      xnorm[q] = bits_to_double(bits[w.W + q]);
+    }
+    return GBLU_OK;
+  }
+
+  // One GMRES(m) solve of op(A) d = r[:,q] left-preconditioned by the FP32 LU;
+  // adds d into x[:,q].  Returns the iteration count in *its.
+  int32_t gmres(int q, int restart, double rtol, int* its) {
+    const double* rq = w.r + (size_t)q * n;
+    double* V = w.V;
+    int32_t st = precond(rq, n, V, n, 1);
+    if (st) return st;
+    double beta = 0;
+    {
+      GBLU_CK(ctx, gemv('T', n, 1, V, n, V, n, 1, 1.0, nullptr, 1, 0.0, w.h, 1, w.partial, nullptr, s),
+              "norm");
+      GBLU_CK(ctx, cudaMemcpyAsync(&beta, w.h, sizeof(double), cudaMemcpyDeviceToHost, s), "norm");
+      GBLU_CK(ctx, cudaStreamSynchronize(s), "norm");
+      beta = std::sqrt(beta);
+    }
+    *its = 0;
+    if (!(beta > 0) || !std::isfinite(beta)) return GBLU_OK;
+    axpby_kernel<<<grid_for(n), 256, 0, s>>>(n, 1.0 / beta, V, 0.0, V);
+    const int m = std::max(1, std::min(restart, (int)kGmresRestart));
+    std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m), sn(m), g(m + 1, 0.0);
+    g[0] = beta;
+    int k = 0;
+    std::vector<double> h(m + 1), h2(m + 1);
+    for (int j = 0; j < m; ++j) {
+      double* vj = V + (size_t)j * n;
+      double* z = V + (size_t)(j + 1) * n;
+      // w = op(A) v_j ; z = M^{-1} w
+      GBLU_CK(ctx, gemv(trans == 'N' ? 'N' : 'T', n, n, f->lu64, f->ld, vj, n, 1, 1.0, nullptr, 1, 0.0,
+                        w.w, n, w.partial, nullptr, s),
+              "matvec");
+      st = precond(w.w, n, z, n, 1);
+      if (st) return st;
+      // classical Gram-Schmidt, twice
+      for (int pass = 0; pass < 2; ++pass) {
+        GBLU_CK(ctx, gemv('T', n, j + 1, V, n, z, n, 1, 1.0, nullptr, 1, 0.0, w.h, 1, w.partial,
+                          nullptr, s),
+                "project");
+        GBLU_CK(ctx, gemv('N', n, j + 1, V, n, w.h, j + 1, 1, -1.0, z, n, 1.0, z, n, w.partial,
+                          nullptr, s),
+                "orthogonalise");
+        GBLU_CK(ctx, cudaMemcpyAsync(pass == 0 ? h.data() : h2.data(), w.h, (j + 1) * sizeof(double),
+                                     cudaMemcpyDeviceToHost, s),
+                "readback");
+      }
+      double nz2 = 0;
+      GBLU_CK(ctx, gemv('T', n, 1, z, n, z, n, 1, 1.0, nullptr, 1, 0.0, w.h, 1, w.partial, nullptr, s),
+              "norm");
+      GBLU_CK(ctx, cudaMemcpyAsync(&nz2, w.h, sizeof(double), cudaMemcpyDeviceToHost, s), "norm");
+      GBLU_CK(ctx, cudaStreamSynchronize(s), "gmres step");
+      double hn = std::sqrt(nz2);
+      for (int i = 0; i <= j; ++i) H[(size_t)j * (m + 1) + i] = h[i] + h2[i];
+      H[(size_t)j * (m + 1) + j + 1] = hn;
+      for (int i = 0; i < j; ++i) {  // previous rotations
+        double a = H[(size_t)j * (m + 1) + i], b = H[(size_t)j * (m + 1) + i + 1];
+        H[(size_t)j * (m + 1) + i] = cs[i] * a + sn[i] * b;
+        H[(size_t)j * (m + 1) + i + 1] = -sn[i] * a + cs[i] * b;
+      }
+      double a = H[(size_t)j * (m + 1) + j], b = H[(size_t)j * (m + 1) + j + 1];
+      double rr = std::hypot(a, b);
+      cs[j] = rr > 0 ? a / rr : 1.0;
+      sn[j] = rr > 0 ? b / rr : 0.0;
+      H[(size_t)j * (m + 1) + j] = rr;
+      H[(size_t)j * (m + 1) + j + 1] = 0.0;
+      g[j + 1] = -sn[j] * g[j];
+      g[j] = cs[j] * g[j];
+      k = j + 1;
+      if (hn > 0 && std::isfinite(hn))
+        axpby_kernel<<<grid_for(n), 256, 0, s>>>(n, 1.0 / hn, z, 0.0, z);
+      if (std::fabs(g[j + 1]) <= rtol * beta || !(hn > 0)) break;
+    }
+    *its = k;
+    // y = H(1:k,1:k) \ g(1:k); d = V(:,1:k) y; x[:,q] += d
+    std::vector<double> y(k);
+    for (int i = k - 1; i >= 0; --i) {
+      double acc = g[i];
+      for (int jj = i + 1; jj < k; ++jj) acc -= H[(size_t)jj * (m + 1) + i] * y[jj];
+      double d = H[(size_t)i * (m + 1) + i];
+      y[i] = d != 0 ? acc / d : 0.0;
+    }
+    GBLU_CK(ctx, cudaMemcpyAsync(w.h, y.data(), k * sizeof(double), cudaMemcpyHostToDevice, s), "y");
+    double* xq = w.x + (size_t)q * n;
+    GBLU_CK(ctx, gemv('N', n, k, V, n, w.h, k, 1, 1.0, xq, n, 1.0, xq, n, w.partial, nullptr, s),
+            "update");
+    return GBLU_OK;
+  }
+};
+
+}  // namespace
+
+int32_t refine_solve(gblu_ctx* ctx, gblu_factor* f, char trans, int64_t nrhs, double* B, int64_t ldb,
+                     int32_t b_loc, const gblu_refine_opts* opts_in, gblu_refine_stats* stats) {
+  gblu_refine_opts o = opts_in ? *opts_in : refine_default_opts();
+  const int64_t n = f->n;
+  RefineWork& w = f->refine;
+  cudaStream_t s = ctx->stream;
+  trans = (trans == 'n') ? 'N' : (trans == 't' || trans == 'c' || trans == 'C') ? 'T' : trans;
+  const double tol = o.tol > 0 ? o.tol : (double)std::max<int64_t>(n, 1) * 2.220446049250313e-16;
+  const int W = (int)w.W;
+  gblu_refine_stats st_acc{};
+  st_acc.converged = 1;
+  Solver S{ctx, f, w, trans, s, n};
+  if (stats) *stats = gblu_refine_stats{};
+  for (int64_t c0 = 0; c0 < nrhs; c0 += W) {
+    const int nc = (int)std::min<int64_t>(W, nrhs - c0);
+    double* Bc = B + c0 * ldb;
+    cudaMemcpyKind k_in = b_loc == GBLU_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    cudaMemcpyKind k_out = b_loc == GBLU_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    GBLU_CK(ctx, cudaMemcpy2DAsync(w.b, n * sizeof(double), Bc, ldb * sizeof(double),
+                                   n * sizeof(double), nc, k_in, s),
+            "copying B");
+    bool done = false, fell_back = false;
+    double berr_final = 0;
+    int iters = 0;
+    if (!f->use_fb) {
+      // x0 = 0, r0 = b
+      GBLU_CK(ctx, cudaMemsetAsync(w.x, 0, (size_t)n * nc * sizeof(double), s), "x0");
+      std::vector<double> rn(nc), xn(nc), bn(nc), prev(nc, INFINITY);
+      std::vector<int> slow(nc, 0);
+      for (int it = 0; it <= o.max_iter; ++it) {
+        int32_t e = S.residual(nc, rn.data(), xn.data());
+        if (e) return e;
+        if (it == 0) bn = rn;  // x = 0: r = b
+        bool all_ok = true, stalled = false;
+        double worst = 0;
+        for (int q = 0; q < nc; ++q) {
+          double den = w.anorm * xn[q] + bn[q];
+          double be = den > 0 ? rn[q] / den : (rn[q] == 0 ? 0.0 : INFINITY);
+          if (!std::isfinite(be) && it > 0) stalled = true;
+          worst = std::max(worst, std::isnan(be) ? INFINITY : be);
+          if (!(be <= tol)) {
+            all_ok = false;
+            if (it >= 2 && be > 0.9 * prev[q]) {
+              if (++slow[q] >= 2) stalled = true;
+            } else {
+              slow[q] = 0;
+            }
+          }
+          prev[q] = be;
+        }
+        berr_final = worst;
+        iters = it;
+        if (all_ok) { done = true; break; }
+        if (stalled || it == o.max_iter) break;
+        if (o.mode == GBLU_REFINE_GMRES) {
+          for (int q = 0; q < nc; ++q) {
+            int its = 0;
+            e = S.gmres(q, o.gmres_restart, o.gmres_tol, &its);
+            if (e) return e;
+            st_acc.inner_iterations += its;
+          }
+        } else {
+          e = S.precond(w.r, n, w.r, n, nc);  // d = M^{-1} r (in place), scaled
+          if (e) return e;
+          for (int q = 0; q < nc; ++q)
+            axpby_kernel<<<grid_for(n), 256, 0, s>>>(n, 1.0, w.r + (size_t)q * n, 1.0, w.x + (size_t)q * n);
+          GBLU_CK(ctx, cudaGetLastError(), "update");
+        }
+      }
+    }
+    if (done) {
+      GBLU_CK(ctx, cudaMemcpy2DAsync(Bc, ldb * sizeof(double), w.x, n * sizeof(double),
+                                     n * sizeof(double), nc, k_out, s),
+              "copying X");
+    } else {
+      if (!o.fallback && !f->use_fb) return fail(ctx, GBLU_ESTALL, "refinement stalled at backward error %.3e", berr_final);
+      if (!f->fb_valid) {
+        int64_t info64 = 0;
+        int32_t e = factor_fp64_fallback(ctx, f, &info64);
+        if (e) return e;
+        if (info64 != 0) return fail(ctx, GBLU_EINVAL, "matrix is singular in FP64 (info = %lld)", (long long)info64);
+      }
+      // plain FP64 solve on the FP64 factors, x <- b
+      GBLU_CK(ctx, cudaMemcpyAsync(w.x, w.b, (size_t)n * nc * sizeof(double), cudaMemcpyDeviceToDevice, s),
+              "copy b");
+      GBLU_CK(ctx, getrs_launch<double>(f->fb_rs, trans, nc, w.x, n, nullptr, s), "FP64 getrs");
+      std::vector<double> rn(nc), xn(nc), bn(nc);
+      int32_t e = S.residual(nc, rn.data(), xn.data());
+      if (e) return e;
+      // ||b||: one more pass over b
+      GBLU_CK(ctx, cudaMemsetAsync(w.colmax + 2 * w.W, 0, nc * sizeof(unsigned long long), s), "memset");
+      colmax_kernel<<<grid_for(n), 256, 0, s>>>(n, nc, w.b, n, w.colmax + 2 * w.W);
+      std::vector<unsigned long long> bits(nc);
+      GBLU_CK(ctx, cudaMemcpyAsync(bits.data(), w.colmax + 2 * w.W, nc * sizeof(unsigned long long),
+                                   cudaMemcpyDeviceToHost, s), "readback");
+      GBLU_CK(ctx, cudaStreamSynchronize(s), "fallback");
+      berr_final = 0;
+      for (int q = 0; q < nc; ++q) {
+        double den = w.anorm * xn[q] + bits_to_double(bits[q]);
+        berr_final = std::max(berr_final, den > 0 ? rn[q] / den : 0.0);
+      }
+      fell_back = true;
+      GBLU_CK(ctx, cudaMemcpy2DAsync(Bc, ldb * sizeof(double), w.x, n * sizeof(double),
+                                     n * sizeof(double), nc, k_out, s),
+              "copying X");
+    }
+    GBLU_CK(ctx, cudaStreamSynchronize(s), "refined solve");
+    int32_t e = check_device_errors(ctx, {f->rs32.scratch, f->fb_rs.scratch});
+    if (e) return e;
+    st_acc.iterations = std::max(st_acc.iterations, iters);
+    st_acc.fell_back |= fell_back ? 1 : 0;
+    if (!done) st_acc.converged = fell_back ? st_acc.converged : 0;
+    st_acc.backward_error = std::max(st_acc.backward_error, berr_final);
+  }
+  if (stats) *stats = st_acc;
+  return GBLU_OK;
+}
+
+}  // namespace gblu
+
+extern "C" {
+
+int32_t gblu_refine_opts_default(gblu_refine_opts* opts) {
+  if (!opts) return GBLU_EINVAL;
+  *opts = gblu::refine_default_opts();
+  return GBLU_OK;
+}
+
+}  // extern "C"

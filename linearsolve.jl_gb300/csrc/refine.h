@@ -1,0 +1,49 @@
+// Mixed-precision refinement: FP32 factors, FP64 residuals and updates.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gblu_internal.h"
+
+struct gblu_ctx;
+struct gblu_factor;
+
+namespace gblu {
+
+// Device buffers of the refinement loop for an n x n factor and up to W
+// right-hand sides at a time, plus the GMRES basis.
+struct RefineWork {
+  int64_t n = 0, W = 0, restart = 0;
+  double* x = nullptr;      // n x W   solution iterate
+  double* r = nullptr;      // n x W   residual / GMRES work vector
+  double* b = nullptr;      // n x W   right-hand sides
+  float* d32 = nullptr;     // n x W   low-precision correction
+  double* partial = nullptr;  // kSplit x n x W  deterministic partial sums
+  double* V = nullptr;      // n x (restart + 1)   GMRES basis
+  double* w = nullptr;      // n        GMRES work vector
+  double* h = nullptr;      // restart + 1   projections
+  unsigned long long* colmax = nullptr;  // 4 x W   |.|_inf per column (bit patterns)
+  double* dots = nullptr;   // kDotBlocks x (restart + 1)
+  double anorm = 0;         // ||A||_inf of the FP64 matrix (host copy)
+  double* anorm_dev = nullptr;
+};
+
+constexpr int kSplit = 16;       // column chunks of the residual GEMV
+constexpr int kDotBlocks = 64;   // blocks of the deterministic dot products
+constexpr int kGmresRestart = 30;
+
+size_t refine_bytes(int64_t n, int64_t W);
+void refine_carve(RefineWork& w, char* base, int64_t n, int64_t W);
+
+// FP64 A (ld) -> FP32 A32 (ld32) and ||A||_inf, before the FP32 getrf.
+cudaError_t refine_prepare(RefineWork& w, int64_t n, const double* A, int64_t lda, float* A32,
+                           int64_t ld32, cudaStream_t s);
+
+gblu_refine_opts refine_default_opts();
+
+// The refined solve behind gblu_getrs / gblu_solve_refined for a factor.
+int32_t refine_solve(gblu_ctx* ctx, gblu_factor* f, char trans, int64_t nrhs, double* B,
+                     int64_t ldb, int32_t b_loc, const gblu_refine_opts* opts,
+                     gblu_refine_stats* stats);
+
+}  // namespace gblu

@@ -1,0 +1,300 @@
+"""LinearSolve.jl's problem / cache / solve interface over the GB300 library.
+
+This mirrors, name for name, the part of LinearSolve.jl's public interface
+that the dense LU path sits behind, so that a caller (and the tests) read
+like the reference:
+
+    prob  = LinearProblem(A, b)                     # SciMLBase.LinearProblem
+    cache = init(prob, GB300LUFactorization())      # src/common.jl:700-931
+    sol   = solve_bang(cache)                       # solve!(cache), common.jl:1012-1017
+    cache.b = b2;  solve_bang(cache)                # getrs only   (common.jl:351-353)
+    cache.A = A2;  solve_bang(cache)                # refactor     (common.jl:330-348)
+    sol   = solve(prob, alg)                        # common.jl:988-993
+
+The algorithm types follow the plugin contract of
+docs/src/advanced/algorithm_interface.md: refactor only when ``isfresh``
+and then clear it; write into ``cache.u``; a failed factorization is a
+``ReturnCode.Failure`` retcode (not an exception) and leaves ``isfresh``
+set (src/factorization.jl:16-28, :716-722).
+"""
+from __future__ import annotations
+
+import enum
+import math
+from dataclasses import dataclass, field
+from typing import Any, Optional
+
+import numpy as np
+
+from ._cuda import DeviceMatrix
+from .device import default_context
+
+
+class ReturnCode(enum.Enum):
+    """The SciMLBase retcodes the LU path produces."""
+    Default = "Default"
+    Success = "Success"
+    Failure = "Failure"
+    APosterioriSafetyFailure = "APosterioriSafetyFailure"
+
+
+def successful_retcode(rc: "ReturnCode | LinearSolution") -> bool:
+    if isinstance(rc, LinearSolution):
+        rc = rc.retcode
+    return rc == ReturnCode.Success
+
+
+@dataclass
+class LinearAliasSpecifier:
+    """Aliasing of init (src/common.jl:818-842): dense defaults are no alias."""
+    alias_A: Optional[bool] = None
+    alias_b: Optional[bool] = None
+
+
+@dataclass
+class LinearProblem:
+    """SciMLBase.LinearProblem(A, b; u0, p)."""
+    A: Any
+    b: Any
+    u0: Any = None
+    p: Any = None
+
+
+@dataclass
+class LinearSolution:
+    """SciMLBase.LinearSolution fields used by the LU path."""
+    u: Any
+    resid: Any
+    alg: Any
+    retcode: ReturnCode
+    iters: int = 0
+    cache: Any = None
+    stats: dict = field(default_factory=dict)
+
+
+# ---------------------------------------------------------------------------
+# Algorithms (SciMLLinearSolveAlgorithm subtypes in the Julia binding)
+
+class AbstractDenseFactorization:
+    """src/LinearSolve.jl:211.  needs_concrete_A = true; needs_square_A = true."""
+
+    needs_concrete_A = True
+    needs_square_A = True
+    default_alias_A = False
+    default_alias_b = False
+    precision = "fp64"
+    residualsafety = False
+
+    def factor_precision(self) -> str:
+        return self.precision
+
+
+class GB300LUFactorization(AbstractDenseFactorization):
+    """Plain FP64 partial-pivot LU on the GB300: getrf + getrs in FP64.
+
+    The drop-in for LUFactorization (src/factorization.jl:306-311) /
+    CudaOffloadLUFactorization (src/extension_algs.jl:344-356).  Factors and
+    ipiv are bit-identical to the reference's blocked LU
+    (src/blocked_lufact.jl), and the solve to its back-solve
+    (src/factorization.jl:433-457)."""
+
+    def __init__(self, residualsafety: bool = False, device: int = 0):
+        self.residualsafety = bool(residualsafety)
+        self.device = int(device)
+
+    def __repr__(self):
+        return f"GB300LUFactorization(residualsafety={self.residualsafety})"
+
+
+class GB300MixedLUFactorization(AbstractDenseFactorization):
+    """Mixed precision: FP32 LU, FP64 accuracy by refinement.
+
+    factor:  "fp32"           (the FP32 factors on the device)
+    refine:  "ir" | "gmres_ir" (classic IR, or GMRES-IR preconditioned by the LU)
+    maxiters, tol: outer refinement limits (tol None: n * eps64)
+    fallback: FP64 LU when refinement stalls.
+
+    Unlike the reference's CUDAOffload32MixedLUFactorization
+    (ext/LinearSolveCUDAExt.jl:211-242) the result is FP64-accurate."""
+
+    def __init__(self, factor: str = "fp32", refine: str = "ir", maxiters: int = 30,
+                 tol: Optional[float] = None, fallback: bool = True, gmres_restart: int = 30,
+                 gmres_tol: float = 1e-10, device: int = 0):
+        if factor != "fp32":
+            raise ValueError(f"unsupported factor precision {factor!r}")
+        if refine not in ("ir", "gmres_ir"):
+            raise ValueError("refine must be 'ir' or 'gmres_ir'")
+        self.precision = factor
+        self.refine = refine
+        self.maxiters = int(maxiters)
+        self.tol = tol
+        self.fallback = bool(fallback)
+        self.gmres_restart = int(gmres_restart)
+        self.gmres_tol = float(gmres_tol)
+        self.device = int(device)
+
+    def __repr__(self):
+        return f"GB300MixedLUFactorization(factor={self.precision!r}, refine={self.refine!r})"
+
+
+# ---------------------------------------------------------------------------
+# Cache
+
+def _shape(x):
+    return (x.rows, x.cols) if isinstance(x, DeviceMatrix) else np.shape(x)
+
+
+class LinearCache:
+    """src/common.jl:281-306 with the setproperty! freshness logic of :313-360."""
+
+    _tracked = ("A", "b")
+
+    def __init__(self, A, b, u, alg, abstol, reltol, verbose, alias_A, alias_b, context):
+        object.__setattr__(self, "isfresh", True)
+        object.__setattr__(self, "_ctx", context)
+        object.__setattr__(self, "cacheval", None)
+        object.__setattr__(self, "alg", alg)
+        object.__setattr__(self, "abstol", abstol)
+        object.__setattr__(self, "reltol", reltol)
+        object.__setattr__(self, "verbose", verbose)
+        object.__setattr__(self, "alias_A", alias_A)
+        object.__setattr__(self, "alias_b", alias_b)
+        object.__setattr__(self, "A", A)
+        object.__setattr__(self, "b", b)
+        object.__setattr__(self, "u", u)
+        object.__setattr__(self, "stats", {})
+
+    def __setattr__(self, name, value):
+        if name == "A":
+            # cache.A = X  =>  isfresh = true (common.jl:330-348)
+            if not isinstance(value, DeviceMatrix):
+                value = np.asarray(value)
+            object.__setattr__(self, "A", value)
+            object.__setattr__(self, "isfresh", True)
+        elif name == "b":
+            # cache.b = y  =>  no refactorization (common.jl:351-353)
+            if not isinstance(value, DeviceMatrix):
+                value = np.asarray(value)
+            object.__setattr__(self, "b", value)
+        else:
+            object.__setattr__(self, name, value)
+
+
+def _default_tolerances(A):
+    dt = np.float64
+    eps = float(np.finfo(dt).eps)
+    return math.sqrt(eps), math.sqrt(eps)  # abstol, reltol defaults of common.jl
+
+
+def init(prob: LinearProblem, alg=None, alias: Optional[LinearAliasSpecifier] = None,
+         abstol: Optional[float] = None, reltol: Optional[float] = None, verbose: bool = False,
+         context=None) -> LinearCache:
+    """SciMLBase.init(prob, alg; alias, abstol, reltol, verbose) (common.jl:700-931)."""
+    if alg is None:
+        alg = GB300LUFactorization()
+    A, b = prob.A, prob.b
+    m, n = _shape(A)
+    if getattr(alg, "needs_square_A", False) and m != n:
+        raise ValueError(f"{type(alg).__name__} requires a square A, got {m}x{n}")
+    if _shape(b)[0] != m:
+        raise ValueError("b has the wrong number of rows")
+    alias = alias or LinearAliasSpecifier()
+    alias_A = alg.default_alias_A if alias.alias_A is None else bool(alias.alias_A)
+    alias_b = alg.default_alias_b if alias.alias_b is None else bool(alias.alias_b)
+    if not isinstance(A, DeviceMatrix):
+        A = np.asarray(A, dtype=np.float64)
+        if not alias_A:
+            A = np.array(A, order="F", copy=True)
+    if not isinstance(b, DeviceMatrix):
+        b = np.asarray(b, dtype=np.float64)
+        if not alias_b:
+            b = np.array(b, copy=True)
+    if prob.u0 is not None:
+        u = np.array(prob.u0, dtype=np.float64, copy=True)
+    elif isinstance(b, DeviceMatrix):
+        u = DeviceMatrix(b.rows, b.cols)
+    else:
+        u = np.zeros(np.shape(b), dtype=np.float64)
+    d_abs, d_rel = _default_tolerances(A)
+    ctx = context if context is not None else default_context(getattr(alg, "device", 0))
+    cache = LinearCache(A, b, u, alg, d_abs if abstol is None else abstol,
+                        d_rel if reltol is None else reltol, verbose, alias_A, alias_b, ctx)
+    # init_cacheval: the device-resident factorization object, allocated once
+    cache.cacheval = ctx.factor(m, n, alg.factor_precision())
+    return cache
+
+
+def _solve_into(cache: LinearCache, fact, b):
+    alg = cache.alg
+    if isinstance(alg, GB300MixedLUFactorization):
+        if isinstance(b, DeviceMatrix):
+            out = cache.u if isinstance(cache.u, DeviceMatrix) else DeviceMatrix(b.rows, b.cols)
+            out.copy_from(b)
+            from ._cuda import device_synchronize
+            device_synchronize()
+            X, stats = fact.solve_refined(out, mode=alg.refine, max_iter=alg.maxiters,
+                                          tol=alg.tol or 0.0, fallback=alg.fallback,
+                                          gmres_restart=alg.gmres_restart, gmres_tol=alg.gmres_tol)
+            return out, stats
+        X, stats = fact.solve_refined(b, mode=alg.refine, max_iter=alg.maxiters,
+                                      tol=alg.tol or 0.0, fallback=alg.fallback,
+                                      gmres_restart=alg.gmres_restart, gmres_tol=alg.gmres_tol)
+        return X, stats
+    if isinstance(b, DeviceMatrix):
+        out = cache.u if isinstance(cache.u, DeviceMatrix) else DeviceMatrix(b.rows, b.cols)
+        out.copy_from(b)
+        from ._cuda import device_synchronize
+        device_synchronize()
+        fact.getrs(out)
+        return out, {}
+    return fact.getrs(b), {}
+
+
+def solve_bang(cache: LinearCache, **kwargs) -> LinearSolution:
+    """solve!(cache) for the GB300 algorithms (factorization.jl:643-736 shape)."""
+    alg = cache.alg
+    fact = cache.cacheval
+    if cache.isfresh:
+        A_now = cache.A
+        info = fact.getrf(A_now)
+        if info != 0:
+            # Failure without resetting isfresh (factorization.jl:16-28, :716-722)
+            if cache.verbose:
+                print("Solver failed")
+            return LinearSolution(cache.u, None, alg, ReturnCode.Failure, cache=cache,
+                                  stats={"info": info})
+        cache.isfresh = False
+    u, stats = _solve_into(cache, fact, cache.b)
+    if isinstance(u, DeviceMatrix):
+        cache.u = u
+    else:
+        if isinstance(cache.u, np.ndarray) and cache.u.shape == np.shape(u):
+            cache.u[...] = u
+        else:
+            cache.u = np.array(u)
+    cache.stats = stats
+    if getattr(alg, "residualsafety", False) and not isinstance(cache.A, DeviceMatrix):
+        # _check_residual_safety (factorization.jl:127-156), 2-norms as the reference
+        A = np.asarray(cache.A, dtype=np.float64)
+        bb = np.asarray(cache.b, dtype=np.float64)
+        res = np.linalg.norm(A @ cache.u - bb)
+        tol = cache.abstol + cache.reltol * np.linalg.norm(bb)
+        if res > tol:
+            return LinearSolution(cache.u, None, alg, ReturnCode.APosterioriSafetyFailure,
+                                  cache=cache, stats=stats)
+    return LinearSolution(cache.u, None, alg, ReturnCode.Success, iters=stats.get("iterations", 0),
+                          cache=cache, stats=stats)
+
+
+def solve(prob: LinearProblem, alg=None, **kwargs) -> LinearSolution:
+    """solve(prob, alg; kwargs...) = solve!(init(prob, alg; kwargs...)) (common.jl:988-993)."""
+    return solve_bang(init(prob, alg, **kwargs))
+
+
+def reinit(cache: LinearCache, A=None, b=None) -> LinearCache:
+    """reinit!(cache; A, b) funnels into the same setters (common.jl:933-964)."""
+    if A is not None:
+        cache.A = A
+    if b is not None:
+        cache.b = b
+    return cache

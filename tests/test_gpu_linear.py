@@ -1,0 +1,115 @@
+"""The LinearProblem / init / solve! interface on the GPU (the reference's
+test/Core/basictests.jl:64-91 test_interface, resolve.jl, lu_refactorization.jl,
+batch.jl assertions, restated)."""
+import numpy as np
+import pytest
+
+from conftest import EPS64
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(params=["plain", "mixed_ir", "mixed_gmres"])
+def alg(request, pkg):
+    if request.param == "plain":
+        return pkg.GB300LUFactorization()
+    if request.param == "mixed_ir":
+        return pkg.GB300MixedLUFactorization(refine="ir")
+    return pkg.GB300MixedLUFactorization(refine="gmres_ir")
+
+
+def test_known_answer_resolve(pkg, golden, alg):
+    # test/Core/resolve.jl:78-106
+    prob = pkg.LinearProblem(golden["known_A"], golden["known_b"])
+    cache = pkg.init(prob, alg, alias=pkg.LinearAliasSpecifier(alias_A=False, alias_b=False))
+    np.testing.assert_allclose(pkg.solve_bang(cache).u, golden["known_x"], rtol=1e-12)
+    assert not cache.isfresh
+    np.testing.assert_allclose(pkg.solve_bang(cache).u, golden["known_x"], rtol=1e-12)
+
+
+def test_interface_A_then_b(pkg, oracle_mod, alg):
+    # test/Core/basictests.jl:64-91: solve, cache.A = A2, cache.b = b2
+    rng = np.random.default_rng(21)
+    n = 80
+    A1 = rng.random((n, n)) + n * np.eye(n)
+    A2 = rng.random((n, n)) + n * np.eye(n)
+    b1, b2 = rng.random(n), rng.random(n)
+    cache = pkg.init(pkg.LinearProblem(A1, b1), alg)
+    sol = pkg.solve_bang(cache)
+    assert pkg.successful_retcode(sol)
+    assert oracle_mod.backward_error(A1, sol.u, b1) <= 10 * n * EPS64
+    cache.A = A2
+    assert cache.isfresh
+    sol = pkg.solve_bang(cache)
+    assert oracle_mod.backward_error(A2, sol.u, b1) <= 10 * n * EPS64
+    cache.b = b2
+    assert not cache.isfresh
+    sol = pkg.solve_bang(cache)
+    assert oracle_mod.backward_error(A2, sol.u, b2) <= 10 * n * EPS64
+
+
+def test_b_only_resolve_skips_getrf(pkg):
+    rng = np.random.default_rng(22)
+    n = 64
+    A = rng.standard_normal((n, n)) + n * np.eye(n)
+    cache = pkg.init(pkg.LinearProblem(A, rng.random(n)), pkg.GB300LUFactorization())
+    pkg.solve_bang(cache)
+    calls = []
+    orig = cache.cacheval.getrf
+    cache.cacheval.getrf = lambda *a, **k: calls.append(1) or orig(*a, **k)
+    for _ in range(3):
+        cache.b = rng.random(n)
+        pkg.solve_bang(cache)
+    assert calls == []
+    cache.A = A * 2.0
+    pkg.solve_bang(cache)
+    assert calls == [1]
+
+
+def test_singular_failure_and_recovery(pkg, golden, alg):
+    # test/Core/lu_refactorization.jl:83-110
+    cache = pkg.init(pkg.LinearProblem(golden["sing_Agood"].copy(), np.ones(8)), alg,
+                     alias=pkg.LinearAliasSpecifier(alias_A=True))
+    assert pkg.solve_bang(cache).retcode == pkg.ReturnCode.Success
+    cache.A = golden["sing_A"].copy()
+    sol = pkg.solve_bang(cache)
+    assert sol.retcode == pkg.ReturnCode.Failure
+    assert cache.isfresh  # not reset on failure
+    cache.A = golden["sing_Agood"].copy()
+    sol = pkg.solve_bang(cache)
+    assert sol.retcode == pkg.ReturnCode.Success
+    np.testing.assert_allclose(sol.u, np.linalg.solve(golden["sing_Agood"], np.ones(8)), rtol=1e-12)
+
+
+def test_multi_rhs(pkg, oracle_mod, alg):
+    # test/Core/batch.jl:9-57: matrix RHS
+    rng = np.random.default_rng(23)
+    n, k = 12, 4
+    A = rng.random((n, n)) + n * np.eye(n)
+    B = rng.random((n, k))
+    sol = pkg.solve(pkg.LinearProblem(A, B), alg)
+    assert pkg.successful_retcode(sol)
+    assert sol.u.shape == (n, k)
+    np.testing.assert_allclose(sol.u, np.linalg.solve(A, B), rtol=1e-12)
+
+
+def test_residual_safety(pkg):
+    rng = np.random.default_rng(24)
+    n = 12
+    A = rng.random((n, n)) + n * np.eye(n)
+    B = rng.random((n, 3))
+    sol = pkg.solve(pkg.LinearProblem(A, B), pkg.GB300LUFactorization(residualsafety=True))
+    assert pkg.successful_retcode(sol)
+
+
+def test_device_resident_inputs(pkg, oracle_mod):
+    rng = np.random.default_rng(25)
+    n = 300
+    A = rng.standard_normal((n, n))
+    b = rng.standard_normal((n, 2))
+    dA = pkg.DeviceMatrix.from_host(A)
+    db = pkg.DeviceMatrix.from_host(b)
+    sol = pkg.solve(pkg.LinearProblem(dA, db), pkg.GB300LUFactorization())
+    u = sol.u.to_host()
+    LU, ipiv, _ = oracle_mod.getrf(A)
+    assert np.array_equal(u, oracle_mod.getrs(LU, ipiv, b))

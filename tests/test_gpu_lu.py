@@ -1,0 +1,240 @@
+"""getrf / getrs on the GPU against the oracle (bit-exact) and LAPACK.
+
+The GPU factorization keeps the reference's per-element operation order, so
+ipiv and the packed factors must equal the C restatement of
+src/blocked_lufact.jl bit for bit, and the solve must equal the restated
+src/factorization.jl:433-457 back-solve bit for bit."""
+import numpy as np
+import pytest
+
+from conftest import EPS64
+
+pytestmark = pytest.mark.gpu
+
+SQUARE = [1, 2, 3, 5, 7, 8, 9, 13, 16, 17, 31, 32, 33, 40, 41, 63, 64, 65, 100, 127, 128, 129,
+          200, 250, 256, 257, 300, 500, 512, 1000]
+
+
+@pytest.mark.parametrize("n", SQUARE)
+def test_getrf_bit_exact(ctx, oracle_mod, n):
+    rng = np.random.default_rng(1000 + n)
+    A = rng.standard_normal((n, n))
+    f = ctx.factor(n, n)
+    info = f.getrf(A)
+    LU, ipiv, info_ref = oracle_mod.getrf(A)
+    assert info == info_ref == 0
+    assert np.array_equal(f.ipiv(), ipiv)
+    assert np.array_equal(f.factors(), LU)
+    f.close()
+
+
+@pytest.mark.parametrize("m,n", [(100, 3), (3, 100), (128, 40), (40, 128), (257, 130), (130, 257),
+                                 (65, 64), (64, 65), (513, 100), (100, 513), (2000, 70)])
+def test_getrf_rectangular_bit_exact(ctx, oracle_mod, m, n):
+    rng = np.random.default_rng(m * 1000 + n)
+    A = rng.standard_normal((m, n))
+    f = ctx.factor(m, n)
+    f.getrf(A)
+    LU, ipiv, info_ref = oracle_mod.getrf(A)
+    assert np.array_equal(f.ipiv(), ipiv)
+    assert np.array_equal(f.factors(), LU)
+    assert oracle_mod.scaled_residual(A, f.factors(), f.ipiv()) < 20
+    f.close()
+
+
+def test_getrf_matches_lapack_golden(ctx, golden):
+    for key in golden["cases"]:
+        A = golden[key + "_A"]
+        m, n = A.shape
+        f = ctx.factor(m, n)
+        info = f.getrf(A)
+        assert info == int(golden[key + "_info"])
+        assert np.array_equal(f.ipiv(), golden[key + "_ipiv"]), key
+        scale = max(1.0, np.abs(golden[key + "_LU"]).max())
+        assert np.abs(f.factors() - golden[key + "_LU"]).max() <= 1e-11 * scale
+        if key + "_b" in golden:
+            np.testing.assert_allclose(f.getrs(golden[key + "_b"]), golden[key + "_x"], rtol=1e-9,
+                                       atol=1e-12)
+            np.testing.assert_allclose(f.getrs(golden[key + "_b"], trans="T"), golden[key + "_xt"],
+                                       rtol=1e-9, atol=1e-12)
+        f.close()
+
+
+@pytest.mark.parametrize("n", [1, 5, 63, 64, 65, 127, 200, 513, 1000])
+@pytest.mark.parametrize("nrhs", [1, 3, 8, 11])
+def test_getrs_bit_exact(ctx, oracle_mod, n, nrhs):
+    rng = np.random.default_rng(n * 31 + nrhs)
+    A = rng.standard_normal((n, n))
+    B = rng.standard_normal((n, nrhs))
+    f = ctx.factor(n, n)
+    f.getrf(A)
+    LU, ipiv, _ = oracle_mod.getrf(A)
+    X = f.getrs(B)
+    assert np.array_equal(X, oracle_mod.getrs(LU, ipiv, B))
+    XT = f.getrs(B, trans="T")
+    assert np.array_equal(XT, oracle_mod.getrs(LU, ipiv, B, trans="T"))
+    assert oracle_mod.backward_error(A, X, B) <= 10 * n * EPS64
+    assert oracle_mod.backward_error(A.T, XT, B) <= 10 * n * EPS64
+    f.close()
+
+
+def test_known_answer(ctx, golden):
+    f = ctx.factor(2, 2)
+    f.getrf(golden["known_A"])
+    np.testing.assert_allclose(f.getrs(golden["known_b"]), golden["known_x"], rtol=1e-12)
+    f.close()
+
+
+def test_singular_zero_column(ctx, oracle_mod, golden):
+    f = ctx.factor(8, 8)
+    info = f.getrf(golden["sing_A"])
+    LU, ipiv, info_ref = oracle_mod.getrf(golden["sing_A"])
+    assert info == info_ref == 1
+    assert np.array_equal(f.ipiv(), ipiv)
+    assert np.array_equal(f.factors(), LU)
+    # solving with a singular factorization is refused, not silently wrong
+    with pytest.raises(Exception):
+        f.getrs(np.ones(8))
+    # the same object recovers on the next nonsingular matrix
+    assert f.getrf(golden["sing_Agood"]) == 0
+    x = f.getrs(np.ones(8))
+    assert oracle_mod.backward_error(golden["sing_Agood"], x, np.ones(8)) <= 80 * EPS64
+    f.close()
+
+
+def test_zero_pivot_later_column(ctx, oracle_mod):
+    # rank-deficient: column 5 a combination of columns 0..4 -> exact zero pivot possible
+    rng = np.random.default_rng(11)
+    n = 70
+    A = rng.integers(-3, 4, size=(n, n)).astype(np.float64)
+    A[:, 40] = 0.0
+    f = ctx.factor(n, n)
+    info = f.getrf(A)
+    LU, ipiv, info_ref = oracle_mod.getrf(A)
+    assert info == info_ref and info > 0
+    assert np.array_equal(f.ipiv(), ipiv)
+    assert np.array_equal(f.factors(), LU)
+    f.close()
+
+
+def test_ties_and_small_integers(ctx, oracle_mod):
+    # many exactly equal |a| candidates: the first-index rule must match
+    rng = np.random.default_rng(12)
+    for n in (17, 96, 300):
+        A = rng.choice([-2.0, -1.0, 1.0, 2.0], size=(n, n))
+        f = ctx.factor(n, n)
+        info = f.getrf(A)
+        LU, ipiv, info_ref = oracle_mod.getrf(A)
+        assert info == info_ref
+        assert np.array_equal(f.ipiv(), ipiv)
+        assert np.array_equal(f.factors(), LU)
+        f.close()
+
+
+def test_nan_input_propagates(ctx, oracle_mod):
+    rng = np.random.default_rng(13)
+    n = 50
+    A = rng.standard_normal((n, n))
+    A[7, 3] = np.nan
+    f = ctx.factor(n, n)
+    info = f.getrf(A)
+    LU, ipiv, info_ref = oracle_mod.getrf(A)
+    assert info == info_ref
+    assert np.array_equal(f.ipiv(), ipiv)
+    np.testing.assert_array_equal(np.isnan(f.factors()), np.isnan(LU))
+    f.close()
+
+
+def test_empty(ctx):
+    f = ctx.factor(0, 0)
+    assert f.getrf(np.zeros((0, 0))) == 0
+    f.close()
+
+
+def test_factor_reuse_no_reallocation(ctx, oracle_mod):
+    # refactor cycles A2, A1, A2 on one factor object (test/Core/lu_refactorization.jl:28-66)
+    rng = np.random.default_rng(14)
+    n = 51
+    A1 = rng.random((n, n)) + n * np.eye(n)
+    A2 = rng.random((n, n)) + n * np.eye(n)
+    b = rng.random(n)
+    f = ctx.factor(n, n)
+    f.getrf(A1)
+    f.getrs(b)
+    used = ctx.memory()[0]
+    for Ak in (A2, A1, A2):
+        assert f.getrf(Ak) == 0
+        x = f.getrs(b)
+        LU, ipiv, _ = oracle_mod.getrf(Ak)
+        assert np.array_equal(x, oracle_mod.getrs(LU, ipiv, b))
+        assert ctx.memory()[0] == used  # refactor + solve allocate nothing
+    f.close()
+
+
+@pytest.mark.parametrize("n", [2048])
+def test_getrf_bit_exact_medium(ctx, oracle_mod, n):
+    rng = np.random.default_rng(n)
+    A = rng.standard_normal((n, n))
+    f = ctx.factor(n, n)
+    f.getrf(A)
+    LU, ipiv, _ = oracle_mod.getrf(A)
+    assert np.array_equal(f.ipiv(), ipiv)
+    assert np.array_equal(f.factors(), LU)
+    b = rng.standard_normal(n)
+    assert np.array_equal(f.getrs(b), oracle_mod.getrs(LU, ipiv, b))
+    f.close()
+
+
+def test_full_size_config_backward_error(ctx, oracle_mod, pkg):
+    # n = 8192, 16 RHS through one factorization: the size-independent bound
+    n = 8192
+    A, B = pkg.workloads.plain(n, 16, seed=0)
+    f = ctx.factor(n, n)
+    assert f.getrf(A) == 0
+    X = f.getrs(B)
+    be = oracle_mod.backward_error(A, X, B)
+    assert be <= 10 * n * EPS64, be
+    # forward error against the LAPACK solve of the same system, reported
+    Xl, _ = oracle_mod.lapack_solve(A, B)
+    fe = oracle_mod.forward_error(X, Xl)
+    print(f"n={n}: backward error {be:.3e}, forward error vs LAPACK {fe:.3e}")
+    assert fe < 1e-6
+    f.close()
+
+
+def test_lapack_shaped_entries(pkg, oracle_mod):
+    rng = np.random.default_rng(15)
+    for (m, n) in ((40, 40), (130, 70), (70, 130)):
+        A = rng.standard_normal((m, n))
+        LU, ipiv, info = pkg.dgetrf(A)
+        LUo, ipivo, infoo = oracle_mod.getrf(A)
+        assert info == infoo
+        assert np.array_equal(ipiv, ipivo) and np.array_equal(LU, LUo)
+    A = rng.standard_normal((90, 90))
+    LU, ipiv, info = oracle_mod.getrf(A)
+    B = rng.standard_normal((90, 3))
+    assert np.array_equal(pkg.dgetrs(LU, ipiv, B), oracle_mod.getrs(LU, ipiv, B))
+    assert np.array_equal(pkg.dgetrs(LU, ipiv, B, "T"), oracle_mod.getrs(LU, ipiv, B, "T"))
+
+
+def test_lapack_shaped_single(pkg, oracle_mod):
+    import ctypes
+    lib = pkg.load_library()
+    rng = np.random.default_rng(16)
+    n = 77
+    A = np.asfortranarray(rng.standard_normal((n, n)).astype(np.float32))
+    LU = A.copy(order="F")
+    ipiv = np.zeros(n, dtype=np.int64)
+    m_, n_, lda, info = (ctypes.c_int64(n), ctypes.c_int64(n), ctypes.c_int64(n), ctypes.c_int64())
+    lib.gblu_sgetrf_(ctypes.byref(m_), ctypes.byref(n_), LU.ctypes.data, ctypes.byref(lda),
+                     ipiv.ctypes.data, ctypes.byref(info))
+    LUo, ipivo, infoo = oracle_mod.getrf(A)
+    assert info.value == infoo == 0
+    assert np.array_equal(ipiv, ipivo) and np.array_equal(LU, LUo)
+    b = np.asfortranarray(rng.standard_normal((n, 2)).astype(np.float32))
+    x = b.copy(order="F")
+    nrhs, ldb = ctypes.c_int64(2), ctypes.c_int64(n)
+    lib.gblu_sgetrs_(b"N", ctypes.byref(n_), ctypes.byref(nrhs), LU.ctypes.data, ctypes.byref(lda),
+                     ipiv.ctypes.data, x.ctypes.data, ctypes.byref(ldb), ctypes.byref(info), 1)
+    assert info.value == 0
+    assert np.array_equal(x, oracle_mod.getrs(LUo, ipivo, b))
