@@ -1,0 +1,433 @@
+#!/usr/bin/env python
+"""Benchmark: FP64-accurate solves/s of the dense LU path on GB300.
+
+Workload (one step): plain FP64 LU of an n = 8192 matrix (A iid N(0,1)) and
+16 successive single right-hand-side solves through that one cached
+factorization (1 getrf + 16 getrs), the cached-LinearCache pattern of
+solve!(cache) / cache.b = b.  Inputs are seeded synthetic arrays.
+
+  value  solves/s with A and B resident in HBM (device-timed, CUDA events on
+         the library's stream)
+  e2e    the same step through the public interface (LinearProblem / init /
+         solve!) with pinned host buffers: the H2D copy of A and of each b and
+         the D2H copy of each solution are inside the timed region.
+
+--impl reference times the CPU implementation of the same path (LAPACK
+dgetrf/dgetrs on OpenBLAS, the routines LinearSolve.jl's LUFactorization calls)
+on the host cores.
+
+--suite adds the mixed-precision comparison at n = 16384 (A = G + 4 sqrt(n) I,
+4 RHS): FP32 LU + FP64 refinement vs the plain FP64 LU, both to the FP64
+backward-error bound.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+EPS64 = float(np.finfo(np.float64).eps)
+METRIC = "FP64-accurate solves/s (1 getrf + 16 cached getrs, n=8192, plain FP64 LU)"
+UNIT = "solves/s"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return rank, world, local
+
+
+class Dist:
+    """Barrier and max-over-ranks for N > 1 (gloo: host-side plumbing only)."""
+
+    def __init__(self, world: int):
+        self.world = world
+        self.pg = None
+        if world > 1:
+            import torch.distributed as td
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            td.init_process_group("gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def max(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.td.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def peak_fp64_tflops(device: int):
+    import ctypes
+    path = os.path.join(ROOT, "linearsolve.jl_gb300", "libgblu_tools.so")
+    lib = ctypes.CDLL(path)
+    lib.gblu_tool_peak_fp64.argtypes = [ctypes.c_int32, ctypes.POINTER(ctypes.c_double)]
+    lib.gblu_tool_peak_fp64.restype = ctypes.c_int32
+    out = ctypes.c_double()
+    st = lib.gblu_tool_peak_fp64(device, ctypes.byref(out))
+    return float(out.value) if st == 0 else None
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh)
+    except (OSError, ValueError):
+        return {}
+
+
+def profile_traffic(kind: str):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as fh:
+            return json.load(fh).get(kind)
+    except (OSError, ValueError):
+        return None
+
+
+# ---------------------------------------------------------------------------
+# CPU reference arm
+
+def cpu_lapack_steps(A, B, steps: int):
+    """LAPACK getrf + one getrs per RHS column (the cached-solve pattern)."""
+    import oracle
+    times = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        LU, ipiv, info = oracle.lapack_getrf(A)
+        for j in range(B.shape[1]):
+            oracle.lapack_getrs(LU, ipiv, B[:, j:j + 1])
+        times.append(time.perf_counter() - t0)
+    return times
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    import oracle  # noqa: F401  (CPU implementation of the path; not the product)
+    pkg = load_pkg()
+    n, nrhs = args.n, args.nrhs
+    A, B = pkg.workloads.plain(n, nrhs, seed=0)
+    for _ in range(max(1, min(args.warmup, 1))):
+        cpu_lapack_steps(A, B, 1)
+    times = cpu_lapack_steps(A, B, args.steps)
+    total = sum(times)
+    value = args.steps * nrhs / total
+    cores = os.cpu_count()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000 * total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded N(0,1))",
+        "impl": "reference",
+        "config": {"workload": f"plain FP64 LU n={n}, 1 getrf + {nrhs} cached getrs", "n": n,
+                   "nrhs": nrhs, "global_batch": nrhs, "parallelism": "host threads"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} full steps: scipy.linalg.lapack dgetrf + {nrhs} dgetrs "
+                                   f"(OpenBLAS, all {cores} host threads) -- the LAPACK routines "
+                                   "LUFactorization reaches through LinearAlgebra.lu!/ldiv!"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+
+def load_pkg():
+    import __graft_entry__ as ge
+    return ge.load_package()
+
+
+def run_gpu(args, rank, world, local):
+    dist = Dist(world)
+    pkg = load_pkg()
+    from importlib import import_module
+    cu = import_module(pkg.__name__ + "._cuda")
+    n, nrhs = args.n, args.nrhs
+    ctx = pkg.Context(local)
+    stream = ctx.stream
+    A, B = pkg.workloads.plain(n, nrhs, seed=0)
+
+    # ---- device-resident workload (value) ----
+    dA = pkg.DeviceMatrix.from_host(A)
+    dB0 = pkg.DeviceMatrix.from_host(B)
+    dB = pkg.DeviceMatrix(n, nrhs)
+    f = ctx.factor(n, n, "fp64")
+    cols = [cu.DeviceColumn(dB, j) for j in range(nrhs)]
+
+    def step():
+        dB.copy_from(dB0, stream)
+        info = f.getrf(dA)
+        if info != 0:
+            raise RuntimeError(f"getrf info={info}")
+        for c in cols:
+            f.getrs(c)
+
+    for _ in range(args.warmup):
+        step()
+    cu.device_synchronize()
+    # accuracy of the last step (not timed)
+    X = dB.to_host()
+    berr = max(pkg_backward_error(A, X[:, j], B[:, j]) for j in range(nrhs))
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    ctx.profile_enable(True)
+    dist.barrier()
+    cu.device_synchronize()
+    e0, e1 = cu.Event(), cu.Event()
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    e1.synchronize()
+    cu.device_synchronize()
+    dist.barrier()
+    prof = ctx.profile_read(reset=True)
+    ctx.profile_enable(False)
+    clk = clocks.stop()
+    t_ms = dist.max(e0.elapsed_ms(e1))
+    total_solves = dist.sum(args.steps * nrhs)
+    value = total_solves / (t_ms / 1000.0)
+
+    # ---- end to end through the public interface, pinned host buffers ----
+    pA = cu.PinnedArray((n, n))
+    pA.array[...] = A
+    pB = cu.PinnedArray((n, nrhs))
+    pB.array[...] = B
+    alg = pkg.GB300LUFactorization()
+    cache = pkg.init(pkg.LinearProblem(pA.array, pB.array[:, 0]), alg,
+                     alias=pkg.LinearAliasSpecifier(alias_A=True, alias_b=True), context=ctx)
+
+    def e2e_step():
+        cache.A = pA.array
+        for j in range(nrhs):
+            cache.b = pB.array[:, j]
+            sol = pkg.solve_bang(cache)
+            if sol.retcode != pkg.ReturnCode.Success:
+                raise RuntimeError("e2e solve failed")
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    t_e2e = dist.max(time.perf_counter() - t0)
+    e2e_value = dist.sum(args.steps * nrhs) / t_e2e
+
+    # ---- roofline of the dominant kernel (event-timed inside the timed region) ----
+    kinds = [k for k in prof if k != "launches"]
+    dom = max(kinds, key=lambda k: prof[k]["ms"])
+    d = prof[dom]
+    peaks = measured_peaks()
+    peak_fp64 = peak_fp64_tflops(local) if rank == 0 else None
+    if dom in ("gemm", "panel", "trsm"):
+        achieved = d["flops"] / (d["ms"] / 1000.0) / 1e12 if d["ms"] > 0 else 0.0
+        peak = peak_fp64
+        roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": (achieved / peak) if peak else None,
+                "peak_source": "FP64 FMA throughput measured in this run by a register-only DFMA "
+                               "loop (MEASURED_PEAKS.json has no FP64 figure; tcgen05 has no FP64 "
+                               "kind, so the FP64 update runs on the FP64 pipe)",
+                "kernel": f"{dom} (FP64)", "launches": d["count"],
+                "flops_per_launch": d["flops"] / max(d["count"], 1),
+                "ms_per_launch": d["ms"] / max(d["count"], 1)}
+    else:
+        achieved = d["bytes"] / (d["ms"] / 1000.0) / 1e9 if d["ms"] > 0 else 0.0
+        peak = peaks.get("hbm_gbs")
+        roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": (achieved / peak) if peak else None,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs", "kernel": dom,
+                "launches": d["count"]}
+    tr = profile_traffic(dom)
+    roof["traffic"] = tr
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded N(0,1), numpy default_rng(0))",
+        "config": {"workload": f"plain FP64 LU n={n}, 1 getrf + {nrhs} cached single-RHS getrs per step",
+                   "n": n, "nrhs": nrhs, "global_batch": nrhs * world, "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (A = %.0f MB)" % (8 * n * n / 1e6)},
+        "accuracy": {"backward_error": berr, "bound": 10 * n * EPS64},
+        "clocks": clk,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * n * n + nrhs * 8 * n,
+                "d2h_bytes_per_step": nrhs * 8 * n + 8},
+        "gpu_launches": prof["launches"],
+        "roofline": roof,
+        "kernel_ms": {k: round(prof[k]["ms"] / args.steps, 3) for k in kinds if prof[k]["count"]},
+    }
+
+    if args.suite and rank == 0:
+        line["mixed"] = run_mixed_suite(pkg, cu, ctx, args)
+
+    if rank == 0 and not args.no_cpu:
+        # bounded CPU sample of the same workload on this host
+        ts = cpu_lapack_steps(A, B, args.cpu_steps)
+        cv = args.cpu_steps * nrhs / sum(ts)
+        line["cpu_baseline"] = {
+            "value": cv, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+            "sample": f"{args.cpu_steps} full steps: scipy.linalg.lapack dgetrf + {nrhs} dgetrs (OpenBLAS, "
+                      f"{os.cpu_count()} host threads), the LAPACK routines LUFactorization calls"}
+    if rank == 0:
+        print(json.dumps(line))
+    dist.close()
+    return 0
+
+
+def pkg_backward_error(A, x, b):
+    r = b - A @ x
+    nA = np.abs(A).sum(axis=1).max()
+    return float(np.abs(r).max() / (nA * np.abs(x).max() + np.abs(b).max()))
+
+
+def run_mixed_suite(pkg, cu, ctx, args):
+    """n = 16384, A = G + 4 sqrt(n) I, 4 RHS: FP32 LU + IR vs plain FP64 LU."""
+    n, nrhs = args.mixed_n, 4
+    A, B = pkg.workloads.shifted(n, nrhs, seed=1)
+    dA = pkg.DeviceMatrix.from_host(A)
+    dB0 = pkg.DeviceMatrix.from_host(B)
+    dB = pkg.DeviceMatrix(n, nrhs)
+    out = {"n": n, "nrhs": nrhs, "A": "G + 4 sqrt(n) I"}
+    for label, prec in (("fp32_ir", "fp32"), ("fp64_plain", "fp64")):
+        f = ctx.factor(n, n, prec)
+        reps = 2 if prec == "fp64" else 3
+
+        def once():
+            dB.copy_from(dB0, ctx.stream)
+            f.getrf(dA)
+            if prec == "fp64":
+                f.getrs(dB)
+                return {}
+            _, st = f.solve_refined(dB, mode="ir")
+            return st
+
+        once()
+        cu.device_synchronize()
+        e0, e1 = cu.Event(), cu.Event()
+        e0.record(ctx.stream)
+        st = {}
+        for _ in range(reps):
+            st = once()
+        e1.record(ctx.stream)
+        e1.synchronize()
+        ms = e0.elapsed_ms(e1) / reps
+        X = dB.to_host()
+        be = max(pkg_backward_error(A, X[:, j], B[:, j]) for j in range(nrhs))
+        out[label] = {"ms_per_solve_set": ms, "solves_per_s": nrhs / (ms / 1000), "backward_error": be,
+                      "stats": st}
+        f.close()
+    out["speedup_fp32_ir_vs_fp64"] = out["fp32_ir"]["solves_per_s"] / out["fp64_plain"]["solves_per_s"]
+    out["bound"] = 10 * n * EPS64
+    dA.free(); dB0.free(); dB.free()
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gblu", choices=["gblu", "reference"])
+    ap.add_argument("--n", type=int, default=8192)
+    ap.add_argument("--nrhs", type=int, default=16)
+    ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--suite", action="store_true")
+    ap.add_argument("--mixed-n", type=int, default=16384)
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    return run_gpu(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

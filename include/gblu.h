@@ -70,6 +70,26 @@ int32_t gblu_ctx_stream(gblu_ctx* ctx, void** stream_out);
 /* Device bytes currently held by the context's objects, and its budget. */
 int32_t gblu_ctx_memory(gblu_ctx* ctx, uint64_t* in_use, uint64_t* budget);
 
+/* ---- launch accounting ---------------------------------------------------------
+ * Counts every kernel the context launches and, when enabled, times each
+ * launch with CUDA events on the context's stream.  Kinds (index into the
+ * arrays): 0 trailing GEMM update, 1 panel getf2, 2 row interchanges, 3 TRSM,
+ * 4 permutation build, 5 getrs sweeps, 6 refinement kernels, 7 batched,
+ * 8 other.  flops/bytes are the algorithmic work the launches were given.
+ * Measurement utility; no counterpart in the reference. */
+#define GBLU_PROFILE_KINDS 9
+typedef struct gblu_profile {
+  uint64_t launches;
+  uint64_t count[GBLU_PROFILE_KINDS];
+  double ms[GBLU_PROFILE_KINDS];
+  double flops[GBLU_PROFILE_KINDS];
+  double bytes[GBLU_PROFILE_KINDS];
+} gblu_profile;
+/* Enable (1) or disable (0) event timing; always resets the counters. */
+int32_t gblu_profile_enable(gblu_ctx* ctx, int32_t enable);
+/* Synchronise the stream and read the counters (reset != 0 clears them). */
+int32_t gblu_profile_read(gblu_ctx* ctx, gblu_profile* out, int32_t reset);
+
 /* ---- factorization objects -------------------------------------------------
  * A factor owns, in HBM, everything getrf/getrs need for an m x n matrix:
  * the factors, ipiv, the row permutation, and all scratch.  It is the

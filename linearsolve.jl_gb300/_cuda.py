@@ -91,15 +91,30 @@ class DeviceMatrix:
                                       stream), "cudaMemcpyAsync D2D")
 
     def free(self) -> None:
-        if self.ptr:
+        if self.ptr and getattr(self, "_owner", True):
             runtime().cudaFree(self.ptr)
-            self.ptr = None
+        self.ptr = None
+
+    def view(self, col0: int, ncols: int = 1) -> "DeviceMatrix":
+        """Non-owning view of columns [col0, col0 + ncols)."""
+        v = DeviceMatrix.__new__(DeviceMatrix)
+        v.rows, v.cols, v.dtype, v.ld = self.rows, int(ncols), self.dtype, self.ld
+        v.nbytes = v.ld * v.cols * v.dtype.itemsize
+        v.ptr = self.ptr + col0 * self.ld * self.dtype.itemsize
+        v._owner = False
+        v._base = self
+        return v
+
 
     def __del__(self):  # pragma: no cover - interpreter shutdown order
         try:
             self.free()
         except Exception:
             pass
+
+
+def DeviceColumn(m: DeviceMatrix, j: int) -> DeviceMatrix:
+    return m.view(j, 1)
 
 
 class Event:

@@ -60,6 +60,20 @@ class RefineStats(ctypes.Structure):
     ]
 
 
+PROFILE_KINDS = 9
+KIND_NAMES = ["gemm", "panel", "laswp", "trsm", "perm", "getrs", "refine", "batched", "other"]
+
+
+class Profile(ctypes.Structure):
+    _fields_ = [
+        ("launches", ctypes.c_uint64),
+        ("count", ctypes.c_uint64 * PROFILE_KINDS),
+        ("ms", ctypes.c_double * PROFILE_KINDS),
+        ("flops", ctypes.c_double * PROFILE_KINDS),
+        ("bytes", ctypes.c_double * PROFILE_KINDS),
+    ]
+
+
 _P = ctypes.c_void_p
 _I32 = ctypes.c_int32
 _I64 = ctypes.c_int64
@@ -74,6 +88,8 @@ SIGNATURES = {
     "gblu_last_error": (ctypes.c_char_p, [_P]),
     "gblu_ctx_stream": (_I32, [_P, ctypes.POINTER(_P)]),
     "gblu_ctx_memory": (_I32, [_P, ctypes.POINTER(_U64), ctypes.POINTER(_U64)]),
+    "gblu_profile_enable": (_I32, [_P, _I32]),
+    "gblu_profile_read": (_I32, [_P, ctypes.POINTER(Profile), _I32]),
     "gblu_factor_create": (_I32, [_P, _I64, _I64, _I32, ctypes.POINTER(_P)]),
     "gblu_factor_destroy": (_I32, [_P, _P]),
     "gblu_getrf": (_I32, [_P, _P, _P, _I64, _I32, _PI64]),

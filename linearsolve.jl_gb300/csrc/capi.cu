@@ -19,6 +19,8 @@ using namespace gblu;
 
 namespace gblu {
 
+thread_local Profiler* tl_profiler = nullptr;
+
 const DeviceInfo& device_info(int device) {
   static std::mutex mu;
   static DeviceInfo cache[64];
@@ -246,6 +248,35 @@ int32_t gblu_ctx_memory(gblu_ctx* ctx, uint64_t* in_use, uint64_t* budget) {
   return GBLU_OK;
 }
 
+int32_t gblu_profile_enable(gblu_ctx* ctx, int32_t enable) {
+  if (!ctx) return fail(ctx, GBLU_EINVAL, "gblu_profile_enable: NULL ctx");
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  DeviceGuard g(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  ctx->prof.drain();
+  ctx->prof.reset();
+  ctx->prof.enabled = enable != 0;
+  return GBLU_OK;
+}
+
+int32_t gblu_profile_read(gblu_ctx* ctx, gblu_profile* out, int32_t reset) {
+  if (!ctx || !out) return fail(ctx, GBLU_EINVAL, "gblu_profile_read: NULL argument");
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  DeviceGuard g(ctx->device);
+  GBLU_CK(ctx, cudaStreamSynchronize(ctx->stream), "gblu_profile_read");
+  ctx->prof.drain();
+  std::memset(out, 0, sizeof(*out));
+  out->launches = ctx->prof.launches;
+  for (int k = 0; k < K_NKINDS && k < GBLU_PROFILE_KINDS; ++k) {
+    out->count[k] = ctx->prof.count[k];
+    out->ms[k] = ctx->prof.ms[k];
+    out->flops[k] = ctx->prof.flops[k];
+    out->bytes[k] = ctx->prof.bytes[k];
+  }
+  if (reset) ctx->prof.reset();
+  return GBLU_OK;
+}
+
 int32_t gblu_factor_create(gblu_ctx* ctx, int64_t m, int64_t n, int32_t precision,
                            gblu_factor** out) {
   if (!ctx || !out) return fail(ctx, GBLU_EINVAL, "gblu_factor_create: NULL argument");
@@ -414,6 +445,7 @@ int32_t gblu_getrf(gblu_ctx* ctx, gblu_factor* f, const double* A, int64_t lda, 
   if (a_loc != GBLU_HOST && a_loc != GBLU_DEVICE) return fail(ctx, GBLU_EINVAL, "gblu_getrf: bad a_loc");
   std::lock_guard<std::recursive_mutex> lk(ctx->mu);
   DeviceGuard g(ctx->device);
+  ActiveProfiler ap(&ctx->prof);
   return factor_getrf(ctx, f, A, lda, a_loc, info);
 }
 
@@ -434,6 +466,7 @@ int32_t gblu_getrs(gblu_ctx* ctx, gblu_factor* f, char trans, int64_t nrhs, doub
   if (!B) return fail(ctx, GBLU_EINVAL, "gblu_getrs: B is NULL");
   std::lock_guard<std::recursive_mutex> lk(ctx->mu);
   DeviceGuard g(ctx->device);
+  ActiveProfiler ap(&ctx->prof);
   if (f->precision != GBLU_FP64) {
     gblu_refine_opts o = refine_default_opts();
     return refine_solve(ctx, f, trans, nrhs, B, ldb, b_loc, &o, nullptr);
@@ -494,6 +527,7 @@ int32_t gblu_solve_refined(gblu_ctx* ctx, gblu_factor* f, char trans, int64_t nr
   if (!B) return fail(ctx, GBLU_EINVAL, "gblu_solve_refined: B is NULL");
   std::lock_guard<std::recursive_mutex> lk(ctx->mu);
   DeviceGuard g(ctx->device);
+  ActiveProfiler ap(&ctx->prof);
   return refine_solve(ctx, f, trans, nrhs, B, ldb, b_loc, opts, stats);
 }
 
@@ -701,6 +735,7 @@ int32_t factor_getrs_f64_host(gblu_ctx* ctx, gblu_factor* f, char trans, int64_t
   if (st) return st;
   CK(ctx, cudaMemcpyAsync(f->ipiv, ipiv, n * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream),
      "copying ipiv");
+  ActiveProfiler ap(&ctx->prof);
   upload_ipiv_check_kernel<<<std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 1024)), 256, 0,
                              ctx->stream>>>(f->ipiv, n, f->rf64.scratch);
   CK(ctx, cudaGetLastError(), "checking ipiv");
@@ -716,6 +751,7 @@ int32_t factor_getrs_f64_host(gblu_ctx* ctx, gblu_factor* f, char trans, int64_t
 int32_t factor_getrf_f32_host(gblu_ctx* ctx, int64_t m, int64_t n, float* A, int64_t lda,
                               int64_t* ipiv, int64_t* info) {
   DeviceGuard g(ctx->device);
+  ActiveProfiler ap(&ctx->prof);
   const int64_t ld = std::max<int64_t>(32, ((m + 31) / 32) * 32);
   size_t bytes = set_bytes<float>(m, n, ld, ctx->device, kWorkCols);
   void* arena = nullptr;
@@ -750,6 +786,7 @@ int32_t factor_getrf_f32_host(gblu_ctx* ctx, int64_t m, int64_t n, float* A, int
 int32_t factor_getrs_f32_host(gblu_ctx* ctx, char trans, int64_t n, int64_t nrhs, const float* A,
                               int64_t lda, const int64_t* ipiv, float* B, int64_t ldb) {
   DeviceGuard g(ctx->device);
+  ActiveProfiler ap(&ctx->prof);
   const int64_t ld = std::max<int64_t>(32, ((n + 31) / 32) * 32);
   size_t bytes = set_bytes<float>(n, n, ld, ctx->device, kWorkCols) + align256((size_t)ld * nrhs * 4);
   void* arena = nullptr;

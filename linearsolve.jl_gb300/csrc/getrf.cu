@@ -23,6 +23,7 @@
 
 #include "device_util.cuh"
 #include "gblu_internal.h"
+#include "profile.h"
 
 namespace gblu {
 
@@ -474,13 +475,19 @@ struct Driver {
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    check(cudaLaunchKernelEx(&cfg, panel_kernel<T>, p.A, p.lda, p.m, c0, w, p.ipiv, p.info,
-                             p.scratch, p.slots, R));
+    {
+      double fl = 0;  // getf2 flops of the leaf: scale + rank-1 updates
+      for (int k = 0; k < w; ++k) fl += (double)(M - k - 1) * (1.0 + 2.0 * (w - k - 1));
+      LaunchScope ls(K_PANEL, fl, 2.0 * M * w * sizeof(T), s);
+      check(cudaLaunchKernelEx(&cfg, panel_kernel<T>, p.A, p.lda, p.m, c0, w, p.ipiv, p.info,
+                               p.scratch, p.slots, R));
+    }
     // interchanges on every other column
     const int64_t nother = p.n - w;
     if (nother > 0) {
       int64_t warps_needed = nother;
       int blocks = (int)std::min<int64_t>((warps_needed + 7) / 8, (int64_t)di.num_sms * 16);
+      LaunchScope ls(K_LASWP, 0.0, 4.0 * w * nother * sizeof(T), s);
       laswp_leaf_kernel<T><<<blocks, 256, 0, s>>>(p.A, p.lda, p.m, p.n, c0, w, p.ipiv, p.scratch);
       check(cudaGetLastError());
     }
@@ -490,6 +497,7 @@ struct Driver {
             T* C, int64_t ldc) {
     if (M <= 0 || N <= 0 || K <= 0) return;
     dim3 grid((unsigned)((M + kGBM - 1) / kGBM), (unsigned)((N + kGBN - 1) / kGBN));
+    LaunchScope ls(K_GEMM, 2.0 * M * N * K, (2.0 * M * N + (double)M * K + (double)K * N) * sizeof(T), s);
     gemm_sub_kernel<T><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc);
     check(cudaGetLastError());
   }
@@ -500,6 +508,7 @@ struct Driver {
     if (k <= p.trsm_base && k <= kTrsmMax) {
       size_t smem = (size_t)(kTrsmMax * kTrsmMax + kTrsmMax * kTrsmCols) * sizeof(T);
       unsigned blocks = (unsigned)((ncols + kTrsmCols - 1) / kTrsmCols);
+      LaunchScope ls(K_TRSM, (double)k * (k - 1) * ncols, (2.0 * k * ncols + (double)k * k) * sizeof(T), s);
       trsm_lunit_kernel<T><<<blocks, kTrsmCols, smem, s>>>(at(r0, r0), p.lda, (int)k,
                                                            at(r0, bc0), p.lda, ncols);
       check(cudaGetLastError());
@@ -532,6 +541,7 @@ struct Driver {
 cudaError_t perm_build_launch(const int64_t* ipiv, int64_t kmax, int64_t m, int32_t* perm,
                               DevScratch* scr, cudaStream_t s) {
   size_t smem = m <= kPermSmemMax ? (size_t)m * sizeof(int32_t) : 0;
+  LaunchScope ls(K_PERM, 0.0, 8.0 * kmax + 4.0 * m, s);
   perm_from_ipiv_kernel<<<1, 1024, smem, s>>>(ipiv, kmax, m, perm, scr);
   return cudaGetLastError();
 }

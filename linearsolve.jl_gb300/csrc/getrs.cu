@@ -19,6 +19,7 @@
 
 #include "device_util.cuh"
 #include "gblu_internal.h"
+#include "profile.h"
 
 namespace gblu {
 
@@ -237,16 +238,24 @@ cudaError_t run_chunk(const GetrsPlan<T>& p, char trans, int nr, T* B, int64_t l
   e = cudaMemsetAsync(&p.scratch->ticket, 0, sizeof(unsigned), s);
   if (e != cudaSuccess) return e;
   const bool tr = trans == 'T' || trans == 't' || trans == 'C' || trans == 'c';
+  // algorithmic work of one sweep: the triangle (n^2/2 elements) read once,
+  // n^2 flops per right-hand side
+  const double tri_bytes = 0.5 * (double)p.n * (double)p.n * sizeof(T) + 2.0 * p.n * nr * sizeof(T);
+  const double sweep_flops = (double)p.n * (double)p.n * nr;
+  {
+  LaunchScope ls(K_SOLVE, sweep_flops, tri_bytes, s);
   if (!tr)
     solve_fwd_kernel<T, NR, false><<<(unsigned)nblk, kTS, 0, s>>>(
         p.n, p.LU, p.lda, p.perm, B, ldb, p.work, p.n, nr, ffwd, p.scratch);
   else
     solve_fwd_kernel<T, NR, true><<<(unsigned)nblk, kTS, 0, s>>>(
         p.n, p.LU, p.lda, p.perm, B, ldb, p.work, p.n, nr, ffwd, p.scratch);
+  }
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(&p.scratch->ticket, 0, sizeof(unsigned), s);
   if (e != cudaSuccess) return e;
+  LaunchScope ls(K_SOLVE, sweep_flops, tri_bytes, s);
   if (!tr)
     solve_bwd_kernel<T, NR, false><<<(unsigned)nblk, kTS, 0, s>>>(
         p.n, p.LU, p.lda, p.perm, p.work, p.n, B, ldb, nr, fbwd, p.scratch);

@@ -8,6 +8,7 @@
 #include <string>
 
 #include "gblu_internal.h"
+#include "profile.h"
 #include "refine.h"
 
 struct gblu_ctx {
@@ -17,6 +18,7 @@ struct gblu_ctx {
   uint64_t in_use = 0;
   std::recursive_mutex mu;
   std::string last_error;
+  gblu::Profiler prof;
 };
 
 struct gblu_factor {

@@ -15,6 +15,7 @@
 #include "device_util.cuh"
 #include "gblu_internal.h"
 #include "objects.h"
+#include "profile.h"
 #include "refine.h"
 
 namespace gblu {
@@ -252,15 +253,21 @@ cudaError_t gemv(char op, int64_t rows, int64_t cols, const double* A, int64_t l
   if (op == 'N') {
     len = rows;
     dim3 grid((unsigned)((rows + kRowsPerCta - 1) / kRowsPerCta), kSplit);
+    { LaunchScope ls_(K_REFINE, 0.0, 0.0, s);
     gemv_n_partial_kernel<<<grid, kRowsPerCta, 0, s>>>(rows, cols, A, lda, X, ldx, W, P, absval ? 1 : 0);
+    }
   } else {
     len = cols;
     dim3 grid((unsigned)((cols + 7) / 8), kSplit);
+    { LaunchScope ls_(K_REFINE, 0.0, 0.0, s);
     gemv_t_partial_kernel<<<grid, 256, 0, s>>>(rows, cols, A, lda, X, ldx, W, P);
+    }
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
+  { LaunchScope ls_(K_REFINE, 0.0, 0.0, s);
   gemv_reduce_kernel<<<grid_for(len), 256, 0, s>>>(len, W, P, alpha, C, ldc, beta, out, ldo, colmax);
+  }
   return cudaGetLastError();
 }
 
@@ -275,7 +282,9 @@ double bits_to_double(unsigned long long b) {
 cudaError_t refine_prepare(RefineWork& w, int64_t n, const double* A, int64_t lda, float* A32,
                            int64_t ld32, cudaStream_t s) {
   if (n == 0) { w.anorm = 0; return cudaSuccess; }
+  { LaunchScope ls_(K_REFINE, 0.0, 0.0, s);
   convert_f64_f32_kernel<<<grid_for(n * n), 256, 0, s>>>(n, n, A, lda, A32, ld32);
+  }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   // ||A||_inf = max_i sum_j |A[i,j]|
@@ -316,7 +325,9 @@ struct Solver {
   int32_t precond(const double* v, int64_t ldv, double* out, int64_t ldo, int W) {
     std::vector<unsigned long long> bits(W);
     GBLU_CK(ctx, cudaMemsetAsync(w.colmax + 3 * w.W, 0, W * sizeof(unsigned long long), s), "memset");
+    { LaunchScope ls_(K_REFINE, 0.0, 0.0, s);
     colmax_kernel<<<grid_for(n), 256, 0, s>>>(n, W, v, ldv, w.colmax + 3 * w.W);
+    }
     GBLU_CK(ctx, cudaGetLastError(), "colmax");
     GBLU_CK(ctx, cudaMemcpyAsync(bits.data(), w.colmax + 3 * w.W, W * sizeof(unsigned long long),
                                  cudaMemcpyDeviceToHost, s), "colmax readback");
@@ -332,10 +343,14 @@ struct Solver {
     double* dsc = w.anorm_dev;  // 4*W doubles of scale storage
     GBLU_CK(ctx, cudaMemcpyAsync(dsc, sc, 2 * kMaxW * sizeof(double), cudaMemcpyHostToDevice, s),
             "scales");
+    { LaunchScope ls_(K_REFINE, 0.0, 0.0, s);
     scale_to_f32_kernel<<<grid_for(n * W), 256, 0, s>>>(n, W, v, ldv, dsc, w.d32, n);
+    }
     GBLU_CK(ctx, cudaGetLastError(), "scale");
     GBLU_CK(ctx, getrs_launch<float>(f->rs32, trans, W, w.d32, n, nullptr, s), "FP32 getrs");
+    { LaunchScope ls_(K_REFINE, 0.0, 0.0, s);
     update_from_f32_kernel<<<grid_for(n * W), 256, 0, s>>>(n, W, out, ldo, w.d32, n, dsc + kMaxW, 0.0);
+    }
     GBLU_CK(ctx, cudaGetLastError(), "update");
     return GBLU_OK;
   }
@@ -346,7 +361,9 @@ struct Solver {
     GBLU_CK(ctx, gemv(trans == 'N' ? 'N' : 'T', n, n, f->lu64, f->ld, w.x, n, W, -1.0, w.b, n, 1.0,
                       w.r, n, w.partial, w.colmax, s),
             "residual");
+    { LaunchScope ls_(K_REFINE, 0.0, 0.0, s);
     colmax_kernel<<<grid_for(n), 256, 0, s>>>(n, W, w.x, n, w.colmax + w.W);
+    }
     GBLU_CK(ctx, cudaGetLastError(), "colmax");
     std::vector<unsigned long long> bits(2 * w.W);
     GBLU_CK(ctx, cudaMemcpyAsync(bits.data(), w.colmax, 2 * w.W * sizeof(unsigned long long),
@@ -376,7 +393,9 @@ struct Solver {
     }
     *its = 0;
     if (!(beta > 0) || !std::isfinite(beta)) return GBLU_OK;
+    { LaunchScope ls_(K_REFINE, 0.0, 0.0, s);
     axpby_kernel<<<grid_for(n), 256, 0, s>>>(n, 1.0 / beta, V, 0.0, V);
+    }
     const int m = std::max(1, std::min(restart, (int)kGmresRestart));
     std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m), sn(m), g(m + 1, 0.0);
     g[0] = beta;
@@ -426,7 +445,9 @@ struct Solver {
       g[j] = cs[j] * g[j];
       k = j + 1;
       if (hn > 0 && std::isfinite(hn))
+        { LaunchScope ls_(K_REFINE, 0.0, 0.0, s);
         axpby_kernel<<<grid_for(n), 256, 0, s>>>(n, 1.0 / hn, z, 0.0, z);
+        }
       if (std::fabs(g[j + 1]) <= rtol * beta || !(hn > 0)) break;
     }
     *its = k;
@@ -513,7 +534,9 @@ int32_t refine_solve(gblu_ctx* ctx, gblu_factor* f, char trans, int64_t nrhs, do
           e = S.precond(w.r, n, w.r, n, nc);  // d = M^{-1} r (in place), scaled
           if (e) return e;
           for (int q = 0; q < nc; ++q)
+            { LaunchScope ls_(K_REFINE, 0.0, 0.0, s);
             axpby_kernel<<<grid_for(n), 256, 0, s>>>(n, 1.0, w.r + (size_t)q * n, 1.0, w.x + (size_t)q * n);
+            }
           GBLU_CK(ctx, cudaGetLastError(), "update");
         }
       }
@@ -539,7 +562,9 @@ int32_t refine_solve(gblu_ctx* ctx, gblu_factor* f, char trans, int64_t nrhs, do
       if (e) return e;
       // ||b||: one more pass over b
       GBLU_CK(ctx, cudaMemsetAsync(w.colmax + 2 * w.W, 0, nc * sizeof(unsigned long long), s), "memset");
+      { LaunchScope ls_(K_REFINE, 0.0, 0.0, s);
       colmax_kernel<<<grid_for(n), 256, 0, s>>>(n, nc, w.b, n, w.colmax + 2 * w.W);
+      }
       std::vector<unsigned long long> bits(nc);
       GBLU_CK(ctx, cudaMemcpyAsync(bits.data(), w.colmax + 2 * w.W, nc * sizeof(unsigned long long),
                                    cudaMemcpyDeviceToHost, s), "readback");

@@ -39,6 +39,20 @@ class Context:
         check(self.lib.gblu_ctx_memory(self.handle, ctypes.byref(a), ctypes.byref(b)), self.handle)
         return a.value, b.value
 
+    def profile_enable(self, enable: bool = True) -> None:
+        check(self.lib.gblu_profile_enable(self.handle, 1 if enable else 0), self.handle)
+
+    def profile_read(self, reset: bool = False) -> dict:
+        """Launch counts, event-timed ms, flops and bytes per kernel kind."""
+        pr = _lib.Profile()
+        check(self.lib.gblu_profile_read(self.handle, ctypes.byref(pr), 1 if reset else 0),
+              self.handle)
+        out = {"launches": int(pr.launches)}
+        for i, name in enumerate(_lib.KIND_NAMES):
+            out[name] = {"count": int(pr.count[i]), "ms": float(pr.ms[i]),
+                         "flops": float(pr.flops[i]), "bytes": float(pr.bytes[i])}
+        return out
+
     def factor(self, m: int, n: int | None = None, precision: str = "fp64") -> "Factorization":
         return Factorization(self, m, m if n is None else n, precision)
 
