@@ -326,7 +326,13 @@ def run_gpu(args, rank, world, local):
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs", "kernel": dom,
                 "launches": d["count"]}
     tr = profile_traffic(dom)
-    roof["traffic"] = tr
+    if tr and d["count"]:
+        # captured DRAM bytes scale with the algorithmic bytes of a launch
+        roof["traffic"] = tr["ratio_to_algorithmic"] * d["bytes"] / d["count"]
+        roof["traffic_source"] = ("ncu dram__bytes_read+write of one captured launch (%s), scaled "
+                                  "per launch by algorithmic bytes" % tr["captured_launch"])
+    else:
+        roof["traffic"] = None
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
