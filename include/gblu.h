@@ -182,6 +182,25 @@ void gblu_sgetrs_(const char* trans, const int64_t* n, const int64_t* nrhs,
                   const float* A, const int64_t* lda, const int64_t* ipiv, float* B,
                   const int64_t* ldb, int64_t* info, long trans_len);
 
+/* ---- allocation-free solve -------------------------------------------------
+ * No counterpart in the reference.  For callers that must not allocate device
+ * memory: per-step solver loops (e.g. Newton iterations inside an ODE
+ * integrator) where cudaMalloc/cudaFree would synchronise the device, threads
+ * running while a global-mode stream capture is open elsewhere (cudaMalloc is
+ * an error then), and hosts that committed all device memory to a budget.
+ * Solves op(A) X = B in place with factors dLU (lda) and 1-based int64 pivots
+ * d_ipiv from getrf, all three in device memory, on `stream` (NULL: the
+ * default stream); returns when the solve has finished.  It allocates
+ * nothing: its scratch is one fixed ~1.1 MB device array compiled into the
+ * library, held on every device that loads it until the process exits.
+ * Limit: n <= 16384 (larger n returns GBLU_EUNSUPPORTED); any nrhs.  The first
+ * call on a device looks up that array's address; make that call before any
+ * stream capture.  All calls share the one array, so calls that overlap on
+ * the GPU (different streams or threads at once) race; serialise them.
+ * Errors are reported through gblu_last_error(NULL). */
+int32_t gblu_dgetrs_noalloc(char trans, int64_t n, int64_t nrhs, const double* dLU, int64_t lda,
+                            const int64_t* d_ipiv, double* dB, int64_t ldb, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
