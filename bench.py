@@ -382,7 +382,8 @@ def run_mixed_suite(pkg, cu, ctx, args):
     dB0 = pkg.DeviceMatrix.from_host(B)
     dB = pkg.DeviceMatrix(n, nrhs)
     out = {"n": n, "nrhs": nrhs, "A": "G + 4 sqrt(n) I"}
-    for label, prec in (("fp32_ir", "fp32"), ("fp64_plain", "fp64")):
+    for label, prec in (("fp32_ir", "fp32"), ("bf16_ir", "bf16"), ("fp16_ir", "fp16"),
+                        ("fp64_plain", "fp64")):
         f = ctx.factor(n, n, prec)
         reps = 2 if prec == "fp64" else 3
 
@@ -410,7 +411,8 @@ def run_mixed_suite(pkg, cu, ctx, args):
         out[label] = {"ms_per_solve_set": ms, "solves_per_s": nrhs / (ms / 1000), "backward_error": be,
                       "stats": st}
         f.close()
-    out["speedup_fp32_ir_vs_fp64"] = out["fp32_ir"]["solves_per_s"] / out["fp64_plain"]["solves_per_s"]
+    for label in ("fp32_ir", "bf16_ir", "fp16_ir"):
+        out["speedup_%s_vs_fp64" % label] = out[label]["solves_per_s"] / out["fp64_plain"]["solves_per_s"]
     out["bound"] = 10 * n * EPS64
     dA.free(); dB0.free(); dB.free()
     return out

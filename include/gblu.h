@@ -44,6 +44,10 @@ extern "C" {
 /* ---- factor precisions ---------------------------------------------------- */
 #define GBLU_FP64 0 /* plain FP64 LU, FP64 getrs                              */
 #define GBLU_FP32 1 /* FP32 LU, FP64 iterative refinement                      */
+#define GBLU_BF16 2 /* FP32 LU whose trailing updates run on tcgen05 with BF16
+                       operands (FP32 accumulation), FP64 refinement         */
+#define GBLU_FP16 3 /* as GBLU_BF16 with FP16 operands, each column of the
+                       right operand scaled by a power of two              */
 
 /* ---- buffer locations ---------------------------------------------------- */
 #define GBLU_HOST 0
@@ -163,6 +167,19 @@ int32_t gblu_refine_opts_default(gblu_refine_opts* opts);
 int32_t gblu_solve_refined(gblu_ctx* ctx, gblu_factor* f, char trans, int64_t nrhs, double* B,
                            int64_t ldb, int32_t b_loc, const gblu_refine_opts* opts,
                            gblu_refine_stats* stats);
+
+/* The trailing-update contraction of the mixed-precision getrf on its own:
+ * C (m x n, FP32) -= A (m x k) * B (k x n), all column-major FP32 in memory.
+ * precision GBLU_BF16 / GBLU_FP16: operands rounded to 16 bits (FP16 with a
+ * power-of-two scale per column of B), products accumulated in FP32 on the
+ * tensor cores (tcgen05, TMEM accumulator); GBLU_FP32: the FP32 SIMT kernel,
+ * each C element updated by fma in k order.  loc: GBLU_HOST or GBLU_DEVICE
+ * for all three matrices.
+ * Replaces: the Schur update of src/blocked_lufact.jl:186-656 as a standalone
+ * call (A22 -= L21 * U12). */
+int32_t gblu_gemm_update(gblu_ctx* ctx, int32_t precision, int64_t m, int64_t n, int64_t k,
+                         const float* A, int64_t lda, const float* B, int64_t ldb, float* C,
+                         int64_t ldc, int32_t loc);
 
 /* ---- LAPACK-shaped entries ---------------------------------------------------
  * Same argument lists as LAPACK dgetrf_/dgetrs_/sgetrf_/sgetrs_ with 64-bit

@@ -25,6 +25,8 @@ GBLU_ENODEVICE = 8
 
 GBLU_FP64 = 0
 GBLU_FP32 = 1
+GBLU_BF16 = 2
+GBLU_FP16 = 3
 
 GBLU_HOST = 0
 GBLU_DEVICE = 1
@@ -94,6 +96,7 @@ SIGNATURES = {
     "gblu_factor_destroy": (_I32, [_P, _P]),
     "gblu_getrf": (_I32, [_P, _P, _P, _I64, _I32, _PI64]),
     "gblu_getrs": (_I32, [_P, _P, ctypes.c_char, _I64, _P, _I64, _I32]),
+    "gblu_gemm_update": (_I32, [_P, _I32, _I64, _I64, _I64, _P, _I64, _P, _I64, _P, _I64, _I32]),
     "gblu_get_ipiv": (_I32, [_P, _P, _P]),
     "gblu_get_factors": (_I32, [_P, _P, _P, _I64]),
     "gblu_get_info": (_I32, [_P, _P, _PI64]),

@@ -105,7 +105,7 @@ int32_t check_device_errors(gblu_ctx* ctx, std::initializer_list<DevScratch*> sc
       int32_t zero = 0;
       cudaMemcpyAsync(&s->error, &zero, sizeof(zero), cudaMemcpyHostToDevice, ctx->stream);
       cudaStreamSynchronize(ctx->stream);
-      if (err == DEV_TIMEOUT_PANEL || err == DEV_TIMEOUT_SOLVE)
+      if (err == DEV_TIMEOUT_PANEL || err == DEV_TIMEOUT_SOLVE || err == DEV_TIMEOUT_GEMM)
         return fail(ctx, GBLU_ETIMEOUT, "device wait timed out (code %d)", err);
       return fail(ctx, GBLU_EINVAL, "device detected invalid pivot data (code %d)", err);
     }
@@ -283,7 +283,8 @@ int32_t gblu_factor_create(gblu_ctx* ctx, int64_t m, int64_t n, int32_t precisio
   *out = nullptr;
   if (m < 0 || n < 0) return fail(ctx, GBLU_EINVAL, "gblu_factor_create: negative size %lld x %lld",
                                   (long long)m, (long long)n);
-  if (precision != GBLU_FP64 && precision != GBLU_FP32)
+  if (precision != GBLU_FP64 && precision != GBLU_FP32 && precision != GBLU_BF16 &&
+      precision != GBLU_FP16)
     return fail(ctx, GBLU_EUNSUPPORTED, "gblu_factor_create: unknown precision %d", precision);
   if (m > (int64_t)INT32_MAX || n > (int64_t)INT32_MAX)
     return fail(ctx, GBLU_EUNSUPPORTED, "gblu_factor_create: dimension too large");
@@ -298,12 +299,17 @@ int32_t gblu_factor_create(gblu_ctx* ctx, int64_t m, int64_t n, int32_t precisio
   f->precision = precision;
   f->ld = std::max<int64_t>(32, ((m + 31) / 32) * 32);
   size_t bytes;
+  size_t tc_bytes = 0;
   if (precision == GBLU_FP64) {
     bytes = set_bytes<double>(m, n, f->ld, ctx->device, kWorkCols);
   } else {
     bytes = set_bytes<float>(m, n, f->ld, ctx->device, kWorkCols);
     bytes += align256((size_t)f->ld * n * sizeof(double));  // FP64 copy of A
     bytes += refine_bytes(m, kWorkCols);
+    if (precision == GBLU_BF16 || precision == GBLU_FP16) {
+      tc_bytes = align256(tc_work_bytes(n, n / 2 + 64, n / 2 + 64));
+      bytes += tc_bytes;
+    }
   }
   int32_t st = ctx_alloc(ctx, bytes, &f->arena);
   if (st) {
@@ -321,6 +327,13 @@ int32_t gblu_factor_create(gblu_ctx* ctx, int64_t m, int64_t n, int32_t precisio
     f->lu64 = reinterpret_cast<double*>(c);
     c += align256((size_t)f->ld * n * sizeof(double));
     refine_carve(f->refine, c, m, kWorkCols);
+    c += refine_bytes(m, kWorkCols);
+    if (tc_bytes) {
+      f->rf32.tc_mode = precision == GBLU_BF16 ? 1 : 2;
+      f->rf32.tc_work = c;
+      f->rf32.tc_work_bytes = tc_bytes;
+      c += tc_bytes;
+    }
   }
   cudaError_t e = cudaMemsetAsync(f->arena, 0, bytes, ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
@@ -529,6 +542,60 @@ int32_t gblu_solve_refined(gblu_ctx* ctx, gblu_factor* f, char trans, int64_t nr
   DeviceGuard g(ctx->device);
   ActiveProfiler ap(&ctx->prof);
   return refine_solve(ctx, f, trans, nrhs, B, ldb, b_loc, opts, stats);
+}
+
+int32_t gblu_gemm_update(gblu_ctx* ctx, int32_t precision, int64_t m, int64_t n, int64_t k,
+                         const float* A, int64_t lda, const float* B, int64_t ldb, float* C,
+                         int64_t ldc, int32_t loc) {
+  if (!ctx) return fail(ctx, GBLU_EINVAL, "gblu_gemm_update: NULL ctx");
+  if (m < 0 || n < 0 || k < 0) return fail(ctx, GBLU_EINVAL, "gblu_gemm_update: negative size");
+  if (lda < std::max<int64_t>(1, m) || ldb < std::max<int64_t>(1, k) || ldc < std::max<int64_t>(1, m))
+    return fail(ctx, GBLU_EINVAL, "gblu_gemm_update: leading dimension too small");
+  if (precision != GBLU_FP32 && precision != GBLU_BF16 && precision != GBLU_FP16)
+    return fail(ctx, GBLU_EUNSUPPORTED, "gblu_gemm_update: precision must be FP32, BF16 or FP16");
+  if (loc != GBLU_HOST && loc != GBLU_DEVICE) return fail(ctx, GBLU_EINVAL, "gblu_gemm_update: bad loc");
+  if (m == 0 || n == 0 || k == 0) return GBLU_OK;
+  if (!A || !B || !C) return fail(ctx, GBLU_EINVAL, "gblu_gemm_update: NULL pointer");
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  DeviceGuard g(ctx->device);
+  ActiveProfiler ap(&ctx->prof);
+  // device staging for host operands + the conversion buffers + an error word
+  const size_t a_b = align256((size_t)m * k * 4), b_b = align256((size_t)k * n * 4),
+               c_b = align256((size_t)m * n * 4);
+  const size_t w_b = precision == GBLU_FP32 ? 0 : align256(tc_work_bytes(m, n, k));
+  const size_t total = (loc == GBLU_HOST ? a_b + b_b + c_b : 0) + w_b + 256;
+  void* arena = nullptr;
+  int32_t st = ctx_alloc(ctx, total, &arena);
+  if (st) return st;
+  char* c = reinterpret_cast<char*>(arena);
+  int* derr = reinterpret_cast<int*>(c);
+  c += 256;
+  const float *dA = A, *dB = B;
+  float* dC = C;
+  int64_t la = lda, lb = ldb, lc = ldc;
+  cudaError_t e = cudaMemsetAsync(derr, 0, 256, ctx->stream);
+  if (loc == GBLU_HOST) {
+    float* pa = reinterpret_cast<float*>(c); c += a_b;
+    float* pb = reinterpret_cast<float*>(c); c += b_b;
+    float* pc = reinterpret_cast<float*>(c); c += c_b;
+    if (e == cudaSuccess) e = cudaMemcpy2DAsync(pa, m * 4, A, lda * 4, m * 4, k, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpy2DAsync(pb, k * 4, B, ldb * 4, k * 4, n, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpy2DAsync(pc, m * 4, C, ldc * 4, m * 4, n, cudaMemcpyHostToDevice, ctx->stream);
+    dA = pa; dB = pb; dC = pc; la = m; lb = k; lc = m;
+  }
+  if (e == cudaSuccess) {
+    if (precision == GBLU_FP32) e = simt_gemm_sub_f32(m, n, k, dA, la, dB, lb, dC, lc, ctx->stream);
+    else e = tc_gemm_sub(precision == GBLU_BF16 ? 1 : 2, m, n, k, dA, la, dB, lb, dC, lc, c, derr, ctx->stream);
+  }
+  if (e == cudaSuccess && loc == GBLU_HOST)
+    e = cudaMemcpy2DAsync(C, ldc * 4, dC, lc * 4, m * 4, n, cudaMemcpyDeviceToHost, ctx->stream);
+  int herr = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  ctx_free(ctx, arena, total);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "gblu_gemm_update");
+  if (herr) return fail(ctx, GBLU_ETIMEOUT, "gblu_gemm_update: device wait timed out (code %d)", herr);
+  return GBLU_OK;
 }
 
 int32_t gblu_get_ipiv(gblu_ctx* ctx, gblu_factor* f, int64_t* ipiv_host) {

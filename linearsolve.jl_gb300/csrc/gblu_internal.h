@@ -24,6 +24,7 @@ enum : int32_t {
   DEV_TIMEOUT_PANEL = 1,    // grid barrier in the panel kernel gave up
   DEV_TIMEOUT_SOLVE = 2,    // a getrs block row waited too long for a predecessor
   DEV_BAD_PIVOT_INDEX = 3,  // ipiv entry out of range (corrupt input)
+  DEV_TIMEOUT_GEMM = 4,     // tcgen05 GEMM pipeline wait gave up
 };
 
 // Scratch words used by the cooperative panel kernel and the wavefront solve.
@@ -72,13 +73,29 @@ struct GetrfPlan {
   int panel_width = 32;      // leaf width of the recursion
   int panel_ctas = 0;        // CTAs of the cooperative panel kernel (0: auto)
   int trsm_base = 64;        // base size of the recursive TRSM
+  // FP32 working matrix only: trailing updates on tcgen05 with 16-bit operands
+  int tc_mode = 0;           // 0 SIMT FP32, 1 BF16 operands, 2 FP16 operands (scaled)
+  void* tc_work = nullptr;   // conversion buffers for the operands
+  size_t tc_work_bytes = 0;
 };
+
+// FP32 SIMT update C -= A * B in the reference's per-element order (getrf.cu).
+cudaError_t simt_gemm_sub_f32(int64_t M, int64_t N, int64_t K, const float* A, int64_t lda,
+                              const float* B, int64_t ldb, float* C, int64_t ldc, cudaStream_t s);
+
+// tcgen05 trailing update C -= round16(A) * round16(B) (gemm_tc.cu).
+size_t tc_work_bytes(int64_t M, int64_t N, int64_t K);
+void tc_configure(int device);
+cudaError_t tc_gemm_sub(int mode, int64_t M, int64_t N, int64_t K, const float* A, int64_t lda,
+                        const float* B, int64_t ldb, float* C, int64_t ldc, void* work, int* err,
+                        cudaStream_t s);
 
 template <typename T>
 cudaError_t getrf_launch(const GetrfPlan<T>& p, cudaStream_t stream);
 
 // Per-device kernel attributes (shared-memory opt-in); once per device, outside capture.
 void getrf_configure(int device);
+void getrs_configure(int device);
 cudaError_t perm_build_launch(const int64_t* ipiv, int64_t kmax, int64_t m, int32_t* perm,
                               DevScratch* scr, cudaStream_t s);
 

@@ -1,0 +1,413 @@
+// Trailing update C -= A * B on the 5th-generation tensor cores (tcgen05).
+//
+// The mixed-precision getrf stores its working matrix in FP32; the trailing
+// update -- the one dense contraction of LU (src/blocked_lufact.jl:186-656,
+// A22 -= L21 * U12) -- rounds its two operands to BF16 or FP16 and accumulates
+// in FP32 in tensor memory:
+//
+//   1. conversion kernels write A (M x K) and B (K x N) as K-major 16-bit
+//      copies (FP16: each column of B scaled by an exact power of two so that
+//      its largest entry lies in [2^14, 2^15); |L21| <= 1 needs no scale);
+//   2. tc_gemm_kernel: per 128 x 128 output tile, one warp issues TMA loads
+//      (128-byte swizzled 128 x 64 boxes, 4-stage mbarrier ring), one thread
+//      issues tcgen05.mma (M=128, N=128, K=16 per instruction) into a
+//      128-column FP32 accumulator in TMEM, and four warps read the
+//      accumulator back with tcgen05.ld and apply C -= acc * 2^-s in the
+//      epilogue (coalesced along the column-major C).
+//
+// All mbarrier waits are bounded (globaltimer, 2 s); an expired wait records
+// DEV_TIMEOUT_GEMM, every CTA then skips to its teardown and frees TMEM.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <mutex>
+#include <type_traits>
+
+#include "device_util.cuh"
+#include "gblu_internal.h"
+#include "profile.h"
+
+namespace gblu {
+namespace tc {
+
+constexpr int BM = 128, BN = 128, BK = 64, STAGES = 4, THREADS = 192;
+constexpr int UMMA_K = 16;
+constexpr uint32_t A_BYTES = BM * BK * 2;
+constexpr uint32_t B_BYTES = BN * BK * 2;
+constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
+constexpr uint32_t TMEM_COLS = 128;
+constexpr size_t SMEM_BYTES = (size_t)STAGES * STAGE_BYTES + 1024 + 256;
+
+__device__ __forceinline__ uint32_t saddr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint32_t a, uint32_t cnt) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(cnt) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t a, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(a), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint32_t a, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(a), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait; false when it gave up (error recorded) or another CTA failed.
+__device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity, int* err) {
+  unsigned long long t0 = 0;
+  for (uint32_t it = 0;; ++it) {
+    if (mbar_try(a, parity)) return true;
+    if ((it & 127u) == 0) {
+      if (ld_volatile_i32(err) != 0) return false;
+      const unsigned long long now = global_ns();
+      if (t0 == 0) t0 = now;
+      else if (now - t0 > kSpinTimeoutNs) {
+        atomicCAS(err, 0, (int)DEV_TIMEOUT_GEMM);
+        return false;
+      }
+    }
+  }
+}
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y,
+                                            uint32_t mbar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(mbar)
+      : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_alloc(uint32_t slot, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot),
+               "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish() {
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
+                                       uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void tc_commit(uint32_t mbar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+      : "memory");
+}
+__device__ __forceinline__ void tmem_ld_32cols(uint32_t taddr, uint32_t (&v)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+        "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]),
+        "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]),
+        "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// Shared-memory matrix descriptor: K-major operand tile whose rows are 128
+// bytes (64 16-bit elements) with the 128-byte swizzle; 8-row groups are
+// 1024 bytes apart (stride byte offset); the leading byte offset is unused
+// for swizzled K-major layouts.
+__device__ __forceinline__ uint64_t sdesc_k128(uint32_t a) {
+  return (uint64_t)((a & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+// Instruction descriptor, kind::f16: D = F32, A/B = F16 (fmt 0) or BF16 (fmt 1),
+// both K-major, N = BN, M = BM.
+__host__ __device__ constexpr uint32_t idesc_f16(uint32_t fmt) {
+  return (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(BN >> 3) << 17) |
+         ((uint32_t)(BM >> 4) << 24);
+}
+
+template <uint32_t FMT>
+__global__ void __launch_bounds__(THREADS, 1)
+tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+               float* __restrict__ C, int64_t ldc, int M, int N, int K,
+               const float* __restrict__ inv_scale, int* __restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem =
+      reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);
+  uint64_t* full = bars;
+  uint64_t* empty = bars + STAGES;
+  uint64_t* tfull = bars + 2 * STAGES;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+  const int kblocks = (K + BK - 1) / BK;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(saddr(&full[s]), 1);
+      mbar_init(saddr(&empty[s]), 1);
+    }
+    mbar_init(saddr(tfull), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    tmem_alloc(saddr(tslot), TMEM_COLS);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tbase = *tslot;
+
+  if (warp == 0 && lane == 0) {
+    // TMA producer
+    for (int kb = 0; kb < kblocks; ++kb) {
+      const int s = kb % STAGES;
+      if (kb >= STAGES && !mbar_wait(saddr(&empty[s]), ((kb / STAGES) & 1) ^ 1, err)) break;
+      const uint32_t a_dst = saddr(smem + s * STAGE_BYTES);
+      const uint32_t b_dst = a_dst + A_BYTES;
+      mbar_expect_tx(saddr(&full[s]), STAGE_BYTES);
+      tma_load_2d(a_dst, &tmA, kb * BK, m0, saddr(&full[s]));
+      tma_load_2d(b_dst, &tmB, kb * BK, n0, saddr(&full[s]));
+    }
+  } else if (warp == 1 && lane == 0) {
+    // MMA issuer
+    constexpr uint32_t idesc = idesc_f16(FMT);
+    bool ok = true;
+    for (int kb = 0; kb < kblocks && ok; ++kb) {
+      const int s = kb % STAGES;
+      if (!mbar_wait(saddr(&full[s]), (kb / STAGES) & 1, err)) { ok = false; break; }
+      tc_fence_after();
+      const uint32_t a_base = saddr(smem + s * STAGE_BYTES);
+      const uint32_t b_base = a_base + A_BYTES;
+#pragma unroll
+      for (int k = 0; k < BK / UMMA_K; ++k) {
+        const uint64_t ad = sdesc_k128(a_base + k * UMMA_K * 2);
+        const uint64_t bd = sdesc_k128(b_base + k * UMMA_K * 2);
+        tc_mma(tbase, ad, bd, idesc, (kb > 0 || k > 0) ? 1u : 0u);
+      }
+      tc_commit(saddr(&empty[s]));  // stage s is free once these MMAs have read it
+    }
+    tc_commit(saddr(tfull));  // accumulator complete (or abandoned)
+  } else if (warp >= 2) {
+    // epilogue: TMEM lanes [32*(warp%4), +32) are this warp's rows
+    const int q = warp & 3;
+    if (mbar_wait(saddr(tfull), 0, err)) {
+      tc_fence_after();
+      const int row = m0 + q * 32 + lane;
+#pragma unroll 1
+      for (int c0 = 0; c0 < BN; c0 += 32) {
+        uint32_t v[32];
+        tmem_ld_32cols(tbase + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, v);
+        if (row < M) {
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const int col = n0 + c0 + j;
+            if (col < N) {
+              float a = __uint_as_float(v[j]);
+              if (inv_scale) a *= inv_scale[col];
+              float* cp = C + (int64_t)row + (int64_t)col * ldc;
+              *cp = *cp - a;
+            }
+          }
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    tmem_dealloc(tbase, TMEM_COLS);
+  }
+}
+
+// A (M x K, column-major, lda) -> Ah (M rows of K, row-major, ldh): 32 x 32
+// tiles through shared memory so both sides are coalesced.
+template <typename H>
+__global__ void conv_a_kernel(int M, int K, const float* __restrict__ A, int64_t lda,
+                              H* __restrict__ Ah, int64_t ldh) {
+  __shared__ float t[32][33];
+  const int k0 = blockIdx.x * 32, m0 = blockIdx.y * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
+  for (int i = ty; i < 32; i += 8) {
+    const int k = k0 + i, m = m0 + tx;
+    t[i][tx] = (k < K && m < M) ? A[(int64_t)m + (int64_t)k * lda] : 0.f;
+  }
+  __syncthreads();
+  for (int i = ty; i < 32; i += 8) {
+    const int m = m0 + i, k = k0 + tx;
+    if (m < M && k < ldh) {
+      const float v = (k < K) ? t[tx][i] : 0.f;
+      if constexpr (sizeof(H) == 2 && std::is_same<H, __nv_bfloat16>::value)
+        Ah[(int64_t)m * ldh + k] = __float2bfloat16_rn(v);
+      else
+        Ah[(int64_t)m * ldh + k] = __float2half_rn(v);
+    }
+  }
+}
+
+// B (K x N, column-major, ldb) -> Bh (N rows of K, ldh), row n scaled by scale[n].
+template <typename H>
+__global__ void conv_b_kernel(int K, int N, const float* __restrict__ B, int64_t ldb,
+                              H* __restrict__ Bh, int64_t ldh, const float* __restrict__ scale) {
+  const int n = blockIdx.x;
+  if (n >= N) return;
+  const float s = scale ? scale[n] : 1.f;
+  for (int k = threadIdx.x; k < ldh; k += blockDim.x) {
+    const float v = (k < K) ? B[(int64_t)k + (int64_t)n * ldb] * s : 0.f;
+    if constexpr (std::is_same<H, __nv_bfloat16>::value)
+      Bh[(int64_t)n * ldh + k] = __float2bfloat16_rn(v);
+    else
+      Bh[(int64_t)n * ldh + k] = __float2half_rn(v);
+  }
+}
+
+// Per-column power-of-two scale for FP16: max |B[:,n]| -> [2^14, 2^15).
+__global__ void col_scale_kernel(int K, int N, const float* __restrict__ B, int64_t ldb,
+                                 float* __restrict__ scale, float* __restrict__ inv_scale) {
+  __shared__ float red[8];
+  const int n = blockIdx.x;
+  if (n >= N) return;
+  float mx = 0.f;
+  for (int k = threadIdx.x; k < K; k += blockDim.x) mx = fmaxf(mx, fabsf(B[(int64_t)k + (int64_t)n * ldb]));
+  for (int off = 16; off; off >>= 1) mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, off));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float m = 0.f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmaxf(m, red[w]);
+    int e = 0;
+    if (m > 0.f && isfinite(m)) e = ilogbf(m) - 14;  // m * 2^-e in [2^14, 2^15)
+    e = max(-120, min(120, e));
+    scale[n] = ldexpf(1.f, -e);
+    inv_scale[n] = ldexpf(1.f, e);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static std::once_flag once;
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  return fn;
+}
+
+// 2D K-major map: rows of `inner` 16-bit elements, `outer` rows, pitch in bytes.
+bool make_map(CUtensorMap* m, const void* base, uint64_t inner, uint64_t outer, uint64_t pitch_bytes,
+              bool bf16) {
+  auto fn = encode_fn();
+  if (!fn) return false;
+  if ((reinterpret_cast<uintptr_t>(base) & 15) || (pitch_bytes & 15)) return false;
+  cuuint64_t dims[2] = {inner, outer};
+  cuuint64_t strides[1] = {pitch_bytes};
+  cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)BM};
+  cuuint32_t es[2] = {1, 1};
+  CUresult r = fn(m, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2,
+                  const_cast<void*>(base), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+}  // namespace tc
+
+size_t tc_work_bytes(int64_t M, int64_t N, int64_t K) {
+  const int64_t Kp = ((K + 7) / 8) * 8;
+  return (size_t)(M * Kp + N * Kp) * 2 + 2 * (size_t)N * sizeof(float) + 1024;
+}
+
+void tc_configure(int /*device*/) {
+  cudaFuncSetAttribute(tc::tc_gemm_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::SMEM_BYTES);
+  cudaFuncSetAttribute(tc::tc_gemm_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::SMEM_BYTES);
+}
+
+// C (M x N, FP32, ldc) -= round16(A) (M x K, FP32 col-major, lda) * round16(B) (K x N, ldb).
+// mode: 1 = BF16 operands, 2 = FP16 operands with per-column power-of-two scaling.
+// work: tc_work_bytes(M, N, K) bytes of device scratch (256-byte aligned).
+cudaError_t tc_gemm_sub(int mode, int64_t M, int64_t N, int64_t K, const float* A, int64_t lda,
+                        const float* B, int64_t ldb, float* C, int64_t ldc, void* work, int* err,
+                        cudaStream_t s) {
+  if (M <= 0 || N <= 0 || K <= 0) return cudaSuccess;
+  if (M > INT32_MAX || N > INT32_MAX || K > INT32_MAX) return cudaErrorInvalidValue;
+  const bool bf16 = mode == 1;
+  const int64_t Kp = ((K + 7) / 8) * 8;
+  unsigned char* w = reinterpret_cast<unsigned char*>(work);
+  void* Ah = w;
+  void* Bh = w + (((size_t)M * Kp * 2 + 255) & ~size_t(255));
+  float* scale = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(Bh) +
+                                          (((size_t)N * Kp * 2 + 255) & ~size_t(255)));
+  float* inv_scale = scale + N;
+  {
+    LaunchScope ls(K_GEMM, 0.0, (double)(M * K + K * N) * 6.0, s);
+    dim3 ga((unsigned)((Kp + 31) / 32), (unsigned)((M + 31) / 32));
+    if (bf16)
+      tc::conv_a_kernel<__nv_bfloat16><<<ga, 256, 0, s>>>((int)M, (int)K, A, lda,
+                                                          reinterpret_cast<__nv_bfloat16*>(Ah), Kp);
+    else
+      tc::conv_a_kernel<__half><<<ga, 256, 0, s>>>((int)M, (int)K, A, lda, reinterpret_cast<__half*>(Ah), Kp);
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  {
+    LaunchScope ls(K_GEMM, 0.0, (double)(K * N) * 6.0, s);
+    if (bf16) {
+      tc::conv_b_kernel<__nv_bfloat16><<<(unsigned)N, 256, 0, s>>>(
+          (int)K, (int)N, B, ldb, reinterpret_cast<__nv_bfloat16*>(Bh), Kp, nullptr);
+    } else {
+      tc::col_scale_kernel<<<(unsigned)N, 256, 0, s>>>((int)K, (int)N, B, ldb, scale, inv_scale);
+      tc::conv_b_kernel<__half><<<(unsigned)N, 256, 0, s>>>((int)K, (int)N, B, ldb,
+                                                             reinterpret_cast<__half*>(Bh), Kp, scale);
+    }
+  }
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  CUtensorMap ta, tb;
+  if (!tc::make_map(&ta, Ah, (uint64_t)K, (uint64_t)M, (uint64_t)Kp * 2, bf16) ||
+      !tc::make_map(&tb, Bh, (uint64_t)K, (uint64_t)N, (uint64_t)Kp * 2, bf16))
+    return cudaErrorInvalidValue;
+  dim3 grid((unsigned)((M + tc::BM - 1) / tc::BM), (unsigned)((N + tc::BN - 1) / tc::BN));
+  LaunchScope ls(K_GEMM, 2.0 * M * N * K, (2.0 * M * N + (double)(M + N) * K / 2.0) * 4.0, s);
+  if (bf16)
+    tc::tc_gemm_kernel<1><<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(ta, tb, C, ldc, (int)M, (int)N, (int)K,
+                                                                     nullptr, err);
+  else
+    tc::tc_gemm_kernel<0><<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(ta, tb, C, ldc, (int)M, (int)N, (int)K,
+                                                                     inv_scale, err);
+  return cudaGetLastError();
+}
+
+}  // namespace gblu

@@ -20,6 +20,7 @@
 // are bit-identical to the reference's blocked LU for any blocking.
 #include <algorithm>
 #include <cstdio>
+#include <type_traits>
 
 #include "device_util.cuh"
 #include "gblu_internal.h"
@@ -269,42 +270,36 @@ laswp_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t ncols_total
 
 // ---------------------------------------------------------------------------
 // Unit-lower TRSM base case: B[0:k, cols] := L \ B with L = k x k (k <= 64)
-// held in shared memory; one thread per right-hand-side column, forward
-// substitution k ascending (blocked_lufact.jl:146-178 order).
+// held in shared memory.  One warp per right-hand-side column: lane l holds
+// rows l and l + 32 in registers; x_kk is broadcast with a shuffle and every
+// row below it is updated, kk ascending (blocked_lufact.jl:146-178 order).
 constexpr int kTrsmMax = 64;
-constexpr int kTrsmCols = 128;
+constexpr int kTrsmWarps = 8;
 
 template <typename T>
-__global__ void __launch_bounds__(kTrsmCols)
+__global__ void __launch_bounds__(kTrsmWarps * 32)
 trsm_lunit_kernel(const T* __restrict__ L, int64_t ldl, int k, T* __restrict__ B,
                   int64_t ldb, int64_t ncols) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* sL = reinterpret_cast<T*>(smem_raw);       // [k][k], column c at sL + c*k
-  T* sB = sL + kTrsmMax * kTrsmMax;             // [k][kTrsmCols], row i at sB + i*kTrsmCols
-  const int tid = threadIdx.x;
-  const int64_t col0 = (int64_t)blockIdx.x * kTrsmCols;
-  const int nc = (int)min((int64_t)kTrsmCols, ncols - col0);
-  for (int idx = tid; idx < k * k; idx += blockDim.x) {
+  __shared__ T sL[kTrsmMax][kTrsmMax + 1];  // sL[c][r] = L[r, c]
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int idx = threadIdx.x; idx < k * k; idx += blockDim.x) {
     int c = idx / k, r = idx - c * k;
-    sL[idx] = L[r + (int64_t)c * ldl];
-  }
-  for (int idx = tid; idx < k * nc; idx += blockDim.x) {
-    int c = idx / k, r = idx - c * k;
-    sB[r * kTrsmCols + c] = B[r + (col0 + c) * ldb];
+    sL[c][r] = L[r + (int64_t)c * ldl];
   }
   __syncthreads();
-  if (tid < nc) {
-    for (int kk = 0; kk < k; ++kk) {
-      const T bk = sB[kk * kTrsmCols + tid];
-      const T* lc = sL + kk * k;
-      for (int i = kk + 1; i < k; ++i)
-        sB[i * kTrsmCols + tid] = fma(-lc[i], bk, sB[i * kTrsmCols + tid]);
+  const int r0 = lane, r1 = lane + 32;
+  for (int64_t col = (int64_t)blockIdx.x * kTrsmWarps + warp; col < ncols;
+       col += (int64_t)gridDim.x * kTrsmWarps) {
+    T* b = B + col * ldb;
+    T b0 = r0 < k ? b[r0] : T(0);
+    T b1 = r1 < k ? b[r1] : T(0);
+    for (int kk = 0; kk < k - 1; ++kk) {
+      const T xk = __shfl_sync(0xffffffffu, kk < 32 ? b0 : b1, kk & 31);
+      if (r0 > kk && r0 < k) b0 = fma(-sL[kk][r0], xk, b0);
+      if (r1 > kk && r1 < k) b1 = fma(-sL[kk][r1], xk, b1);
     }
-  }
-  __syncthreads();
-  for (int idx = tid; idx < k * nc; idx += blockDim.x) {
-    int c = idx / k, r = idx - c * k;
-    B[r + (col0 + c) * ldb] = sB[r * kTrsmCols + c];
+    if (r0 < k) b[r0] = b0;
+    if (r1 < k) b[r1] = b1;
   }
 }
 
@@ -496,6 +491,13 @@ struct Driver {
   void gemm(int64_t M, int64_t N, int64_t K, const T* A, int64_t lda, const T* B, int64_t ldb,
             T* C, int64_t ldc) {
     if (M <= 0 || N <= 0 || K <= 0) return;
+    if constexpr (std::is_same<T, float>::value) {
+      if (p.tc_mode != 0 && M >= 128 && N >= 128 && K >= 64 &&
+          tc_work_bytes(M, N, K) <= p.tc_work_bytes) {
+        check(tc_gemm_sub(p.tc_mode, M, N, K, A, lda, B, ldb, C, ldc, p.tc_work, &p.scratch->error, s));
+        return;
+      }
+    }
     dim3 grid((unsigned)((M + kGBM - 1) / kGBM), (unsigned)((N + kGBN - 1) / kGBN));
     LaunchScope ls(K_GEMM, 2.0 * M * N * K, (2.0 * M * N + (double)M * K + (double)K * N) * sizeof(T), s);
     gemm_sub_kernel<T><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc);
@@ -506,11 +508,12 @@ struct Driver {
   void trsm(int64_t r0, int64_t k, int64_t bc0, int64_t ncols) {
     if (k <= 0 || ncols <= 0) return;
     if (k <= p.trsm_base && k <= kTrsmMax) {
-      size_t smem = (size_t)(kTrsmMax * kTrsmMax + kTrsmMax * kTrsmCols) * sizeof(T);
-      unsigned blocks = (unsigned)((ncols + kTrsmCols - 1) / kTrsmCols);
+      const DeviceInfo& di = device_info(device);
+      unsigned blocks = (unsigned)std::min<int64_t>((ncols + kTrsmWarps - 1) / kTrsmWarps,
+                                                    (int64_t)di.num_sms * 8);
       LaunchScope ls(K_TRSM, (double)k * (k - 1) * ncols, (2.0 * k * ncols + (double)k * k) * sizeof(T), s);
-      trsm_lunit_kernel<T><<<blocks, kTrsmCols, smem, s>>>(at(r0, r0), p.lda, (int)k,
-                                                           at(r0, bc0), p.lda, ncols);
+      trsm_lunit_kernel<T><<<blocks, kTrsmWarps * 32, 0, s>>>(at(r0, r0), p.lda, (int)k,
+                                                              at(r0, bc0), p.lda, ncols);
       check(cudaGetLastError());
       return;
     }
@@ -538,6 +541,15 @@ struct Driver {
 
 }  // namespace
 
+cudaError_t simt_gemm_sub_f32(int64_t M, int64_t N, int64_t K, const float* A, int64_t lda,
+                              const float* B, int64_t ldb, float* C, int64_t ldc, cudaStream_t s) {
+  if (M <= 0 || N <= 0 || K <= 0) return cudaSuccess;
+  dim3 grid((unsigned)((M + kGBM - 1) / kGBM), (unsigned)((N + kGBN - 1) / kGBN));
+  LaunchScope ls(K_GEMM, 2.0 * M * N * K, (2.0 * M * N + (double)M * K + (double)K * N) * 4.0, s);
+  gemm_sub_kernel<float><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc);
+  return cudaGetLastError();
+}
+
 cudaError_t perm_build_launch(const int64_t* ipiv, int64_t kmax, int64_t m, int32_t* perm,
                               DevScratch* scr, cudaStream_t s) {
   size_t smem = m <= kPermSmemMax ? (size_t)m * sizeof(int32_t) : 0;
@@ -551,11 +563,10 @@ void getrf_configure(int device) {
   const int cap = (int)std::min<size_t>(di.smem_optin, 200 * 1024);
   cudaFuncSetAttribute(panel_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
   cudaFuncSetAttribute(panel_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
-  const int tsm = (kTrsmMax * kTrsmMax + kTrsmMax * kTrsmCols) * (int)sizeof(double);
-  cudaFuncSetAttribute(trsm_lunit_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsm);
-  cudaFuncSetAttribute(trsm_lunit_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsm / 2);
   cudaFuncSetAttribute(perm_from_ipiv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        kPermSmemMax * (int)sizeof(int32_t));
+  getrs_configure(device);
+  tc_configure(device);
 }
 
 template <typename T>

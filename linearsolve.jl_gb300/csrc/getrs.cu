@@ -50,162 +50,209 @@ __device__ __forceinline__ bool wait_flag(const int32_t* flags, int j, DevScratc
   return ok != 0;
 }
 
-// Load tile (rows r0.., cols c0..) of op(LU) into shared memory as t[c][r]
-// (element op(LU)[r0 + r, c0 + c]).  trans: op(LU)[i,j] = LU[j,i].
+constexpr int kSweepThreads = 128;  // all issue copies; threads 0..63 own one row each
+constexpr int kStages = 3;          // tiles in flight per CTA
+
+template <typename T>
+__device__ __forceinline__ void cp_async_elem(T* dst, const T* src, bool valid) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  const int sz = valid ? (int)sizeof(T) : 0;  // 0: zero-fill, nothing read
+  if (sizeof(T) == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(d), "l"(src), "r"(sz) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(d), "l"(src), "r"(sz) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// Issue the copies of tile element (r, c) = op(LU)[r0 + r, c0 + c] into t[c][r];
+// 'N': LU[r0+r + (c0+c)*lda] (contiguous in r), 'T': LU[c0+c + (r0+r)*lda]
+// (contiguous in c).  Elements outside nr x nc are zero-filled.
 template <typename T, bool TRANS>
-__device__ __forceinline__ void load_tile(T (*t)[kTS + 1], const T* __restrict__ LU, int64_t lda,
-                                          int64_t n, int64_t r0, int64_t c0, int nr, int nc) {
-#pragma unroll 16
-  for (int idx = threadIdx.x; idx < kTS * kTS; idx += blockDim.x) {
-    int a = idx >> 6, b = idx & 63;  // b fastest -> contiguous in memory
-    if (!TRANS) {                    // element (r = b, c = a): LU[r0+b, c0+a]
-      t[a][b] = (b < nr && a < nc) ? LU[(r0 + b) + (c0 + a) * lda] : T(0);
-    } else {                         // element (r = a, c = b): LU[c0+b, r0+a]
-      t[b][a] = (a < nr && b < nc) ? LU[(c0 + b) + (r0 + a) * lda] : T(0);
-    }
+__device__ __forceinline__ void issue_tile(T (*t)[kTS + 1], const T* __restrict__ LU, int64_t lda,
+                                           int64_t r0, int64_t c0, int nr, int nc) {
+#pragma unroll 8
+  for (int idx = threadIdx.x; idx < kTS * kTS; idx += kSweepThreads) {
+    const int a = idx >> 6, b = idx & 63;  // b runs along the contiguous direction
+    const int r = TRANS ? a : b, c = TRANS ? b : a;
+    const bool ok = r < nr && c < nc;
+    const T* src = ok ? (TRANS ? LU + (c0 + c) + (r0 + r) * lda : LU + (r0 + r) + (c0 + c) * lda) : LU;
+    cp_async_elem(&t[c][r], src, ok);
   }
 }
 
-// Forward sweep with a unit-lower (trans 'N': L) or non-unit-lower
-// (trans 'T': U^T) triangle.  Input row i of the RHS is In[src(i)] where
-// src = perm for 'N' and identity for 'T'; the result goes to Y.
-template <typename T, int NR, bool TRANS>
-__global__ void __launch_bounds__(kTS)
-solve_fwd_kernel(int64_t n, const T* __restrict__ LU, int64_t lda, const int32_t* __restrict__ perm,
-                 const T* __restrict__ In, int64_t ldi, T* __restrict__ Y, int64_t ldy, int nrhs,
-                 int32_t* __restrict__ flags, DevScratch* __restrict__ scr) {
-  __shared__ T tile[kTS][kTS + 1];
+// One triangular sweep over 64-row block rows.
+//   FWD  : block rows first-to-last, columns ascending; 'N' unit-lower L with
+//          the right-hand side gathered through perm, 'T' non-unit U^T.
+//   !FWD : block rows last-to-first, columns descending; 'N' non-unit U,
+//          'T' unit L^T; results also scattered to Out (through perm for 'T').
+// Each row accumulates its updates in exactly the reference's order; the
+// diagonal block is solved by warp shuffles (no block barrier per column).
+template <typename T, int NR, bool TRANS, bool FWD>
+__global__ void __launch_bounds__(kSweepThreads)
+solve_sweep_kernel(int64_t n, const T* __restrict__ LU, int64_t lda, const int32_t* __restrict__ perm,
+                   const T* __restrict__ In, int64_t ldi, T* __restrict__ Y, int64_t ldy,
+                   T* __restrict__ Out, int64_t ldo, int nrhs, int32_t* __restrict__ flags,
+                   DevScratch* __restrict__ scr) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T(*tiles)[kTS][kTS + 1] = reinterpret_cast<T(*)[kTS][kTS + 1]>(smem_raw);
   __shared__ T sx[kTS][NR];
   __shared__ int s_blk;
-  if (threadIdx.x == 0) s_blk = (int)atomicAdd(&scr->ticket, 1u);
+  constexpr bool kUnit = FWD != TRANS;  // fwd 'N' (L) and bwd 'T' (L^T) have unit diagonals
+  const int nblk = (int)((n + kTS - 1) / kTS);
+  if (threadIdx.x == 0) {
+    const int t = (int)atomicAdd(&scr->ticket, 1u);
+    s_blk = FWD ? t : nblk - 1 - t;
+  }
   __syncthreads();
   const int blk = s_blk;
   const int64_t r0 = (int64_t)blk * kTS;
   const int nr = (int)min((int64_t)kTS, n - r0);
-  const int r = threadIdx.x;
-  const int64_t row = r0 + r;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int r = tid;  // row within the block (threads 0..63)
   const bool valid = r < nr;
   T acc[NR];
 #pragma unroll
   for (int q = 0; q < NR; ++q) {
-    int64_t src = valid ? (TRANS ? row : (int64_t)perm[row]) : 0;
-    acc[q] = (valid && q < nrhs) ? In[src + q * ldi] : T(0);
-  }
-  for (int j = 0; j < blk; ++j) {
-    const int64_t c0 = (int64_t)j * kTS;
-    load_tile<T, TRANS>(tile, LU, lda, n, r0, c0, nr, kTS);
-    if (!wait_flag(flags, j, scr)) return;
-    for (int idx = threadIdx.x; idx < kTS * NR; idx += blockDim.x) {
-      int c = idx / NR, q = idx - c * NR;
-      sx[c][q] = q < nrhs ? ldcg(&Y[(c0 + c) + q * ldy]) : T(0);
+    acc[q] = T(0);
+    if (valid && q < nrhs) {
+      if (FWD) acc[q] = In[(TRANS ? r0 + r : (int64_t)perm[r0 + r]) + q * ldi];
+      else acc[q] = Y[(r0 + r) + q * ldy];
     }
+  }
+  const int noff = FWD ? blk : nblk - 1 - blk;  // off-diagonal tiles of this block row
+  const int ntiles = noff + 1;                  // + the diagonal tile
+  auto col_block = [&](int t) -> int { return t < noff ? (FWD ? t : nblk - 1 - t) : blk; };
+  auto issue = [&](int t) {
+    const int cb = col_block(t);
+    const int64_t c0 = (int64_t)cb * kTS;
+    const int nc = (int)min((int64_t)kTS, n - c0);
+    issue_tile<T, TRANS>(tiles[t % kStages], LU, lda, r0, c0, nr, nc);
+  };
+#pragma unroll
+  for (int t = 0; t < kStages - 1; ++t) {
+    if (t < ntiles) issue(t);
+    cp_async_commit();
+  }
+  for (int t = 0; t < ntiles; ++t) {
+    if (t + kStages - 1 < ntiles) issue(t + kStages - 1);
+    cp_async_commit();
+    cp_async_wait<kStages - 1>();
     __syncthreads();
+    T(*tile)[kTS + 1] = tiles[t % kStages];
+    if (t < noff) {
+      const int cb = col_block(t);
+      const int64_t c0 = (int64_t)cb * kTS;
+      const int nc = (int)min((int64_t)kTS, n - c0);
+      if (!wait_flag(flags, cb, scr)) {
+        cp_async_wait<0>();  // no copy may land after the CTA has left
+        return;
+      }
+      for (int idx = tid; idx < kTS * NR; idx += kSweepThreads) {
+        const int c = idx / NR, q = idx - c * NR;
+        sx[c][q] = (q < nrhs && c < nc) ? ldcg(&Y[(c0 + c) + q * ldy]) : T(0);
+      }
+      __syncthreads();
+      if (tid < kTS) {
+        if (FWD) {
 #pragma unroll 8
-    for (int c = 0; c < kTS; ++c) {
-      const T l = tile[c][r];
+          for (int c = 0; c < kTS; ++c) {
+            const T l = tile[c][r];
 #pragma unroll
-      for (int q = 0; q < NR; ++q) acc[q] = fma(-l, sx[c][q], acc[q]);
+            for (int q = 0; q < NR; ++q) acc[q] = fma(-l, sx[c][q], acc[q]);
+          }
+        } else {
+          for (int c = nc - 1; c >= 0; --c) {
+            const T u = tile[c][r];
+#pragma unroll
+            for (int q = 0; q < NR; ++q) acc[q] = fma(-u, sx[c][q], acc[q]);
+          }
+        }
+      }
+      __syncthreads();
+      continue;
+    }
+    // ---- diagonal block: warp shuffles within each 32-row half ----
+    const int w_first = FWD ? 0 : 1, w_second = FWD ? 1 : 0;
+    const int lo_second = FWD ? 32 : 0;  // first row of the second half
+    (void)lo_second;
+    if (warp == w_first) {
+      // columns of the first half, in sweep order
+      const int cbeg = FWD ? 0 : min(nr, kTS) - 1;
+      const int cend = FWD ? min(nr, 32) : 32;  // exclusive bound (fwd) / inclusive low (bwd)
+      if (FWD) {
+        for (int c = cbeg; c < cend; ++c) {
+#pragma unroll
+          for (int q = 0; q < NR; ++q) {
+            if (!kUnit && lane == c) acc[q] = acc[q] / tile[c][c];
+            const T xc = __shfl_sync(0xffffffffu, acc[q], c);
+            if (r > c && r < nr) acc[q] = fma(-tile[c][r], xc, acc[q]);
+          }
+        }
+      } else {
+        for (int c = cbeg; c >= cend; --c) {
+#pragma unroll
+          for (int q = 0; q < NR; ++q) {
+            if (!kUnit && r == c) acc[q] = acc[q] / tile[c][c];
+            const T xc = __shfl_sync(0xffffffffu, acc[q], c - 32);
+            if (r < c) acc[q] = fma(-tile[c][r], xc, acc[q]);
+          }
+        }
+      }
+      if (valid)
+#pragma unroll
+        for (int q = 0; q < NR; ++q) sx[r][q] = acc[q];
     }
     __syncthreads();
-  }
-  // diagonal block
-  load_tile<T, TRANS>(tile, LU, lda, n, r0, r0, nr, nr);
-  __syncthreads();
-  for (int c = 0; c < nr; ++c) {
-    if (r == c) {
+    if (warp == w_second) {
+      if (FWD) {
+        if (nr > 32) {
+          for (int c = 0; c < 32; ++c) {
 #pragma unroll
-      for (int q = 0; q < NR; ++q) {
-        if (TRANS) acc[q] = acc[q] / tile[c][c];
-        sx[c][q] = acc[q];
+            for (int q = 0; q < NR; ++q) acc[q] = fma(-tile[c][r], sx[c][q], acc[q]);
+          }
+          for (int c = 32; c < nr; ++c) {
+#pragma unroll
+            for (int q = 0; q < NR; ++q) {
+              if (!kUnit && r == c) acc[q] = acc[q] / tile[c][c];
+              const T xc = __shfl_sync(0xffffffffu, acc[q], c - 32);
+              if (r > c && r < nr) acc[q] = fma(-tile[c][r], xc, acc[q]);
+            }
+          }
+        }
+      } else {
+        for (int c = nr - 1; c >= 32; --c) {
+#pragma unroll
+          for (int q = 0; q < NR; ++q) acc[q] = fma(-tile[c][r], sx[c][q], acc[q]);
+        }
+        for (int c = min(nr, 32) - 1; c >= 0; --c) {
+#pragma unroll
+          for (int q = 0; q < NR; ++q) {
+            if (!kUnit && lane == c) acc[q] = acc[q] / tile[c][c];
+            const T xc = __shfl_sync(0xffffffffu, acc[q], c);
+            if (r < c) acc[q] = fma(-tile[c][r], xc, acc[q]);
+          }
+        }
       }
     }
-    __syncthreads();
-    if (r > c && valid) {
-      const T l = tile[c][r];
-#pragma unroll
-      for (int q = 0; q < NR; ++q) acc[q] = fma(-l, sx[c][q], acc[q]);
-    }
   }
-  if (valid)
+  cp_async_wait<0>();
+  if (valid && tid < kTS) {
 #pragma unroll
     for (int q = 0; q < NR; ++q)
-      if (q < nrhs) Y[row + q * ldy] = acc[q];
+      if (q < nrhs) {
+        Y[(r0 + r) + q * ldy] = acc[q];
+        if (!FWD) Out[(TRANS ? (int64_t)perm[r0 + r] : r0 + r) + q * ldo] = acc[q];
+      }
+  }
   __threadfence();
   __syncthreads();
   if (threadIdx.x == 0) st_release_i32(flags + blk, 1);
 }
 
-// Backward sweep with a non-unit upper (trans 'N': U) or unit upper
-// (trans 'T': L^T) triangle; block rows are taken last-first.  Results go
-// to Y (for the other block rows) and to Out[dst(i)] (dst = identity for 'N',
-// perm for 'T', i.e. x = P^T z).
-template <typename T, int NR, bool TRANS>
-__global__ void __launch_bounds__(kTS)
-solve_bwd_kernel(int64_t n, const T* __restrict__ LU, int64_t lda, const int32_t* __restrict__ perm,
-                 T* __restrict__ Y, int64_t ldy, T* __restrict__ Out, int64_t ldo, int nrhs,
-                 int32_t* __restrict__ flags, DevScratch* __restrict__ scr) {
-  __shared__ T tile[kTS][kTS + 1];
-  __shared__ T sx[kTS][NR];
-  __shared__ int s_blk;
-  const int nblk = (int)((n + kTS - 1) / kTS);
-  if (threadIdx.x == 0) s_blk = nblk - 1 - (int)atomicAdd(&scr->ticket, 1u);
-  __syncthreads();
-  const int blk = s_blk;
-  const int64_t r0 = (int64_t)blk * kTS;
-  const int nr = (int)min((int64_t)kTS, n - r0);
-  const int r = threadIdx.x;
-  const int64_t row = r0 + r;
-  const bool valid = r < nr;
-  T acc[NR];
-#pragma unroll
-  for (int q = 0; q < NR; ++q) acc[q] = (valid && q < nrhs) ? Y[row + q * ldy] : T(0);
-  for (int j = nblk - 1; j > blk; --j) {
-    const int64_t c0 = (int64_t)j * kTS;
-    const int nc = (int)min((int64_t)kTS, n - c0);
-    load_tile<T, TRANS>(tile, LU, lda, n, r0, c0, nr, nc);
-    if (!wait_flag(flags, j, scr)) return;
-    for (int idx = threadIdx.x; idx < kTS * NR; idx += blockDim.x) {
-      int c = idx / NR, q = idx - c * NR;
-      sx[c][q] = (q < nrhs && c < nc) ? ldcg(&Y[(c0 + c) + q * ldy]) : T(0);
-    }
-    __syncthreads();
-    for (int c = nc - 1; c >= 0; --c) {
-      const T u = tile[c][r];
-#pragma unroll
-      for (int q = 0; q < NR; ++q) acc[q] = fma(-u, sx[c][q], acc[q]);
-    }
-    __syncthreads();
-  }
-  load_tile<T, TRANS>(tile, LU, lda, n, r0, r0, nr, nr);
-  __syncthreads();
-  for (int c = nr - 1; c >= 0; --c) {
-    if (r == c) {
-#pragma unroll
-      for (int q = 0; q < NR; ++q) {
-        if (!TRANS) acc[q] = acc[q] / tile[c][c];
-        sx[c][q] = acc[q];
-      }
-    }
-    __syncthreads();
-    if (r < c) {
-      const T u = tile[c][r];
-#pragma unroll
-      for (int q = 0; q < NR; ++q) acc[q] = fma(-u, sx[c][q], acc[q]);
-    }
-  }
-  if (valid) {
-    const int64_t dst = TRANS ? (int64_t)perm[row] : row;
-#pragma unroll
-    for (int q = 0; q < NR; ++q)
-      if (q < nrhs) {
-        Y[row + q * ldy] = acc[q];
-        Out[dst + q * ldo] = acc[q];
-      }
-  }
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) st_release_i32(flags + blk, 1);
-}
+template <typename T>
+constexpr size_t sweep_smem() { return (size_t)kStages * kTS * (kTS + 1) * sizeof(T); }
 
 size_t getrs_scratch_bytes(int64_t n, int elem_size, int64_t work_cols) {
   int64_t nblk = (n + kTS - 1) / kTS;
@@ -242,14 +289,15 @@ cudaError_t run_chunk(const GetrsPlan<T>& p, char trans, int nr, T* B, int64_t l
   // n^2 flops per right-hand side
   const double tri_bytes = 0.5 * (double)p.n * (double)p.n * sizeof(T) + 2.0 * p.n * nr * sizeof(T);
   const double sweep_flops = (double)p.n * (double)p.n * nr;
+  const size_t smem = sweep_smem<T>();
   {
-  LaunchScope ls(K_SOLVE, sweep_flops, tri_bytes, s);
-  if (!tr)
-    solve_fwd_kernel<T, NR, false><<<(unsigned)nblk, kTS, 0, s>>>(
-        p.n, p.LU, p.lda, p.perm, B, ldb, p.work, p.n, nr, ffwd, p.scratch);
-  else
-    solve_fwd_kernel<T, NR, true><<<(unsigned)nblk, kTS, 0, s>>>(
-        p.n, p.LU, p.lda, p.perm, B, ldb, p.work, p.n, nr, ffwd, p.scratch);
+    LaunchScope ls(K_SOLVE, sweep_flops, tri_bytes, s);
+    if (!tr)
+      solve_sweep_kernel<T, NR, false, true><<<(unsigned)nblk, kSweepThreads, smem, s>>>(
+          p.n, p.LU, p.lda, p.perm, B, ldb, p.work, p.n, nullptr, 0, nr, ffwd, p.scratch);
+    else
+      solve_sweep_kernel<T, NR, true, true><<<(unsigned)nblk, kSweepThreads, smem, s>>>(
+          p.n, p.LU, p.lda, p.perm, B, ldb, p.work, p.n, nullptr, 0, nr, ffwd, p.scratch);
   }
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
@@ -257,14 +305,28 @@ cudaError_t run_chunk(const GetrsPlan<T>& p, char trans, int nr, T* B, int64_t l
   if (e != cudaSuccess) return e;
   LaunchScope ls(K_SOLVE, sweep_flops, tri_bytes, s);
   if (!tr)
-    solve_bwd_kernel<T, NR, false><<<(unsigned)nblk, kTS, 0, s>>>(
-        p.n, p.LU, p.lda, p.perm, p.work, p.n, B, ldb, nr, fbwd, p.scratch);
+    solve_sweep_kernel<T, NR, false, false><<<(unsigned)nblk, kSweepThreads, smem, s>>>(
+        p.n, p.LU, p.lda, p.perm, nullptr, 0, p.work, p.n, B, ldb, nr, fbwd, p.scratch);
   else
-    solve_bwd_kernel<T, NR, true><<<(unsigned)nblk, kTS, 0, s>>>(
-        p.n, p.LU, p.lda, p.perm, p.work, p.n, B, ldb, nr, fbwd, p.scratch);
+    solve_sweep_kernel<T, NR, true, false><<<(unsigned)nblk, kSweepThreads, smem, s>>>(
+        p.n, p.LU, p.lda, p.perm, nullptr, 0, p.work, p.n, B, ldb, nr, fbwd, p.scratch);
   return cudaGetLastError();
 }
 }  // namespace
+
+template <typename T, int NR>
+void configure_nr() {
+  const int b = (int)sweep_smem<T>();
+  cudaFuncSetAttribute(solve_sweep_kernel<T, NR, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+  cudaFuncSetAttribute(solve_sweep_kernel<T, NR, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+  cudaFuncSetAttribute(solve_sweep_kernel<T, NR, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+  cudaFuncSetAttribute(solve_sweep_kernel<T, NR, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+}
+
+void getrs_configure(int /*device*/) {
+  configure_nr<double, 1>(); configure_nr<double, 2>(); configure_nr<double, 4>(); configure_nr<double, 8>();
+  configure_nr<float, 1>(); configure_nr<float, 2>(); configure_nr<float, 4>(); configure_nr<float, 8>();
+}
 
 template <typename T>
 cudaError_t getrs_launch(const GetrsPlan<T>& p, char trans, int64_t nrhs, T* B, int64_t ldb,

@@ -13,7 +13,8 @@ from . import _lib
 from ._cuda import DeviceMatrix
 from ._lib import GBLUError, RefineOpts, RefineStats, check
 
-PRECISIONS = {"fp64": _lib.GBLU_FP64, "fp32": _lib.GBLU_FP32}
+PRECISIONS = {"fp64": _lib.GBLU_FP64, "fp32": _lib.GBLU_FP32, "bf16": _lib.GBLU_BF16,
+              "fp16": _lib.GBLU_FP16}
 REFINE_MODES = {"ir": _lib.GBLU_REFINE_IR, "gmres_ir": _lib.GBLU_REFINE_GMRES}
 
 
@@ -52,6 +53,18 @@ class Context:
             out[name] = {"count": int(pr.count[i]), "ms": float(pr.ms[i]),
                          "flops": float(pr.flops[i]), "bytes": float(pr.bytes[i])}
         return out
+
+    def gemm_update(self, C: np.ndarray, A: np.ndarray, B: np.ndarray, precision: str = "bf16"):
+        """C - A @ B with the getrf trailing-update kernel (host arrays, FP32)."""
+        Cf = np.array(C, dtype=np.float32, order="F", copy=True)
+        Af = np.asfortranarray(np.asarray(A, dtype=np.float32))
+        Bf = np.asfortranarray(np.asarray(B, dtype=np.float32))
+        m, k = Af.shape
+        n = Bf.shape[1]
+        check(self.lib.gblu_gemm_update(self.handle, PRECISIONS[precision], m, n, k, Af.ctypes.data,
+                                        max(m, 1), Bf.ctypes.data, max(k, 1), Cf.ctypes.data,
+                                        max(m, 1), _lib.GBLU_HOST), self.handle)
+        return Cf
 
     def factor(self, m: int, n: int | None = None, precision: str = "fp64") -> "Factorization":
         return Factorization(self, m, m if n is None else n, precision)

@@ -109,7 +109,9 @@ class GB300LUFactorization(AbstractDenseFactorization):
 class GB300MixedLUFactorization(AbstractDenseFactorization):
     """Mixed precision: FP32 LU, FP64 accuracy by refinement.
 
-    factor:  "fp32"           (the FP32 factors on the device)
+    factor:  "fp32"           FP32 LU (SIMT FP32 trailing updates)
+             "bf16" | "fp16"  FP32 LU whose trailing updates run on the tensor
+                              cores (tcgen05) with 16-bit operands
     refine:  "ir" | "gmres_ir" (classic IR, or GMRES-IR preconditioned by the LU)
     maxiters, tol: outer refinement limits (tol None: n * eps64)
     fallback: FP64 LU when refinement stalls.
@@ -120,7 +122,7 @@ class GB300MixedLUFactorization(AbstractDenseFactorization):
     def __init__(self, factor: str = "fp32", refine: str = "ir", maxiters: int = 30,
                  tol: Optional[float] = None, fallback: bool = True, gmres_restart: int = 30,
                  gmres_tol: float = 1e-10, device: int = 0):
-        if factor != "fp32":
+        if factor not in ("fp32", "bf16", "fp16"):
             raise ValueError(f"unsupported factor precision {factor!r}")
         if refine not in ("ir", "gmres_ir"):
             raise ValueError("refine must be 'ir' or 'gmres_ir'")

@@ -84,3 +84,70 @@ def test_fp32_factors_bit_exact(ctx, oracle_mod, pkg):
     LU, ipiv, _ = oracle_mod.getrf(A.astype(np.float32))
     assert np.array_equal(f.ipiv(), ipiv)
     assert np.array_equal(f.factors(), LU.astype(np.float64))
+
+
+def _round_bf16(x):
+    x = np.ascontiguousarray(np.asarray(x, dtype=np.float32))
+    u = x.view(np.uint32).astype(np.uint64)
+    r = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return r.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def _fp16_scaled(B):
+    B = np.asarray(B, dtype=np.float32)
+    mx = np.abs(B).max(axis=0)
+    e = np.where(mx > 0, np.frexp(mx)[1] - 1 - 14, 0)  # ilogb(mx) - 14
+    s = np.ldexp(np.float32(1.0), -e).astype(np.float32)
+    Bh = (B * s).astype(np.float16).astype(np.float64)
+    return Bh / s.astype(np.float64)
+
+
+@pytest.mark.parametrize("prec", ["bf16", "fp16", "fp32"])
+@pytest.mark.parametrize("m,n,k", [(5, 7, 3), (128, 128, 64), (129, 130, 65), (300, 200, 100),
+                                   (1000, 513, 777), (256, 384, 1024)])
+def test_gemm_update_against_rounded_operands(ctx, prec, m, n, k):
+    """The trailing-update contraction: C - A B with 16-bit operands and FP32
+    accumulation (tcgen05), checked against float64 products of the rounded
+    operands; FP32 mode is checked the same way with unrounded operands."""
+    rng = np.random.default_rng(m * 7 + n * 3 + k)
+    A = rng.uniform(-1, 1, size=(m, k)).astype(np.float32)      # |L21| <= 1
+    B = (rng.standard_normal((k, n)) * 37.0).astype(np.float32)  # U12-like
+    C = rng.standard_normal((m, n)).astype(np.float32)
+    out = ctx.gemm_update(C, A, B, prec)
+    if prec == "bf16":
+        Ar, Br = _round_bf16(A), _round_bf16(B)
+    elif prec == "fp16":
+        Ar, Br = A.astype(np.float16).astype(np.float64), _fp16_scaled(B)
+    else:
+        Ar, Br = A.astype(np.float64), B.astype(np.float64)
+    ref = C.astype(np.float64) - Ar @ Br
+    scale = np.abs(Ar) @ np.abs(Br) + np.abs(C)
+    err = np.abs(out.astype(np.float64) - ref) / scale
+    assert err.max() < 4 * (k + 2) * 2.0 ** -24, err.max()
+
+
+@pytest.mark.parametrize("prec", ["bf16", "fp16"])
+@pytest.mark.parametrize("mode", ["ir", "gmres_ir"])
+@pytest.mark.parametrize("n", [256, 1000, 2048])
+def test_tensor_core_lu_reaches_fp64(ctx, oracle_mod, pkg, prec, mode, n):
+    A, B = pkg.workloads.shifted(n, 2, seed=100 + n)
+    f = ctx.factor(n, n, prec)
+    assert f.getrf(A) == 0
+    X, st = f.solve_refined(B, mode=mode)
+    be = oracle_mod.backward_error(A, X, B)
+    assert be <= 10 * n * EPS64, (be, st)
+    assert st["fell_back"] == 0, st
+    # the 16-bit-operand factors are close to, not equal to, the FP32 ones
+    LU32, ipiv32, _ = oracle_mod.getrf(A.astype(np.float32))
+    F = f.factors()
+    assert np.abs(F - LU32).max() < 0.05 * np.abs(LU32).max()
+    f.close()
+
+
+def test_tensor_core_lu_ill_conditioned_gmres(ctx, oracle_mod, pkg):
+    n = 600
+    A, B = pkg.workloads.svd_conditioned(n, 2, cond=1e4, seed=11)
+    f = ctx.factor(n, n, "fp16")
+    assert f.getrf(A) == 0
+    X, st = f.solve_refined(B, mode="gmres_ir")
+    assert oracle_mod.backward_error(A, X, B) <= 10 * n * EPS64, st
