@@ -181,6 +181,34 @@ int32_t gblu_gemm_update(gblu_ctx* ctx, int32_t precision, int64_t m, int64_t n,
                          const float* A, int64_t lda, const float* B, int64_t ldb, float* C,
                          int64_t ldc, int32_t loc);
 
+/* ---- batched uneven LU ------------------------------------------------------
+ * `count` independent square systems A_i x_i = b_i, 1 <= n_i <= 256, one RHS
+ * each, packed back to back: A_i column-major (lda = n_i) at element offset
+ * sum_{k<i} n_k^2 of A, b_i at sum_{k<i} n_k of B.  gblu_batch_create sorts
+ * the systems into size buckets and captures one CUDA graph holding one
+ * persistent kernel per bucket (each takes systems from a queue, largest
+ * first); gblu_batch_solve copies the inputs, launches the graph once and
+ * overwrites B with the solutions.  precision GBLU_FP64: per-system getrf +
+ * getrs in FP64 (bit-identical to src/blocked_lufact.jl + the back-solve of
+ * src/factorization.jl:433-457 applied to each system); GBLU_FP32: FP32
+ * factors + FP64 refinement per system, systems that do not converge re-solved
+ * in FP64 by a second kernel of the same graph.  info_host (may be NULL)
+ * receives each system's getrf info.
+ * No counterpart in the reference (LinearProblem holds one A); it batches
+ * what a caller of solve(LinearProblem(A_i, b_i), LUFactorization()) loops over. */
+typedef struct gblu_batch gblu_batch;
+int32_t gblu_batch_create(gblu_ctx* ctx, int64_t count, const int64_t* sizes, int32_t precision,
+                          gblu_batch** out);
+/* Replace the bucket schedule (from the autotuner): nbuckets (<= 8) buckets
+ * with inclusive upper size edges (the last must be 256), threads per CTA and
+ * panel width per bucket ((128|256, 8|16) or (512, 16)), CTAs per bucket
+ * (NULL or <= 0 entries: fill the GPU).  Re-captures the graph. */
+int32_t gblu_batch_schedule(gblu_ctx* ctx, gblu_batch* b, int32_t nbuckets, const int32_t* upper,
+                            const int32_t* threads, const int32_t* panel, const int32_t* ctas);
+int32_t gblu_batch_solve(gblu_ctx* ctx, gblu_batch* b, const double* A, double* B, int32_t loc,
+                         int64_t* info_host);
+int32_t gblu_batch_destroy(gblu_ctx* ctx, gblu_batch* b);
+
 /* ---- LAPACK-shaped entries ---------------------------------------------------
  * Same argument lists as LAPACK dgetrf_/dgetrs_/sgetrf_/sgetrs_ with 64-bit
  * integers (the ILP64 BlasInt of src/LinearSolve.jl:52-63), so a binding can

@@ -103,6 +103,10 @@ SIGNATURES = {
     "gblu_refine_opts_default": (_I32, [ctypes.POINTER(RefineOpts)]),
     "gblu_solve_refined": (_I32, [_P, _P, ctypes.c_char, _I64, _P, _I64, _I32,
                                   ctypes.POINTER(RefineOpts), ctypes.POINTER(RefineStats)]),
+    "gblu_batch_create": (_I32, [_P, _I64, _P, _I32, ctypes.POINTER(_P)]),
+    "gblu_batch_schedule": (_I32, [_P, _P, _I32, _P, _P, _P, _P]),
+    "gblu_batch_solve": (_I32, [_P, _P, _P, _P, _I32, _P]),
+    "gblu_batch_destroy": (_I32, [_P, _P]),
     "gblu_dgetrs_noalloc": (_I32, [ctypes.c_char, _I64, _I64, _P, _I64, _P, _P, _I64, _P]),
     "gblu_dgetrf_": (None, [_PI64, _PI64, _P, _PI64, _P, _PI64]),
     "gblu_dgetrs_": (None, [ctypes.c_char_p, _PI64, _PI64, _P, _PI64, _P, _P, _PI64, _PI64,
