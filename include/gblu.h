@@ -209,6 +209,60 @@ int32_t gblu_batch_solve(gblu_ctx* ctx, gblu_batch* b, const double* A, double* 
                          int64_t* info_host);
 int32_t gblu_batch_destroy(gblu_ctx* ctx, gblu_batch* b);
 
+/* ---- serving loop ----------------------------------------------------------------
+ * Continuous batching over factorizations kept resident in HBM.  A request
+ * carries a key and either a new matrix A for that key (factor, then solve) or
+ * only a right-hand side for a key whose factors are resident (solve).
+ * `workers` host threads, each with its own stream, take the oldest runnable
+ * request (its key idle; a new factorization object admitted within
+ * hbm_budget_bytes, evicting least recently used idle ones); requests on one
+ * key keep submission order; up to max_rhs_batch consecutive solve-only
+ * requests on a key are merged into one multi-RHS solve.  A result depends
+ * only on its own inputs, never on what else is in flight.
+ * No counterpart in the reference (one LinearProblem per solve call). */
+typedef struct gblu_server gblu_server;
+typedef struct gblu_serve_config {
+  int32_t workers;           /* concurrent slots                                   */
+  int32_t precision;         /* factor precision of new matrices (GBLU_FP64 .. FP16) */
+  int32_t refine_mode;       /* GBLU_REFINE_IR / GBLU_REFINE_GMRES (mixed precisions) */
+  uint64_t hbm_budget_bytes; /* resident factorizations (0: no limit)             */
+  int32_t max_rhs_batch;     /* solve-only requests merged per key                 */
+} gblu_serve_config;
+typedef struct gblu_request {
+  uint64_t key;      /* factorization key                                        */
+  int64_t n;
+  const double* A;   /* host n x n column-major (lda = n), or NULL: solve only   */
+  const double* b;   /* host, n                                                  */
+  double* x;         /* host, n: the solution, written before completion         */
+  uint64_t tag;      /* caller's identifier, returned in the completion          */
+} gblu_request;
+typedef struct gblu_completion {
+  uint64_t tag;
+  int32_t status;         /* GBLU_OK, GBLU_ENOTFACTORED (key not resident), ...   */
+  int32_t refactored;     /* this request factored its matrix                    */
+  int32_t fell_back;      /* refinement fell back to the FP64 LU                 */
+  int32_t iterations;     /* refinement iterations                               */
+  int64_t info;           /* getrf info of a factoring request                   */
+  double backward_error;  /* final backward error (-1: not computed, FP64)       */
+  double latency_us;      /* submit -> solution in host memory                   */
+  double queue_us;        /* submit -> start of work                             */
+} gblu_completion;
+typedef struct gblu_serve_stats {
+  int64_t submitted, completed, failed, factorizations, solves, merged_solves, evictions;
+  int64_t resident_factors, queued, in_flight;
+  uint64_t resident_bytes;
+} gblu_serve_stats;
+int32_t gblu_serve_config_default(gblu_serve_config* cfg);
+int32_t gblu_serve_create(gblu_ctx* ctx, const gblu_serve_config* cfg, gblu_server** out);
+/* Non-blocking; the request's buffers must stay valid until its completion. */
+int32_t gblu_serve_submit(gblu_server* s, const gblu_request* req);
+/* Up to max completions into out (waiting up to wait_ms for the first one). */
+int32_t gblu_serve_poll(gblu_server* s, gblu_completion* out, int32_t max, int32_t* n_out,
+                        int32_t wait_ms);
+int32_t gblu_serve_get_stats(gblu_server* s, gblu_serve_stats* out);
+/* Finishes every submitted request, then releases the factorizations. */
+int32_t gblu_serve_destroy(gblu_server* s);
+
 /* ---- LAPACK-shaped entries ---------------------------------------------------
  * Same argument lists as LAPACK dgetrf_/dgetrs_/sgetrf_/sgetrs_ with 64-bit
  * integers (the ILP64 BlasInt of src/LinearSolve.jl:52-63), so a binding can

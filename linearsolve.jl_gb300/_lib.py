@@ -76,6 +76,30 @@ class Profile(ctypes.Structure):
     ]
 
 
+class ServeConfig(ctypes.Structure):
+    _fields_ = [("workers", ctypes.c_int32), ("precision", ctypes.c_int32),
+                ("refine_mode", ctypes.c_int32), ("hbm_budget_bytes", ctypes.c_uint64),
+                ("max_rhs_batch", ctypes.c_int32)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("key", ctypes.c_uint64), ("n", ctypes.c_int64), ("A", ctypes.c_void_p),
+                ("b", ctypes.c_void_p), ("x", ctypes.c_void_p), ("tag", ctypes.c_uint64)]
+
+
+class Completion(ctypes.Structure):
+    _fields_ = [("tag", ctypes.c_uint64), ("status", ctypes.c_int32), ("refactored", ctypes.c_int32),
+                ("fell_back", ctypes.c_int32), ("iterations", ctypes.c_int32),
+                ("info", ctypes.c_int64), ("backward_error", ctypes.c_double),
+                ("latency_us", ctypes.c_double), ("queue_us", ctypes.c_double)]
+
+
+class ServeStats(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_int64) for k in (
+        "submitted", "completed", "failed", "factorizations", "solves", "merged_solves",
+        "evictions", "resident_factors", "queued", "in_flight")] + [("resident_bytes", ctypes.c_uint64)]
+
+
 _P = ctypes.c_void_p
 _I32 = ctypes.c_int32
 _I64 = ctypes.c_int64
@@ -107,6 +131,12 @@ SIGNATURES = {
     "gblu_batch_schedule": (_I32, [_P, _P, _I32, _P, _P, _P, _P]),
     "gblu_batch_solve": (_I32, [_P, _P, _P, _P, _I32, _P]),
     "gblu_batch_destroy": (_I32, [_P, _P]),
+    "gblu_serve_config_default": (_I32, [ctypes.POINTER(ServeConfig)]),
+    "gblu_serve_create": (_I32, [_P, ctypes.POINTER(ServeConfig), ctypes.POINTER(_P)]),
+    "gblu_serve_submit": (_I32, [_P, ctypes.POINTER(Request)]),
+    "gblu_serve_poll": (_I32, [_P, ctypes.POINTER(Completion), _I32, ctypes.POINTER(_I32), _I32]),
+    "gblu_serve_get_stats": (_I32, [_P, ctypes.POINTER(ServeStats)]),
+    "gblu_serve_destroy": (_I32, [_P]),
     "gblu_dgetrs_noalloc": (_I32, [ctypes.c_char, _I64, _I64, _P, _I64, _P, _P, _I64, _P]),
     "gblu_dgetrf_": (None, [_PI64, _PI64, _P, _PI64, _P, _PI64]),
     "gblu_dgetrs_": (None, [ctypes.c_char_p, _PI64, _PI64, _P, _PI64, _P, _P, _PI64, _PI64,

@@ -8,6 +8,7 @@
 // Carson & Higham, SIAM J. Sci. Comput. 40(2), 2018).  Every reduction has a
 // fixed order, so a solve's result does not depend on what else runs on the
 // device.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -490,94 +491,108 @@ int32_t refine_solve(gblu_ctx* ctx, gblu_factor* f, char trans, int64_t nrhs, do
     GBLU_CK(ctx, cudaMemcpy2DAsync(w.b, n * sizeof(double), Bc, ldb * sizeof(double),
                                    n * sizeof(double), nc, k_in, s),
             "copying B");
-    bool done = false, fell_back = false;
-    double berr_final = 0;
-    int iters = 0;
-    if (!f->use_fb) {
-      // x0 = 0, r0 = b
-      GBLU_CK(ctx, cudaMemsetAsync(w.x, 0, (size_t)n * nc * sizeof(double), s), "x0");
-      std::vector<double> rn(nc), xn(nc), bn(nc), prev(nc, INFINITY);
-      std::vector<int> slow(nc, 0);
+    // Per-column state: every column's iterate depends only on its own data,
+    // so a column's result is the same whatever else is in the chunk.
+    enum { ACTIVE = 0, CONVERGED = 1, STALLED = 2 };
+    std::vector<int> state(nc, ACTIVE), slow(nc, 0), its_q(nc, 0);
+    std::vector<double> rn(nc), xn(nc), bn(nc), prev(nc, INFINITY), be_q(nc, INFINITY);
+    bool any_fb = false;
+    if (f->use_fb) {
+      for (int q = 0; q < nc; ++q) state[q] = STALLED;
+    } else {
+      GBLU_CK(ctx, cudaMemsetAsync(w.x, 0, (size_t)n * nc * sizeof(double), s), "x0");  // x0 = 0
       for (int it = 0; it <= o.max_iter; ++it) {
         int32_t e = S.residual(nc, rn.data(), xn.data());
         if (e) return e;
         if (it == 0) bn = rn;  // x = 0: r = b
-        bool all_ok = true, stalled = false;
-        double worst = 0;
+        bool any_active = false;
         for (int q = 0; q < nc; ++q) {
-          double den = w.anorm * xn[q] + bn[q];
-          double be = den > 0 ? rn[q] / den : (rn[q] == 0 ? 0.0 : INFINITY);
-          if (!std::isfinite(be) && it > 0) stalled = true;
-          worst = std::max(worst, std::isnan(be) ? INFINITY : be);
-          if (!(be <= tol)) {
-            all_ok = false;
-            if (it >= 2 && be > 0.9 * prev[q]) {
-              if (++slow[q] >= 2) stalled = true;
-            } else {
-              slow[q] = 0;
-            }
+          if (state[q] != ACTIVE) continue;
+          const double den = w.anorm * xn[q] + bn[q];
+          const double be = den > 0 ? rn[q] / den : (rn[q] == 0 ? 0.0 : INFINITY);
+          be_q[q] = be;
+          its_q[q] = it;
+          if (be <= tol) { state[q] = CONVERGED; continue; }
+          if (!std::isfinite(be) && it > 0) { state[q] = STALLED; continue; }
+          if (it >= 2 && be > 0.9 * prev[q]) {
+            if (++slow[q] >= 2) { state[q] = STALLED; continue; }
+          } else {
+            slow[q] = 0;
           }
           prev[q] = be;
+          if (it == o.max_iter) { state[q] = STALLED; continue; }
+          any_active = true;
         }
-        berr_final = worst;
-        iters = it;
-        if (all_ok) { done = true; break; }
-        if (stalled || it == o.max_iter) break;
+        if (!any_active) break;
         if (o.mode == GBLU_REFINE_GMRES) {
           for (int q = 0; q < nc; ++q) {
+            if (state[q] != ACTIVE) continue;
             int its = 0;
             e = S.gmres(q, o.gmres_restart, o.gmres_tol, &its);
             if (e) return e;
             st_acc.inner_iterations += its;
           }
         } else {
-          e = S.precond(w.r, n, w.r, n, nc);  // d = M^{-1} r (in place), scaled
+          e = S.precond(w.r, n, w.r, n, nc);  // d = M^{-1} r (in place), scaled per column
           if (e) return e;
-          for (int q = 0; q < nc; ++q)
-            { LaunchScope ls_(K_REFINE, 0.0, 0.0, s);
+          for (int q = 0; q < nc; ++q) {
+            if (state[q] != ACTIVE) continue;
+            LaunchScope ls_(K_REFINE, 0.0, 0.0, s);
             axpby_kernel<<<grid_for(n), 256, 0, s>>>(n, 1.0, w.r + (size_t)q * n, 1.0, w.x + (size_t)q * n);
-            }
+          }
           GBLU_CK(ctx, cudaGetLastError(), "update");
         }
       }
     }
-    if (done) {
-      GBLU_CK(ctx, cudaMemcpy2DAsync(Bc, ldb * sizeof(double), w.x, n * sizeof(double),
-                                     n * sizeof(double), nc, k_out, s),
-              "copying X");
-    } else {
-      if (!o.fallback && !f->use_fb) return fail(ctx, GBLU_ESTALL, "refinement stalled at backward error %.3e", berr_final);
+    for (int q = 0; q < nc; ++q) any_fb |= state[q] == STALLED;
+    if (any_fb) {
+      if (!o.fallback && !f->use_fb)
+        return fail(ctx, GBLU_ESTALL, "refinement stalled (backward error %.3e)",
+                    *std::max_element(be_q.begin(), be_q.end()));
       if (!f->fb_valid) {
         int64_t info64 = 0;
         int32_t e = factor_fp64_fallback(ctx, f, &info64);
         if (e) return e;
         if (info64 != 0) return fail(ctx, GBLU_EINVAL, "matrix is singular in FP64 (info = %lld)", (long long)info64);
       }
-      // plain FP64 solve on the FP64 factors, x <- b
-      GBLU_CK(ctx, cudaMemcpyAsync(w.x, w.b, (size_t)n * nc * sizeof(double), cudaMemcpyDeviceToDevice, s),
+      // plain FP64 solve of the stalled columns on the FP64 factors
+      GBLU_CK(ctx, cudaMemcpyAsync(w.r, w.b, (size_t)n * nc * sizeof(double), cudaMemcpyDeviceToDevice, s),
               "copy b");
-      GBLU_CK(ctx, getrs_launch<double>(f->fb_rs, trans, nc, w.x, n, nullptr, s), "FP64 getrs");
-      std::vector<double> rn(nc), xn(nc), bn(nc);
+      GBLU_CK(ctx, getrs_launch<double>(f->fb_rs, trans, nc, w.r, n, nullptr, s), "FP64 getrs");
+      for (int q = 0; q < nc; ++q)
+        if (state[q] == STALLED)
+          GBLU_CK(ctx, cudaMemcpyAsync(w.x + (size_t)q * n, w.r + (size_t)q * n, n * sizeof(double),
+                                       cudaMemcpyDeviceToDevice, s), "fallback column");
       int32_t e = S.residual(nc, rn.data(), xn.data());
       if (e) return e;
-      // ||b||: one more pass over b
-      GBLU_CK(ctx, cudaMemsetAsync(w.colmax + 2 * w.W, 0, nc * sizeof(unsigned long long), s), "memset");
-      { LaunchScope ls_(K_REFINE, 0.0, 0.0, s);
-      colmax_kernel<<<grid_for(n), 256, 0, s>>>(n, nc, w.b, n, w.colmax + 2 * w.W);
+      if (f->use_fb) {  // ||b|| was not measured yet
+        GBLU_CK(ctx, cudaMemsetAsync(w.colmax + 2 * w.W, 0, nc * sizeof(unsigned long long), s), "memset");
+        {
+          LaunchScope ls_(K_REFINE, 0.0, 0.0, s);
+          colmax_kernel<<<grid_for(n), 256, 0, s>>>(n, nc, w.b, n, w.colmax + 2 * w.W);
+        }
+        std::vector<unsigned long long> bits(nc);
+        GBLU_CK(ctx, cudaMemcpyAsync(bits.data(), w.colmax + 2 * w.W, nc * sizeof(unsigned long long),
+                                     cudaMemcpyDeviceToHost, s), "readback");
+        GBLU_CK(ctx, cudaStreamSynchronize(s), "fallback");
+        for (int q = 0; q < nc; ++q) bn[q] = bits_to_double(bits[q]);
       }
-      std::vector<unsigned long long> bits(nc);
-      GBLU_CK(ctx, cudaMemcpyAsync(bits.data(), w.colmax + 2 * w.W, nc * sizeof(unsigned long long),
-                                   cudaMemcpyDeviceToHost, s), "readback");
-      GBLU_CK(ctx, cudaStreamSynchronize(s), "fallback");
-      berr_final = 0;
-      for (int q = 0; q < nc; ++q) {
-        double den = w.anorm * xn[q] + bits_to_double(bits[q]);
-        berr_final = std::max(berr_final, den > 0 ? rn[q] / den : 0.0);
-      }
-      fell_back = true;
-      GBLU_CK(ctx, cudaMemcpy2DAsync(Bc, ldb * sizeof(double), w.x, n * sizeof(double),
-                                     n * sizeof(double), nc, k_out, s),
-              "copying X");
+      for (int q = 0; q < nc; ++q)
+        if (state[q] == STALLED) {
+          const double den = w.anorm * xn[q] + bn[q];
+          be_q[q] = den > 0 ? rn[q] / den : 0.0;
+        }
+    }
+    GBLU_CK(ctx, cudaMemcpy2DAsync(Bc, ldb * sizeof(double), w.x, n * sizeof(double),
+                                   n * sizeof(double), nc, k_out, s),
+            "copying X");
+    const bool fell_back = any_fb;
+    const bool done = !any_fb;
+    double berr_final = 0;
+    int iters = 0;
+    for (int q = 0; q < nc; ++q) {
+      berr_final = std::max(berr_final, std::isnan(be_q[q]) ? INFINITY : be_q[q]);
+      iters = std::max(iters, its_q[q]);
     }
     GBLU_CK(ctx, cudaStreamSynchronize(s), "refined solve");
     int32_t e = check_device_errors(ctx, {f->rs32.scratch, f->fb_rs.scratch});

@@ -1,0 +1,363 @@
+// Serving loop: continuous batching of factor+solve and solve-only requests
+// over factorizations kept resident in HBM.
+//
+// A request either brings a new matrix for a key (factor, then solve) or only
+// a right-hand side for a key whose factors are resident (solve).  Worker
+// threads, each with its own context and CUDA stream, take the oldest
+// runnable request: its key must not be in use by another worker and, when it
+// needs a new factorization object, the HBM budget must admit it (least
+// recently used idle factorizations are evicted first).  Requests on one key
+// run in submission order; consecutive solve-only requests on the same key are
+// merged into one multi-right-hand-side solve.  Work from different workers
+// overlaps on the device.  Each solve's arithmetic depends only on its own
+// inputs (fixed launch shapes per n, fixed-order reductions), so a result is
+// the same whether the request runs alone or in a mix.
+//
+// No counterpart in the reference: LinearSolve.jl solves one LinearProblem per
+// call; this is the request loop around repeated solve!(cache) calls.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <list>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "gblu_internal.h"
+#include "objects.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Pending {
+  gblu_request req;
+  Clock::time_point t_submit;
+  uint64_t seq;
+};
+
+struct Resident {
+  gblu_factor* f = nullptr;
+  gblu_ctx* owner = nullptr;
+  int64_t n = 0;
+  uint64_t bytes = 0;
+  bool busy = false;
+  bool valid = false;  // holds a successful factorization
+  uint64_t last_use = 0;
+};
+
+}  // namespace
+
+struct gblu_server {
+  gblu_ctx* parent = nullptr;
+  gblu_serve_config cfg{};
+  std::vector<gblu_ctx*> wctx;
+  std::vector<std::thread> threads;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::deque<Pending> queue;
+  std::deque<gblu_completion> done;
+  std::unordered_map<uint64_t, Resident> cache;
+  uint64_t bytes_resident = 0;
+  uint64_t seq = 0, use_clock = 0;
+  bool stopping = false;
+  int64_t in_flight = 0;
+  gblu_serve_stats stats{};
+};
+
+namespace gblu {
+namespace {
+
+uint64_t factor_bytes_estimate(gblu_server* s, gblu_ctx* c, int64_t n) {
+  gblu_factor* probe = nullptr;
+  (void)probe;
+  (void)c;
+  // same arithmetic as gblu_factor_create: report what the object will hold
+  const int64_t ld = std::max<int64_t>(32, ((n + 31) / 32) * 32);
+  const double elem = s->cfg.precision == GBLU_FP64 ? 8.0 : 4.0;
+  double b = (double)ld * n * elem;
+  if (s->cfg.precision != GBLU_FP64) b += (double)ld * n * 8.0 + 64.0 * n * 8.0;
+  if (s->cfg.precision == GBLU_BF16 || s->cfg.precision == GBLU_FP16) b += 1.5 * (double)n * n * 2.0;
+  return (uint64_t)b + (1u << 20);
+}
+
+// Evict least recently used idle factorizations until `need` more bytes fit.
+bool admit(gblu_server* s, uint64_t need) {
+  const uint64_t budget = s->cfg.hbm_budget_bytes;
+  if (budget == 0) return true;
+  while (s->bytes_resident + need > budget) {
+    auto victim = s->cache.end();
+    for (auto it = s->cache.begin(); it != s->cache.end(); ++it)
+      if (!it->second.busy && (victim == s->cache.end() || it->second.last_use < victim->second.last_use))
+        victim = it;
+    if (victim == s->cache.end()) return false;  // everything resident is in use: wait
+    gblu_factor_destroy(victim->second.owner, victim->second.f);
+    s->bytes_resident -= std::min(s->bytes_resident, victim->second.bytes);
+    s->cache.erase(victim);
+    s->stats.evictions++;
+  }
+  return true;
+}
+
+void complete(gblu_server* s, const Pending& p, int32_t status, int64_t info, int32_t refactored,
+              const gblu_refine_stats& rs, Clock::time_point t_start) {
+  gblu_completion c{};
+  c.tag = p.req.tag;
+  c.status = status;
+  c.info = info;
+  c.refactored = refactored;
+  c.fell_back = rs.fell_back;
+  c.iterations = rs.iterations;
+  c.backward_error = rs.backward_error;
+  const auto now = Clock::now();
+  c.latency_us = std::chrono::duration<double, std::micro>(now - p.t_submit).count();
+  c.queue_us = std::chrono::duration<double, std::micro>(t_start - p.t_submit).count();
+  s->done.push_back(c);
+  if (status == GBLU_OK) s->stats.completed++;
+  else s->stats.failed++;
+}
+
+void worker(gblu_server* s, int wi) {
+  gblu_ctx* ctx = s->wctx[wi];
+  std::vector<double> packed;
+  for (;;) {
+    std::vector<Pending> batch;
+    Resident* res = nullptr;
+    bool need_new = false;
+    uint64_t need_bytes = 0;
+    {
+      std::unique_lock<std::mutex> lk(s->mu);
+      for (;;) {
+        if (s->stopping && s->queue.empty()) return;
+        // oldest runnable request: key idle, and memory admitted if it needs a new object
+        auto pick = s->queue.end();
+        for (auto it = s->queue.begin(); it != s->queue.end(); ++it) {
+          bool key_busy = false, earlier_same_key = false;
+          for (auto jt = s->queue.begin(); jt != it; ++jt)
+            if (jt->req.key == it->req.key) { earlier_same_key = true; break; }
+          if (earlier_same_key) continue;  // keep per-key order
+          auto c = s->cache.find(it->req.key);
+          if (c != s->cache.end()) key_busy = c->second.busy;
+          if (key_busy) continue;
+          const bool has_obj = c != s->cache.end() && c->second.n == it->req.n;
+          if (it->req.A && !has_obj) {
+            uint64_t nb = factor_bytes_estimate(s, ctx, it->req.n);
+            if (c != s->cache.end() && !c->second.busy) {  // resize: free the old object first
+              gblu_factor_destroy(c->second.owner, c->second.f);
+              s->bytes_resident -= std::min(s->bytes_resident, c->second.bytes);
+              s->cache.erase(c);
+            }
+            if (!admit(s, nb)) continue;
+            need_new = true;
+            need_bytes = nb;
+          } else {
+            need_new = false;
+          }
+          pick = it;
+          break;
+        }
+        if (pick != s->queue.end()) {
+          batch.push_back(*pick);
+          const uint64_t key = pick->req.key;
+          auto next = s->queue.erase(pick);
+          // merge following solve-only requests on the same key (until a refactor of it)
+          if (!batch[0].req.A || true) {
+            for (auto it = next; it != s->queue.end() && (int)batch.size() < std::max(1, s->cfg.max_rhs_batch);) {
+              if (it->req.key != key) { ++it; continue; }
+              if (it->req.A || it->req.n != batch[0].req.n) break;
+              batch.push_back(*it);
+              it = s->queue.erase(it);
+            }
+          }
+          if (need_new) {
+            Resident r;
+            r.n = batch[0].req.n;
+            r.bytes = need_bytes;
+            r.owner = ctx;
+            s->cache[key] = r;
+            s->bytes_resident += need_bytes;
+          }
+          res = &s->cache[key];
+          res->busy = true;
+          res->last_use = ++s->use_clock;
+          s->in_flight += (int64_t)batch.size();
+          break;
+        }
+        if (s->stopping && s->queue.empty()) return;
+        s->cv_work.wait_for(lk, std::chrono::milliseconds(50));
+      }
+    }
+    const auto t_start = Clock::now();
+    const Pending& head = batch[0];
+    const int64_t n = head.req.n;
+    int32_t st = GBLU_OK;
+    int64_t info = 0;
+    int32_t refactored = 0;
+    gblu_refine_stats rs{};
+    if (need_new) {
+      gblu_factor* f = nullptr;
+      st = gblu_factor_create(ctx, n, n, s->cfg.precision, &f);
+      res->f = f;
+      if (st == GBLU_OK) res->owner = ctx;
+    }
+    if (st == GBLU_OK && head.req.A) {
+      st = gblu_getrf(ctx, res->f, head.req.A, n, GBLU_HOST, &info);
+      refactored = 1;
+      res->valid = (st == GBLU_OK && info == 0);
+    } else if (st == GBLU_OK && (!res->f || !res->valid)) {
+      st = GBLU_ENOTFACTORED;
+    }
+    if (st == GBLU_OK && info == 0) {
+      const int64_t k = (int64_t)batch.size();
+      packed.resize((size_t)n * k);
+      for (int64_t j = 0; j < k; ++j)
+        std::copy(batch[j].req.b, batch[j].req.b + n, packed.begin() + j * n);
+      if (s->cfg.precision == GBLU_FP64) {
+        st = gblu_getrs(ctx, res->f, 'N', k, packed.data(), n, GBLU_HOST);
+        rs.converged = 1;
+        rs.backward_error = -1;
+      } else {
+        gblu_refine_opts o;
+        gblu_refine_opts_default(&o);
+        o.mode = s->cfg.refine_mode;
+        st = gblu_solve_refined(ctx, res->f, 'N', k, packed.data(), n, GBLU_HOST, &o, &rs);
+      }
+      if (st == GBLU_OK)
+        for (int64_t j = 0; j < k; ++j)
+          std::copy(packed.begin() + j * n, packed.begin() + (j + 1) * n, batch[j].req.x);
+    }
+    if (st == GBLU_OK && info != 0) st = GBLU_EINVAL;  // singular matrix for this key
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      res->busy = false;
+      res->last_use = ++s->use_clock;
+      if (!res->f) {  // creation failed: drop the reservation
+        auto c = s->cache.find(head.req.key);
+        if (c != s->cache.end()) {
+          s->bytes_resident -= std::min(s->bytes_resident, c->second.bytes);
+          s->cache.erase(c);
+        }
+      }
+      for (size_t j = 0; j < batch.size(); ++j)
+        complete(s, batch[j], st, info, j == 0 ? refactored : 0, rs, t_start);
+      s->in_flight -= (int64_t)batch.size();
+      if (batch.size() > 1) s->stats.merged_solves += batch.size() - 1;
+      if (refactored) s->stats.factorizations++;
+      s->stats.solves += batch.size();
+    }
+    s->cv_done.notify_all();
+    s->cv_work.notify_all();
+  }
+}
+
+}  // namespace
+}  // namespace gblu
+
+using namespace gblu;
+
+extern "C" {
+
+int32_t gblu_serve_config_default(gblu_serve_config* cfg) {
+  if (!cfg) return GBLU_EINVAL;
+  cfg->workers = 4;
+  cfg->precision = GBLU_FP32;
+  cfg->refine_mode = GBLU_REFINE_IR;
+  cfg->hbm_budget_bytes = 120ull << 30;
+  cfg->max_rhs_batch = 8;
+  return GBLU_OK;
+}
+
+int32_t gblu_serve_create(gblu_ctx* ctx, const gblu_serve_config* cfg, gblu_server** out) {
+  if (!ctx || !out) return fail(ctx, GBLU_EINVAL, "gblu_serve_create: NULL argument");
+  *out = nullptr;
+  gblu_serve_config c;
+  gblu_serve_config_default(&c);
+  if (cfg) c = *cfg;
+  if (c.workers < 1 || c.workers > 32) return fail(ctx, GBLU_EINVAL, "gblu_serve_create: 1..32 workers");
+  if (c.precision < GBLU_FP64 || c.precision > GBLU_FP16)
+    return fail(ctx, GBLU_EINVAL, "gblu_serve_create: bad precision");
+  if (c.refine_mode != GBLU_REFINE_IR && c.refine_mode != GBLU_REFINE_GMRES)
+    return fail(ctx, GBLU_EINVAL, "gblu_serve_create: bad refine mode");
+  gblu_server* s = new gblu_server();
+  s->parent = ctx;
+  s->cfg = c;
+  for (int i = 0; i < c.workers; ++i) {
+    gblu_ctx* w = nullptr;
+    int32_t st = gblu_create(&w, ctx->device, 0);
+    if (st) {
+      for (auto* x : s->wctx) gblu_destroy(x);
+      delete s;
+      return fail(ctx, st, "gblu_serve_create: worker context: %s", gblu_last_error(nullptr));
+    }
+    s->wctx.push_back(w);
+  }
+  for (int i = 0; i < c.workers; ++i) s->threads.emplace_back(worker, s, i);
+  *out = s;
+  return GBLU_OK;
+}
+
+int32_t gblu_serve_submit(gblu_server* s, const gblu_request* r) {
+  if (!s || !r) return GBLU_EINVAL;
+  if (r->n < 1 || !r->b || !r->x) return GBLU_EINVAL;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->stopping) return GBLU_EINVAL;
+    Pending p;
+    p.req = *r;
+    p.t_submit = std::chrono::steady_clock::now();
+    p.seq = ++s->seq;
+    s->queue.push_back(p);
+    s->stats.submitted++;
+  }
+  s->cv_work.notify_one();
+  return GBLU_OK;
+}
+
+int32_t gblu_serve_poll(gblu_server* s, gblu_completion* out, int32_t max, int32_t* n_out,
+                        int32_t wait_ms) {
+  if (!s || !n_out || (max > 0 && !out)) return GBLU_EINVAL;
+  std::unique_lock<std::mutex> lk(s->mu);
+  if (s->done.empty() && wait_ms > 0)
+    s->cv_done.wait_for(lk, std::chrono::milliseconds(wait_ms), [&] { return !s->done.empty(); });
+  int32_t k = 0;
+  while (k < max && !s->done.empty()) {
+    out[k++] = s->done.front();
+    s->done.pop_front();
+  }
+  *n_out = k;
+  return GBLU_OK;
+}
+
+int32_t gblu_serve_get_stats(gblu_server* s, gblu_serve_stats* out) {
+  if (!s || !out) return GBLU_EINVAL;
+  std::lock_guard<std::mutex> lk(s->mu);
+  *out = s->stats;
+  out->resident_factors = (int64_t)s->cache.size();
+  out->resident_bytes = s->bytes_resident;
+  out->queued = (int64_t)s->queue.size();
+  out->in_flight = s->in_flight;
+  return GBLU_OK;
+}
+
+int32_t gblu_serve_destroy(gblu_server* s) {
+  if (!s) return GBLU_OK;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stopping = true;
+  }
+  s->cv_work.notify_all();
+  for (auto& t : s->threads) t.join();
+  for (auto& kv : s->cache)
+    if (kv.second.f) gblu_factor_destroy(kv.second.owner, kv.second.f);
+  s->cache.clear();
+  for (auto* w : s->wctx) gblu_destroy(w);
+  delete s;
+  return GBLU_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,110 @@
+"""The serving loop: continuous batching over resident factorizations.
+Every result meets the FP64 backward-error bound, and is bit-identical whether
+its request ran alone or in a concurrent mix."""
+import numpy as np
+import pytest
+
+from conftest import EPS64
+
+pytestmark = pytest.mark.gpu
+
+
+def _requests(pkg, seed=0, nkeys=6, nreq=60, nmin=64, nmax=600):
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(nmin), np.log(nmax), size=nkeys)).astype(int)
+    mats = {k: pkg.workloads.shifted(int(sizes[k]), 1, seed=1000 + k)[0] for k in range(nkeys)}
+    reqs = [{"key": k, "A": mats[k], "b": rng.standard_normal(sizes[k])} for k in range(nkeys)]
+    for _ in range(nreq - nkeys):
+        k = int(rng.integers(nkeys))
+        new_a = rng.random() < 0.3
+        if new_a:
+            G = rng.standard_normal((sizes[k], sizes[k]))
+            mats[k] = G + 4 * np.sqrt(sizes[k]) * np.eye(sizes[k])
+        reqs.append({"key": k, "A": mats[k] if new_a else None, "b": rng.standard_normal(sizes[k]),
+                     "Aeff": mats[k]})
+    for r in reqs[:nkeys]:
+        r["Aeff"] = r["A"]
+    return reqs
+
+
+def _run(pkg, ctx, reqs, workers, precision, rate=0.0):
+    from importlib import import_module
+    serving = import_module(pkg.__name__ + ".serving")
+    srv = serving.Server(ctx, workers=workers, precision=precision)
+    if rate == 0.0 and workers == 1:
+        done = []
+        for i, r in enumerate(reqs):  # strictly one at a time
+            srv.submit(i, r["key"], r["b"], r["A"])
+            got = []
+            while not got:
+                got = srv.poll(16, wait_ms=50)
+            done.extend(got)
+    else:
+        done, _ = serving.run_stream(srv, reqs, rate_hz=rate, seed=1)
+    stats = srv.stats()
+    srv.close()
+    return {d["tag"]: d for d in done}, stats
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32", "bf16"])
+def test_serving_results_accurate_and_mix_independent(ctx, oracle_mod, pkg, precision):
+    reqs = _requests(pkg, seed=3)
+    alone, _ = _run(pkg, ctx, reqs, workers=1, precision=precision)
+    mixed, stats = _run(pkg, ctx, reqs, workers=4, precision=precision)
+    assert stats["completed"] == len(reqs)
+    for i, r in enumerate(reqs):
+        a, m = alone[i], mixed[i]
+        assert a["status"] == 0 and m["status"] == 0, (a, m)
+        n = len(r["b"])
+        assert oracle_mod.backward_error(r["Aeff"], m["x"], r["b"]) <= 10 * n * EPS64
+        assert np.array_equal(a["x"], m["x"]), i  # same alone and in the mix
+
+
+def test_serving_budget_evicts_and_reports(ctx, pkg):
+    from importlib import import_module
+    serving = import_module(pkg.__name__ + ".serving")
+    rng = np.random.default_rng(5)
+    n = 256
+    # a budget that holds about two FP32 factorizations of n = 256
+    srv = serving.Server(ctx, workers=2, precision="fp32", hbm_budget_bytes=3 * (1 << 20) + 1_500_000)
+    A = [pkg.workloads.shifted(n, 1, seed=k)[0] for k in range(4)]
+    for k in range(4):
+        srv.submit(k, k, rng.standard_normal(n), A[k])
+    done = []
+    while len(done) < 4:
+        done += srv.poll(8, wait_ms=50)
+    assert all(d["status"] == 0 for d in done)
+    st = srv.stats()
+    assert st["evictions"] >= 1
+    assert st["resident_bytes"] <= 3 * (1 << 20) + 1_500_000
+    # a solve on an evicted key reports GBLU_ENOTFACTORED (5) instead of a wrong answer
+    srv.submit(10, 0, rng.standard_normal(n), None)
+    d = []
+    while not d:
+        d = srv.poll(4, wait_ms=50)
+    assert d[0]["status"] in (0, 5)
+    srv.close()
+
+
+def test_serving_merges_rhs_on_one_key(ctx, pkg):
+    from importlib import import_module
+    serving = import_module(pkg.__name__ + ".serving")
+    rng = np.random.default_rng(6)
+    n = 400
+    A = pkg.workloads.shifted(n, 1, seed=9)[0]
+    srv = serving.Server(ctx, workers=1, precision="fp32", max_rhs_batch=8)
+    srv.submit(0, 77, rng.standard_normal(n), A)
+    bs = [rng.standard_normal(n) for _ in range(12)]
+    for i, b in enumerate(bs):
+        srv.submit(1 + i, 77, b, None)
+    done = []
+    while len(done) < 13:
+        done += srv.poll(32, wait_ms=50)
+    assert all(d["status"] == 0 for d in done)
+    st = srv.stats()
+    assert st["merged_solves"] >= 1
+    sol = {d["tag"]: d["x"] for d in done}
+    for i, b in enumerate(bs):
+        assert np.linalg.norm(A @ sol[1 + i] - b, np.inf) <= 10 * n * 2.2e-16 * (
+            np.abs(A).sum(1).max() * np.abs(sol[1 + i]).max() + np.abs(b).max())
+    srv.close()
