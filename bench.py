@@ -352,7 +352,13 @@ def run_gpu(args, rank, world, local):
     }
 
     if args.suite and rank == 0:
-        line["mixed"] = run_mixed_suite(pkg, cu, ctx, args)
+        parts = set(args.suite.split(","))
+        if "mixed" in parts or "all" in parts:
+            line["mixed"] = run_mixed_suite(pkg, cu, ctx, args)
+        if "batched" in parts or "all" in parts:
+            line["batched"] = run_batched_suite(pkg, cu, ctx, args)
+        if "serving" in parts or "all" in parts:
+            line["serving"] = run_serving_suite(pkg, cu, ctx, args)
 
     if rank == 0 and not args.no_cpu:
         # bounded CPU sample of the same workload on this host
@@ -418,6 +424,118 @@ def run_mixed_suite(pkg, cu, ctx, args):
     return out
 
 
+def run_batched_suite(pkg, cu, ctx, args):
+    """20,000 systems, n_i ~ U{8..256}, A_i = I - g_i J_i: one graph launch per solve."""
+    import ctypes
+    lib = ctx.lib
+    sizes, A, b, _ = pkg.workloads.batch(args.batch_count, seed=0)
+    a_off, b_off = pkg.workloads.offsets(sizes)
+    dA = pkg.DeviceMatrix.from_host(A.reshape(-1, 1))
+    dB0 = pkg.DeviceMatrix.from_host(b.reshape(-1, 1))
+    dB = pkg.DeviceMatrix(len(b), 1)
+    out = {"count": int(len(sizes)), "n_range": [int(sizes.min()), int(sizes.max())],
+           "a_bytes": int(A.nbytes), "lu_flops": float(sum(pkg_lu_flops(int(n)) for n in sizes))}
+    for label, prec in (("fp64", 0), ("fp32_ir", 1)):
+        h = ctypes.c_void_p()
+        sz = np.ascontiguousarray(sizes, dtype=np.int64)
+        st = lib.gblu_batch_create(ctx.handle, len(sz), sz.ctypes.data, prec, ctypes.byref(h))
+        if st != 0:
+            out[label] = {"error": lib.gblu_last_error(ctx.handle).decode()}
+            continue
+        info = np.zeros(len(sz), dtype=np.int64)
+
+        def once():
+            dB.copy_from(dB0, ctx.stream)
+            st2 = lib.gblu_batch_solve(ctx.handle, h, dA.ptr, dB.ptr, 1, info.ctypes.data)
+            if st2 != 0:
+                raise RuntimeError(lib.gblu_last_error(ctx.handle).decode())
+
+        once()
+        e0, e1 = cu.Event(), cu.Event()
+        reps = 3
+        e0.record(ctx.stream)
+        for _ in range(reps):
+            once()
+        e1.record(ctx.stream)
+        e1.synchronize()
+        ms = e0.elapsed_ms(e1) / reps
+        X = dB.to_host()[:, 0]
+        worst = 0.0
+        rng = np.random.default_rng(1)
+        for i in rng.choice(len(sizes), size=min(200, len(sizes)), replace=False):
+            n = int(sizes[i])
+            Ai = A[a_off[i]:a_off[i] + n * n].reshape(n, n, order="F")
+            worst = max(worst, pkg_backward_error(Ai, X[b_off[i]:b_off[i] + n], b[b_off[i]:b_off[i] + n]) / n)
+        out[label] = {"ms_per_batch": ms, "solves_per_s": len(sizes) / (ms / 1000.0),
+                      "gflops": out["lu_flops"] / (ms / 1000.0) / 1e9,
+                      "max_backward_error_over_n_eps": worst / EPS64,
+                      "failed_info": int((info != 0).sum())}
+        lib.gblu_batch_destroy(ctx.handle, h)
+    out["speedup_fp32_ir_vs_fp64"] = out["fp32_ir"]["solves_per_s"] / out["fp64"]["solves_per_s"]
+    # CPU: LAPACK loop over a bounded sample of the same systems, all host threads
+    import oracle
+    k = min(2000, len(sizes))
+    t0 = time.perf_counter()
+    for i in range(k):
+        n = int(sizes[i])
+        LU, ipiv, _ = oracle.lapack_getrf(A[a_off[i]:a_off[i] + n * n].reshape(n, n, order="F"))
+        oracle.lapack_getrs(LU, ipiv, b[b_off[i]:b_off[i] + n])
+    dt = time.perf_counter() - t0
+    out["cpu_baseline"] = {"solves_per_s": k / dt, "sample": f"first {k} systems, scipy LAPACK loop",
+                           "cores": os.cpu_count()}
+    dA.free(); dB0.free(); dB.free()
+    return out
+
+
+def pkg_lu_flops(n):
+    return 2.0 * n ** 3 / 3.0 + 2.0 * n * n
+
+
+def run_serving_suite(pkg, cu, ctx, args):
+    """Poisson stream: n log-uniform in [64, 4096], 30% new A (G + 4 sqrt(n) I),
+    70% new b on a resident factorization; mixed FP32 factors with FP64
+    refinement; budget 120 GB; p50/p99 latency at swept rates."""
+    from importlib import import_module
+    serving = import_module(pkg.__name__ + ".serving")
+    rng = np.random.default_rng(0)
+    nkeys = 24
+    sizes = np.exp(rng.uniform(np.log(64), np.log(4096), size=nkeys)).astype(int)
+    pool = {k: [pkg.workloads.shifted(int(sizes[k]), 1, seed=100 * k + v)[0] for v in range(2)]
+            for k in range(nkeys)}
+    nreq = args.serve_requests
+    reqs, eff = [], []
+    cur = {k: 0 for k in range(nkeys)}
+    for k in range(nkeys):  # every key starts with its matrix
+        reqs.append({"key": k, "A": pool[k][0], "b": rng.standard_normal(sizes[k])})
+        eff.append(pool[k][0])
+    for _ in range(nreq):
+        k = int(rng.integers(nkeys))
+        if rng.random() < 0.3:
+            cur[k] ^= 1
+            reqs.append({"key": k, "A": pool[k][cur[k]], "b": rng.standard_normal(sizes[k])})
+        else:
+            reqs.append({"key": k, "A": None, "b": rng.standard_normal(sizes[k])})
+        eff.append(pool[k][cur[k]])
+    out = {"keys": nkeys, "requests": len(reqs), "n_range": [int(sizes.min()), int(sizes.max())],
+           "new_A_fraction": 0.3, "budget_gb": 120, "precision": "fp32 factors + FP64 IR", "rates": []}
+    for rate in args.serve_rates:
+        srv = serving.Server(ctx, workers=4, precision="fp32", hbm_budget_bytes=120 << 30)
+        done, wall = serving.run_stream(srv, reqs, rate_hz=rate, seed=int(rate))
+        st = srv.stats()
+        srv.close()
+        summ = serving.latency_summary(done, wall)
+        worst = 0.0
+        for d in done:
+            if d["status"] == 0 and d["tag"] % 7 == 0:
+                i = d["tag"]
+                n = len(reqs[i]["b"])
+                worst = max(worst, pkg_backward_error(eff[i], d["x"], reqs[i]["b"]) / (n * EPS64))
+        summ.update({"offered_rate_hz": rate, "max_backward_error_over_n_eps": worst,
+                     "merged_solves": st["merged_solves"], "factorizations": st["factorizations"]})
+        out["rates"].append(summ)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -428,8 +546,11 @@ def main():
     ap.add_argument("--nrhs", type=int, default=16)
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--suite", action="store_true")
+    ap.add_argument("--suite", default="", help="comma list: mixed,batched,serving (or all)")
+    ap.add_argument("--batch-count", type=int, default=20000)
+    ap.add_argument("--serve-requests", type=int, default=300)
     ap.add_argument("--mixed-n", type=int, default=16384)
+    ap.add_argument("--serve-rates", type=float, nargs="*", default=[100.0, 400.0, 0.0])
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":

@@ -20,7 +20,10 @@
 // are bit-identical to the reference's blocked LU for any blocking.
 #include <algorithm>
 #include <cstdio>
+#include <mutex>
 #include <type_traits>
+
+#include <cooperative_groups.h>
 
 #include "device_util.cuh"
 #include "gblu_internal.h"
@@ -200,6 +203,147 @@ panel_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w,
     if (i < nloc) A[(base + i) + (c0 + j) * lda] = tile[idx];
   }
   if (cta == 0 && tid == 0 && info_local != 0 && *info_out == 0) *info_out = info_local;
+}
+
+// ---------------------------------------------------------------------------
+// Cluster panel kernel: the same getf2 on rows [c0, m) x columns [c0, c0+w),
+// for panels that fit in the shared memory of one thread-block cluster (up to
+// 16 CTAs).  Pivot candidates, the candidate rows and the diagonal row live in
+// each CTA's shared memory; after the hardware cluster barrier every CTA reads
+// the others' slots through distributed shared memory, so a column costs one
+// cluster barrier and one round of DSMEM loads instead of a grid barrier and
+// two L2 round trips.  The arithmetic per element is the grid kernel's.
+template <typename T>
+__global__ void __launch_bounds__(kPanelThreads)
+panel_cluster_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w,
+                     int64_t* __restrict__ ipiv, int64_t* __restrict__ info_out, int R) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* tile = reinterpret_cast<T*>(smem_raw);  // column j at tile + j*R
+  __shared__ T s_cval[2];
+  __shared__ int64_t s_crow[2];
+  __shared__ T s_crowv[2][kPanelMaxW];
+  __shared__ T s_diagv[2][kPanelMaxW];
+  __shared__ T pivrow[kPanelMaxW];
+  __shared__ T diagrow[kPanelMaxW];
+  __shared__ T red_v[kPanelThreads / 32];
+  __shared__ int64_t red_g[kPanelThreads / 32];
+  __shared__ int64_t s_best_g;
+  __shared__ int s_best_c;
+
+  const int G = (int)cluster.num_blocks();
+  const int cta = (int)cluster.block_rank();
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t base = c0 + (int64_t)cta * R;
+  const int nloc = (int)max((int64_t)0, min((int64_t)R, m - base));
+
+  for (int idx = tid; idx < w * R; idx += blockDim.x) {
+    int j = idx / R, i = idx - j * R;
+    tile[idx] = (i < nloc) ? A[(base + i) + (c0 + j) * lda] : T(0);
+  }
+  int64_t info_local = 0;
+  __syncthreads();
+
+  for (int k = 0; k < w; ++k) {
+    const int64_t d = c0 + k;
+    const int buf = k & 1;
+    const T* colk = tile + (size_t)k * R;
+    T bv = T(0);
+    int64_t bg = -1;
+    for (int i = tid; i < nloc; i += blockDim.x) {
+      int64_t g = base + i;
+      T v = absval(colk[i]);
+      if (g >= d && v > bv) { bv = v; bg = g; }
+    }
+    for (int off = 16; off; off >>= 1) {
+      T ov = __shfl_down_sync(0xffffffffu, bv, off);
+      int64_t og = __shfl_down_sync(0xffffffffu, bg, off);
+      if (cand_better(ov, og, bv, bg)) { bv = ov; bg = og; }
+    }
+    if (lane == 0) { red_v[warp] = bv; red_g[warp] = bg; }
+    __syncthreads();
+    if (warp == 0) {
+      bv = lane < (kPanelThreads / 32) ? red_v[lane] : T(0);
+      bg = lane < (kPanelThreads / 32) ? red_g[lane] : -1;
+      for (int off = 16; off; off >>= 1) {
+        T ov = __shfl_down_sync(0xffffffffu, bv, off);
+        int64_t og = __shfl_down_sync(0xffffffffu, bg, off);
+        if (cand_better(ov, og, bv, bg)) { bv = ov; bg = og; }
+      }
+      if (lane == 0) { s_cval[buf] = bv; s_crow[buf] = bg; s_best_g = bg; }
+    }
+    __syncthreads();
+    if (tid < w) {
+      if (s_best_g >= 0) s_crowv[buf][tid] = tile[(size_t)tid * R + (s_best_g - base)];
+      if (d >= base && d < base + nloc) s_diagv[buf][tid] = tile[(size_t)tid * R + (d - base)];
+    }
+    cluster.sync();  // publishes the slots of step k (release/acquire across the cluster)
+
+    // winner over the G candidates, read through distributed shared memory
+    bv = T(0);
+    bg = -1;
+    int bc = -1;
+    if (tid < G) {
+      const T* rv = cluster.map_shared_rank(&s_cval[buf], tid);
+      const int64_t* rr = cluster.map_shared_rank(&s_crow[buf], tid);
+      bv = *rv;
+      bg = *rr;
+      bc = bg >= 0 ? tid : -1;
+    }
+    if (warp == 0) {
+      for (int off = 16; off; off >>= 1) {
+        T ov = __shfl_down_sync(0xffffffffu, bv, off);
+        int64_t og = __shfl_down_sync(0xffffffffu, bg, off);
+        int oc = __shfl_down_sync(0xffffffffu, bc, off);
+        if (cand_better(ov, og, bv, bg)) { bv = ov; bg = og; bc = oc; }
+      }
+      if (lane == 0) { s_best_g = bg; s_best_c = bc; }
+    }
+    __syncthreads();
+    const int64_t p = s_best_g < 0 ? d : s_best_g;
+    const int pc = s_best_c;
+    const int downer = (int)((d - c0) / R);
+    if (tid < w) {
+      const T dv = *cluster.map_shared_rank(&s_diagv[buf][tid], downer);
+      diagrow[tid] = dv;
+      pivrow[tid] = (p == d) ? dv : *cluster.map_shared_rank(&s_crowv[buf][tid], pc);
+    }
+    if (cta == 0 && tid == 0) ipiv[d] = p + 1;
+    __syncthreads();
+    const T piv = pivrow[k];
+    if (piv != T(0)) {
+      if (p != d) {
+        if (tid < w) {
+          if (d >= base && d < base + nloc) tile[(size_t)tid * R + (d - base)] = pivrow[tid];
+          if (p >= base && p < base + nloc) tile[(size_t)tid * R + (p - base)] = diagrow[tid];
+        }
+        __syncthreads();
+      }
+      const T inv = T(1) / piv;
+      for (int i = tid; i < nloc; i += blockDim.x)
+        if (base + i > d) tile[(size_t)k * R + i] *= inv;
+    } else if (info_local == 0) {
+      info_local = d + 1;
+    }
+    __syncthreads();
+    const int ncols = w - k - 1;
+    for (int idx = tid; idx < ncols * nloc; idx += blockDim.x) {
+      int jj = idx / nloc, i = idx - jj * nloc;
+      int j = k + 1 + jj;
+      if (base + i > d) {
+        T l = tile[(size_t)k * R + i];
+        tile[(size_t)j * R + i] = fma(-l, pivrow[j], tile[(size_t)j * R + i]);
+      }
+    }
+    __syncthreads();
+  }
+  for (int idx = tid; idx < w * R; idx += blockDim.x) {
+    int j = idx / R, i = idx - j * R;
+    if (i < nloc) A[(base + i) + (c0 + j) * lda] = tile[idx];
+  }
+  if (cta == 0 && tid == 0 && info_local != 0 && *info_out == 0) *info_out = info_local;
+  cluster.sync();  // no CTA leaves while another may still read its shared memory
 }
 
 // ---------------------------------------------------------------------------
@@ -437,9 +581,69 @@ struct Driver {
     if (err == cudaSuccess && e != cudaSuccess) err = e;
   }
 
+  // Cluster panel when the whole panel fits in one cluster's shared memory and
+  // each CTA's share of the rank-1 updates stays small; 0 if not launchable.
+  bool panel_cluster(int64_t c0, int w) {
+    const int64_t M = p.m - c0;
+    const int64_t rmax = sizeof(T) == 4 ? 1536 : 192;  // rows per CTA
+    int cs = (int)std::min<int64_t>(16, std::max<int64_t>(1, (M + 255) / 256));
+    int64_t R = (M + cs - 1) / cs;
+    if (R > rmax) return false;
+    const size_t smem = (size_t)R * w * sizeof(T);
+    if (!cluster_ok(cs, smem)) return false;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(cs);
+    cfg.blockDim = dim3(kPanelThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = cs;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    double fl = 0;
+    for (int k = 0; k < w; ++k) fl += (double)(M - k - 1) * (1.0 + 2.0 * (w - k - 1));
+    LaunchScope ls(K_PANEL, fl, 2.0 * M * w * sizeof(T), s);
+    check(cudaLaunchKernelEx(&cfg, panel_cluster_kernel<T>, p.A, p.lda, p.m, c0, w, p.ipiv, p.info,
+                             (int)R));
+    return true;
+  }
+
+  static bool cluster_ok(int cs, size_t smem) {
+    static std::mutex mu;
+    static int cache[17][2] = {};  // [cs][T] : 0 unknown, 1 ok, -1 no (per process, one device family)
+    std::lock_guard<std::mutex> g(mu);
+    int& c = cache[cs][sizeof(T) == 4 ? 0 : 1];
+    if (c == 0) {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(cs);
+      cfg.blockDim = dim3(kPanelThreads);
+      cfg.dynamicSmemBytes = (sizeof(T) == 4 ? 1536 : 192) * kPanelMaxW * sizeof(T);
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeClusterDimension;
+      attr[0].val.clusterDim.x = cs;
+      attr[0].val.clusterDim.y = 1;
+      attr[0].val.clusterDim.z = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      int nclusters = 0;
+      cudaError_t e = cudaOccupancyMaxActiveClusters(&nclusters, panel_cluster_kernel<T>, &cfg);
+      c = (e == cudaSuccess && nclusters >= 1) ? 1 : -1;
+      cudaGetLastError();
+    }
+    (void)smem;
+    return c == 1;
+  }
+
   void panel(int64_t c0, int w) {
     const int64_t M = p.m - c0;
     const DeviceInfo& di = device_info(device);
+    if (p.use_cluster_panel && panel_cluster(c0, w)) {
+      laswp(c0, w);
+      return;
+    }
     int G = p.panel_ctas > 0 ? p.panel_ctas
                              : (int)std::max<int64_t>(1, (M + kPanelRowsTarget - 1) / kPanelRowsTarget);
     int R = (int)((M + G - 1) / G);
@@ -477,7 +681,12 @@ struct Driver {
       check(cudaLaunchKernelEx(&cfg, panel_kernel<T>, p.A, p.lda, p.m, c0, w, p.ipiv, p.info,
                                p.scratch, p.slots, R));
     }
-    // interchanges on every other column
+    laswp(c0, w);
+  }
+
+  // interchanges of the leaf on every other column
+  void laswp(int64_t c0, int w) {
+    const DeviceInfo& di = device_info(device);
     const int64_t nother = p.n - w;
     if (nother > 0) {
       int64_t warps_needed = nother;
@@ -563,6 +772,10 @@ void getrf_configure(int device) {
   const int cap = (int)std::min<size_t>(di.smem_optin, 200 * 1024);
   cudaFuncSetAttribute(panel_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
   cudaFuncSetAttribute(panel_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  cudaFuncSetAttribute(panel_cluster_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  cudaFuncSetAttribute(panel_cluster_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  cudaFuncSetAttribute(panel_cluster_kernel<double>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  cudaFuncSetAttribute(panel_cluster_kernel<float>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
   cudaFuncSetAttribute(perm_from_ipiv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        kPermSmemMax * (int)sizeof(int32_t));
   getrs_configure(device);

@@ -74,8 +74,6 @@ namespace gblu {
 namespace {
 
 uint64_t factor_bytes_estimate(gblu_server* s, gblu_ctx* c, int64_t n) {
-  gblu_factor* probe = nullptr;
-  (void)probe;
   (void)c;
   // same arithmetic as gblu_factor_create: report what the object will hold
   const int64_t ld = std::max<int64_t>(32, ((n + 31) / 32) * 32);
