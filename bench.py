@@ -404,6 +404,7 @@ def run_mixed_suite(pkg, cu, ctx, args):
 
         once()
         cu.device_synchronize()
+        ctx.profile_enable(True)
         e0, e1 = cu.Event(), cu.Event()
         e0.record(ctx.stream)
         st = {}
@@ -412,10 +413,14 @@ def run_mixed_suite(pkg, cu, ctx, args):
         e1.record(ctx.stream)
         e1.synchronize()
         ms = e0.elapsed_ms(e1) / reps
+        prof = ctx.profile_read(reset=True)
+        ctx.profile_enable(False)
         X = dB.to_host()
         be = max(pkg_backward_error(A, X[:, j], B[:, j]) for j in range(nrhs))
         out[label] = {"ms_per_solve_set": ms, "solves_per_s": nrhs / (ms / 1000), "backward_error": be,
-                      "stats": st}
+                      "stats": st,
+                      "kernel_ms": {k: round(v["ms"] / reps, 3) for k, v in prof.items()
+                                    if k != "launches" and v["count"]}}
         f.close()
     for label in ("fp32_ir", "bf16_ir", "fp16_ir"):
         out["speedup_%s_vs_fp64" % label] = out[label]["solves_per_s"] / out["fp64_plain"]["solves_per_s"]

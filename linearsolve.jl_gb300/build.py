@@ -80,24 +80,26 @@ def build(verbose: bool = False, force: bool = False, jobs: int | None = None) -
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
         os.replace(tmp, LIB)
-    _build_tool(nvcc, "peak_fp64.cu", TOOL_LIB)
+    _build_tool(nvcc, TOOL_LIB)
     return LIB
 
 
 TOOL_LIB = os.path.join(HERE, "libgblu_tools.so")
 
 
-def _build_tool(nvcc: str, name: str, out: str) -> None:
-    """Measurement helpers used by bench.py (not part of the C ABI)."""
-    src = os.path.join(CSRC, "tools", name)
-    if os.path.exists(out) and os.path.getmtime(out) >= os.path.getmtime(src):
+def _build_tool(nvcc: str, out: str) -> None:
+    """Measurement and check helpers used by bench.py and tests (not part of the C ABI)."""
+    srcs = sorted(glob.glob(os.path.join(CSRC, "tools", "*.cu")))
+    newest = max([os.path.getmtime(x) for x in srcs] + [_headers_mtime()])
+    if os.path.exists(out) and os.path.getmtime(out) >= newest:
         return
     tmp = out + f".{os.getpid()}.tmp"
-    cmd = [nvcc, *ARCH, "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", "-cudart", "shared",
-           "-o", tmp, src, "-Xlinker", "-rpath", "-Xlinker", _cuda_lib_dir(nvcc)]
+    cmd = [nvcc, *ARCH, "-O3", "-std=c++17", "--fmad=false", "-Xcompiler", "-fPIC", "-shared",
+           "-cudart", "shared", "-I", CSRC, "-I", INCLUDE, "-o", tmp, *srcs,
+           "-Xlinker", "-rpath", "-Xlinker", _cuda_lib_dir(nvcc)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
-        raise RuntimeError(f"nvcc failed on tools/{name}:\n{r.stdout}\n{r.stderr}")
+        raise RuntimeError(f"nvcc failed on tools/:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, out)
 
 

@@ -69,6 +69,33 @@ __device__ __forceinline__ bool grid_barrier(DevScratch* s, unsigned target) {
   return ok != 0;
 }
 
+// Correctly rounded a / b from y = RN(1/b), following Markstein's division
+// (P. Markstein, IBM J. Res. Develop. 34(1):111-119, 1990): q = RN(a*y) is
+// within one ulp of a/b, the remainder r = a - b*q is exact with one fused
+// multiply-add, and RN(q + r*y) is the correctly rounded quotient.  The
+// sequence needs q, y and r*y clear of underflow and overflow; outside that
+// range (and for zeros, infinities and NaNs) the IEEE division is used.
+template <typename T>
+struct DivRange;
+template <>
+struct DivRange<double> {
+  static constexpr double lo = 0x1p-960, hi = 0x1p+960;
+};
+template <>
+struct DivRange<float> {
+  static constexpr float lo = 0x1p-100f, hi = 0x1p+100f;
+};
+
+template <typename T>
+__device__ __forceinline__ T div_markstein(T a, T b, T y) {
+  const T q = a * y;
+  const T aq = fabs(q), ay = fabs(y);
+  if (!(aq > DivRange<T>::lo && aq < DivRange<T>::hi && ay > DivRange<T>::lo && ay < DivRange<T>::hi))
+    return a / b;
+  const T r = fma(-b, q, a);
+  return fma(r, y, q);
+}
+
 template <typename T>
 __device__ __forceinline__ T ldcg(const T* p) { return __ldcg(p); }
 template <typename T>

@@ -77,10 +77,9 @@ panel_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w,
   const int64_t base = c0 + (int64_t)cta * R;
   const int nloc = (int)max((int64_t)0, min((int64_t)R, m - base));
 
-  for (int idx = tid; idx < w * R; idx += blockDim.x) {
-    int j = idx / R, i = idx - j * R;
-    tile[idx] = (i < nloc) ? A[(base + i) + (c0 + j) * lda] : T(0);
-  }
+  for (int j = 0; j < w; ++j)
+    for (int i = tid; i < R; i += blockDim.x)
+      tile[(size_t)j * R + i] = (i < nloc) ? A[(base + i) + (c0 + j) * lda] : T(0);
   int64_t info_local = 0;
   __syncthreads();
 
@@ -186,22 +185,19 @@ panel_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w,
       info_local = d + 1;
     }
     __syncthreads();
-    const int ncols = w - k - 1;
-    for (int idx = tid; idx < ncols * nloc; idx += blockDim.x) {
-      int jj = idx / nloc, i = idx - jj * nloc;
-      int j = k + 1 + jj;
-      if (base + i > d) {
-        T l = tile[(size_t)k * R + i];
+    // rank-1 update of this CTA's rows below the diagonal: one row per thread,
+    // columns k+1..w-1 in order (per element: one fma, k ascending)
+    for (int i = tid; i < nloc; i += blockDim.x) {
+      if (base + i <= d) continue;
+      const T l = tile[(size_t)k * R + i];
+      for (int j = k + 1; j < w; ++j)
         tile[(size_t)j * R + i] = fma(-l, pivrow[j], tile[(size_t)j * R + i]);
-      }
     }
     __syncthreads();
   }
 
-  for (int idx = tid; idx < w * R; idx += blockDim.x) {
-    int j = idx / R, i = idx - j * R;
-    if (i < nloc) A[(base + i) + (c0 + j) * lda] = tile[idx];
-  }
+  for (int j = 0; j < w; ++j)
+    for (int i = tid; i < nloc; i += blockDim.x) A[(base + i) + (c0 + j) * lda] = tile[(size_t)j * R + i];
   if (cta == 0 && tid == 0 && info_local != 0 && *info_out == 0) *info_out = info_local;
 }
 
@@ -238,10 +234,9 @@ panel_cluster_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int 
   const int64_t base = c0 + (int64_t)cta * R;
   const int nloc = (int)max((int64_t)0, min((int64_t)R, m - base));
 
-  for (int idx = tid; idx < w * R; idx += blockDim.x) {
-    int j = idx / R, i = idx - j * R;
-    tile[idx] = (i < nloc) ? A[(base + i) + (c0 + j) * lda] : T(0);
-  }
+  for (int j = 0; j < w; ++j)
+    for (int i = tid; i < R; i += blockDim.x)
+      tile[(size_t)j * R + i] = (i < nloc) ? A[(base + i) + (c0 + j) * lda] : T(0);
   int64_t info_local = 0;
   __syncthreads();
 
@@ -327,21 +322,18 @@ panel_cluster_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int 
       info_local = d + 1;
     }
     __syncthreads();
-    const int ncols = w - k - 1;
-    for (int idx = tid; idx < ncols * nloc; idx += blockDim.x) {
-      int jj = idx / nloc, i = idx - jj * nloc;
-      int j = k + 1 + jj;
-      if (base + i > d) {
-        T l = tile[(size_t)k * R + i];
+    // rank-1 update of this CTA's rows below the diagonal: one row per thread,
+    // columns k+1..w-1 in order (per element: one fma, k ascending)
+    for (int i = tid; i < nloc; i += blockDim.x) {
+      if (base + i <= d) continue;
+      const T l = tile[(size_t)k * R + i];
+      for (int j = k + 1; j < w; ++j)
         tile[(size_t)j * R + i] = fma(-l, pivrow[j], tile[(size_t)j * R + i]);
-      }
     }
     __syncthreads();
   }
-  for (int idx = tid; idx < w * R; idx += blockDim.x) {
-    int j = idx / R, i = idx - j * R;
-    if (i < nloc) A[(base + i) + (c0 + j) * lda] = tile[idx];
-  }
+  for (int j = 0; j < w; ++j)
+    for (int i = tid; i < nloc; i += blockDim.x) A[(base + i) + (c0 + j) * lda] = tile[(size_t)j * R + i];
   if (cta == 0 && tid == 0 && info_local != 0 && *info_out == 0) *info_out = info_local;
   cluster.sync();  // no CTA leaves while another may still read its shared memory
 }

@@ -50,6 +50,60 @@ __device__ __forceinline__ bool wait_flag(const int32_t* flags, int j, DevScratc
   return ok != 0;
 }
 
+// Published solution values are polled directly: the buffers a sweep's
+// dependents read are filled with an all-ones bit pattern (a NaN no
+// computation produces, outputs are written with canonical NaNs) before the
+// sweep, and each 4/8-byte value is single-copy atomic, so a value that is not
+// the sentinel is final.  This saves the flag round trip per tile.
+template <typename T>
+struct SweepBits;
+template <>
+struct SweepBits<double> {
+  using U = unsigned long long;
+  static constexpr U kSentinel = ~0ull;
+  static __device__ __forceinline__ U load(const double* p) {
+    U v;
+    asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+  }
+  static __device__ __forceinline__ double as_t(U v) { return __longlong_as_double((long long)v); }
+  static __device__ __forceinline__ double canon(double v) {
+    return v != v ? __longlong_as_double(0x7ff8000000000000ll) : v;
+  }
+};
+template <>
+struct SweepBits<float> {
+  using U = unsigned;
+  static constexpr U kSentinel = ~0u;
+  static __device__ __forceinline__ U load(const float* p) {
+    U v;
+    asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+  }
+  static __device__ __forceinline__ float as_t(U v) { return __uint_as_float(v); }
+  static __device__ __forceinline__ float canon(float v) { return v != v ? __uint_as_float(0x7fc00000u) : v; }
+};
+
+// Wait for one published value; false on timeout or when another CTA failed.
+template <typename T>
+__device__ __forceinline__ bool poll_value(const T* p, DevScratch* scr, T* out) {
+  using B = SweepBits<T>;
+  unsigned long long t0 = 0;
+  for (unsigned it = 0;; ++it) {
+    const typename B::U v = B::load(p);
+    if (v != B::kSentinel) { *out = B::as_t(v); return true; }
+    if ((it & 63u) == 63u) {
+      if (ld_volatile_i32(&scr->error) != 0) return false;
+      const unsigned long long now = global_ns();
+      if (t0 == 0) t0 = now;
+      else if (now - t0 > kSpinTimeoutNs) {
+        atomicCAS(&scr->error, 0, (int)DEV_TIMEOUT_SOLVE);
+        return false;
+      }
+    }
+  }
+}
+
 constexpr int kSweepThreads = 128;  // all issue copies; threads 0..63 own one row each
 constexpr int kStages = 3;          // tiles in flight per CTA
 
@@ -145,15 +199,22 @@ solve_sweep_kernel(int64_t n, const T* __restrict__ LU, int64_t lda, const int32
       const int cb = col_block(t);
       const int64_t c0 = (int64_t)cb * kTS;
       const int nc = (int)min((int64_t)kTS, n - c0);
-      if (!wait_flag(flags, cb, scr)) {
+      // solution values of block cb: FWD from Y, BWD from Out (through perm for 'T')
+      int ok = 1;
+      for (int idx = tid; idx < kTS * NR; idx += kSweepThreads) {
+        const int c = idx / NR, q = idx - c * NR;
+        T v = T(0);
+        if (q < nrhs && c < nc) {
+          const T* src = FWD ? &Y[(c0 + c) + q * ldy]
+                             : &Out[(TRANS ? (int64_t)perm[c0 + c] : c0 + c) + q * ldo];
+          if (!poll_value(src, scr, &v)) ok = 0;
+        }
+        sx[c][q] = v;
+      }
+      if (!__syncthreads_and(ok)) {
         cp_async_wait<0>();  // no copy may land after the CTA has left
         return;
       }
-      for (int idx = tid; idx < kTS * NR; idx += kSweepThreads) {
-        const int c = idx / NR, q = idx - c * NR;
-        sx[c][q] = (q < nrhs && c < nc) ? ldcg(&Y[(c0 + c) + q * ldy]) : T(0);
-      }
-      __syncthreads();
       if (tid < kTS) {
         if (FWD) {
 #pragma unroll 8
@@ -174,6 +235,8 @@ solve_sweep_kernel(int64_t n, const T* __restrict__ LU, int64_t lda, const int32
       continue;
     }
     // ---- diagonal block: warp shuffles within each 32-row half ----
+    // reciprocal of this row's diagonal entry, off the dependency chain
+    const T yrow = (!kUnit && valid && tid < kTS) ? T(1) / tile[r][r] : T(1);
     const int w_first = FWD ? 0 : 1, w_second = FWD ? 1 : 0;
     const int lo_second = FWD ? 32 : 0;  // first row of the second half
     (void)lo_second;
@@ -185,7 +248,7 @@ solve_sweep_kernel(int64_t n, const T* __restrict__ LU, int64_t lda, const int32
         for (int c = cbeg; c < cend; ++c) {
 #pragma unroll
           for (int q = 0; q < NR; ++q) {
-            if (!kUnit && lane == c) acc[q] = acc[q] / tile[c][c];
+            if (!kUnit && lane == c) acc[q] = div_markstein(acc[q], tile[c][c], yrow);
             const T xc = __shfl_sync(0xffffffffu, acc[q], c);
             if (r > c && r < nr) acc[q] = fma(-tile[c][r], xc, acc[q]);
           }
@@ -194,7 +257,7 @@ solve_sweep_kernel(int64_t n, const T* __restrict__ LU, int64_t lda, const int32
         for (int c = cbeg; c >= cend; --c) {
 #pragma unroll
           for (int q = 0; q < NR; ++q) {
-            if (!kUnit && r == c) acc[q] = acc[q] / tile[c][c];
+            if (!kUnit && r == c) acc[q] = div_markstein(acc[q], tile[c][c], yrow);
             const T xc = __shfl_sync(0xffffffffu, acc[q], c - 32);
             if (r < c) acc[q] = fma(-tile[c][r], xc, acc[q]);
           }
@@ -215,7 +278,7 @@ solve_sweep_kernel(int64_t n, const T* __restrict__ LU, int64_t lda, const int32
           for (int c = 32; c < nr; ++c) {
 #pragma unroll
             for (int q = 0; q < NR; ++q) {
-              if (!kUnit && r == c) acc[q] = acc[q] / tile[c][c];
+              if (!kUnit && r == c) acc[q] = div_markstein(acc[q], tile[c][c], yrow);
               const T xc = __shfl_sync(0xffffffffu, acc[q], c - 32);
               if (r > c && r < nr) acc[q] = fma(-tile[c][r], xc, acc[q]);
             }
@@ -229,7 +292,7 @@ solve_sweep_kernel(int64_t n, const T* __restrict__ LU, int64_t lda, const int32
         for (int c = min(nr, 32) - 1; c >= 0; --c) {
 #pragma unroll
           for (int q = 0; q < NR; ++q) {
-            if (!kUnit && lane == c) acc[q] = acc[q] / tile[c][c];
+            if (!kUnit && lane == c) acc[q] = div_markstein(acc[q], tile[c][c], yrow);
             const T xc = __shfl_sync(0xffffffffu, acc[q], c);
             if (r < c) acc[q] = fma(-tile[c][r], xc, acc[q]);
           }
@@ -242,13 +305,12 @@ solve_sweep_kernel(int64_t n, const T* __restrict__ LU, int64_t lda, const int32
 #pragma unroll
     for (int q = 0; q < NR; ++q)
       if (q < nrhs) {
-        Y[(r0 + r) + q * ldy] = acc[q];
-        if (!FWD) Out[(TRANS ? (int64_t)perm[r0 + r] : r0 + r) + q * ldo] = acc[q];
+        const T v = SweepBits<T>::canon(acc[q]);
+        if (FWD) Y[(r0 + r) + q * ldy] = v;
+        else Out[(TRANS ? (int64_t)perm[r0 + r] : r0 + r) + q * ldo] = v;
       }
   }
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) st_release_i32(flags + blk, 1);
+  (void)flags;
 }
 
 template <typename T>
@@ -280,7 +342,8 @@ cudaError_t run_chunk(const GetrsPlan<T>& p, char trans, int nr, T* B, int64_t l
   const int64_t nblk = (p.n + kTS - 1) / kTS;
   int32_t* ffwd = p.flags;
   int32_t* fbwd = p.flags + nblk;
-  cudaError_t e = cudaMemsetAsync(p.flags, 0, 2 * nblk * sizeof(int32_t), s);
+  // dependents poll Y (forward) and B (backward): fill both with the sentinel
+  cudaError_t e = cudaMemsetAsync(p.work, 0xFF, (size_t)p.n * nr * sizeof(T), s);
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(&p.scratch->ticket, 0, sizeof(unsigned), s);
   if (e != cudaSuccess) return e;
@@ -302,6 +365,8 @@ cudaError_t run_chunk(const GetrsPlan<T>& p, char trans, int nr, T* B, int64_t l
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(&p.scratch->ticket, 0, sizeof(unsigned), s);
+  if (e != cudaSuccess) return e;
+  e = cudaMemset2DAsync(B, ldb * sizeof(T), 0xFF, p.n * sizeof(T), nr, s);
   if (e != cudaSuccess) return e;
   LaunchScope ls(K_SOLVE, sweep_flops, tri_bytes, s);
   if (!tr)

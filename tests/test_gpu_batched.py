@@ -128,3 +128,21 @@ def test_batch_rejects_oversize(ctx):
     sizes = np.array([10, 257], dtype=np.int64)
     st = ctx.lib.gblu_batch_create(ctx.handle, 2, sizes.ctypes.data, 0, ctypes.byref(h))
     assert st == 7
+
+
+def test_autotuner_finds_valid_schedule(ctx, oracle_mod, pkg, tmp_path, monkeypatch):
+    monkeypatch.setenv("GBLU_AUTOTUNE_FILE", str(tmp_path / "autotune.json"))
+    from importlib import import_module
+    at = import_module(pkg.__name__ + ".autotune")
+    sizes, A, b, _ = pkg.workloads.batch(300, seed=8)
+    sched = at.tune(ctx, sizes, "fp64", A=A, b=b, budget_s=5.0)
+    assert sched["upper"][-1] == 256 and sched["ms"] > 0
+    assert (tmp_path / "autotune.json").exists()
+    again = at.tune(ctx, sizes, "fp64", A=A, b=b)  # served from the cache
+    assert again["signature"] == sched["signature"]
+    bt = Batch(ctx, sizes, 0)
+    at.apply(ctx, bt.h, sched)
+    X, info = bt.solve(A, b)
+    _, Xref, _ = oracle_mod.gesv_batched(sizes, A, b)
+    assert np.array_equal(X, Xref)
+    bt.close()

@@ -238,3 +238,19 @@ def test_lapack_shaped_single(pkg, oracle_mod):
                      ipiv.ctypes.data, x.ctypes.data, ctypes.byref(ldb), ctypes.byref(info), 1)
     assert info.value == 0
     assert np.array_equal(x, oracle_mod.getrs(LUo, ipivo, b))
+
+
+def test_markstein_division_matches_ieee():
+    """The back-solve divides by U[j,j] with Markstein's FMA-based division
+    from a precomputed reciprocal; it must give the IEEE quotient bit for bit
+    (2^26 random operand pairs per type, edge significands included)."""
+    import ctypes
+    import os
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    lib = ctypes.CDLL(os.path.join(root, "linearsolve.jl_gb300", "libgblu_tools.so"))
+    lib.gblu_tool_divcheck.argtypes = [ctypes.c_int64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64),
+                                       ctypes.POINTER(ctypes.c_uint64)]
+    lib.gblu_tool_divcheck.restype = ctypes.c_int32
+    m64, m32 = ctypes.c_uint64(), ctypes.c_uint64()
+    assert lib.gblu_tool_divcheck(1 << 26, 12345, ctypes.byref(m64), ctypes.byref(m32)) == 0
+    assert m64.value == 0 and m32.value == 0, (m64.value, m32.value)
