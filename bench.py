@@ -231,6 +231,19 @@ def run_gpu(args, rank, world, local):
     n, nrhs = args.n, args.nrhs
     ctx = pkg.Context(local)
     stream = ctx.stream
+    if args.only_suite:  # profiling aid: the suite parts alone, one JSON object
+        parts = set(args.suite.split(","))
+        out = {}
+        if "mixed" in parts or "all" in parts:
+            out["mixed"] = run_mixed_suite(pkg, cu, ctx, args)
+        if "batched" in parts or "all" in parts:
+            out["batched"] = run_batched_suite(pkg, cu, ctx, args)
+        if "serving" in parts or "all" in parts:
+            out["serving"] = run_serving_suite(pkg, cu, ctx, args)
+        if rank == 0:
+            print(json.dumps(out))
+        dist.close()
+        return 0
     A, B = pkg.workloads.plain(n, nrhs, seed=0)
 
     # ---- device-resident workload (value) ----
@@ -553,6 +566,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--suite", default="", help="comma list: mixed,batched,serving (or all)")
     ap.add_argument("--batch-count", type=int, default=20000)
+    ap.add_argument("--only-suite", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=300)
     ap.add_argument("--mixed-n", type=int, default=16384)
     ap.add_argument("--serve-rates", type=float, nargs="*", default=[100.0, 400.0, 0.0])

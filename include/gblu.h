@@ -207,6 +207,9 @@ int32_t gblu_batch_schedule(gblu_ctx* ctx, gblu_batch* b, int32_t nbuckets, cons
                             const int32_t* threads, const int32_t* panel, const int32_t* ctas);
 int32_t gblu_batch_solve(gblu_ctx* ctx, gblu_batch* b, const double* A, double* B, int32_t loc,
                          int64_t* info_host);
+/* Per system, the refinement iterations of the last GBLU_FP32 solve (-1: the
+ * system was re-solved by the FP64 kernel; 0 for GBLU_FP64 batches). */
+int32_t gblu_batch_iterations(gblu_ctx* ctx, gblu_batch* b, int32_t* iterations_host);
 int32_t gblu_batch_destroy(gblu_ctx* ctx, gblu_batch* b);
 
 /* ---- serving loop ----------------------------------------------------------------

@@ -130,6 +130,7 @@ SIGNATURES = {
     "gblu_batch_create": (_I32, [_P, _I64, _P, _I32, ctypes.POINTER(_P)]),
     "gblu_batch_schedule": (_I32, [_P, _P, _I32, _P, _P, _P, _P]),
     "gblu_batch_solve": (_I32, [_P, _P, _P, _P, _I32, _P]),
+    "gblu_batch_iterations": (_I32, [_P, _P, _P]),
     "gblu_batch_destroy": (_I32, [_P, _P]),
     "gblu_serve_config_default": (_I32, [ctypes.POINTER(ServeConfig)]),
     "gblu_serve_create": (_I32, [_P, ctypes.POINTER(ServeConfig), ctypes.POINTER(_P)]),

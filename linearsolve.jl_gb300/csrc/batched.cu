@@ -40,6 +40,7 @@ struct BatchDev {
   unsigned* queue;        // next index into order (zeroed before the launch)
   int64_t* info;          // per system: getrf info; refinement failure sets flag
   int32_t* flag;          // per system: 1 = needs the FP64 path
+  int32_t* iters;         // per system: refinement iterations, -1 = FP64 re-solve
 };
 
 template <typename T>
@@ -97,10 +98,8 @@ __device__ int64_t factor_system(T* __restrict__ A, int n, int32_t* __restrict__
   for (int k0 = 0; k0 < n; k0 += NB) {
     const int kb = min(NB, n - k0);
     // panel rows [0, n) of columns k0..k0+kb-1 into shared memory (rows < k0 unused)
-    for (int idx = tid; idx < kb * n; idx += NT) {
-      const int j = idx / n, i = idx - j * n;
-      sm.P[j * kBatchMaxN + i] = A[i + (int64_t)(k0 + j) * n];
-    }
+    for (int j = 0; j < kb; ++j)
+      for (int i = k0 + tid; i < n; i += NT) sm.P[j * kBatchMaxN + i] = A[i + (int64_t)(k0 + j) * n];
     __syncthreads();
     for (int j = 0; j < kb; ++j) {
       const int col = k0 + j;
@@ -124,18 +123,17 @@ __device__ int64_t factor_system(T* __restrict__ A, int n, int32_t* __restrict__
         info = col + 1;
       }
       __syncthreads();
-      for (int idx = tid; idx < (kb - j - 1) * (n - col - 1); idx += NT) {
-        const int jj = j + 1 + idx / (n - col - 1);
-        const int i = col + 1 + idx % (n - col - 1);
-        T* q = sm.P + jj * kBatchMaxN;
-        q[i] = fma(-pc[i], q[col], q[i]);
+      for (int i = col + 1 + tid; i < n; i += NT) {  // one row per thread, columns in order
+        const T l = pc[i];
+        for (int jj = j + 1; jj < kb; ++jj) {
+          T* q = sm.P + jj * kBatchMaxN;
+          q[i] = fma(-l, q[col], q[i]);
+        }
       }
       __syncthreads();
     }
-    for (int idx = tid; idx < kb * (n - k0); idx += NT) {
-      const int j = idx / (n - k0), i = k0 + idx % (n - k0);
-      A[i + (int64_t)(k0 + j) * n] = sm.P[j * kBatchMaxN + i];
-    }
+    for (int j = 0; j < kb; ++j)
+      for (int i = k0 + tid; i < n; i += NT) A[i + (int64_t)(k0 + j) * n] = sm.P[j * kBatchMaxN + i];
     // interchanges on the other columns, in order (blocked_lufact.jl:126-141)
     for (int c = tid; c < n; c += NT) {
       if (c >= k0 && c < k0 + kb) continue;
@@ -173,14 +171,19 @@ __device__ int64_t factor_system(T* __restrict__ A, int n, int32_t* __restrict__
       __syncthreads();
       // A22 -= L21 * U12, each element k ascending (:186-656)
       const int nr = n - c1;
-      for (int idx = tid; idx < nr * nc; idx += NT) {
-        const int c = idx / nr, i = idx - c * nr;
-        T* a = A + (c1 + i) + (int64_t)(c1 + c) * n;
-        T v = *a;
+      const int lane = tid & 31, warp = tid >> 5;
+      for (int c = warp; c < nc; c += NT / 32) {   // a warp per column, lanes down the rows
+        T u[NB];
 #pragma unroll
-        for (int j = 0; j < NB; ++j)
-          if (j < kb) v = fma(-sm.P[j * kBatchMaxN + c1 + i], sm.U[j * kBatchMaxN + c], v);
-        *a = v;
+        for (int j = 0; j < NB; ++j) u[j] = j < kb ? sm.U[j * kBatchMaxN + c] : T(0);
+        T* acol = A + c1 + (int64_t)(c1 + c) * n;
+        for (int i = lane; i < nr; i += 32) {
+          T v = acol[i];
+#pragma unroll
+          for (int j = 0; j < NB; ++j)
+            if (j < kb) v = fma(-sm.P[j * kBatchMaxN + c1 + i], u[j], v);
+          acol[i] = v;
+        }
       }
     }
     __syncthreads();
@@ -313,9 +316,11 @@ batch_mixed_kernel(BatchDev d, const double* __restrict__ A64, float* __restrict
     const double bnorm = block_max<NT>(bm, redd);
     const double tol = tol_per_n * n;
     bool ok = false;
+    int iters_done = 0;
     if (info == 0) {
       double prev = INFINITY;
       for (int it = 0; it <= maxit; ++it) {
+        iters_done = it;
         if (it > 0) {  // r = b - A x (FP64, row-parallel, column order fixed)
           for (int i = threadIdx.x; i < n; i += NT) {
             double acc = b[i];
@@ -348,6 +353,7 @@ batch_mixed_kernel(BatchDev d, const double* __restrict__ A64, float* __restrict
     if (threadIdx.x == 0) {
       d.info[s] = 0;
       d.flag[s] = ok ? 0 : 1;  // the FP64 kernel re-solves flagged systems from A64
+      d.iters[s] = ok ? iters_done : -1;
     }
     __syncthreads();
   }
@@ -382,6 +388,7 @@ struct gblu_batch {
   int64_t* d_boff = nullptr;
   int64_t* d_info = nullptr;
   int32_t* d_flag = nullptr;
+  int32_t* d_iters = nullptr;
   unsigned* d_queues = nullptr;
   double* d_A = nullptr;      // FP64 A (input copy; factored in place by the FP64 path)
   double* d_Awork = nullptr;  // FP64 work for the fallback of the mixed path
@@ -436,6 +443,7 @@ cudaError_t launch_bucket(gblu_batch* b, const BatchBucket& k, bool mixed, int o
   d.queue = k.queue;
   d.info = b->d_info;
   d.flag = b->d_flag;
+  d.iters = b->d_iters;
   const int ctas = std::max(1, k.ctas);
 #define GBLU_BATCH_CASE(NT_, NB_)                                                   \
   if (k.nt == NT_ && k.nb == NB_)                                                   \
@@ -593,6 +601,7 @@ int32_t gblu_batch_create(gblu_ctx* ctx, int64_t count, const int64_t* sizes, in
   auto add = [&](size_t x) { size_t o = bytes; bytes += align256(x); return o; };
   size_t o_sizes = add(count * 4 + 4), o_order = add(count * 4 + 4), o_aoff = add(count * 8 + 8),
          o_boff = add(count * 8 + 8), o_info = add(count * 8 + 8), o_flag = add(count * 4 + 4),
+         o_iters = add(count * 4 + 4),
          o_q = add(2 * nbuckets_max * 4), o_A = add(b->a_total * 8 + 8), o_X = add(b->b_total * 8 + 8),
          o_ipiv = add(b->b_total * 4 + 4);
   size_t o_A32 = 0, o_B = 0, o_Aw = 0;
@@ -611,6 +620,7 @@ int32_t gblu_batch_create(gblu_ctx* ctx, int64_t count, const int64_t* sizes, in
   b->d_boff = reinterpret_cast<int64_t*>(base + o_boff);
   b->d_info = reinterpret_cast<int64_t*>(base + o_info);
   b->d_flag = reinterpret_cast<int32_t*>(base + o_flag);
+  b->d_iters = reinterpret_cast<int32_t*>(base + o_iters);
   b->d_queues = reinterpret_cast<unsigned*>(base + o_q);
   b->d_A = reinterpret_cast<double*>(base + o_A);
   b->d_X = reinterpret_cast<double*>(base + o_X);
@@ -711,6 +721,18 @@ int32_t gblu_batch_solve(gblu_ctx* ctx, gblu_batch* b, const double* A, double* 
   if (info_host)
     GBLU_CK(ctx, cudaMemcpyAsync(info_host, b->d_info, b->count * 8, cudaMemcpyDeviceToHost, s), "batch info");
   GBLU_CK(ctx, cudaStreamSynchronize(s), "batch solve");
+  return GBLU_OK;
+}
+
+int32_t gblu_batch_iterations(gblu_ctx* ctx, gblu_batch* b, int32_t* iterations_host) {
+  if (!ctx || !b || (b->count > 0 && !iterations_host))
+    return fail(ctx, GBLU_EINVAL, "gblu_batch_iterations: NULL argument");
+  if (b->count == 0) return GBLU_OK;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  DeviceGuard g(ctx->device);
+  GBLU_CK(ctx, cudaMemcpyAsync(iterations_host, b->d_iters, b->count * 4, cudaMemcpyDeviceToHost, ctx->stream),
+          "batch iterations");
+  GBLU_CK(ctx, cudaStreamSynchronize(ctx->stream), "batch iterations");
   return GBLU_OK;
 }
 
