@@ -9,7 +9,8 @@
 //      copies (FP16: each column of B scaled by an exact power of two so that
 //      its largest entry lies in [2^14, 2^15); |L21| <= 1 needs no scale);
 //   2. tc_gemm_kernel: per 128 x 128 output tile, one warp issues TMA loads
-//      (128-byte swizzled 128 x 64 boxes, 4-stage mbarrier ring), one thread
+//      (128-byte swizzled 128 x 64 boxes, 3-stage mbarrier ring, two CTAs per SM so
+//      one CTA's epilogue overlaps the other's main loop), one thread
 //      issues tcgen05.mma (M=128, N=128, K=16 per instruction) into a
 //      128-column FP32 accumulator in TMEM, and four warps read the
 //      accumulator back with tcgen05.ld and apply C -= acc * 2^-s in the
@@ -34,7 +35,7 @@
 namespace gblu {
 namespace tc {
 
-constexpr int BM = 128, BN = 128, BK = 64, STAGES = 4, THREADS = 192;
+constexpr int BM = 128, BN = 128, BK = 64, STAGES = 3, THREADS = 192;
 constexpr int UMMA_K = 16;
 constexpr uint32_t A_BYTES = BM * BK * 2;
 constexpr uint32_t B_BYTES = BN * BK * 2;
@@ -149,7 +150,7 @@ __host__ __device__ constexpr uint32_t idesc_f16(uint32_t fmt) {
 }
 
 template <uint32_t FMT>
-__global__ void __launch_bounds__(THREADS, 1)
+__global__ void __launch_bounds__(THREADS, 2)
 tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                float* __restrict__ C, int64_t ldc, int M, int N, int K,
                const float* __restrict__ inv_scale, int* __restrict__ err) {
@@ -221,17 +222,24 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
       const int row = m0 + q * 32 + lane;
 #pragma unroll 1
       for (int c0 = 0; c0 < BN; c0 += 32) {
+        // the 32 C values of this row first (independent loads in flight),
+        // then the accumulator columns, then C - acc * 2^-s
+        float cv[32];
+        const float* crow = C + (int64_t)row + (int64_t)(n0 + c0) * ldc;
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+          cv[j] = (row < M && n0 + c0 + j < N) ? crow[(int64_t)j * ldc] : 0.f;
         uint32_t v[32];
         tmem_ld_32cols(tbase + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, v);
         if (row < M) {
+          float* cw = C + (int64_t)row + (int64_t)(n0 + c0) * ldc;
 #pragma unroll
           for (int j = 0; j < 32; ++j) {
             const int col = n0 + c0 + j;
             if (col < N) {
               float a = __uint_as_float(v[j]);
               if (inv_scale) a *= inv_scale[col];
-              float* cp = C + (int64_t)row + (int64_t)col * ldc;
-              *cp = *cp - a;
+              cw[(int64_t)j * ldc] = cv[j] - a;
             }
           }
         }

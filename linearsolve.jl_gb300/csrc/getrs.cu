@@ -189,6 +189,27 @@ solve_sweep_kernel(int64_t n, const T* __restrict__ LU, int64_t lda, const int32
     if (t < ntiles) issue(t);
     cp_async_commit();
   }
+  // Solution values of the next off-diagonal tile are fetched one tile ahead
+  // (most are published long before they are needed); a value still equal to
+  // the sentinel is polled until it arrives.
+  using UB = typename SweepBits<T>::U;
+  constexpr int KP = (kTS * NR + kSweepThreads - 1) / kSweepThreads;
+  UB pre[KP];
+  auto src_of = [&](int cb, int c, int q) -> const T* {
+    const int64_t c0 = (int64_t)cb * kTS;
+    return FWD ? &Y[(c0 + c) + q * ldy] : &Out[(TRANS ? (int64_t)perm[c0 + c] : c0 + c) + q * ldo];
+  };
+  auto prefetch = [&](int t) {
+    const int cb = col_block(t);
+    const int nc = (int)min((int64_t)kTS, n - (int64_t)cb * kTS);
+#pragma unroll
+    for (int k = 0; k < KP; ++k) {
+      const int idx = tid + k * kSweepThreads;
+      const int c = idx / NR, q = idx - c * NR;
+      pre[k] = (idx < kTS * NR && q < nrhs && c < nc) ? SweepBits<T>::load(src_of(cb, c, q)) : UB(0);
+    }
+  };
+  if (noff > 0) prefetch(0);
   for (int t = 0; t < ntiles; ++t) {
     if (t + kStages - 1 < ntiles) issue(t + kStages - 1);
     cp_async_commit();
@@ -199,15 +220,16 @@ solve_sweep_kernel(int64_t n, const T* __restrict__ LU, int64_t lda, const int32
       const int cb = col_block(t);
       const int64_t c0 = (int64_t)cb * kTS;
       const int nc = (int)min((int64_t)kTS, n - c0);
-      // solution values of block cb: FWD from Y, BWD from Out (through perm for 'T')
       int ok = 1;
-      for (int idx = tid; idx < kTS * NR; idx += kSweepThreads) {
+#pragma unroll
+      for (int k = 0; k < KP; ++k) {
+        const int idx = tid + k * kSweepThreads;
+        if (idx >= kTS * NR) continue;
         const int c = idx / NR, q = idx - c * NR;
         T v = T(0);
         if (q < nrhs && c < nc) {
-          const T* src = FWD ? &Y[(c0 + c) + q * ldy]
-                             : &Out[(TRANS ? (int64_t)perm[c0 + c] : c0 + c) + q * ldo];
-          if (!poll_value(src, scr, &v)) ok = 0;
+          if (pre[k] != SweepBits<T>::kSentinel) v = SweepBits<T>::as_t(pre[k]);
+          else if (!poll_value(src_of(cb, c, q), scr, &v)) ok = 0;
         }
         sx[c][q] = v;
       }
@@ -215,6 +237,7 @@ solve_sweep_kernel(int64_t n, const T* __restrict__ LU, int64_t lda, const int32
         cp_async_wait<0>();  // no copy may land after the CTA has left
         return;
       }
+      if (t + 1 < noff) prefetch(t + 1);
       if (tid < kTS) {
         if (FWD) {
 #pragma unroll 8
@@ -222,6 +245,13 @@ solve_sweep_kernel(int64_t n, const T* __restrict__ LU, int64_t lda, const int32
             const T l = tile[c][r];
 #pragma unroll
             for (int q = 0; q < NR; ++q) acc[q] = fma(-l, sx[c][q], acc[q]);
+          }
+        } else if (nc == kTS) {
+#pragma unroll 8
+          for (int c = kTS - 1; c >= 0; --c) {
+            const T u = tile[c][r];
+#pragma unroll
+            for (int q = 0; q < NR; ++q) acc[q] = fma(-u, sx[c][q], acc[q]);
           }
         } else {
           for (int c = nc - 1; c >= 0; --c) {

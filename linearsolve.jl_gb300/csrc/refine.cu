@@ -48,24 +48,25 @@ __device__ __forceinline__ void atomic_max_nonneg(unsigned long long* p, double 
 //   'N': op(A)[i,j] = A[i + j*lda], A is rows x cols, i < rows
 //   'T': op(A)[i,j] = A[j + i*lda], i < cols (one warp per output row)
 // Chunks are fixed by (cols or rows) and kSplit, so the sum order is fixed.
+template <int W>
 __global__ void __launch_bounds__(kRowsPerCta)
 gemv_n_partial_kernel(int64_t rows, int64_t cols, const double* __restrict__ A, int64_t lda,
-                      const double* __restrict__ X, int64_t ldx, int W, double* __restrict__ P,
+                      const double* __restrict__ X, int64_t ldx, int wreal, double* __restrict__ P,
                       int absval) {
-  __shared__ double sx[kXTile][kMaxW];
+  __shared__ double sx[kXTile][W];
   const int s = blockIdx.y;
   const int64_t cs = (cols + kSplit - 1) / kSplit;
   const int64_t j0 = s * cs, j1 = min(cols, j0 + cs);
   const int64_t i = (int64_t)blockIdx.x * kRowsPerCta + threadIdx.x;
-  double acc[kMaxW];
+  double acc[W];
 #pragma unroll
-  for (int q = 0; q < kMaxW; ++q) acc[q] = 0.0;
+  for (int q = 0; q < W; ++q) acc[q] = 0.0;
   for (int64_t jt = j0; jt < j1; jt += kXTile) {
     const int nt = (int)min((int64_t)kXTile, j1 - jt);
     __syncthreads();
     for (int idx = threadIdx.x; idx < nt * W; idx += blockDim.x) {
-      int jj = idx / W, q = idx - jj * W;
-      sx[jj][q] = X ? X[(jt + jj) + q * ldx] : 1.0;
+      const int jj = idx / W, q = idx - jj * W;
+      sx[jj][q] = X ? (q < wreal ? X[(jt + jj) + q * ldx] : 0.0) : 1.0;
     }
     __syncthreads();
     if (i < rows) {
@@ -74,31 +75,36 @@ gemv_n_partial_kernel(int64_t rows, int64_t cols, const double* __restrict__ A, 
       for (int jj = 0; jj < nt; ++jj) {
         double v = a[jj * lda];
         if (absval) v = fabs(v);
+#pragma unroll
         for (int q = 0; q < W; ++q) acc[q] = fma(v, sx[jj][q], acc[q]);
       }
     }
   }
   if (i < rows)
+#pragma unroll
     for (int q = 0; q < W; ++q) P[((size_t)s * W + q) * rows + i] = acc[q];
 }
 
+template <int W>
 __global__ void __launch_bounds__(256)
 gemv_t_partial_kernel(int64_t rows, int64_t cols, const double* __restrict__ A, int64_t lda,
-                      const double* __restrict__ X, int64_t ldx, int W, double* __restrict__ P) {
+                      const double* __restrict__ X, int64_t ldx, int wreal, double* __restrict__ P) {
   const int s = blockIdx.y;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t i = (int64_t)blockIdx.x * 8 + warp;  // output index = column of A
   const int64_t cs = (rows + kSplit - 1) / kSplit;
   const int64_t j0 = s * cs, j1 = min(rows, j0 + cs);
   if (i >= cols) return;
-  double acc[kMaxW];
+  double acc[W];
 #pragma unroll
-  for (int q = 0; q < kMaxW; ++q) acc[q] = 0.0;
+  for (int q = 0; q < W; ++q) acc[q] = 0.0;
   const double* a = A + i * lda;
   for (int64_t j = j0 + lane; j < j1; j += 32) {
-    double v = a[j];
-    for (int q = 0; q < W; ++q) acc[q] = fma(v, X[j + q * ldx], acc[q]);
+    const double v = a[j];
+#pragma unroll
+    for (int q = 0; q < W; ++q) acc[q] = fma(v, q < wreal ? X[j + q * ldx] : 0.0, acc[q]);
   }
+#pragma unroll
   for (int q = 0; q < W; ++q) {
     double v = acc[q];
     for (int off = 16; off; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
@@ -107,7 +113,7 @@ gemv_t_partial_kernel(int64_t rows, int64_t cols, const double* __restrict__ A, 
 }
 
 // out[i,q] = beta*C[i,q] + alpha*sum_s P[s][q][i]; optional column max of |out|.
-__global__ void gemv_reduce_kernel(int64_t len, int W, const double* __restrict__ P, double alpha,
+__global__ void gemv_reduce_kernel(int64_t len, int W, int Wp, const double* __restrict__ P, double alpha,
                                    const double* __restrict__ C, int64_t ldc, double beta,
                                    double* __restrict__ out, int64_t ldo,
                                    unsigned long long* __restrict__ colmax) {
@@ -117,7 +123,7 @@ __global__ void gemv_reduce_kernel(int64_t len, int W, const double* __restrict_
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len;
          i += (int64_t)gridDim.x * blockDim.x) {
       double sum = 0.0;
-      for (int s = 0; s < kSplit; ++s) sum += P[((size_t)s * W + q) * len + i];
+      for (int s = 0; s < kSplit; ++s) sum += P[((size_t)s * Wp + q) * len + i];
       double v = alpha * sum;
       if (beta != 0.0) v = fma(beta, C[i + q * ldc], v);
       out[i + q * ldo] = v;
@@ -251,23 +257,31 @@ cudaError_t gemv(char op, int64_t rows, int64_t cols, const double* A, int64_t l
                  double* out, int64_t ldo, double* P, unsigned long long* colmax, cudaStream_t s,
                  bool absval = false) {
   int64_t len;
+  // the partial-sum layout is P[s][q][i] with the padded width Wp
+  const int Wp = W <= 1 ? 1 : W <= 2 ? 2 : W <= 4 ? 4 : 8;
   if (op == 'N') {
     len = rows;
     dim3 grid((unsigned)((rows + kRowsPerCta - 1) / kRowsPerCta), kSplit);
-    { LaunchScope ls_(K_REFINE, 0.0, 0.0, s);
-    gemv_n_partial_kernel<<<grid, kRowsPerCta, 0, s>>>(rows, cols, A, lda, X, ldx, W, P, absval ? 1 : 0);
-    }
+    LaunchScope ls_(K_REFINE, 2.0 * rows * cols * W, 8.0 * rows * cols, s);
+    const int ab = absval ? 1 : 0;
+    if (Wp == 1 || X == nullptr) gemv_n_partial_kernel<1><<<grid, kRowsPerCta, 0, s>>>(rows, cols, A, lda, X, ldx, W, P, ab);
+    else if (Wp == 2) gemv_n_partial_kernel<2><<<grid, kRowsPerCta, 0, s>>>(rows, cols, A, lda, X, ldx, W, P, ab);
+    else if (Wp == 4) gemv_n_partial_kernel<4><<<grid, kRowsPerCta, 0, s>>>(rows, cols, A, lda, X, ldx, W, P, ab);
+    else gemv_n_partial_kernel<8><<<grid, kRowsPerCta, 0, s>>>(rows, cols, A, lda, X, ldx, W, P, ab);
   } else {
     len = cols;
     dim3 grid((unsigned)((cols + 7) / 8), kSplit);
-    { LaunchScope ls_(K_REFINE, 0.0, 0.0, s);
-    gemv_t_partial_kernel<<<grid, 256, 0, s>>>(rows, cols, A, lda, X, ldx, W, P);
-    }
+    LaunchScope ls_(K_REFINE, 2.0 * rows * cols * W, 8.0 * rows * cols, s);
+    if (Wp == 1) gemv_t_partial_kernel<1><<<grid, 256, 0, s>>>(rows, cols, A, lda, X, ldx, W, P);
+    else if (Wp == 2) gemv_t_partial_kernel<2><<<grid, 256, 0, s>>>(rows, cols, A, lda, X, ldx, W, P);
+    else if (Wp == 4) gemv_t_partial_kernel<4><<<grid, 256, 0, s>>>(rows, cols, A, lda, X, ldx, W, P);
+    else gemv_t_partial_kernel<8><<<grid, 256, 0, s>>>(rows, cols, A, lda, X, ldx, W, P);
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   { LaunchScope ls_(K_REFINE, 0.0, 0.0, s);
-  gemv_reduce_kernel<<<grid_for(len), 256, 0, s>>>(len, W, P, alpha, C, ldc, beta, out, ldo, colmax);
+  const int Wp_used = (op == 'N' && X == nullptr) ? 1 : Wp;
+  gemv_reduce_kernel<<<grid_for(len), 256, 0, s>>>(len, W, Wp_used, P, alpha, C, ldc, beta, out, ldo, colmax);
   }
   return cudaGetLastError();
 }
