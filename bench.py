@@ -16,9 +16,13 @@ solve!(cache) / cache.b = b.  Inputs are seeded synthetic arrays.
 dgetrf/dgetrs on OpenBLAS, the routines LinearSolve.jl's LUFactorization calls)
 on the host cores.
 
---suite adds the mixed-precision comparison at n = 16384 (A = G + 4 sqrt(n) I,
-4 RHS): FP32 LU + FP64 refinement vs the plain FP64 LU, both to the FP64
-backward-error bound.
+--suite adds sub-objects to the line (comma list, or "all"):
+  mixed       n = 16384, A = G + 4 sqrt(n) I, 4 RHS: FP32/BF16/FP16 LU + FP64
+              refinement vs the plain FP64 LU, both to the FP64 bound
+  mixed_hard  n = 16384, A = Q1 diag(s) Q2^T, s log-spaced 1..1e6, 4 RHS: FP32
+              LU + FP64 GMRES-IR (and plain IR) vs the plain FP64 LU
+  batched     20,000 uneven systems n in [8, 256]: FP64 and FP32 + FP64 IR
+  serving     Poisson stream, n log-uniform in [64, 4096], p50/p99 latency
 """
 from __future__ import annotations
 
@@ -232,14 +236,7 @@ def run_gpu(args, rank, world, local):
     ctx = pkg.Context(local)
     stream = ctx.stream
     if args.only_suite:  # profiling aid: the suite parts alone, one JSON object
-        parts = set(args.suite.split(","))
-        out = {}
-        if "mixed" in parts or "all" in parts:
-            out["mixed"] = run_mixed_suite(pkg, cu, ctx, args)
-        if "batched" in parts or "all" in parts:
-            out["batched"] = run_batched_suite(pkg, cu, ctx, args)
-        if "serving" in parts or "all" in parts:
-            out["serving"] = run_serving_suite(pkg, cu, ctx, args)
+        out = run_suites(pkg, cu, ctx, args)
         if rank == 0:
             print(json.dumps(out))
         dist.close()
@@ -365,13 +362,7 @@ def run_gpu(args, rank, world, local):
     }
 
     if args.suite and rank == 0:
-        parts = set(args.suite.split(","))
-        if "mixed" in parts or "all" in parts:
-            line["mixed"] = run_mixed_suite(pkg, cu, ctx, args)
-        if "batched" in parts or "all" in parts:
-            line["batched"] = run_batched_suite(pkg, cu, ctx, args)
-        if "serving" in parts or "all" in parts:
-            line["serving"] = run_serving_suite(pkg, cu, ctx, args)
+        line.update(run_suites(pkg, cu, ctx, args))
 
     if rank == 0 and not args.no_cpu:
         # bounded CPU sample of the same workload on this host
@@ -393,49 +384,129 @@ def pkg_backward_error(A, x, b):
     return float(np.abs(r).max() / (nA * np.abs(x).max() + np.abs(b).max()))
 
 
+def _timed_solve(pkg, cu, ctx, f, dA, dB0, dB, prec, reps, mode="ir", **refine_kw):
+    """getrf + (getrs | refined solve) from the device-resident A, timed with
+    events on the context stream; returns (ms, refinement stats, kernel_ms)."""
+
+    def once():
+        dB.copy_from(dB0, ctx.stream)
+        f.getrf(dA)
+        if prec == "fp64":
+            f.getrs(dB)
+            return {}
+        _, st = f.solve_refined(dB, mode=mode, **refine_kw)
+        return st
+
+    once()
+    cu.device_synchronize()
+    ctx.profile_enable(True)
+    e0, e1 = cu.Event(), cu.Event()
+    e0.record(ctx.stream)
+    st = {}
+    for _ in range(reps):
+        st = once()
+    e1.record(ctx.stream)
+    e1.synchronize()
+    ms = e0.elapsed_ms(e1) / reps
+    prof = ctx.profile_read(reset=True)
+    ctx.profile_enable(False)
+    kms = {k: round(v["ms"] / reps, 3) for k, v in prof.items() if k != "launches" and v["count"]}
+    return ms, st, kms
+
+
+def _forward_error(X, Xref):
+    return float(np.abs(X - Xref).max() / np.abs(Xref).max())
+
+
+SUITES = ("mixed", "mixed_hard", "batched", "serving")
+
+
+def run_suites(pkg, cu, ctx, args) -> dict:
+    parts = set(args.suite.split(","))
+    if "all" in parts:
+        parts = set(SUITES)
+    runners = {"mixed": run_mixed_suite, "mixed_hard": run_mixed_hard_suite,
+               "batched": run_batched_suite, "serving": run_serving_suite}
+    return {name: runners[name](pkg, cu, ctx, args) for name in SUITES if name in parts}
+
+
 def run_mixed_suite(pkg, cu, ctx, args):
-    """n = 16384, A = G + 4 sqrt(n) I, 4 RHS: FP32 LU + IR vs plain FP64 LU."""
+    """n = 16384, A = G + 4 sqrt(n) I, 4 RHS: FP32/BF16/FP16 LU + FP64 IR vs
+    plain FP64 LU; the forward error of each is taken against the plain FP64
+    solution (the reference algorithm's result, bit for bit)."""
     n, nrhs = args.mixed_n, 4
     A, B = pkg.workloads.shifted(n, nrhs, seed=1)
     dA = pkg.DeviceMatrix.from_host(A)
     dB0 = pkg.DeviceMatrix.from_host(B)
     dB = pkg.DeviceMatrix(n, nrhs)
     out = {"n": n, "nrhs": nrhs, "A": "G + 4 sqrt(n) I"}
-    for label, prec in (("fp32_ir", "fp32"), ("bf16_ir", "bf16"), ("fp16_ir", "fp16"),
-                        ("fp64_plain", "fp64")):
+    X64 = None
+    for label, prec in (("fp64_plain", "fp64"), ("fp32_ir", "fp32"), ("bf16_ir", "bf16"),
+                        ("fp16_ir", "fp16")):
         f = ctx.factor(n, n, prec)
-        reps = 2 if prec == "fp64" else 3
-
-        def once():
-            dB.copy_from(dB0, ctx.stream)
-            f.getrf(dA)
-            if prec == "fp64":
-                f.getrs(dB)
-                return {}
-            _, st = f.solve_refined(dB, mode="ir")
-            return st
-
-        once()
-        cu.device_synchronize()
-        ctx.profile_enable(True)
-        e0, e1 = cu.Event(), cu.Event()
-        e0.record(ctx.stream)
-        st = {}
-        for _ in range(reps):
-            st = once()
-        e1.record(ctx.stream)
-        e1.synchronize()
-        ms = e0.elapsed_ms(e1) / reps
-        prof = ctx.profile_read(reset=True)
-        ctx.profile_enable(False)
+        ms, st, kms = _timed_solve(pkg, cu, ctx, f, dA, dB0, dB, prec, 2 if prec == "fp64" else 3)
         X = dB.to_host()
+        if X64 is None:
+            X64 = X.copy()
         be = max(pkg_backward_error(A, X[:, j], B[:, j]) for j in range(nrhs))
         out[label] = {"ms_per_solve_set": ms, "solves_per_s": nrhs / (ms / 1000), "backward_error": be,
-                      "stats": st,
-                      "kernel_ms": {k: round(v["ms"] / reps, 3) for k, v in prof.items()
-                                    if k != "launches" and v["count"]}}
+                      "forward_error_vs_fp64": _forward_error(X, X64), "stats": st, "kernel_ms": kms}
         f.close()
     for label in ("fp32_ir", "bf16_ir", "fp16_ir"):
+        out["speedup_%s_vs_fp64" % label] = out[label]["solves_per_s"] / out["fp64_plain"]["solves_per_s"]
+    out["bound"] = 10 * n * EPS64
+    dA.free(); dB0.free(); dB.free()
+    return out
+
+
+def svd_conditioned_on_device(n, nrhs, cond, seed):
+    """A = Q1 diag(s) Q2^T, s log-spaced in [1, cond], Q1 and Q2 the Q factors
+    of seeded Gaussian matrices (numpy default_rng(seed)).  At n = 16384 the
+    two QR factorizations and the product are input generation, done with
+    torch on the GPU; the result comes back to the host column-major."""
+    import torch
+    rng = np.random.default_rng(seed)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    s = torch.from_numpy(np.logspace(0.0, np.log10(cond), n)).to(dev)
+    q1, _ = torch.linalg.qr(torch.from_numpy(rng.standard_normal((n, n))).to(dev))
+    q2, _ = torch.linalg.qr(torch.from_numpy(rng.standard_normal((n, n))).to(dev))
+    # A^T = Q2 diag(s) Q1^T in row-major order is A in column-major order
+    at = (q2 * s) @ q1.T
+    del q1, q2
+    A = at.cpu().numpy().T
+    del at
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    B = np.asfortranarray(rng.standard_normal((n, nrhs)))
+    return A, B
+
+
+def run_mixed_hard_suite(pkg, cu, ctx, args):
+    """n = 16384, A = Q1 diag(s) Q2^T with s log-spaced 1..1e6, 4 RHS: FP32 LU
+    with FP64 GMRES-IR vs plain FP64 LU."""
+    n, nrhs, cond = args.mixed_n, 4, 1e6
+    t0 = time.perf_counter()
+    A, B = svd_conditioned_on_device(n, nrhs, cond, seed=2)
+    gen_s = time.perf_counter() - t0
+    dA = pkg.DeviceMatrix.from_host(A)
+    dB0 = pkg.DeviceMatrix.from_host(B)
+    dB = pkg.DeviceMatrix(n, nrhs)
+    out = {"n": n, "nrhs": nrhs, "A": "Q1 diag(s) Q2^T, s log-spaced 1..1e6", "input_generation_s": gen_s}
+    X64 = None
+    for label, prec, mode, kw in (("fp64_plain", "fp64", "ir", {}),
+                                  ("fp32_gmres_ir", "fp32", "gmres_ir", {}),
+                                  ("fp32_gmres_ir_inner_tol_1e-6", "fp32", "gmres_ir", {"gmres_tol": 1e-6}),
+                                  ("fp32_ir", "fp32", "ir", {})):
+        f = ctx.factor(n, n, prec)
+        ms, st, kms = _timed_solve(pkg, cu, ctx, f, dA, dB0, dB, prec, 2, mode=mode, **kw)
+        X = dB.to_host()
+        if X64 is None:
+            X64 = X.copy()
+        be = max(pkg_backward_error(A, X[:, j], B[:, j]) for j in range(nrhs))
+        out[label] = {"ms_per_solve_set": ms, "solves_per_s": nrhs / (ms / 1000), "backward_error": be,
+                      "forward_error_vs_fp64": _forward_error(X, X64), "stats": st, "kernel_ms": kms}
+        f.close()
+    for label in ("fp32_gmres_ir", "fp32_gmres_ir_inner_tol_1e-6", "fp32_ir"):
         out["speedup_%s_vs_fp64" % label] = out[label]["solves_per_s"] / out["fp64_plain"]["solves_per_s"]
     out["bound"] = 10 * n * EPS64
     dA.free(); dB0.free(); dB.free()
@@ -488,6 +559,11 @@ def run_batched_suite(pkg, cu, ctx, args):
                       "gflops": out["lu_flops"] / (ms / 1000.0) / 1e9,
                       "max_backward_error_over_n_eps": worst / EPS64,
                       "failed_info": int((info != 0).sum())}
+        if prec != 0:  # refinement corrections per system; -1 = re-solved by the FP64 kernel
+            its = np.zeros(len(sz), dtype=np.int32)
+            if lib.gblu_batch_iterations(ctx.handle, h, its.ctypes.data) == 0:
+                vals, cnts = np.unique(its, return_counts=True)
+                out[label]["iterations"] = {str(int(v)): int(c) for v, c in zip(vals, cnts)}
         lib.gblu_batch_destroy(ctx.handle, h)
     out["speedup_fp32_ir_vs_fp64"] = out["fp32_ir"]["solves_per_s"] / out["fp64"]["solves_per_s"]
     # CPU: LAPACK loop over a bounded sample of the same systems, all host threads
@@ -564,7 +640,7 @@ def main():
     ap.add_argument("--nrhs", type=int, default=16)
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--suite", default="", help="comma list: mixed,batched,serving (or all)")
+    ap.add_argument("--suite", default="", help="comma list: mixed,mixed_hard,batched,serving (or all)")
     ap.add_argument("--batch-count", type=int, default=20000)
     ap.add_argument("--only-suite", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=300)

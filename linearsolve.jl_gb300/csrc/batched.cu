@@ -7,10 +7,10 @@
 // Schur update) followed by its back-solve (src/factorization.jl:433-457),
 // with the same per-element fused-multiply-add order, so the FP64 results are
 // bit-identical to the oracle's per-system getrf + getrs.  A CTA takes the
-// next system from a queue ordered by decreasing size (longest first), holds
-// the current panel (NB columns) and the U12 row block in shared memory, and
-// updates the trailing matrix in global memory, where the system's working
-// set stays L2-resident.
+// next system from a queue ordered by decreasing size (longest first), keeps
+// the current panel in registers (one row per thread) and its columns and the
+// U12 row block in shared memory, and updates the trailing matrix in global
+// memory, where the system's working set stays L2-resident.
 //
 // The mixed variant factors a FP32 copy with the same code and refines each
 // system in FP64 (residual with the FP64 A, per-system backward-error test,
@@ -43,147 +43,291 @@ struct BatchDev {
   int32_t* iters;         // per system: refinement iterations, -1 = FP64 re-solve
 };
 
-template <typename T>
+constexpr int kBatchUStride = kBatchMaxN + 8;  // U12 rows, padded for the micro-tile loads
+
+// Shared-memory carve of one system's working set (NB <= 16, NT <= 512).
+template <typename T, int NT, int NB>
 struct SysSmem {
-  T* P;    // panel: NB columns x n rows (column j at P + j*kBatchMaxN)
-  T* U;    // U12 block: NB rows x n columns (row j at U + j*kBatchMaxN)
-  T* x;    // solve vector (n)
-  T* red_v;
-  int* red_i;
+  static constexpr int NW = NT / 32;
+  T* L;      // panel columns: column j of the current panel at L + j*kBatchMaxN (row-indexed)
+  T* U;      // U12 rows: row j at U + j*kBatchUStride (indexed by column - c1)
+  T* xs;     // solve vector
+  T* cval;   // [2][NW] pivot candidate |value| per warp (double-buffered by column parity)
+  T* crowv;  // [2][NW][NB] candidate row's panel values
+  T* diagv;  // [2][NB] current diagonal row's panel values
+  int* crow;  // [2][NW] candidate row per warp
+  int* perm;  // [kBatchMaxN] row r of the factored matrix holds original row perm[r]
+  int* list;  // [32] rows moved by the current panel's interchanges
+  int* lsrc;  // [32] row each of them receives its value from
+  int* pidx;  // [NB] pivot rows of the current panel (0-based)
+  int* cnt;   // entries of list
+  double* xd;   // FP64 iterate (mixed kernel)
+  double* rd;   // FP64 residual (mixed kernel)
+  double* red;  // [64] block reductions
+
+  __host__ __device__ static constexpr size_t al(size_t x) { return (x + 15) & ~size_t(15); }
+  __host__ __device__ static constexpr size_t bytes(bool mixed) {
+    return al(NB * kBatchMaxN * sizeof(T)) + al(NB * kBatchUStride * sizeof(T)) +
+           al(kBatchMaxN * sizeof(T)) + al(2 * NW * sizeof(T)) + al(2 * NW * NB * sizeof(T)) +
+           al(2 * NB * sizeof(T)) + al(2 * NW * 4) + al(kBatchMaxN * 4) + 2 * al(32 * 4) + al(NB * 4) +
+           al(4) + (mixed ? 2 * al(kBatchMaxN * 8) : 0) + al(64 * 8);
+  }
+  __device__ explicit SysSmem(unsigned char* p, bool mixed) {
+    auto take = [&](size_t b) { unsigned char* q = p; p += al(b); return q; };
+    L = reinterpret_cast<T*>(take(NB * kBatchMaxN * sizeof(T)));
+    U = reinterpret_cast<T*>(take(NB * kBatchUStride * sizeof(T)));
+    xs = reinterpret_cast<T*>(take(kBatchMaxN * sizeof(T)));
+    cval = reinterpret_cast<T*>(take(2 * NW * sizeof(T)));
+    crowv = reinterpret_cast<T*>(take(2 * NW * NB * sizeof(T)));
+    diagv = reinterpret_cast<T*>(take(2 * NB * sizeof(T)));
+    crow = reinterpret_cast<int*>(take(2 * NW * 4));
+    perm = reinterpret_cast<int*>(take(kBatchMaxN * 4));
+    list = reinterpret_cast<int*>(take(32 * 4));
+    lsrc = reinterpret_cast<int*>(take(32 * 4));
+    pidx = reinterpret_cast<int*>(take(NB * 4));
+    cnt = reinterpret_cast<int*>(take(4));
+    xd = rd = nullptr;
+    if (mixed) {
+      xd = reinterpret_cast<double*>(take(kBatchMaxN * 8));
+      rd = reinterpret_cast<double*>(take(kBatchMaxN * 8));
+    }
+    red = reinterpret_cast<double*>(take(64 * 8));
+  }
 };
 
+// Pivot-candidate order: larger |value| first, then the smaller row; row -1 is
+// no candidate.  A total order, so every reduction tree gives the first row of
+// maximal |value| (NaN never becomes a candidate: `v > best` is false for it).
 template <typename T>
-__device__ __forceinline__ T babs(T v) { return v < T(0) ? -v : v; }
-
-// Block-wide first-index argmax of |v| over rows [lo, n) of column `col` of P.
-template <typename T, int NT>
-__device__ int block_argmax(const T* col, int lo, int n, T* red_v, int* red_i, T* amax_out) {
-  T bv = T(0);
-  int bi = -1;
-  for (int i = lo + threadIdx.x; i < n; i += NT) {
-    const T a = fabs(col[i]);
-    if (a > bv) { bv = a; bi = i; }
-  }
-  for (int off = 16; off; off >>= 1) {
-    const T ov = __shfl_down_sync(0xffffffffu, bv, off);
-    const int oi = __shfl_down_sync(0xffffffffu, bi, off);
-    if (oi >= 0 && (bi < 0 || ov > bv || (ov == bv && oi < bi))) { bv = ov; bi = oi; }
-  }
-  if ((threadIdx.x & 31) == 0) { red_v[threadIdx.x >> 5] = bv; red_i[threadIdx.x >> 5] = bi; }
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    bv = threadIdx.x < NT / 32 ? red_v[threadIdx.x] : T(0);
-    bi = threadIdx.x < NT / 32 ? red_i[threadIdx.x] : -1;
-    for (int off = 16; off; off >>= 1) {
-      const T ov = __shfl_down_sync(0xffffffffu, bv, off);
-      const int oi = __shfl_down_sync(0xffffffffu, bi, off);
-      if (oi >= 0 && (bi < 0 || ov > bv || (ov == bv && oi < bi))) { bv = ov; bi = oi; }
-    }
-    if (threadIdx.x == 0) { red_v[0] = bv; red_i[0] = bi; }
-  }
-  __syncthreads();
-  const int r = red_i[0];
-  *amax_out = red_v[0];
-  __syncthreads();
-  return r;
+__device__ __forceinline__ bool cand_better(T v, int g, T bv, int bg) {
+  if (g < 0) return false;
+  if (bg < 0) return true;
+  return v > bv || (v == bv && g < bg);
 }
 
-// In-place getrf of one n x n column-major system (ld = n) in global memory.
-// ipiv: 1-based.  Returns info (0 or first zero pivot, 1-based).
+// In-place getrf of one n x n column-major system (ld = n) in global memory,
+// blocked by NB columns (src/blocked_lufact.jl:658-679 order):
+//   * panel getf2: the row i of the panel lives in registers of thread i % NT;
+//     per column each warp publishes its candidate (first row of max |a|),
+//     the candidate row's panel values and the diagonal row, one barrier,
+//     then every thread picks the winner, interchanges, scales by the
+//     reciprocal of the pivot and updates its own rows, columns in order;
+//   * interchanges on the other columns: warp 0 composes the panel's
+//     interchanges into "row list[m] takes the value of row lsrc[m]" with
+//     ballots and shuffles, then each column is one gather (independent loads);
+//   * U12 = L11 \ A12 by one thread per column, k ascending;
+//   * A22 -= L21 U12 by register micro-tiles, each element j ascending.
+// The per-element arithmetic is the reference's, so FP64 results are
+// bit-identical to the oracle's getrf.  ipiv: 1-based; sm.perm receives the
+// composed row permutation.  Returns info (0 or first zero pivot, 1-based).
 template <typename T, int NT, int NB>
 __device__ int64_t factor_system(T* __restrict__ A, int n, int32_t* __restrict__ ipiv,
-                                 const SysSmem<T>& sm) {
+                                 const SysSmem<T, NT, NB>& sm) {
+  constexpr int NW = NT / 32;
+  constexpr int RPT = (kBatchMaxN + NT - 1) / NT;  // panel rows per thread
+  static_assert(NB <= 16, "composition warp holds 2*NB rows");
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   int64_t info = 0;
-  const int tid = threadIdx.x;
+  for (int i = tid; i < kBatchMaxN; i += NT) sm.perm[i] = i;
+  __syncthreads();
   for (int k0 = 0; k0 < n; k0 += NB) {
     const int kb = min(NB, n - k0);
-    // panel rows [0, n) of columns k0..k0+kb-1 into shared memory (rows < k0 unused)
-    for (int j = 0; j < kb; ++j)
-      for (int i = k0 + tid; i < n; i += NT) sm.P[j * kBatchMaxN + i] = A[i + (int64_t)(k0 + j) * n];
-    __syncthreads();
-    for (int j = 0; j < kb; ++j) {
-      const int col = k0 + j;
-      T* pc = sm.P + j * kBatchMaxN;
-      T amax;
-      int p = block_argmax<T, NT>(pc, col, n, sm.red_v, sm.red_i, &amax);
-      if (p < 0) p = col;  // amax == 0 (or NaN everywhere): kp = k
-      if (tid == 0) ipiv[col] = p + 1;
-      const T piv = pc[p];
-      if (piv != T(0)) {
-        if (p != col && tid < kb) {
-          T* q = sm.P + tid * kBatchMaxN;
-          const T t = q[col];
-          q[col] = q[p];
-          q[p] = t;
-        }
-        __syncthreads();
-        const T inv = T(1) / pc[col];
-        for (int i = col + 1 + tid; i < n; i += NT) pc[i] *= inv;
-      } else if (info == 0) {
-        info = col + 1;
-      }
-      __syncthreads();
-      for (int i = col + 1 + tid; i < n; i += NT) {  // one row per thread, columns in order
-        const T l = pc[i];
-        for (int jj = j + 1; jj < kb; ++jj) {
-          T* q = sm.P + jj * kBatchMaxN;
-          q[i] = fma(-l, q[col], q[i]);
-        }
-      }
-      __syncthreads();
-    }
-    for (int j = 0; j < kb; ++j)
-      for (int i = k0 + tid; i < n; i += NT) A[i + (int64_t)(k0 + j) * n] = sm.P[j * kBatchMaxN + i];
-    // interchanges on the other columns, in order (blocked_lufact.jl:126-141)
-    for (int c = tid; c < n; c += NT) {
-      if (c >= k0 && c < k0 + kb) continue;
-      T* ac = A + (int64_t)c * n;
-      for (int j = 0; j < kb; ++j) {
-        const int p = ipiv[k0 + j] - 1;
-        if (p != k0 + j) {
-          const T t = ac[k0 + j];
-          ac[k0 + j] = ac[p];
-          ac[p] = t;
-        }
-      }
-    }
-    __syncthreads();  // ipiv writes and global swaps visible to the whole CTA
-    const int c1 = k0 + kb, nc = n - c1;
-    if (nc > 0) {
-      // U12 := L11 \ A12, one thread per column, k ascending (:146-178)
-      for (int c = tid; c < nc; c += NT) {
-        T* ac = A + (int64_t)(c1 + c) * n;
-        T u[NB];
+    const int c1 = k0 + kb;
+    T pr[RPT][NB];
 #pragma unroll
-        for (int j = 0; j < NB; ++j) u[j] = j < kb ? ac[k0 + j] : T(0);
+    for (int m = 0; m < RPT; ++m) {
+      const int i = tid + NT * m;
+#pragma unroll
+      for (int j = 0; j < NB; ++j)
+        pr[m][j] = (i >= k0 && i < n && j < kb) ? A[i + (int64_t)(k0 + j) * n] : T(0);
+    }
+#pragma unroll
+    for (int j = 0; j < NB; ++j) {
+      if (j >= kb) continue;  // uniform; keeps the loop fully unrolled (pr indexed statically)
+      const int col = k0 + j;
+      const int buf = j & 1;
+      T bv = T(0);
+      int bg = -1;
+#pragma unroll
+      for (int m = 0; m < RPT; ++m) {
+        const int i = tid + NT * m;
+        if (i >= col && i < n) {
+          const T v = fabs(pr[m][j]);
+          if (v > bv) { bv = v; bg = i; }
+        }
+      }
+      for (int off = 16; off; off >>= 1) {
+        const T ov = __shfl_xor_sync(0xffffffffu, bv, off);
+        const int og = __shfl_xor_sync(0xffffffffu, bg, off);
+        if (cand_better(ov, og, bv, bg)) { bv = ov; bg = og; }
+      }
+      if (lane == 0) { sm.cval[buf * NW + warp] = bv; sm.crow[buf * NW + warp] = bg; }
+      // the owners publish (row tests, not a computed slot index, so pr stays in registers)
+#pragma unroll
+      for (int m = 0; m < RPT; ++m)
+        if (bg == tid + NT * m)
+#pragma unroll
+          for (int jj = 0; jj < NB; ++jj)
+            if (jj < kb) sm.crowv[(buf * NW + warp) * NB + jj] = pr[m][jj];
+#pragma unroll
+      for (int m = 0; m < RPT; ++m)
+        if (col == tid + NT * m)
+#pragma unroll
+          for (int jj = 0; jj < NB; ++jj)
+            if (jj < kb) sm.diagv[buf * NB + jj] = pr[m][jj];
+      __syncthreads();
+      T wv = lane < NW ? sm.cval[buf * NW + lane] : T(0);
+      int wg = lane < NW ? sm.crow[buf * NW + lane] : -1;
+      int ww = lane;
+      for (int off = 16; off; off >>= 1) {
+        const T ov = __shfl_xor_sync(0xffffffffu, wv, off);
+        const int og = __shfl_xor_sync(0xffffffffu, wg, off);
+        const int ow = __shfl_xor_sync(0xffffffffu, ww, off);
+        if (cand_better(ov, og, wv, wg)) { wv = ov; wg = og; ww = ow; }
+      }
+      const int p = wg < 0 ? col : wg;  // kp = k when the column is zero below the diagonal
+      const T* src = (p == col) ? sm.diagv + buf * NB : sm.crowv + (buf * NW + ww) * NB;
+      const T piv = src[j];
+      if (tid == 0) { sm.pidx[j] = p; ipiv[col] = p + 1; }
+      if (piv == T(0) && info == 0) info = col + 1;
+      const bool swap = piv != T(0) && p != col;
+      const T inv = piv != T(0) ? T(1) / piv : T(0);
+#pragma unroll
+      for (int m = 0; m < RPT; ++m) {
+        const int i = tid + NT * m;
+        if (swap && i == col) {
+#pragma unroll
+          for (int jj = 0; jj < NB; ++jj)
+            if (jj < kb) pr[m][jj] = src[jj];
+        } else if (swap && i == p) {
+#pragma unroll
+          for (int jj = 0; jj < NB; ++jj)
+            if (jj < kb) pr[m][jj] = sm.diagv[buf * NB + jj];
+        }
+        if (i > col && i < n) {
+          T l = pr[m][j];
+          if (piv != T(0)) l *= inv;
+          pr[m][j] = l;
+#pragma unroll
+          for (int jj = j + 1; jj < NB; ++jj)
+            if (jj < kb) pr[m][jj] = fma(-l, src[jj], pr[m][jj]);
+        }
+      }
+    }
+    // panel back to global memory; its columns to shared memory for TRSM and update
+#pragma unroll
+    for (int m = 0; m < RPT; ++m) {
+      const int i = tid + NT * m;
+      if (i >= k0 && i < n)
+#pragma unroll
+        for (int jj = 0; jj < NB; ++jj)
+          if (jj < kb) {
+            A[i + (int64_t)(k0 + jj) * n] = pr[m][jj];
+            sm.L[jj * kBatchMaxN + i] = pr[m][jj];
+          }
+    }
+    if (warp == 0) {
+      // rows touched by the panel's interchanges: k0..c1-1 (lanes 0..kb-1) and
+      // the pivot rows below the panel (lanes NB.., duplicates dropped)
+      int row = -1;
+      if (lane < kb) row = k0 + lane;
+      else if (lane >= NB && lane - NB < kb) {
+        const int pj = sm.pidx[lane - NB];
+        if (pj >= c1) row = pj;
+      }
+      const unsigned same = __match_any_sync(0xffffffffu, row);
+      if (row >= 0 && __ffs(same) - 1 != lane) row = -1;
+      int from = row;  // original row whose value ends at `row`
+      for (int j = 0; j < kb; ++j) {
+        const int b = sm.pidx[j];
+        if (b != k0 + j) {
+          const unsigned hm = __ballot_sync(0xffffffffu, row == b);
+          if (hm != 0u) {
+            const int hb = __ffs(hm) - 1;
+            const int srcl = lane == j ? hb : (lane == hb ? j : lane);
+            from = __shfl_sync(0xffffffffu, from, srcl);
+          }
+        }
+      }
+      const unsigned vm = __ballot_sync(0xffffffffu, row >= 0);
+      const int pos = __popc(vm & ((1u << lane) - 1u));
+      const int pv = row >= 0 ? sm.perm[from] : 0;
+      __syncwarp();
+      if (row >= 0) {
+        sm.list[pos] = row;
+        sm.lsrc[pos] = from;
+        sm.perm[row] = pv;
+      }
+      if (lane == 0) *sm.cnt = __popc(vm);
+    }
+    __syncthreads();
+    // interchanges on the other columns (list entries 0..kb-1 are rows k0..c1-1
+    // in order), fused with U12 := L11 \ A12 for the columns right of the panel
+    const int cnt = *sm.cnt;
+    for (int c = tid; c < n; c += NT) {
+      if (c >= k0 && c < c1) continue;
+      T* ac = A + (int64_t)c * n;
+      T v[2 * NB];
+#pragma unroll
+      for (int m = 0; m < 2 * NB; ++m)
+        if (m < cnt) v[m] = ac[sm.lsrc[m]];
+      if (c >= c1) {
 #pragma unroll
         for (int j = 0; j < NB; ++j)
 #pragma unroll
           for (int i = j + 1; i < NB; ++i)
-            if (i < kb) u[i] = fma(-sm.P[j * kBatchMaxN + k0 + i], u[j], u[i]);
+            if (i < kb) v[i] = fma(-sm.L[j * kBatchMaxN + k0 + i], v[j], v[i]);
 #pragma unroll
         for (int j = 0; j < NB; ++j)
-          if (j < kb) {
-            ac[k0 + j] = u[j];
-            sm.U[j * kBatchMaxN + c] = u[j];
-          }
+          if (j < kb) sm.U[j * kBatchUStride + (c - c1)] = v[j];
       }
-      __syncthreads();
-      // A22 -= L21 * U12, each element k ascending (:186-656)
-      const int nr = n - c1;
-      const int lane = tid & 31, warp = tid >> 5;
-      for (int c = warp; c < nc; c += NT / 32) {   // a warp per column, lanes down the rows
-        T u[NB];
 #pragma unroll
-        for (int j = 0; j < NB; ++j) u[j] = j < kb ? sm.U[j * kBatchMaxN + c] : T(0);
-        T* acol = A + c1 + (int64_t)(c1 + c) * n;
-        for (int i = lane; i < nr; i += 32) {
-          T v = acol[i];
+      for (int m = 0; m < 2 * NB; ++m)
+        if (m < cnt) ac[sm.list[m]] = v[m];
+    }
+    __syncthreads();
+    // A22 -= L21 * U12: warp tiles of 32*RM rows x CN columns, each lane RM x CN
+    const int nr = n - c1;
+    if (nr > 0) {
+      constexpr int RM = 4;
+      constexpr int CN = sizeof(T) == 4 ? 8 : 4;
+      const int RB = (nr + 32 * RM - 1) / (32 * RM), CB = (nr + CN - 1) / CN;
+      for (int t = warp; t < RB * CB; t += NW) {
+        const int rb = t % RB, cb = t / RB;
+        const int i0 = c1 + rb * 32 * RM;
+        const int rg = min(RM, (n - i0 + 31) / 32);  // 32-row groups reaching below n (warp-uniform)
+        const int ib = i0 + lane;
+        const int cc = cb * CN;  // column offset from c1
+        T acc[RM][CN];
 #pragma unroll
-          for (int j = 0; j < NB; ++j)
-            if (j < kb) v = fma(-sm.P[j * kBatchMaxN + c1 + i], u[j], v);
-          acol[i] = v;
+        for (int r = 0; r < RM; ++r)
+#pragma unroll
+          for (int q = 0; q < CN; ++q) {
+            const int i = ib + 32 * r, c = c1 + cc + q;
+            acc[r][q] = (r < rg && i < n && c < n) ? A[i + (int64_t)c * n] : T(0);
+          }
+#pragma unroll
+        for (int jj = 0; jj < NB; ++jj) {
+          if (jj >= kb) continue;
+          T lv[RM], uv[CN];
+#pragma unroll
+          for (int r = 0; r < RM; ++r)
+            lv[r] = r < rg ? sm.L[jj * kBatchMaxN + min(ib + 32 * r, kBatchMaxN - 1)] : T(0);
+#pragma unroll
+          for (int q = 0; q < CN; ++q) uv[q] = sm.U[jj * kBatchUStride + cc + q];
+#pragma unroll
+          for (int r = 0; r < RM; ++r)
+            if (r < rg)
+#pragma unroll
+              for (int q = 0; q < CN; ++q) acc[r][q] = fma(-lv[r], uv[q], acc[r][q]);
         }
+#pragma unroll
+        for (int r = 0; r < RM; ++r)
+#pragma unroll
+          for (int q = 0; q < CN; ++q) {
+            const int i = ib + 32 * r, c = c1 + cc + q;
+            if (r < rg && i < n && c < n) A[i + (int64_t)c * n] = acc[r][q];
+          }
       }
     }
     __syncthreads();
@@ -191,59 +335,114 @@ __device__ int64_t factor_system(T* __restrict__ A, int n, int32_t* __restrict__
   return info;
 }
 
-// x := A \ x with the factors of factor_system (src/factorization.jl:433-457),
-// x held in shared memory.
+// xs := U \ (L \ xs) with the factors of factor_system, xs already permuted
+// (xs[r] = b[perm[r]]).  Blocks of 32: warp 0 solves the diagonal block with
+// shuffles, then every thread applies the block column to its rows.  Per
+// element the order is the reference's back-solve (src/factorization.jl:433-457):
+// forward j ascending, backward j descending with x[j] / U[j,j] (a correctly
+// rounded quotient from the reciprocal, Markstein's method).
 template <typename T, int NT>
-__device__ void solve_system(const T* __restrict__ LU, int n, const int32_t* __restrict__ ipiv,
-                             T* x) {
-  if (threadIdx.x == 0)
-    for (int i = 0; i < n; ++i) {
-      const int p = ipiv[i] - 1;
-      if (p != i) { const T t = x[i]; x[i] = x[p]; x[p] = t; }
+__device__ void lu_solve_permuted(const T* __restrict__ LU, int n, T* xs) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int b0 = 0; b0 < n; b0 += 32) {
+    const int bw = min(32, n - b0);
+    if (warp == 0) {
+      T lr[32];
+#pragma unroll
+      for (int j = 0; j < 32; ++j)
+        lr[j] = (j < lane && lane < bw) ? LU[(b0 + lane) + (int64_t)(b0 + j) * n] : T(0);
+      T x = lane < bw ? xs[b0 + lane] : T(0);
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        const T xj = __shfl_sync(0xffffffffu, x, j);
+        if (j < lane && lane < bw) x = fma(-lr[j], xj, x);
+      }
+      if (lane < bw) xs[b0 + lane] = x;
     }
-  __syncthreads();
-  for (int j = 0; j < n; ++j) {
-    const T xj = x[j];
-    for (int i = j + 1 + threadIdx.x; i < n; i += NT) x[i] = fma(-LU[i + (int64_t)j * n], xj, x[i]);
+    __syncthreads();
+    for (int i = b0 + bw + tid; i < n; i += NT) {
+      T lr[32];
+#pragma unroll
+      for (int j = 0; j < 32; ++j) lr[j] = j < bw ? LU[i + (int64_t)(b0 + j) * n] : T(0);
+      T acc = xs[i];
+#pragma unroll
+      for (int j = 0; j < 32; ++j)
+        if (j < bw) acc = fma(-lr[j], xs[b0 + j], acc);
+      xs[i] = acc;
+    }
     __syncthreads();
   }
-  for (int j = n - 1; j >= 0; --j) {
-    if (threadIdx.x == 0) x[j] = x[j] / LU[j + (int64_t)j * n];
+  for (int b0 = ((n - 1) / 32) * 32; b0 >= 0; b0 -= 32) {
+    const int bw = min(32, n - b0);
+    if (warp == 0) {
+      T ur[32];
+#pragma unroll
+      for (int j = 0; j < 32; ++j)
+        ur[j] = (j > lane && j < bw) ? LU[(b0 + lane) + (int64_t)(b0 + j) * n] : T(0);
+      const T d = lane < bw ? LU[(b0 + lane) + (int64_t)(b0 + lane) * n] : T(1);
+      const T y = T(1) / d;
+      T x = lane < bw ? xs[b0 + lane] : T(0);
+#pragma unroll
+      for (int j = 31; j >= 0; --j) {
+        if (j < bw) {
+          if (lane == j) x = div_markstein(x, d, y);
+          const T xj = __shfl_sync(0xffffffffu, x, j);
+          if (lane < j) x = fma(-ur[j], xj, x);
+        }
+      }
+      if (lane < bw) xs[b0 + lane] = x;
+    }
     __syncthreads();
-    const T xj = x[j];
-    for (int i = threadIdx.x; i < j; i += NT) x[i] = fma(-LU[i + (int64_t)j * n], xj, x[i]);
+    for (int i = tid; i < b0; i += NT) {
+      T ur[32];
+#pragma unroll
+      for (int j = 0; j < 32; ++j) ur[j] = j < bw ? LU[i + (int64_t)(b0 + j) * n] : T(0);
+      T acc = xs[i];
+#pragma unroll
+      for (int j = 31; j >= 0; --j)
+        if (j < bw) acc = fma(-ur[j], xs[b0 + j], acc);
+      xs[i] = acc;
+    }
     __syncthreads();
   }
 }
 
+// NaN-propagating maximum (a NaN residual must not look converged).
+__device__ __forceinline__ double nan_max(double a, double b) {
+  if (a != a) return a;
+  if (b != b) return b;
+  return a > b ? a : b;
+}
+
+// Block-wide maxima of two values (every thread receives both).
 template <int NT>
-__device__ __forceinline__ double block_max(double v, double* red) {
-  for (int off = 16; off; off >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, off));
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+__device__ __forceinline__ void block_max2(double& a, double& b, double* red) {
+  for (int off = 16; off; off >>= 1) {
+    a = nan_max(a, __shfl_down_sync(0xffffffffu, a, off));
+    b = nan_max(b, __shfl_down_sync(0xffffffffu, b, off));
+  }
+  if ((threadIdx.x & 31) == 0) { red[threadIdx.x >> 5] = a; red[32 + (threadIdx.x >> 5)] = b; }
   __syncthreads();
-  double m = 0;
-  for (int w = 0; w < NT / 32; ++w) m = fmax(m, red[w]);
+  a = 0.0;
+  b = 0.0;
+  for (int w = 0; w < NT / 32; ++w) { a = nan_max(a, red[w]); b = nan_max(b, red[32 + w]); }
   __syncthreads();
-  return m;
 }
 
-template <typename T, int NB>
-constexpr size_t batch_smem() {
-  return (size_t)2 * NB * kBatchMaxN * sizeof(T) + kBatchMaxN * sizeof(double) * 3 + 256;
+template <typename T, int NT, int NB>
+__host__ __device__ constexpr size_t batch_smem(bool mixed) {
+  return SysSmem<T, NT, NB>::bytes(mixed);
 }
 
-// FP64: factor in place (Awork holds a copy of A) and solve; x overwrites b.
+// FP64: factor in place and solve; x overwrites b.  With only_flagged, only
+// the systems the mixed kernel flagged are processed, each first copied from
+// Asrc (the untouched FP64 input) into Awork.
 template <int NT, int NB>
-__global__ void __launch_bounds__(NT)
-batch_fp64_kernel(BatchDev d, double* __restrict__ Awork, double* __restrict__ X,
-                  int32_t* __restrict__ ipiv_all, int only_flagged) {
+__global__ void __launch_bounds__(NT, NT <= 128 ? 3 : (NT <= 256 ? 2 : 1))
+batch_fp64_kernel(BatchDev d, double* __restrict__ Awork, const double* __restrict__ Asrc,
+                  double* __restrict__ X, int32_t* __restrict__ ipiv_all, int only_flagged) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  SysSmem<double> sm;
-  sm.P = reinterpret_cast<double*>(smem_raw);
-  sm.U = sm.P + NB * kBatchMaxN;
-  sm.x = sm.U + NB * kBatchMaxN;
-  sm.red_v = sm.x + kBatchMaxN;
-  sm.red_i = reinterpret_cast<int*>(sm.red_v + 32);
+  const SysSmem<double, NT, NB> sm(smem_raw, false);
   __shared__ int s_idx;
   for (;;) {
     if (threadIdx.x == 0) s_idx = (int)atomicAdd(d.queue, 1u);
@@ -255,36 +454,39 @@ batch_fp64_kernel(BatchDev d, double* __restrict__ Awork, double* __restrict__ X
     if (only_flagged && d.flag[s] == 0) continue;
     const int n = d.sizes[s];
     double* A = Awork + d.a_off[s];
+    if (only_flagged) {
+      const double* A0 = Asrc + d.a_off[s];
+      for (int i = threadIdx.x; i < n * n; i += NT) A[i] = A0[i];
+      __syncthreads();
+    }
     int32_t* ipiv = ipiv_all + d.b_off[s];
     const int64_t info = factor_system<double, NT, NB>(A, n, ipiv, sm);
     if (threadIdx.x == 0) { d.info[s] = info; if (only_flagged) d.flag[s] = 0; }
     if (info == 0) {
       double* x = X + d.b_off[s];
-      for (int i = threadIdx.x; i < n; i += NT) sm.x[i] = x[i];
+      for (int i = threadIdx.x; i < n; i += NT) sm.xs[i] = x[sm.perm[i]];
       __syncthreads();
-      solve_system<double, NT>(A, n, ipiv, sm.x);
-      for (int i = threadIdx.x; i < n; i += NT) x[i] = sm.x[i];
+      lu_solve_permuted<double, NT>(A, n, sm.xs);
+      for (int i = threadIdx.x; i < n; i += NT) x[i] = sm.xs[i];
     }
     __syncthreads();
   }
 }
 
-// Mixed: FP32 factors of each system, FP64 refinement against the FP64 A.
+// Mixed: FP32 factors of each system, FP64 refinement against the FP64 A:
+// residual r = b - A x in FP64, correction LU32 \ (r / s) * s with s a power
+// of two near ||r||, stop when ||r|| / (||A|| ||x|| + ||b||) <= n eps (infinity
+// norms), at stagnation, or after maxit corrections.  Systems that do not
+// converge (or whose FP32 factorization hit a zero pivot) are flagged for the
+// FP64 kernel that runs after this one in the same graph.
 template <int NT, int NB>
-__global__ void __launch_bounds__(NT)
+__global__ void __launch_bounds__(NT, NT <= 128 ? 3 : (NT <= 256 ? 2 : 1))
 batch_mixed_kernel(BatchDev d, const double* __restrict__ A64, float* __restrict__ A32,
-                   double* __restrict__ X, double* __restrict__ Bcopy, int32_t* __restrict__ ipiv_all,
-                   int maxit, double tol_per_n) {
+                   double* __restrict__ X, const double* __restrict__ Bcopy,
+                   int32_t* __restrict__ ipiv_all, int maxit, double tol_per_n) {
+  constexpr int RPT = (kBatchMaxN + NT - 1) / NT;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  SysSmem<float> sm;
-  sm.P = reinterpret_cast<float*>(smem_raw);
-  sm.U = sm.P + NB * kBatchMaxN;
-  sm.x = sm.U + NB * kBatchMaxN;
-  double* xd = reinterpret_cast<double*>(sm.x + kBatchMaxN);  // FP64 iterate
-  double* rd = xd + kBatchMaxN;                               // FP64 residual
-  double* redd = rd + kBatchMaxN;
-  sm.red_v = reinterpret_cast<float*>(redd + 32);
-  sm.red_i = reinterpret_cast<int*>(sm.red_v + 32);
+  const SysSmem<float, NT, NB> sm(smem_raw, true);
   __shared__ int s_idx;
   for (;;) {
     if (threadIdx.x == 0) s_idx = (int)atomicAdd(d.queue, 1u);
@@ -299,21 +501,35 @@ batch_mixed_kernel(BatchDev d, const double* __restrict__ A64, float* __restrict
     int32_t* ipiv = ipiv_all + d.b_off[s];
     double* xo = X + d.b_off[s];
     const double* b = Bcopy + d.b_off[s];
-    for (int64_t i = threadIdx.x; i < (int64_t)n * n; i += NT) F[i] = (float)A[i];
-    __syncthreads();
-    const int64_t info = factor_system<float, NT, NB>(F, n, ipiv, sm);
-    // ||A||_inf and ||b||_inf
-    double ra = 0, bm = 0;
-    for (int i = threadIdx.x; i < n; i += NT) {
-      double acc = 0;
-      for (int j = 0; j < n; ++j) acc += fabs(A[i + (int64_t)j * n]);
-      ra = fmax(ra, acc);
-      bm = fmax(bm, fabs(b[i]));
-      xd[i] = 0.0;
-      rd[i] = b[i];
+    // FP32 copy and FP64 row sums of |A| in one pass (thread i % NT owns row i)
+    double rs[RPT];
+#pragma unroll
+    for (int m = 0; m < RPT; ++m) rs[m] = 0.0;
+    for (int j = 0; j < n; ++j) {
+#pragma unroll
+      for (int m = 0; m < RPT; ++m) {
+        const int i = threadIdx.x + NT * m;
+        if (i < n) {
+          const double a = A[i + (int64_t)j * n];
+          F[i + (int64_t)j * n] = (float)a;
+          rs[m] += fabs(a);
+        }
+      }
     }
-    const double anorm = block_max<NT>(ra, redd);
-    const double bnorm = block_max<NT>(bm, redd);
+    double ra = 0.0, bm = 0.0;
+#pragma unroll
+    for (int m = 0; m < RPT; ++m) {
+      const int i = threadIdx.x + NT * m;
+      if (i < n) {
+        ra = nan_max(ra, rs[m]);
+        bm = nan_max(bm, fabs(b[i]));
+        sm.xd[i] = 0.0;
+        sm.rd[i] = b[i];
+      }
+    }
+    block_max2<NT>(ra, bm, sm.red);
+    const double anorm = ra, bnorm = bm;
+    const int64_t info = factor_system<float, NT, NB>(F, n, ipiv, sm);
     const double tol = tol_per_n * n;
     bool ok = false;
     int iters_done = 0;
@@ -324,32 +540,32 @@ batch_mixed_kernel(BatchDev d, const double* __restrict__ A64, float* __restrict
         if (it > 0) {  // r = b - A x (FP64, row-parallel, column order fixed)
           for (int i = threadIdx.x; i < n; i += NT) {
             double acc = b[i];
-            for (int j = 0; j < n; ++j) acc = fma(-A[i + (int64_t)j * n], xd[j], acc);
-            rd[i] = acc;
+            for (int j = 0; j < n; ++j) acc = fma(-A[i + (int64_t)j * n], sm.xd[j], acc);
+            sm.rd[i] = acc;
           }
-          __syncthreads();
         }
-        double rm = 0, xm = 0;
-        for (int i = threadIdx.x; i < n; i += NT) { rm = fmax(rm, fabs(rd[i])); xm = fmax(xm, fabs(xd[i])); }
-        const double rn = block_max<NT>(rm, redd);
-        const double xn = block_max<NT>(xm, redd);
-        const double den = anorm * xn + bnorm;
-        const double be = den > 0 ? rn / den : (rn == 0 ? 0.0 : INFINITY);
+        double rm = 0.0, xm = 0.0;
+        for (int i = threadIdx.x; i < n; i += NT) {
+          rm = nan_max(rm, fabs(sm.rd[i]));
+          xm = nan_max(xm, fabs(sm.xd[i]));
+        }
+        block_max2<NT>(rm, xm, sm.red);
+        const double den = anorm * xm + bnorm;
+        const double be = den > 0 ? rm / den : (rm == 0 ? 0.0 : INFINITY);
         if (be <= tol) { ok = true; break; }
-        if (!(be < 0.9 * prev) && it >= 2) break;  // stagnation
+        if (!(be < 0.9 * prev) && it >= 2) break;  // stagnation (or NaN)
         prev = be;
         if (it == maxit) break;
-        // d = LU32 \ (r / s) * s
-        const double sc = rn > 0 && isfinite(rn) ? ldexp(1.0, ilogb(rn)) : 1.0;
-        for (int i = threadIdx.x; i < n; i += NT) sm.x[i] = (float)(rd[i] / sc);
+        const double sc = rm > 0 && isfinite(rm) ? ldexp(1.0, ilogb(rm)) : 1.0;
+        for (int i = threadIdx.x; i < n; i += NT) sm.xs[i] = (float)(sm.rd[sm.perm[i]] / sc);
         __syncthreads();
-        solve_system<float, NT>(F, n, ipiv, sm.x);
-        for (int i = threadIdx.x; i < n; i += NT) xd[i] += sc * (double)sm.x[i];
+        lu_solve_permuted<float, NT>(F, n, sm.xs);
+        for (int i = threadIdx.x; i < n; i += NT) sm.xd[i] += sc * (double)sm.xs[i];
         __syncthreads();
       }
     }
     if (ok)
-      for (int i = threadIdx.x; i < n; i += NT) xo[i] = xd[i];
+      for (int i = threadIdx.x; i < n; i += NT) xo[i] = sm.xd[i];
     if (threadIdx.x == 0) {
       d.info[s] = 0;
       d.flag[s] = ok ? 0 : 1;  // the FP64 kernel re-solves flagged systems from A64
@@ -409,24 +625,24 @@ namespace {
 template <int NT, int NB>
 void configure_batch_kernels() {
   cudaFuncSetAttribute(batch_fp64_kernel<NT, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)batch_smem<double, NB>());
+                       (int)batch_smem<double, NT, NB>(false));
   cudaFuncSetAttribute(batch_mixed_kernel<NT, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)(batch_smem<float, NB>() + 3 * kBatchMaxN * sizeof(double)));
+                       (int)batch_smem<float, NT, NB>(true));
 }
 
 template <int NT, int NB>
 cudaError_t launch_fp64(const BatchDev& d, int ctas, gblu_batch* b, double* Awork, int only_flagged,
                         cudaStream_t s) {
   LaunchScope ls(K_BATCH, 0.0, 0.0, s);
-  batch_fp64_kernel<NT, NB><<<ctas, NT, batch_smem<double, NB>(), s>>>(d, Awork, b->d_X, b->d_ipiv,
-                                                                       only_flagged);
+  batch_fp64_kernel<NT, NB><<<ctas, NT, batch_smem<double, NT, NB>(false), s>>>(
+      d, Awork, only_flagged ? b->d_A : nullptr, b->d_X, b->d_ipiv, only_flagged);
   return cudaGetLastError();
 }
 
 template <int NT, int NB>
 cudaError_t launch_mixed(const BatchDev& d, int ctas, gblu_batch* b, cudaStream_t s) {
   LaunchScope ls(K_BATCH, 0.0, 0.0, s);
-  batch_mixed_kernel<NT, NB><<<ctas, NT, batch_smem<float, NB>() + 3 * kBatchMaxN * sizeof(double), s>>>(
+  batch_mixed_kernel<NT, NB><<<ctas, NT, batch_smem<float, NT, NB>(true), s>>>(
       d, b->d_A, b->d_A32, b->d_X, b->d_B, b->d_ipiv, b->maxit, 2.220446049250313e-16);
   return cudaGetLastError();
 }
@@ -548,7 +764,8 @@ int32_t build_graph(gblu_ctx* ctx, gblu_batch* b) {
       if (e != cudaSuccess || k.count == 0) continue;
       BatchBucket k2 = k;
       k2.queue = b->d_queues + b->buckets.size() + (&k - &b->buckets[0]);
-      // fallback: copy of A (A64 must stay intact for later solves)
+      // fallback: each flagged system is copied from A64 into the work area and
+      // factored there (A64 stays intact)
       e = launch_bucket(b, k2, false, 1, b->d_Awork, s);
     }
   }
@@ -703,14 +920,13 @@ int32_t gblu_batch_solve(gblu_ctx* ctx, gblu_batch* b, const double* A, double* 
   GBLU_CK(ctx, cudaMemcpyAsync(b->d_X, B, b->b_total * 8, kin, s), "batch B");
   if (b->precision != GBLU_FP64) {
     GBLU_CK(ctx, cudaMemcpyAsync(b->d_B, b->d_X, b->b_total * 8, cudaMemcpyDeviceToDevice, s), "batch B copy");
-    GBLU_CK(ctx, cudaMemcpyAsync(b->d_Awork, b->d_A, b->a_total * 8, cudaMemcpyDeviceToDevice, s), "batch A copy");
   }
   {
     // one graph launch runs every persistent kernel of the schedule; the scope
     // times the whole graph and the counters record each kernel it holds
     int nk = 0;
     for (auto& k : b->buckets) nk += k.count > 0 ? (b->precision != GBLU_FP64 ? 2 : 1) : 0;
-    LaunchScope ls(K_BATCH, batch_flops(b), (double)b->a_total * 8.0 * (b->precision != GBLU_FP64 ? 4.0 : 2.0), s);
+    LaunchScope ls(K_BATCH, batch_flops(b), (double)b->a_total * 8.0 * (b->precision != GBLU_FP64 ? 1.5 : 2.0), s);
     if (tl_profiler && nk > 1) {
       tl_profiler->launches += nk - 1;
       tl_profiler->count[K_BATCH] += nk - 1;

@@ -172,6 +172,19 @@ __global__ void colmax_kernel(int64_t n, int W, const double* __restrict__ X, in
   }
 }
 
+// Per-column power-of-two scale from the column maxima (bit patterns):
+// sc[q] = 1 / 2^ilogb(max), sc[kMaxW + q] = 2^ilogb(max) (1 for a zero or
+// non-finite maximum), so the FP32 right-hand side is O(1).
+__global__ void pow2_scales_kernel(int W, const unsigned long long* __restrict__ colmax,
+                                   double* __restrict__ sc) {
+  const int q = threadIdx.x;
+  if (q >= W) return;
+  const double m = __longlong_as_double((long long)colmax[q]);
+  const double scale = (m > 0 && isfinite(m)) ? ldexp(1.0, ilogb(m)) : 1.0;
+  sc[q] = 1.0 / scale;
+  sc[kMaxW + q] = scale;
+}
+
 // D[:,q] = float(R[:,q] * inv_scale[q])
 __global__ void scale_to_f32_kernel(int64_t n, int W, const double* __restrict__ R, int64_t ldr,
                                     const double* __restrict__ inv_scale, float* __restrict__ D,
@@ -214,12 +227,12 @@ size_t refine_bytes(int64_t n, int64_t W) {
   b += align256((size_t)n * W * sizeof(float));            // d32
   size_t pe = (size_t)kSplit * std::max<int64_t>(n, kGmresRestart + 1) * W;
   b += align256(pe * sizeof(double));                      // partial
-  b += align256((size_t)n * (kGmresRestart + 1) * sizeof(double));  // V
-  b += align256((size_t)n * sizeof(double));               // w
-  b += align256((kGmresRestart + 1) * sizeof(double));     // h
+  b += align256((size_t)n * (kGmresRestart + 1) * W * sizeof(double));  // V
+  b += align256((size_t)n * W * sizeof(double));           // w
+  b += align256(3 * (kGmresRestart + 1) * W * sizeof(double));  // h
   b += align256(4 * W * sizeof(unsigned long long));       // colmax
   b += align256((size_t)kDotBlocks * (kGmresRestart + 1) * sizeof(double));
-  b += align256(4 * sizeof(double) * W);                   // scales
+  b += align256(4 * sizeof(double) * kMaxW);               // scales
   b += align256(sizeof(double));                           // anorm
   return b + 256;
 }
@@ -236,12 +249,12 @@ void refine_carve(RefineWork& w, char* base, int64_t n, int64_t W) {
   w.d32 = reinterpret_cast<float*>(take((size_t)n * W * sizeof(float)));
   size_t pe = (size_t)kSplit * std::max<int64_t>(n, kGmresRestart + 1) * W;
   w.partial = reinterpret_cast<double*>(take(pe * sizeof(double)));
-  w.V = reinterpret_cast<double*>(take((size_t)n * (kGmresRestart + 1) * sizeof(double)));
-  w.w = reinterpret_cast<double*>(take((size_t)n * sizeof(double)));
-  w.h = reinterpret_cast<double*>(take((kGmresRestart + 1) * sizeof(double)));
+  w.V = reinterpret_cast<double*>(take((size_t)n * (kGmresRestart + 1) * W * sizeof(double)));
+  w.w = reinterpret_cast<double*>(take((size_t)n * W * sizeof(double)));
+  w.h = reinterpret_cast<double*>(take(3 * (kGmresRestart + 1) * W * sizeof(double)));
   w.colmax = reinterpret_cast<unsigned long long*>(take(4 * W * sizeof(unsigned long long)));
   w.dots = reinterpret_cast<double*>(take((size_t)kDotBlocks * (kGmresRestart + 1) * sizeof(double)));
-  w.anorm_dev = reinterpret_cast<double*>(take(4 * sizeof(double) * W));
+  w.anorm_dev = reinterpret_cast<double*>(take(4 * sizeof(double) * kMaxW));
 }
 
 namespace {
@@ -335,36 +348,31 @@ struct Solver {
   cudaStream_t s;
   int64_t n;
 
-  // x (len n, W cols) <- M^{-1} v using the FP32 factors with a per-column
-  // power-of-two scale so the FP32 right-hand side is O(1).
+  // out (len n, W cols) <- M^{-1} v using the FP32 factors with a per-column
+  // power-of-two scale so the FP32 right-hand side is O(1).  No host sync.
   int32_t precond(const double* v, int64_t ldv, double* out, int64_t ldo, int W) {
-    std::vector<unsigned long long> bits(W);
-    GBLU_CK(ctx, cudaMemsetAsync(w.colmax + 3 * w.W, 0, W * sizeof(unsigned long long), s), "memset");
-    { LaunchScope ls_(K_REFINE, 0.0, 0.0, s);
-    colmax_kernel<<<grid_for(n), 256, 0, s>>>(n, W, v, ldv, w.colmax + 3 * w.W);
+    unsigned long long* cm = w.colmax + 3 * w.W;
+    double* dsc = w.anorm_dev;  // 2*kMaxW doubles of scale storage
+    GBLU_CK(ctx, cudaMemsetAsync(cm, 0, W * sizeof(unsigned long long), s), "memset");
+    {
+      LaunchScope ls_(K_REFINE, 0.0, 0.0, s);
+      colmax_kernel<<<grid_for(n), 256, 0, s>>>(n, W, v, ldv, cm);
     }
     GBLU_CK(ctx, cudaGetLastError(), "colmax");
-    GBLU_CK(ctx, cudaMemcpyAsync(bits.data(), w.colmax + 3 * w.W, W * sizeof(unsigned long long),
-                                 cudaMemcpyDeviceToHost, s), "colmax readback");
-    GBLU_CK(ctx, cudaStreamSynchronize(s), "precond");
-    double sc[2 * kMaxW];
-    for (int q = 0; q < W; ++q) {
-      double m = bits_to_double(bits[q]);
-      double scale = 1.0;
-      if (m > 0 && std::isfinite(m)) scale = std::ldexp(1.0, std::ilogb(m));
-      sc[q] = 1.0 / scale;
-      sc[kMaxW + q] = scale;
+    {
+      LaunchScope ls_(K_REFINE, 0.0, 0.0, s);
+      pow2_scales_kernel<<<1, 32, 0, s>>>(W, cm, dsc);
     }
-    double* dsc = w.anorm_dev;  // 4*W doubles of scale storage
-    GBLU_CK(ctx, cudaMemcpyAsync(dsc, sc, 2 * kMaxW * sizeof(double), cudaMemcpyHostToDevice, s),
-            "scales");
-    { LaunchScope ls_(K_REFINE, 0.0, 0.0, s);
-    scale_to_f32_kernel<<<grid_for(n * W), 256, 0, s>>>(n, W, v, ldv, dsc, w.d32, n);
+    GBLU_CK(ctx, cudaGetLastError(), "scales");
+    {
+      LaunchScope ls_(K_REFINE, 0.0, 0.0, s);
+      scale_to_f32_kernel<<<grid_for(n * W), 256, 0, s>>>(n, W, v, ldv, dsc, w.d32, n);
     }
     GBLU_CK(ctx, cudaGetLastError(), "scale");
     GBLU_CK(ctx, getrs_launch<float>(f->rs32, trans, W, w.d32, n, nullptr, s), "FP32 getrs");
-    { LaunchScope ls_(K_REFINE, 0.0, 0.0, s);
-    update_from_f32_kernel<<<grid_for(n * W), 256, 0, s>>>(n, W, out, ldo, w.d32, n, dsc + kMaxW, 0.0);
+    {
+      LaunchScope ls_(K_REFINE, 0.0, 0.0, s);
+      update_from_f32_kernel<<<grid_for(n * W), 256, 0, s>>>(n, W, out, ldo, w.d32, n, dsc + kMaxW, 0.0);
     }
     GBLU_CK(ctx, cudaGetLastError(), "update");
     return GBLU_OK;
@@ -391,93 +399,118 @@ struct Solver {
     return GBLU_OK;
   }
 
-  // One GMRES(m) solve of op(A) d = r[:,q] left-preconditioned by the FP32 LU;
-  // adds d into x[:,q].  Returns the iteration count in *its.
-  int32_t gmres(int q, int restart, double rtol, int* its) {
-    const double* rq = w.r + (size_t)q * n;
-    double* V = w.V;
-    int32_t st = precond(rq, n, V, n, 1);
-    if (st) return st;
-    double beta = 0;
-    {
-      GBLU_CK(ctx, gemv('T', n, 1, V, n, V, n, 1, 1.0, nullptr, 1, 0.0, w.h, 1, w.partial, nullptr, s),
-              "norm");
-      GBLU_CK(ctx, cudaMemcpyAsync(&beta, w.h, sizeof(double), cudaMemcpyDeviceToHost, s), "norm");
-      GBLU_CK(ctx, cudaStreamSynchronize(s), "norm");
-      beta = std::sqrt(beta);
-    }
-    *its = 0;
-    if (!(beta > 0) || !std::isfinite(beta)) return GBLU_OK;
-    { LaunchScope ls_(K_REFINE, 0.0, 0.0, s);
-    axpby_kernel<<<grid_for(n), 256, 0, s>>>(n, 1.0 / beta, V, 0.0, V);
-    }
+  // GMRES(m) on op(A) d = r[:,q], left-preconditioned by the FP32 LU, for the
+  // columns q < nc with run[q] set, in lockstep: each inner step does one
+  // nc-column matvec and one nc-column preconditioner solve, while every
+  // column keeps its own basis V_q, Hessenberg matrix, rotations and stopping
+  // step, so its result is the one it would have alone.  Adds d_q into x[:,q];
+  // its[q] receives the column's inner iterations.
+  int32_t gmres_block(int nc, const std::vector<int>& run, int restart, double rtol, std::vector<int>& its) {
     const int m = std::max(1, std::min(restart, (int)kGmresRestart));
-    std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m), sn(m), g(m + 1, 0.0);
-    g[0] = beta;
-    int k = 0;
-    std::vector<double> h(m + 1), h2(m + 1);
+    const int64_t ldV = (int64_t)(kGmresRestart + 1) * n;  // stride between the columns' bases
+    const int hs = kGmresRestart + 1;
+    double* V = w.V;
+    auto Vq = [&](int q, int j) { return V + (size_t)q * ldV + (size_t)j * n; };
+    int32_t st = precond(w.r, n, V, ldV, nc);
+    if (st) return st;
+    // beta_q = ||z_q||_2
+    std::vector<double> hb((size_t)3 * hs * nc);
+    for (int q = 0; q < nc; ++q)
+      if (run[q])
+        GBLU_CK(ctx, gemv('T', n, 1, Vq(q, 0), n, Vq(q, 0), n, 1, 1.0, nullptr, 1, 0.0, w.h + q, 1,
+                          w.partial, nullptr, s), "norm");
+    std::vector<double> beta(nc, 0.0);
+    GBLU_CK(ctx, cudaMemcpyAsync(beta.data(), w.h, nc * sizeof(double), cudaMemcpyDeviceToHost, s), "norm");
+    GBLU_CK(ctx, cudaStreamSynchronize(s), "norm");
+    std::vector<int> step(nc, 0);  // 1 = still extending its basis
+    std::vector<int> k(nc, 0);
+    for (int q = 0; q < nc; ++q) {
+      its[q] = 0;
+      if (!run[q]) continue;
+      beta[q] = std::sqrt(beta[q]);
+      if (!(beta[q] > 0) || !std::isfinite(beta[q])) continue;
+      step[q] = 1;
+      LaunchScope ls_(K_REFINE, 0.0, 0.0, s);
+      axpby_kernel<<<grid_for(n), 256, 0, s>>>(n, 1.0 / beta[q], Vq(q, 0), 0.0, Vq(q, 0));
+    }
+    std::vector<std::vector<double>> H(nc, std::vector<double>((size_t)(m + 1) * m, 0.0));
+    std::vector<std::vector<double>> cs(nc, std::vector<double>(m)), sn(nc, std::vector<double>(m));
+    std::vector<std::vector<double>> g(nc, std::vector<double>(m + 1, 0.0));
+    for (int q = 0; q < nc; ++q) g[q][0] = beta[q];
     for (int j = 0; j < m; ++j) {
-      double* vj = V + (size_t)j * n;
-      double* z = V + (size_t)(j + 1) * n;
-      // w = op(A) v_j ; z = M^{-1} w
-      GBLU_CK(ctx, gemv(trans == 'N' ? 'N' : 'T', n, n, f->lu64, f->ld, vj, n, 1, 1.0, nullptr, 1, 0.0,
-                        w.w, n, w.partial, nullptr, s),
-              "matvec");
-      st = precond(w.w, n, z, n, 1);
+      bool any = false;
+      for (int q = 0; q < nc; ++q) any |= step[q] != 0;
+      if (!any) break;
+      // w = op(A) v_j ; z = M^{-1} w  (all nc columns at once)
+      GBLU_CK(ctx, gemv(trans == 'N' ? 'N' : 'T', n, n, f->lu64, f->ld, Vq(0, j), ldV, nc, 1.0, nullptr, 1,
+                        0.0, w.w, n, w.partial, nullptr, s), "matvec");
+      st = precond(w.w, n, Vq(0, j + 1), ldV, nc);
       if (st) return st;
-      // classical Gram-Schmidt, twice
-      for (int pass = 0; pass < 2; ++pass) {
-        GBLU_CK(ctx, gemv('T', n, j + 1, V, n, z, n, 1, 1.0, nullptr, 1, 0.0, w.h, 1, w.partial,
-                          nullptr, s),
-                "project");
-        GBLU_CK(ctx, gemv('N', n, j + 1, V, n, w.h, j + 1, 1, -1.0, z, n, 1.0, z, n, w.partial,
-                          nullptr, s),
-                "orthogonalise");
-        GBLU_CK(ctx, cudaMemcpyAsync(pass == 0 ? h.data() : h2.data(), w.h, (j + 1) * sizeof(double),
-                                     cudaMemcpyDeviceToHost, s),
-                "readback");
-      }
-      double nz2 = 0;
-      GBLU_CK(ctx, gemv('T', n, 1, z, n, z, n, 1, 1.0, nullptr, 1, 0.0, w.h, 1, w.partial, nullptr, s),
-              "norm");
-      GBLU_CK(ctx, cudaMemcpyAsync(&nz2, w.h, sizeof(double), cudaMemcpyDeviceToHost, s), "norm");
-      GBLU_CK(ctx, cudaStreamSynchronize(s), "gmres step");
-      double hn = std::sqrt(nz2);
-      for (int i = 0; i <= j; ++i) H[(size_t)j * (m + 1) + i] = h[i] + h2[i];
-      H[(size_t)j * (m + 1) + j + 1] = hn;
-      for (int i = 0; i < j; ++i) {  // previous rotations
-        double a = H[(size_t)j * (m + 1) + i], b = H[(size_t)j * (m + 1) + i + 1];
-        H[(size_t)j * (m + 1) + i] = cs[i] * a + sn[i] * b;
-        H[(size_t)j * (m + 1) + i + 1] = -sn[i] * a + cs[i] * b;
-      }
-      double a = H[(size_t)j * (m + 1) + j], b = H[(size_t)j * (m + 1) + j + 1];
-      double rr = std::hypot(a, b);
-      cs[j] = rr > 0 ? a / rr : 1.0;
-      sn[j] = rr > 0 ? b / rr : 0.0;
-      H[(size_t)j * (m + 1) + j] = rr;
-      H[(size_t)j * (m + 1) + j + 1] = 0.0;
-      g[j + 1] = -sn[j] * g[j];
-      g[j] = cs[j] * g[j];
-      k = j + 1;
-      if (hn > 0 && std::isfinite(hn))
-        { LaunchScope ls_(K_REFINE, 0.0, 0.0, s);
-        axpby_kernel<<<grid_for(n), 256, 0, s>>>(n, 1.0 / hn, z, 0.0, z);
+      // classical Gram-Schmidt, twice, and the norm, per stepping column
+      for (int q = 0; q < nc; ++q) {
+        if (!step[q]) continue;
+        double* z = Vq(q, j + 1);
+        for (int pass = 0; pass < 2; ++pass) {
+          double* hq = w.h + (size_t)(q * 3 + pass) * hs;
+          GBLU_CK(ctx, gemv('T', n, j + 1, Vq(q, 0), n, z, n, 1, 1.0, nullptr, 1, 0.0, hq, 1, w.partial,
+                            nullptr, s), "project");
+          GBLU_CK(ctx, gemv('N', n, j + 1, Vq(q, 0), n, hq, j + 1, 1, -1.0, z, n, 1.0, z, n, w.partial,
+                            nullptr, s), "orthogonalise");
         }
-      if (std::fabs(g[j + 1]) <= rtol * beta || !(hn > 0)) break;
+        GBLU_CK(ctx, gemv('T', n, 1, z, n, z, n, 1, 1.0, nullptr, 1, 0.0, w.h + (size_t)(q * 3 + 2) * hs, 1,
+                          w.partial, nullptr, s), "norm");
+      }
+      GBLU_CK(ctx, cudaMemcpyAsync(hb.data(), w.h, (size_t)3 * hs * nc * sizeof(double), cudaMemcpyDeviceToHost,
+                                   s), "readback");
+      GBLU_CK(ctx, cudaStreamSynchronize(s), "gmres step");
+      for (int q = 0; q < nc; ++q) {
+        if (!step[q]) continue;
+        const double* h1 = hb.data() + (size_t)(q * 3) * hs;
+        const double* h2 = h1 + hs;
+        const double hn = std::sqrt(h1[2 * hs]);
+        std::vector<double>& Hq = H[q];
+        for (int i = 0; i <= j; ++i) Hq[(size_t)j * (m + 1) + i] = h1[i] + h2[i];
+        Hq[(size_t)j * (m + 1) + j + 1] = hn;
+        for (int i = 0; i < j; ++i) {  // previous rotations
+          const double a = Hq[(size_t)j * (m + 1) + i], b = Hq[(size_t)j * (m + 1) + i + 1];
+          Hq[(size_t)j * (m + 1) + i] = cs[q][i] * a + sn[q][i] * b;
+          Hq[(size_t)j * (m + 1) + i + 1] = -sn[q][i] * a + cs[q][i] * b;
+        }
+        const double a = Hq[(size_t)j * (m + 1) + j], b = Hq[(size_t)j * (m + 1) + j + 1];
+        const double rr = std::hypot(a, b);
+        cs[q][j] = rr > 0 ? a / rr : 1.0;
+        sn[q][j] = rr > 0 ? b / rr : 0.0;
+        Hq[(size_t)j * (m + 1) + j] = rr;
+        Hq[(size_t)j * (m + 1) + j + 1] = 0.0;
+        g[q][j + 1] = -sn[q][j] * g[q][j];
+        g[q][j] = cs[q][j] * g[q][j];
+        k[q] = j + 1;
+        if (std::fabs(g[q][j + 1]) <= rtol * beta[q] || !(hn > 0) || !std::isfinite(hn)) {
+          step[q] = 0;
+        } else {
+          LaunchScope ls_(K_REFINE, 0.0, 0.0, s);
+          axpby_kernel<<<grid_for(n), 256, 0, s>>>(n, 1.0 / hn, Vq(q, j + 1), 0.0, Vq(q, j + 1));
+        }
+      }
     }
-    *its = k;
-    // y = H(1:k,1:k) \ g(1:k); d = V(:,1:k) y; x[:,q] += d
-    std::vector<double> y(k);
-    for (int i = k - 1; i >= 0; --i) {
-      double acc = g[i];
-      for (int jj = i + 1; jj < k; ++jj) acc -= H[(size_t)jj * (m + 1) + i] * y[jj];
-      double d = H[(size_t)i * (m + 1) + i];
-      y[i] = d != 0 ? acc / d : 0.0;
+    // y_q = H_q(1:k,1:k) \ g_q(1:k); x[:,q] += V_q(:,1:k) y_q
+    std::vector<double> y((size_t)hs * nc, 0.0);
+    for (int q = 0; q < nc; ++q) {
+      its[q] = k[q];
+      for (int i = k[q] - 1; i >= 0; --i) {
+        double acc = g[q][i];
+        for (int jj = i + 1; jj < k[q]; ++jj) acc -= H[q][(size_t)jj * (m + 1) + i] * y[(size_t)q * hs + jj];
+        const double d = H[q][(size_t)i * (m + 1) + i];
+        y[(size_t)q * hs + i] = d != 0 ? acc / d : 0.0;
+      }
     }
-    GBLU_CK(ctx, cudaMemcpyAsync(w.h, y.data(), k * sizeof(double), cudaMemcpyHostToDevice, s), "y");
-    double* xq = w.x + (size_t)q * n;
-    GBLU_CK(ctx, gemv('N', n, k, V, n, w.h, k, 1, 1.0, xq, n, 1.0, xq, n, w.partial, nullptr, s),
-            "update");
+    GBLU_CK(ctx, cudaMemcpyAsync(w.h, y.data(), y.size() * sizeof(double), cudaMemcpyHostToDevice, s), "y");
+    for (int q = 0; q < nc; ++q) {
+      if (k[q] == 0) continue;
+      double* xq = w.x + (size_t)q * n;
+      GBLU_CK(ctx, gemv('N', n, k[q], Vq(q, 0), n, w.h + (size_t)q * hs, k[q], 1, 1.0, xq, n, 1.0, xq, n,
+                        w.partial, nullptr, s), "update");
+    }
     return GBLU_OK;
   }
 };
@@ -539,13 +572,11 @@ int32_t refine_solve(gblu_ctx* ctx, gblu_factor* f, char trans, int64_t nrhs, do
         }
         if (!any_active) break;
         if (o.mode == GBLU_REFINE_GMRES) {
-          for (int q = 0; q < nc; ++q) {
-            if (state[q] != ACTIVE) continue;
-            int its = 0;
-            e = S.gmres(q, o.gmres_restart, o.gmres_tol, &its);
-            if (e) return e;
-            st_acc.inner_iterations += its;
-          }
+          std::vector<int> run(nc), its(nc, 0);
+          for (int q = 0; q < nc; ++q) run[q] = state[q] == ACTIVE;
+          e = S.gmres_block(nc, run, o.gmres_restart, o.gmres_tol, its);
+          if (e) return e;
+          for (int q = 0; q < nc; ++q) st_acc.inner_iterations += its[q];
         } else {
           e = S.precond(w.r, n, w.r, n, nc);  // d = M^{-1} r (in place), scaled per column
           if (e) return e;

@@ -19,9 +19,9 @@ struct RefineWork {
   double* b = nullptr;      // n x W   right-hand sides
   float* d32 = nullptr;     // n x W   low-precision correction
   double* partial = nullptr;  // kSplit x n x W  deterministic partial sums
-  double* V = nullptr;      // n x (restart + 1)   GMRES basis
-  double* w = nullptr;      // n        GMRES work vector
-  double* h = nullptr;      // restart + 1   projections
+  double* V = nullptr;      // n x (restart + 1) x W   GMRES bases, one per column
+  double* w = nullptr;      // n x W    GMRES work vectors
+  double* h = nullptr;      // 3 x (restart + 1) x W   projections and norms
   unsigned long long* colmax = nullptr;  // 4 x W   |.|_inf per column (bit patterns)
   double* dots = nullptr;   // kDotBlocks x (restart + 1)
   double anorm = 0;         // ||A||_inf of the FP64 matrix (host copy)
