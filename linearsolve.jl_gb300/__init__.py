@@ -17,9 +17,9 @@ The directory name is not a Python identifier; load it as a package with
 from ._lib import GBLUError, load as load_library  # noqa: F401
 from .device import Context, Factorization, default_context, dgetrf, dgetrs  # noqa: F401
 from .linear import (  # noqa: F401
-    GB300LUFactorization, GB300MixedLUFactorization, LinearAliasSpecifier, LinearCache,
-    LinearProblem, LinearSolution, ReturnCode, init, reinit, solve, solve_bang,
-    successful_retcode,
+    DefaultAlgorithmChoice, DefaultLinearSolver, GB300LUFactorization, GB300MixedLUFactorization,
+    LinearAliasSpecifier, LinearCache, LinearProblem, LinearSolution, OperatorAssumptions,
+    OperatorCondition, ReturnCode, defaultalg, init, reinit, solve, solve_bang, successful_retcode,
 )
 from ._cuda import DeviceMatrix, Event, PinnedArray  # noqa: F401
 from . import workloads  # noqa: F401

@@ -7,6 +7,7 @@ like the reference:
     prob  = LinearProblem(A, b)                     # SciMLBase.LinearProblem
     cache = init(prob, GB300LUFactorization())      # src/common.jl:700-931
     sol   = solve_bang(cache)                       # solve!(cache), common.jl:1012-1017
+    solve_bang(cache, adjoint=True)                 # A^T u = b, same factors (:1012-1027)
     cache.b = b2;  solve_bang(cache)                # getrs only   (common.jl:351-353)
     cache.A = A2;  solve_bang(cache)                # refactor     (common.jl:330-348)
     sol   = solve(prob, alg)                        # common.jl:988-993
@@ -140,6 +141,77 @@ class GB300MixedLUFactorization(AbstractDenseFactorization):
 
 
 # ---------------------------------------------------------------------------
+# Default algorithm choice (src/default.jl)
+
+class OperatorCondition(enum.Enum):
+    """SciMLOperators' condition hint used by the default chooser."""
+    IllConditioned = "IllConditioned"
+    VeryIllConditioned = "VeryIllConditioned"
+    SuperIllConditioned = "SuperIllConditioned"
+    WellConditioned = "WellConditioned"
+
+
+@dataclass
+class OperatorAssumptions:
+    """OperatorAssumptions(issq; condition) (src/common.jl); the reference's
+    default condition is IllConditioned."""
+    issq: Optional[bool] = None
+    condition: OperatorCondition = OperatorCondition.IllConditioned
+
+
+class DefaultAlgorithmChoice(enum.Enum):
+    """The members of DefaultAlgorithmChoice this library adds
+    (src/LinearSolve.jl:330-357 lists the reference's)."""
+    GB300LUFactorization = "GB300LUFactorization"
+    GB300MixedLUFactorization = "GB300MixedLUFactorization"
+
+
+class DefaultLinearSolver:
+    """DefaultLinearSolver(alg; safetyfallback) (src/default.jl).  Resolved to
+    a concrete algorithm by init; see defaultalg."""
+
+    def __init__(self, alg: DefaultAlgorithmChoice = DefaultAlgorithmChoice.GB300LUFactorization,
+                 safetyfallback: bool = True, device: int = 0):
+        self.alg = DefaultAlgorithmChoice(alg)
+        self.safetyfallback = bool(safetyfallback)
+        self.device = int(device)
+
+    def concrete(self):
+        if self.alg == DefaultAlgorithmChoice.GB300MixedLUFactorization:
+            return GB300MixedLUFactorization(factor="fp32", refine="ir", fallback=True, device=self.device)
+        return GB300LUFactorization(device=self.device)
+
+    def __repr__(self):
+        return f"DefaultLinearSolver({self.alg.name}, safetyfallback={self.safetyfallback})"
+
+
+def defaultalg(A, b, assump: Optional[OperatorAssumptions] = None) -> DefaultLinearSolver:
+    """The dense square branch of defaultalg (src/default.jl:411-520) and its
+    GPU-array branch (:277-284), with the GB300 algorithms registered:
+
+    * square, WellConditioned      -> GB300MixedLUFactorization (FP32 LU + FP64
+      refinement, falling back to the FP64 LU when refinement stalls: the
+      result is FP64-accurate either way);
+    * square, IllConditioned        -> GB300LUFactorization (the reference's
+      default condition; plain FP64 LU as LUFactorization);
+    * VeryIllConditioned / SuperIllConditioned / non-square -> the reference
+      picks QR / SVD / normal equations, which this library does not provide:
+      NotImplementedError."""
+    m, n = _shape(A)
+    assump = assump or OperatorAssumptions(issq=(m == n))
+    issq = (m == n) if assump.issq is None else bool(assump.issq)
+    if not issq:
+        raise NotImplementedError("non-square A: the reference chooses QR / normal equations, "
+                                  "which are outside this library (dense LU only)")
+    if assump.condition == OperatorCondition.WellConditioned:
+        return DefaultLinearSolver(DefaultAlgorithmChoice.GB300MixedLUFactorization)
+    if assump.condition == OperatorCondition.IllConditioned:
+        return DefaultLinearSolver(DefaultAlgorithmChoice.GB300LUFactorization)
+    raise NotImplementedError(f"{assump.condition.name}: the reference chooses QR / SVD, "
+                              "which are outside this library (dense LU only)")
+
+
+# ---------------------------------------------------------------------------
 # Cache
 
 def _shape(x):
@@ -165,6 +237,7 @@ class LinearCache:
         object.__setattr__(self, "b", b)
         object.__setattr__(self, "u", u)
         object.__setattr__(self, "stats", {})
+        object.__setattr__(self, "default", None)  # the DefaultLinearSolver init resolved, if any
 
     def __setattr__(self, name, value):
         if name == "A":
@@ -190,10 +263,14 @@ def _default_tolerances(A):
 
 def init(prob: LinearProblem, alg=None, alias: Optional[LinearAliasSpecifier] = None,
          abstol: Optional[float] = None, reltol: Optional[float] = None, verbose: bool = False,
-         context=None) -> LinearCache:
-    """SciMLBase.init(prob, alg; alias, abstol, reltol, verbose) (common.jl:700-931)."""
+         context=None, assumptions: Optional[OperatorAssumptions] = None) -> LinearCache:
+    """SciMLBase.init(prob, alg; alias, abstol, reltol, verbose, assumptions)
+    (common.jl:700-931).  alg None picks defaultalg(A, b, assumptions)."""
+    default = None
     if alg is None:
-        alg = GB300LUFactorization()
+        alg = defaultalg(prob.A, prob.b, assumptions)
+    if isinstance(alg, DefaultLinearSolver):
+        default, alg = alg, alg.concrete()
     A, b = prob.A, prob.b
     m, n = _shape(A)
     if getattr(alg, "needs_square_A", False) and m != n:
@@ -223,10 +300,11 @@ def init(prob: LinearProblem, alg=None, alias: Optional[LinearAliasSpecifier] = 
                         d_rel if reltol is None else reltol, verbose, alias_A, alias_b, ctx)
     # init_cacheval: the device-resident factorization object, allocated once
     cache.cacheval = ctx.factor(m, n, alg.factor_precision())
+    cache.default = default
     return cache
 
 
-def _solve_into(cache: LinearCache, fact, b):
+def _solve_into(cache: LinearCache, fact, b, trans: str = "N"):
     alg = cache.alg
     if isinstance(alg, GB300MixedLUFactorization):
         if isinstance(b, DeviceMatrix):
@@ -234,11 +312,11 @@ def _solve_into(cache: LinearCache, fact, b):
             out.copy_from(b)
             from ._cuda import device_synchronize
             device_synchronize()
-            X, stats = fact.solve_refined(out, mode=alg.refine, max_iter=alg.maxiters,
+            X, stats = fact.solve_refined(out, trans=trans, mode=alg.refine, max_iter=alg.maxiters,
                                           tol=alg.tol or 0.0, fallback=alg.fallback,
                                           gmres_restart=alg.gmres_restart, gmres_tol=alg.gmres_tol)
             return out, stats
-        X, stats = fact.solve_refined(b, mode=alg.refine, max_iter=alg.maxiters,
+        X, stats = fact.solve_refined(b, trans=trans, mode=alg.refine, max_iter=alg.maxiters,
                                       tol=alg.tol or 0.0, fallback=alg.fallback,
                                       gmres_restart=alg.gmres_restart, gmres_tol=alg.gmres_tol)
         return X, stats
@@ -247,13 +325,53 @@ def _solve_into(cache: LinearCache, fact, b):
         out.copy_from(b)
         from ._cuda import device_synchronize
         device_synchronize()
-        fact.getrs(out)
+        fact.getrs(out, trans=trans)
         return out, {}
-    return fact.getrs(b), {}
+    return fact.getrs(b, trans=trans), {}
 
 
-def solve_bang(cache: LinearCache, **kwargs) -> LinearSolution:
-    """solve!(cache) for the GB300 algorithms (factorization.jl:643-736 shape)."""
+def _store_u(cache: LinearCache, u):
+    if isinstance(u, DeviceMatrix):
+        cache.u = u
+    elif isinstance(cache.u, np.ndarray) and cache.u.shape == np.shape(u):
+        cache.u[...] = u
+    else:
+        cache.u = np.array(u)
+
+
+def _finite(u) -> bool:
+    return bool(np.all(np.isfinite(u.to_host() if isinstance(u, DeviceMatrix) else u)))
+
+
+def solve_bang(cache: LinearCache, adjoint: bool = False, **kwargs) -> LinearSolution:
+    """solve!(cache; adjoint) (common.jl:1012-1027).
+
+    adjoint=True solves A^T u = b with the cached factors (the reuse of
+    _solve_adjoint!, src/adjoint_factorization.jl): getrs / the refined solve
+    with trans 'T', factoring first only when A is fresh."""
+    if adjoint:
+        if cache.isfresh:
+            sol = _solve_bang(cache)
+            if sol.retcode == ReturnCode.Failure:
+                return sol
+        u, stats = _solve_into(cache, cache.cacheval, cache.b, trans="T")
+        _store_u(cache, u)
+        cache.stats = stats
+        return LinearSolution(cache.u, None, cache.alg, ReturnCode.Success,
+                              iters=stats.get("iterations", 0), cache=cache, stats=stats)
+    sol = _solve_bang(cache)
+    default = getattr(cache, "default", None)
+    if default is not None and default.safetyfallback and sol.retcode == ReturnCode.Success \
+            and not _finite(sol.u):
+        # _default_lu_solve_with_fallback (src/default.jl:946-967) retries with
+        # QR, which this library does not provide: report the failure instead
+        sol.retcode = ReturnCode.Failure
+        sol.stats = dict(sol.stats, fallback="non-finite LU solution; QR is outside this library")
+    return sol
+
+
+def _solve_bang(cache: LinearCache) -> LinearSolution:
+    """solve!(cache, alg) for the GB300 algorithms (factorization.jl:643-736 shape)."""
     alg = cache.alg
     fact = cache.cacheval
     if cache.isfresh:
@@ -267,13 +385,7 @@ def solve_bang(cache: LinearCache, **kwargs) -> LinearSolution:
                                   stats={"info": info})
         cache.isfresh = False
     u, stats = _solve_into(cache, fact, cache.b)
-    if isinstance(u, DeviceMatrix):
-        cache.u = u
-    else:
-        if isinstance(cache.u, np.ndarray) and cache.u.shape == np.shape(u):
-            cache.u[...] = u
-        else:
-            cache.u = np.array(u)
+    _store_u(cache, u)
     cache.stats = stats
     if getattr(alg, "residualsafety", False) and not isinstance(cache.A, DeviceMatrix):
         # _check_residual_safety (factorization.jl:127-156), 2-norms as the reference
@@ -288,9 +400,9 @@ def solve_bang(cache: LinearCache, **kwargs) -> LinearSolution:
                           cache=cache, stats=stats)
 
 
-def solve(prob: LinearProblem, alg=None, **kwargs) -> LinearSolution:
+def solve(prob: LinearProblem, alg=None, adjoint: bool = False, **kwargs) -> LinearSolution:
     """solve(prob, alg; kwargs...) = solve!(init(prob, alg; kwargs...)) (common.jl:988-993)."""
-    return solve_bang(init(prob, alg, **kwargs))
+    return solve_bang(init(prob, alg, **kwargs), adjoint=adjoint)
 
 
 def reinit(cache: LinearCache, A=None, b=None) -> LinearCache:

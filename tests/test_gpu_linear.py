@@ -113,3 +113,57 @@ def test_device_resident_inputs(pkg, oracle_mod):
     u = sol.u.to_host()
     LU, ipiv, _ = oracle_mod.getrf(A)
     assert np.array_equal(u, oracle_mod.getrs(LU, ipiv, b))
+
+
+def test_adjoint_solve_reuses_factors(pkg, oracle_mod, alg):
+    # solve!(cache; adjoint = true) (src/common.jl:1012-1027): A^T u = b with
+    # the cached factorization; A is factored once
+    rng = np.random.default_rng(26)
+    n = 150
+    A = rng.standard_normal((n, n)) + 2 * np.sqrt(n) * np.eye(n)
+    b = rng.standard_normal(n)
+    cache = pkg.init(pkg.LinearProblem(A, b), alg)
+    calls = []
+    orig = cache.cacheval.getrf
+    cache.cacheval.getrf = lambda *a, **k: calls.append(1) or orig(*a, **k)
+    sol = pkg.solve_bang(cache, adjoint=True)  # fresh A: factor, then the transposed solve
+    assert pkg.successful_retcode(sol)
+    assert oracle_mod.backward_error(A.T, sol.u, b) <= 10 * n * EPS64
+    sol2 = pkg.solve_bang(cache)  # the plain solve on the same factors
+    assert oracle_mod.backward_error(A, sol2.u, b) <= 10 * n * EPS64
+    sol3 = pkg.solve_bang(cache, adjoint=True)
+    assert oracle_mod.backward_error(A.T, sol3.u, b) <= 10 * n * EPS64
+    assert len(calls) == 1
+    if isinstance(alg, pkg.GB300LUFactorization):
+        LU, ipiv, _ = oracle_mod.getrf(A)
+        assert np.array_equal(sol3.u, oracle_mod.getrs(LU, ipiv, b, trans="T"))
+
+
+def test_default_algorithm(pkg, oracle_mod):
+    # init(prob) without an algorithm: defaultalg picks the GB300 LU
+    # (IllConditioned, the reference's default condition) or the mixed LU
+    # (WellConditioned); both reach the FP64 bound
+    rng = np.random.default_rng(27)
+    n = 200
+    A = rng.standard_normal((n, n)) + 2 * np.sqrt(n) * np.eye(n)
+    b = rng.standard_normal(n)
+    cache = pkg.init(pkg.LinearProblem(A, b))
+    assert isinstance(cache.alg, pkg.GB300LUFactorization)
+    sol = pkg.solve_bang(cache)
+    LU, ipiv, _ = oracle_mod.getrf(A)
+    assert np.array_equal(sol.u, oracle_mod.getrs(LU, ipiv, b))
+    well = pkg.OperatorAssumptions(True, pkg.OperatorCondition.WellConditioned)
+    sol = pkg.solve(pkg.LinearProblem(A, b), assumptions=well)
+    assert isinstance(sol.cache.alg, pkg.GB300MixedLUFactorization)
+    assert oracle_mod.backward_error(A, sol.u, b) <= 10 * n * EPS64
+
+
+def test_default_safety_fallback_reports_failure(pkg):
+    # a matrix whose LU "succeeds" with non-finite results: the default
+    # solver's safety check (src/default.jl:946-967) turns it into a Failure
+    n = 4
+    A = np.eye(n)
+    A[1, 1] = 1e-310  # subnormal pivot: 1/pivot overflows to inf
+    b = np.ones(n)
+    sol = pkg.solve(pkg.LinearProblem(A, b))
+    assert sol.retcode == pkg.ReturnCode.Failure
