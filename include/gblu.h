@@ -201,7 +201,7 @@ int32_t gblu_batch_create(gblu_ctx* ctx, int64_t count, const int64_t* sizes, in
                           gblu_batch** out);
 /* Replace the bucket schedule (from the autotuner): nbuckets (<= 8) buckets
  * with inclusive upper size edges (the last must be 256), threads per CTA and
- * panel width per bucket ((128|256, 8|16) or (512, 16)), CTAs per bucket
+ * panel width per bucket ((64, 8), (128|256, 8|16) or (512, 16)), CTAs per bucket
  * (NULL or <= 0 entries: fill the GPU).  Re-captures the graph. */
 int32_t gblu_batch_schedule(gblu_ctx* ctx, gblu_batch* b, int32_t nbuckets, const int32_t* upper,
                             const int32_t* threads, const int32_t* panel, const int32_t* ctas);

@@ -25,7 +25,7 @@ from . import _lib
 from ._cuda import DeviceMatrix, Event
 
 # (threads per CTA, panel width) variants compiled into libgblu
-VARIANTS = [(128, 8), (128, 16), (256, 8), (256, 16), (512, 16)]
+VARIANTS = [(64, 8), (128, 8), (128, 16), (256, 8), (256, 16), (512, 16)]
 EDGE_SETS = [[256], [64, 256], [128, 256], [64, 128, 256], [32, 96, 256], [48, 96, 160, 256]]
 PRECISIONS = {"fp64": _lib.GBLU_FP64, "fp32": _lib.GBLU_FP32}
 

@@ -52,7 +52,7 @@ struct SysSmem {
   T* L;      // panel columns: column j of the current panel at L + j*kBatchMaxN (row-indexed)
   T* U;      // U12 rows: row j at U + j*kBatchUStride (indexed by column - c1)
   T* xs;     // solve vector
-  T* cval;   // [2][NW] pivot candidate |value| per warp (double-buffered by column parity)
+  typename PivKey<T>::K* cval;  // [2][NW] pivot candidate key per warp (double-buffered by column parity)
   T* crowv;  // [2][NW][NB] candidate row's panel values
   T* diagv;  // [2][NB] current diagonal row's panel values
   int* crow;  // [2][NW] candidate row per warp
@@ -77,7 +77,7 @@ struct SysSmem {
     L = reinterpret_cast<T*>(take(NB * kBatchMaxN * sizeof(T)));
     U = reinterpret_cast<T*>(take(NB * kBatchUStride * sizeof(T)));
     xs = reinterpret_cast<T*>(take(kBatchMaxN * sizeof(T)));
-    cval = reinterpret_cast<T*>(take(2 * NW * sizeof(T)));
+    cval = reinterpret_cast<typename PivKey<T>::K*>(take(2 * NW * sizeof(T)));
     crowv = reinterpret_cast<T*>(take(2 * NW * NB * sizeof(T)));
     diagv = reinterpret_cast<T*>(take(2 * NB * sizeof(T)));
     crow = reinterpret_cast<int*>(take(2 * NW * 4));
@@ -95,11 +95,11 @@ struct SysSmem {
   }
 };
 
-// Pivot-candidate order: larger |value| first, then the smaller row; row -1 is
-// no candidate.  A total order, so every reduction tree gives the first row of
-// maximal |value| (NaN never becomes a candidate: `v > best` is false for it).
-template <typename T>
-__device__ __forceinline__ bool cand_better(T v, int g, T bv, int bg) {
+// Candidate order: larger key first, then the smaller row; row -1 is no
+// candidate.  A total order, so every reduction tree gives the first row of
+// maximal |value|.
+template <typename K>
+__device__ __forceinline__ bool cand_better(K v, int g, K bv, int bg) {
   if (g < 0) return false;
   if (bg < 0) return true;
   return v > bv || (v == bv && g < bg);
@@ -125,7 +125,9 @@ __device__ int64_t factor_system(T* __restrict__ A, int n, int32_t* __restrict__
                                  const SysSmem<T, NT, NB>& sm) {
   constexpr int NW = NT / 32;
   constexpr int RPT = (kBatchMaxN + NT - 1) / NT;  // panel rows per thread
+  using K = typename PivKey<T>::K;
   static_assert(NB <= 16, "composition warp holds 2*NB rows");
+  static_assert(sizeof(K) == sizeof(T), "key and value slots share a size");
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   int64_t info = 0;
   for (int i = tid; i < kBatchMaxN; i += NT) sm.perm[i] = i;
@@ -146,18 +148,18 @@ __device__ int64_t factor_system(T* __restrict__ A, int n, int32_t* __restrict__
       if (j >= kb) continue;  // uniform; keeps the loop fully unrolled (pr indexed statically)
       const int col = k0 + j;
       const int buf = j & 1;
-      T bv = T(0);
+      K bv = 0;
       int bg = -1;
 #pragma unroll
       for (int m = 0; m < RPT; ++m) {
         const int i = tid + NT * m;
         if (i >= col && i < n) {
-          const T v = fabs(pr[m][j]);
+          const K v = PivKey<T>::of(pr[m][j]);
           if (v > bv) { bv = v; bg = i; }
         }
       }
       for (int off = 16; off; off >>= 1) {
-        const T ov = __shfl_xor_sync(0xffffffffu, bv, off);
+        const K ov = __shfl_xor_sync(0xffffffffu, bv, off);
         const int og = __shfl_xor_sync(0xffffffffu, bg, off);
         if (cand_better(ov, og, bv, bg)) { bv = ov; bg = og; }
       }
@@ -176,11 +178,11 @@ __device__ int64_t factor_system(T* __restrict__ A, int n, int32_t* __restrict__
           for (int jj = 0; jj < NB; ++jj)
             if (jj < kb) sm.diagv[buf * NB + jj] = pr[m][jj];
       __syncthreads();
-      T wv = lane < NW ? sm.cval[buf * NW + lane] : T(0);
+      K wv = lane < NW ? sm.cval[buf * NW + lane] : K(0);
       int wg = lane < NW ? sm.crow[buf * NW + lane] : -1;
       int ww = lane;
       for (int off = 16; off; off >>= 1) {
-        const T ov = __shfl_xor_sync(0xffffffffu, wv, off);
+        const K ov = __shfl_xor_sync(0xffffffffu, wv, off);
         const int og = __shfl_xor_sync(0xffffffffu, wg, off);
         const int ow = __shfl_xor_sync(0xffffffffu, ww, off);
         if (cand_better(ov, og, wv, wg)) { wv = ov; wg = og; ww = ow; }
@@ -188,10 +190,11 @@ __device__ int64_t factor_system(T* __restrict__ A, int n, int32_t* __restrict__
       const int p = wg < 0 ? col : wg;  // kp = k when the column is zero below the diagonal
       const T* src = (p == col) ? sm.diagv + buf * NB : sm.crowv + (buf * NW + ww) * NB;
       const T piv = src[j];
+      const bool nz = PivKey<T>::nonzero(piv);  // integer test, off the FP64 pipe
       if (tid == 0) { sm.pidx[j] = p; ipiv[col] = p + 1; }
-      if (piv == T(0) && info == 0) info = col + 1;
-      const bool swap = piv != T(0) && p != col;
-      const T inv = piv != T(0) ? T(1) / piv : T(0);
+      if (!nz && info == 0) info = col + 1;
+      const bool swap = nz && p != col;
+      const T inv = nz ? T(1) / piv : T(0);
 #pragma unroll
       for (int m = 0; m < RPT; ++m) {
         const int i = tid + NT * m;
@@ -206,7 +209,7 @@ __device__ int64_t factor_system(T* __restrict__ A, int n, int32_t* __restrict__
         }
         if (i > col && i < n) {
           T l = pr[m][j];
-          if (piv != T(0)) l *= inv;
+          if (nz) l *= inv;
           pr[m][j] = l;
 #pragma unroll
           for (int jj = j + 1; jj < NB; ++jj)
@@ -438,7 +441,7 @@ __host__ __device__ constexpr size_t batch_smem(bool mixed) {
 // the systems the mixed kernel flagged are processed, each first copied from
 // Asrc (the untouched FP64 input) into Awork.
 template <int NT, int NB>
-__global__ void __launch_bounds__(NT, NT <= 128 ? 3 : (NT <= 256 ? 2 : 1))
+__global__ void __launch_bounds__(NT, NT <= 64 ? 8 : NT <= 128 ? (NB <= 8 ? 4 : 3) : (NT <= 256 ? 2 : 1))
 batch_fp64_kernel(BatchDev d, double* __restrict__ Awork, const double* __restrict__ Asrc,
                   double* __restrict__ X, int32_t* __restrict__ ipiv_all, int only_flagged) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -480,7 +483,7 @@ batch_fp64_kernel(BatchDev d, double* __restrict__ Awork, const double* __restri
 // converge (or whose FP32 factorization hit a zero pivot) are flagged for the
 // FP64 kernel that runs after this one in the same graph.
 template <int NT, int NB>
-__global__ void __launch_bounds__(NT, NT <= 128 ? 3 : (NT <= 256 ? 2 : 1))
+__global__ void __launch_bounds__(NT, NT <= 64 ? 8 : NT <= 128 ? (NB <= 8 ? 4 : 3) : (NT <= 256 ? 2 : 1))
 batch_mixed_kernel(BatchDev d, const double* __restrict__ A64, float* __restrict__ A32,
                    double* __restrict__ X, const double* __restrict__ Bcopy,
                    int32_t* __restrict__ ipiv_all, int maxit, double tol_per_n) {
@@ -665,6 +668,7 @@ cudaError_t launch_bucket(gblu_batch* b, const BatchBucket& k, bool mixed, int o
   if (k.nt == NT_ && k.nb == NB_)                                                   \
     return mixed ? launch_mixed<NT_, NB_>(d, ctas, b, s)                           \
                  : launch_fp64<NT_, NB_>(d, ctas, b, Awork, only_flagged, s);
+  GBLU_BATCH_CASE(64, 8)
   GBLU_BATCH_CASE(128, 8)
   GBLU_BATCH_CASE(128, 16)
   GBLU_BATCH_CASE(256, 8)
@@ -677,6 +681,7 @@ cudaError_t launch_bucket(gblu_batch* b, const BatchBucket& k, bool mixed, int o
 }  // namespace
 
 void batch_configure(int /*device*/) {
+  configure_batch_kernels<64, 8>();
   configure_batch_kernels<128, 8>();
   configure_batch_kernels<128, 16>();
   configure_batch_kernels<256, 8>();
@@ -685,8 +690,8 @@ void batch_configure(int /*device*/) {
 }
 
 bool batch_config_supported(int nt, int nb) {
-  return (nt == 128 && (nb == 8 || nb == 16)) || (nt == 256 && (nb == 8 || nb == 16)) ||
-         (nt == 512 && nb == 16);
+  return (nt == 64 && nb == 8) || (nt == 128 && (nb == 8 || nb == 16)) ||
+         (nt == 256 && (nb == 8 || nb == 16)) || (nt == 512 && nb == 16);
 }
 
 }  // namespace gblu
@@ -717,7 +722,7 @@ void default_buckets(gblu_batch* b, std::vector<BatchBucket>& out, const int32_t
     k.hi = e < nedges ? edges[e] : kBatchMaxN;
     k.nt = nts ? nts[e] : 256;
     k.nb = nbs ? nbs[e] : 16;
-    k.ctas = di.num_sms * (k.nt <= 128 ? 4 : (k.nt <= 256 ? 2 : 1));
+    k.ctas = di.num_sms * (k.nt <= 64 ? 8 : k.nt <= 128 ? 4 : (k.nt <= 256 ? 2 : 1));
     out.push_back(k);
     lo = k.hi + 1;
   }
@@ -858,10 +863,19 @@ int32_t gblu_batch_create(gblu_ctx* ctx, int64_t count, const int64_t* sizes, in
     delete b;
     return cuda_fail(ctx, e, "gblu_batch_create");
   }
-  const int32_t edges[2] = {64, 128};
-  const int32_t nts[3] = {128, 256, 256};
-  const int32_t nbs[3] = {8, 16, 16};
-  default_buckets(b, b->buckets, edges, 2, nts, nbs, ctx->device);
+  // default schedules: the autotuner's choice for 20,000 systems with n
+  // uniform in [8, 256] (128-thread CTAs with 8-column panels throughout)
+  if (precision == GBLU_FP64) {
+    const int32_t edges[2] = {32, 96};
+    const int32_t nts[3] = {128, 128, 128};
+    const int32_t nbs[3] = {8, 8, 8};
+    default_buckets(b, b->buckets, edges, 2, nts, nbs, ctx->device);
+  } else {
+    const int32_t edges[3] = {48, 96, 160};
+    const int32_t nts[4] = {128, 128, 128, 128};
+    const int32_t nbs[4] = {8, 8, 8, 8};
+    default_buckets(b, b->buckets, edges, 3, nts, nbs, ctx->device);
+  }
   st = count > 0 ? build_graph(ctx, b) : GBLU_OK;
   if (st) {
     ctx_free(ctx, b->arena, bytes);
@@ -897,7 +911,7 @@ int32_t gblu_batch_schedule(gblu_ctx* ctx, gblu_batch* b, int32_t nbuckets, cons
     k.hi = upper[i];
     k.nt = threads[i];
     k.nb = panel[i];
-    k.ctas = (ctas && ctas[i] > 0) ? ctas[i] : di.num_sms * (k.nt <= 128 ? 4 : (k.nt <= 256 ? 2 : 1));
+    k.ctas = (ctas && ctas[i] > 0) ? ctas[i] : di.num_sms * (k.nt <= 64 ? 8 : k.nt <= 128 ? 4 : (k.nt <= 256 ? 2 : 1));
     b->buckets.push_back(k);
     lo = upper[i] + 1;
   }

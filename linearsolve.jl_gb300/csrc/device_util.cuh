@@ -96,6 +96,34 @@ __device__ __forceinline__ T div_markstein(T a, T b, T y) {
   return fma(r, y, q);
 }
 
+// Pivot candidates are compared by integer keys: the bit pattern of |a|, which
+// orders non-negative floating-point values like the values themselves, with
+// NaN mapped to 0 so it never becomes a candidate (the reference's `v > amax`
+// is false for NaN).  This keeps the reductions off the FP64 pipe.
+template <typename T>
+struct PivKey;
+template <>
+struct PivKey<double> {
+  using K = unsigned long long;
+  static __device__ __forceinline__ K of(double x) {
+    const K a = (K)__double_as_longlong(x) & 0x7fffffffffffffffull;
+    return a > 0x7ff0000000000000ull ? 0ull : a;
+  }
+  // x != 0 (NaN counts as nonzero, as in `x != 0.0`)
+  static __device__ __forceinline__ bool nonzero(double x) {
+    return ((K)__double_as_longlong(x) << 1) != 0ull;
+  }
+};
+template <>
+struct PivKey<float> {
+  using K = unsigned;
+  static __device__ __forceinline__ K of(float x) {
+    const K a = __float_as_uint(x) & 0x7fffffffu;
+    return a > 0x7f800000u ? 0u : a;
+  }
+  static __device__ __forceinline__ bool nonzero(float x) { return (__float_as_uint(x) << 1) != 0u; }
+};
+
 template <typename T>
 __device__ __forceinline__ T ldcg(const T* p) { return __ldcg(p); }
 template <typename T>

@@ -74,6 +74,7 @@ struct GetrfPlan {
   int panel_ctas = 0;        // CTAs of the cooperative panel kernel (0: auto)
   int trsm_base = 64;        // base size of the recursive TRSM
   bool use_cluster_panel = true;  // DSMEM cluster panel when the panel fits
+  bool use_reg_panel = true;      // register-resident cluster panel when the panel fits
   // FP32 working matrix only: trailing updates on tcgen05 with 16-bit operands
   int tc_mode = 0;           // 0 SIMT FP32, 1 BF16 operands, 2 FP16 operands (scaled)
   void* tc_work = nullptr;   // conversion buffers for the operands

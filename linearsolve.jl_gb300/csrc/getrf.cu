@@ -339,6 +339,209 @@ panel_cluster_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int 
 }
 
 // ---------------------------------------------------------------------------
+// Register panel kernel: the same getf2 on rows [c0, m) x columns [c0, c0+w)
+// with every panel row held in registers by one thread for the whole leaf
+// (row base + tid + NT * r of CTA `cta`, r < RPT, the CTA holding R rows).
+// The registers rotate by one slot per column, identically in every thread,
+// so the current column is always slot 0 and the column loop is a plain loop
+// with one small body; rows are exchanged in slot order (16-byte shared
+// memory accesses, no index arithmetic).  Per column: each warp reduces its
+// candidate (integer keys of |a|) and the owners publish the candidate row
+// and the diagonal row; one cluster barrier; warp 0 of every CTA reduces all
+// warp candidates of the cluster and fetches the pivot row through
+// distributed shared memory; one CTA barrier; every thread interchanges,
+// scales and updates its own rows.  The per-element arithmetic is
+// panel_kernel's.
+constexpr int kRegPanelThreads = 512;
+
+template <typename T>
+struct Vec16;  // 16-byte vector of T
+template <>
+struct Vec16<float> {
+  using V = float4;
+  static constexpr int N = 4;
+  static __device__ __forceinline__ float get(const V& v, int e) { return e == 0 ? v.x : e == 1 ? v.y : e == 2 ? v.z : v.w; }
+  static __device__ __forceinline__ V make(const float* x) { return make_float4(x[0], x[1], x[2], x[3]); }
+};
+template <>
+struct Vec16<double> {
+  using V = double2;
+  static constexpr int N = 2;
+  static __device__ __forceinline__ double get(const V& v, int e) { return e == 0 ? v.x : v.y; }
+  static __device__ __forceinline__ V make(const double* x) { return make_double2(x[0], x[1]); }
+};
+
+template <typename T, int W>
+__device__ __forceinline__ void row_store(T* dst, const T (&src)[W]) {
+  using VT = Vec16<T>;
+#pragma unroll
+  for (int q = 0; q < W / VT::N; ++q) reinterpret_cast<typename VT::V*>(dst)[q] = VT::make(&src[q * VT::N]);
+}
+
+template <typename T, int W>
+__device__ __forceinline__ void row_load(T (&dst)[W], const T* src) {
+  using VT = Vec16<T>;
+#pragma unroll
+  for (int q = 0; q < W / VT::N; ++q) {
+    const typename VT::V v = reinterpret_cast<const typename VT::V*>(src)[q];
+#pragma unroll
+    for (int e = 0; e < VT::N; ++e) dst[q * VT::N + e] = VT::get(v, e);
+  }
+}
+
+template <typename T, int RPT>
+__global__ void __launch_bounds__(kRegPanelThreads, 1)
+panel_reg_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w,
+                 int64_t* __restrict__ ipiv, int64_t* __restrict__ info_out, int R) {
+  namespace cg = cooperative_groups;
+  using K = typename PivKey<T>::K;
+  using VT = Vec16<T>;
+  cg::cluster_group cluster = cg::this_cluster();
+  constexpr int NT = kRegPanelThreads, NW = NT / 32, W = kPanelMaxW;
+  __shared__ __align__(16) T s_crowv[2][NW][W];  // each warp's candidate row, slot order
+  __shared__ __align__(16) T s_diagv[2][W];      // the diagonal row (owner CTA), slot order
+  __shared__ __align__(16) T s_piv[W];           // the pivot row, slot order
+  __shared__ __align__(16) T s_old[W];           // the old diagonal row, for the pivot row's owner
+  __shared__ K s_cval[2][NW];
+  __shared__ int s_crow[2][NW];
+  __shared__ int s_p;
+
+  const int G = (int)cluster.num_blocks();
+  const int cta = (int)cluster.block_rank();
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t base = c0 + (int64_t)cta * R;
+  const int nloc = (int)max((int64_t)0, min((int64_t)R, m - base));
+  const int nwr = min(NW, (R + 31) >> 5);  // warps of a CTA that own rows
+  const int ncand = G * nwr;
+
+  T pr[RPT][W];  // slot j: column (k + j) mod 32 at step k
+#pragma unroll
+  for (int r = 0; r < RPT; ++r) {
+    const int i = tid + NT * r;
+#pragma unroll
+    for (int j = 0; j < W; ++j) pr[r][j] = (i < nloc && j < w) ? A[(base + i) + (c0 + j) * lda] : T(0);
+  }
+  int64_t info_local = 0;
+
+  for (int k = 0; k < w; ++k) {
+    const int64_t d = c0 + k;
+    const int buf = k & 1;
+    // 1. this warp's candidate: first row of max |a| among rows >= d (NaN ignored)
+    K bv = 0;
+    int bg = -1;
+#pragma unroll
+    for (int r = 0; r < RPT; ++r) {
+      const int i = tid + NT * r;
+      const K v = PivKey<T>::of(pr[r][0]);
+      if (i < nloc && base + i >= d && v > bv) { bv = v; bg = (int)(base + i); }
+    }
+    for (int off = 16; off; off >>= 1) {
+      const K ov = __shfl_xor_sync(0xffffffffu, bv, off);
+      const int og = __shfl_xor_sync(0xffffffffu, bg, off);
+      if (cand_better(ov, (int64_t)og, bv, (int64_t)bg)) { bv = ov; bg = og; }
+    }
+    if (lane == 0) { s_cval[buf][warp] = bv; s_crow[buf][warp] = bg; }
+#pragma unroll
+    for (int r = 0; r < RPT; ++r) {
+      const int64_t g = base + tid + NT * r;
+      if (g == bg) row_store<T, W>(s_crowv[buf][warp], pr[r]);
+      if (g == d && tid + NT * r < nloc) row_store<T, W>(s_diagv[buf], pr[r]);
+    }
+    cluster.sync();  // publishes every CTA's slots of column k (release/acquire)
+    // 2. warp 0: the winner over every warp of the cluster, the pivot row and,
+    //    for the pivot row's CTA, the old diagonal row
+    if (warp == 0) {
+      K v = 0;
+      int g = -1, e = -1;
+      for (int c = lane; c < ncand; c += 32) {
+        const int rc = c / nwr, rw = c - rc * nwr;
+        const K cv = *cluster.map_shared_rank(&s_cval[buf][rw], rc);
+        const int cg_ = *cluster.map_shared_rank(&s_crow[buf][rw], rc);
+        if (cand_better(cv, (int64_t)cg_, v, (int64_t)g)) { v = cv; g = cg_; e = c; }
+      }
+      for (int off = 16; off; off >>= 1) {
+        const K ov = __shfl_xor_sync(0xffffffffu, v, off);
+        const int og = __shfl_xor_sync(0xffffffffu, g, off);
+        const int oe = __shfl_xor_sync(0xffffffffu, e, off);
+        if (cand_better(ov, (int64_t)og, v, (int64_t)g)) { v = ov; g = og; e = oe; }
+      }
+      const int64_t p = g < 0 ? d : (int64_t)g;  // kp = k when amax == 0
+      const int downer = (int)((d - c0) / R);
+      const T dv = *cluster.map_shared_rank(&s_diagv[buf][lane], downer);
+      if (p == d) {
+        s_piv[lane] = dv;
+      } else {
+        const int rc = e / nwr, rw = e - rc * nwr;
+        s_piv[lane] = *cluster.map_shared_rank(&s_crowv[buf][rw][lane], rc);
+        if (p >= base && p < base + nloc) s_old[lane] = dv;
+      }
+      if (lane == 0) s_p = (int)p;
+    }
+    __syncthreads();
+    const int64_t p = s_p;
+    const T piv = s_piv[0];
+    const bool nz = PivKey<T>::nonzero(piv);
+    if (cta == 0 && tid == 0) {
+      ipiv[d] = p + 1;
+      if (!nz && info_local == 0) info_local = d + 1;
+    }
+    // 3. interchange (nonzero pivot only), scale, rank-1 update, rotate
+    const bool swap = nz && p != d;
+    const T inv = nz ? T(1) / piv : T(0);
+    const int lim = w - k;  // slots 1..lim-1 hold columns k+1..w-1
+    T l[RPT];
+    bool upd[RPT];
+#pragma unroll
+    for (int r = 0; r < RPT; ++r) {
+      const int i = tid + NT * r;
+      const int64_t gi = base + i;
+      upd[r] = i < nloc && gi > d;
+      if (i < nloc && swap) {
+        if (gi == d) row_load<T, W>(pr[r], s_piv);
+        else if (gi == p) row_load<T, W>(pr[r], s_old);
+      }
+      l[r] = pr[r][0];
+      if (upd[r] && nz) l[r] *= inv;
+      if (upd[r]) pr[r][0] = l[r];
+    }
+#pragma unroll
+    for (int q = 0; q < W / VT::N; ++q) {
+      const typename VT::V pv = reinterpret_cast<const typename VT::V*>(s_piv)[q];
+#pragma unroll
+      for (int e = 0; e < VT::N; ++e) {
+        const int j = q * VT::N + e;
+        if (j >= 1 && j < lim) {
+          const T u = VT::get(pv, e);
+#pragma unroll
+          for (int r = 0; r < RPT; ++r)
+            if (upd[r]) pr[r][j] = fma(-l[r], u, pr[r][j]);
+        }
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < RPT; ++r) {
+      const T t0 = pr[r][0];
+#pragma unroll
+      for (int j = 0; j < W - 1; ++j) pr[r][j] = pr[r][j + 1];
+      pr[r][W - 1] = t0;
+    }
+  }
+  // after w steps slot j holds column (w + j) mod 32
+#pragma unroll
+  for (int r = 0; r < RPT; ++r) {
+    const int i = tid + NT * r;
+    if (i < nloc)
+#pragma unroll
+      for (int j = 0; j < W; ++j) {
+        const int c = (w + j) & (W - 1);
+        if (c < w) A[(base + i) + (c0 + c) * lda] = pr[r][j];
+      }
+  }
+  if (cta == 0 && tid == 0 && info_local != 0 && *info_out == 0) *info_out = info_local;
+  cluster.sync();  // no CTA exits while another may still read its shared memory
+}
+
+// ---------------------------------------------------------------------------
 // laswp for one leaf: interchanges ipiv[c0, c0+w) applied to every column
 // outside [c0, c0+w) (blocked_lufact.jl:126-141 applies them to [1, j0) and
 // (j1, n]).  Warp 0 of every CTA composes the w swaps into at most 2w moves
@@ -629,9 +832,80 @@ struct Driver {
     return c == 1;
   }
 
+  template <int RPT>
+  bool panel_reg_launch(int64_t c0, int w, int cs) {
+    const int64_t M = p.m - c0;
+    const int64_t R = (M + cs - 1) / cs;
+    if (R > (int64_t)kRegPanelThreads * RPT || !reg_cluster_ok<RPT>(cs)) return false;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(cs);
+    cfg.blockDim = dim3(kRegPanelThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = cs;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    double fl = 0;
+    for (int k = 0; k < w; ++k) fl += (double)(M - k - 1) * (1.0 + 2.0 * (w - k - 1));
+    LaunchScope ls(K_PANEL, fl, 2.0 * M * w * sizeof(T), s);
+    check(cudaLaunchKernelEx(&cfg, panel_reg_kernel<T, RPT>, p.A, p.lda, p.m, c0, w, p.ipiv, p.info, (int)R));
+    return true;
+  }
+
+  // Register panel: the rows spread evenly over up to 16 CTAs of one cluster
+  // (at least 128 rows each), one or two rows per thread; false when the
+  // panel is taller or not launchable.
+  bool panel_reg(int64_t c0, int w) {
+    const int64_t M = p.m - c0;
+    // FP64: 16 SMs' FP64 pipes bound the updates of a tall leaf; above 4096
+    // rows the grid kernel, spread over the whole GPU, is faster
+    if (sizeof(T) == 8 && M > 4096) return false;
+    const int cs = (int)std::min<int64_t>(16, std::max<int64_t>(1, (M + 127) / 128));
+    const int64_t R = (M + cs - 1) / cs;
+    if (R <= kRegPanelThreads) return panel_reg_launch<1>(c0, w, cs);
+    if constexpr (sizeof(T) == 4) {
+      if (R <= 2 * kRegPanelThreads) return panel_reg_launch<2>(c0, w, cs);
+    }
+    return false;
+  }
+
+  template <int RPT>
+  static bool reg_cluster_ok(int cs) {
+    static std::mutex mu;
+    static int cache[17] = {};  // 0 unknown, 1 ok, -1 no (per process and instantiation)
+    std::lock_guard<std::mutex> g(mu);
+    int& c = cache[cs];
+    if (c == 0) {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(cs);
+      cfg.blockDim = dim3(kRegPanelThreads);
+      cfg.dynamicSmemBytes = 0;
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeClusterDimension;
+      attr[0].val.clusterDim.x = cs;
+      attr[0].val.clusterDim.y = 1;
+      attr[0].val.clusterDim.z = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      int nclusters = 0;
+      cudaError_t e = cudaOccupancyMaxActiveClusters(&nclusters, panel_reg_kernel<T, RPT>, &cfg);
+      c = (e == cudaSuccess && nclusters >= 1) ? 1 : -1;
+      cudaGetLastError();
+    }
+    return c == 1;
+  }
+
   void panel(int64_t c0, int w) {
     const int64_t M = p.m - c0;
     const DeviceInfo& di = device_info(device);
+    if (p.use_reg_panel && panel_reg(c0, w)) {
+      laswp(c0, w);
+      return;
+    }
     if (p.use_cluster_panel && panel_cluster(c0, w)) {
       laswp(c0, w);
       return;
@@ -768,6 +1042,9 @@ void getrf_configure(int device) {
   cudaFuncSetAttribute(panel_cluster_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
   cudaFuncSetAttribute(panel_cluster_kernel<double>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
   cudaFuncSetAttribute(panel_cluster_kernel<float>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  cudaFuncSetAttribute(panel_reg_kernel<double, 1>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  cudaFuncSetAttribute(panel_reg_kernel<float, 1>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  cudaFuncSetAttribute(panel_reg_kernel<float, 2>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
   cudaFuncSetAttribute(perm_from_ipiv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        kPermSmemMax * (int)sizeof(int32_t));
   getrs_configure(device);

@@ -50,7 +50,8 @@ def test_fp64_batch_bit_exact(ctx, oracle_mod, pkg):
 
 
 @pytest.mark.parametrize("sched", [([256], [256], [16]), ([32, 96, 256], [128, 256, 512], [8, 16, 16]),
-                                   ([64, 128, 256], [128, 128, 256], [16, 8, 8])])
+                                   ([64, 128, 256], [128, 128, 256], [16, 8, 8]),
+                                   ([48, 256], [64, 64], [8, 8])])
 def test_fp64_batch_schedules(ctx, oracle_mod, pkg, sched):
     sizes, A, b, _ = pkg.workloads.batch(200, seed=2)
     bt = Batch(ctx, sizes, 0)
