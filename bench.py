@@ -16,7 +16,9 @@ solve!(cache) / cache.b = b.  Inputs are seeded synthetic arrays.
 dgetrf/dgetrs on OpenBLAS, the routines LinearSolve.jl's LUFactorization calls)
 on the host cores.
 
---suite adds sub-objects to the line (comma list, or "all"):
+--suite adds sub-objects to the line (comma list, or "all"; by default
+mixed,batched,serving on one GPU, about a minute and a half, and none on
+several; --suite '' for none):
   mixed       n = 16384, A = G + 4 sqrt(n) I, 4 RHS: FP32/BF16/FP16 LU + FP64
               refinement vs the plain FP64 LU, both to the FP64 bound
   mixed_hard  n = 16384, A = Q1 diag(s) Q2^T, s log-spaced 1..1e6, 4 RHS: FP32
@@ -236,6 +238,8 @@ def run_gpu(args, rank, world, local):
     ctx = pkg.Context(local)
     stream = ctx.stream
     if args.only_suite:  # profiling aid: the suite parts alone, one JSON object
+        if args.suite == "auto":
+            args.suite = "mixed,batched,serving"
         out = run_suites(pkg, cu, ctx, args)
         if rank == 0:
             print(json.dumps(out))
@@ -361,6 +365,8 @@ def run_gpu(args, rank, world, local):
         "kernel_ms": {k: round(prof[k]["ms"] / args.steps, 3) for k in kinds if prof[k]["count"]},
     }
 
+    if args.suite == "auto":
+        args.suite = "mixed,batched,serving" if world == 1 else ""
     if args.suite and rank == 0:
         line.update(run_suites(pkg, cu, ctx, args))
 
@@ -422,12 +428,24 @@ SUITES = ("mixed", "mixed_hard", "batched", "serving")
 
 
 def run_suites(pkg, cu, ctx, args) -> dict:
-    parts = set(args.suite.split(","))
+    """The comparison suites, each in its own sub-object; a suite that fails
+    records its error instead of losing the line."""
+    parts = set(p for p in args.suite.split(",") if p)
     if "all" in parts:
         parts = set(SUITES)
     runners = {"mixed": run_mixed_suite, "mixed_hard": run_mixed_hard_suite,
                "batched": run_batched_suite, "serving": run_serving_suite}
-    return {name: runners[name](pkg, cu, ctx, args) for name in SUITES if name in parts}
+    out = {}
+    for name in SUITES:
+        if name not in parts:
+            continue
+        t0 = time.perf_counter()
+        try:
+            out[name] = runners[name](pkg, cu, ctx, args)
+        except Exception as e:  # noqa: BLE001 - reported in the line
+            out[name] = {"error": f"{type(e).__name__}: {e}"}
+        out[name]["suite_wall_s"] = round(time.perf_counter() - t0, 1)
+    return out
 
 
 def run_mixed_suite(pkg, cu, ctx, args):
@@ -640,7 +658,9 @@ def main():
     ap.add_argument("--nrhs", type=int, default=16)
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--suite", default="", help="comma list: mixed,mixed_hard,batched,serving (or all)")
+    ap.add_argument("--suite", default="auto",
+                    help="comma list of mixed,mixed_hard,batched,serving (or all); '' for none; "
+                         "auto = mixed,batched,serving on one GPU, none on several")
     ap.add_argument("--batch-count", type=int, default=20000)
     ap.add_argument("--only-suite", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=300)

@@ -96,6 +96,33 @@ __device__ __forceinline__ T div_markstein(T a, T b, T y) {
   return fma(r, y, q);
 }
 
+// a[i] / b for N > 1 dividends with one divisor, as N independent chains
+// without branches in the common case (so the compiler can interleave them;
+// with one dividend the plain div_markstein is faster).  A zero
+// dividend gives q = a*y, which is the correctly signed zero a/b; any other
+// operand outside the safe range sends all N through the IEEE division.
+template <typename T, int N>
+__device__ __forceinline__ void div_markstein_n(T (&a)[N], T b, T y) {
+  const T ay = fabs(y);
+  bool bad = !(ay > DivRange<T>::lo && ay < DivRange<T>::hi);
+  T res[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    const T q = a[i] * y;
+    const T aq = fabs(q);
+    const bool zero = a[i] == T(0);
+    bad |= !zero && !(aq > DivRange<T>::lo && aq < DivRange<T>::hi);
+    const T r = fma(-b, q, a[i]);
+    res[i] = zero ? q : fma(r, y, q);
+  }
+  if (bad) {
+#pragma unroll
+    for (int i = 0; i < N; ++i) res[i] = a[i] / b;
+  }
+#pragma unroll
+  for (int i = 0; i < N; ++i) a[i] = res[i];
+}
+
 // Pivot candidates are compared by integer keys: the bit pattern of |a|, which
 // orders non-negative floating-point values like the values themselves, with
 // NaN mapped to 0 so it never becomes a candidate (the reference's `v > amax`

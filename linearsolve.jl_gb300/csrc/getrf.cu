@@ -550,7 +550,7 @@ template <typename T>
 __global__ void __launch_bounds__(256)
 laswp_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t ncols_total,
                   int64_t c0, int w, const int64_t* __restrict__ ipiv,
-                  DevScratch* __restrict__ scr) {
+                  DevScratch* __restrict__ scr, int32_t* __restrict__ perm) {
   __shared__ int64_t mv_dst[2 * kPanelMaxW];
   __shared__ int64_t mv_src[2 * kPanelMaxW];
   __shared__ int s_nmv;
@@ -593,6 +593,15 @@ laswp_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t ncols_total
   __syncthreads();
   const int nmv = s_nmv;
   if (nmv == 0) return;
+  if (perm != nullptr && blockIdx.x == 0 && warp == 0) {
+    // the row permutation (original row of each row) moves like one more column
+    int32_t p0 = 0, p1 = 0;
+    if (lane < nmv) p0 = perm[mv_src[lane]];
+    if (lane + 32 < nmv) p1 = perm[mv_src[lane + 32]];
+    __syncwarp();
+    if (lane < nmv) perm[mv_dst[lane]] = p0;
+    if (lane + 32 < nmv) perm[mv_dst[lane + 32]] = p1;
+  }
   const int64_t nother = ncols_total - w;
   const int warps = blockDim.x >> 5;
   for (int64_t q = (int64_t)blockIdx.x * warps + warp; q < nother; q += (int64_t)gridDim.x * warps) {
@@ -703,26 +712,46 @@ gemm_sub_kernel(int64_t M, int64_t N, int64_t K, const T* __restrict__ A, int64_
 // perm from ipiv: (P A)[i] = A[perm[i]].  One CTA; the interchanges are
 // inherently sequential, the rest is parallel.
 constexpr int kPermSmemMax = 48 * 1024;  // rows held in shared memory
+constexpr int kPermChunk = 4096;         // pivots staged in shared memory at a time
 
 __global__ void __launch_bounds__(1024)
 perm_from_ipiv_kernel(const int64_t* __restrict__ ipiv, int64_t kmax, int64_t m,
                       int32_t* __restrict__ perm, DevScratch* __restrict__ scr) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  int32_t* sp = reinterpret_cast<int32_t*>(smem_raw);
   const bool in_smem = m <= kPermSmemMax;
+  int32_t* st = reinterpret_cast<int32_t*>(smem_raw);  // kPermChunk pivot targets
+  int32_t* sp = st + kPermChunk;
   int32_t* p = in_smem ? sp : perm;
+  __shared__ int s_bad;
   for (int64_t i = threadIdx.x; i < m; i += blockDim.x) p[i] = (int32_t)i;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    for (int64_t k = 0; k < kmax; ++k) {
-      int64_t t = ipiv[k] - 1;
-      if (t < k || t >= m) { atomicCAS(&scr->error, 0, (int)DEV_BAD_PIVOT_INDEX); break; }
-      int32_t x = p[k]; p[k] = p[t]; p[t] = x;
+  if (threadIdx.x == 0) s_bad = 0;
+  for (int64_t k0 = 0; k0 < kmax; k0 += kPermChunk) {
+    const int kc = (int)min((int64_t)kPermChunk, kmax - k0);
+    __syncthreads();
+    for (int i = threadIdx.x; i < kc; i += blockDim.x) {
+      const int64_t t = ipiv[k0 + i] - 1;
+      st[i] = (t < k0 + i || t >= m) ? -1 : (int32_t)t;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && s_bad == 0) {
+      for (int k = 0; k < kc; ++k) {  // the swaps in order, in shared memory only
+        const int t = st[k];
+        if (t < 0) { s_bad = 1; atomicCAS(&scr->error, 0, (int)DEV_BAD_PIVOT_INDEX); break; }
+        const int64_t r = k0 + k;
+        const int32_t x = p[r];
+        p[r] = p[t];
+        p[t] = x;
+      }
     }
   }
   __syncthreads();
   if (in_smem)
     for (int64_t i = threadIdx.x; i < m; i += blockDim.x) perm[i] = sp[i];
+}
+
+__global__ void iota_kernel(int32_t* __restrict__ perm, int64_t m) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x)
+    perm[i] = (int32_t)i;
 }
 
 // ---------------------------------------------------------------------------
@@ -951,16 +980,15 @@ struct Driver {
   }
 
   // interchanges of the leaf on every other column
+  // The leaf's interchanges on every other column, and on the row permutation
+  // (so getrs can gather through it without replaying ipiv).
   void laswp(int64_t c0, int w) {
     const DeviceInfo& di = device_info(device);
     const int64_t nother = p.n - w;
-    if (nother > 0) {
-      int64_t warps_needed = nother;
-      int blocks = (int)std::min<int64_t>((warps_needed + 7) / 8, (int64_t)di.num_sms * 16);
-      LaunchScope ls(K_LASWP, 0.0, 4.0 * w * nother * sizeof(T), s);
-      laswp_leaf_kernel<T><<<blocks, 256, 0, s>>>(p.A, p.lda, p.m, p.n, c0, w, p.ipiv, p.scratch);
-      check(cudaGetLastError());
-    }
+    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((nother + 7) / 8, (int64_t)di.num_sms * 16));
+    LaunchScope ls(K_LASWP, 0.0, 4.0 * w * std::max<int64_t>(nother, 0) * sizeof(T), s);
+    laswp_leaf_kernel<T><<<blocks, 256, 0, s>>>(p.A, p.lda, p.m, p.n, c0, w, p.ipiv, p.scratch, p.perm);
+    check(cudaGetLastError());
   }
 
   void gemm(int64_t M, int64_t N, int64_t K, const T* A, int64_t lda, const T* B, int64_t ldb,
@@ -1027,7 +1055,7 @@ cudaError_t simt_gemm_sub_f32(int64_t M, int64_t N, int64_t K, const float* A, i
 
 cudaError_t perm_build_launch(const int64_t* ipiv, int64_t kmax, int64_t m, int32_t* perm,
                               DevScratch* scr, cudaStream_t s) {
-  size_t smem = m <= kPermSmemMax ? (size_t)m * sizeof(int32_t) : 0;
+  size_t smem = (size_t)kPermChunk * sizeof(int32_t) + (m <= kPermSmemMax ? (size_t)m * sizeof(int32_t) : 0);
   LaunchScope ls(K_PERM, 0.0, 8.0 * kmax + 4.0 * m, s);
   perm_from_ipiv_kernel<<<1, 1024, smem, s>>>(ipiv, kmax, m, perm, scr);
   return cudaGetLastError();
@@ -1046,7 +1074,7 @@ void getrf_configure(int device) {
   cudaFuncSetAttribute(panel_reg_kernel<float, 1>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
   cudaFuncSetAttribute(panel_reg_kernel<float, 2>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
   cudaFuncSetAttribute(perm_from_ipiv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       kPermSmemMax * (int)sizeof(int32_t));
+                       (kPermSmemMax + kPermChunk) * (int)sizeof(int32_t));
   getrs_configure(device);
   tc_configure(device);
 }
@@ -1059,9 +1087,13 @@ cudaError_t getrf_launch(const GetrfPlan<T>& p, cudaStream_t stream) {
   const int64_t minmn = std::min(p.m, p.n);
   d.check(cudaMemsetAsync(p.info, 0, sizeof(int64_t), stream));
   if (minmn > 0) {
-    d.rec(0, minmn);
+    {
+      LaunchScope ls(K_PERM, 0.0, 4.0 * p.m, stream);
+      iota_kernel<<<(unsigned)std::min<int64_t>((p.m + 255) / 256, 1024), 256, 0, stream>>>(p.perm, p.m);
+      d.check(cudaGetLastError());
+    }
+    d.rec(0, minmn);  // each leaf's laswp also permutes p.perm
     if (p.n > p.m) d.trsm(0, p.m, p.m, p.n - p.m);  // wide: U12 := L11 \ A12
-    d.check(perm_build_launch(p.ipiv, minmn, p.m, p.perm, p.scratch, stream));
   }
   return d.err;
 }

@@ -270,28 +270,30 @@ solve_sweep_kernel(int64_t n, const T* __restrict__ LU, int64_t lda, const int32
     const int w_first = FWD ? 0 : 1, w_second = FWD ? 1 : 0;
     const int lo_second = FWD ? 32 : 0;  // first row of the second half
     (void)lo_second;
+    // One column of the diagonal chain for all NR right-hand sides: the
+    // divisions (lane `src` only, non-unit diagonal), then the broadcasts,
+    // then the updates, so the NR chains overlap.
+    auto chain_step = [&](int c, int src, bool divide_here, bool update) {
+      if (!kUnit && divide_here) {
+        if constexpr (NR == 1) acc[0] = div_markstein(acc[0], tile[c][c], yrow);
+        else div_markstein_n<T, NR>(acc, tile[c][c], yrow);
+      }
+      T xc[NR];
+#pragma unroll
+      for (int q = 0; q < NR; ++q) xc[q] = __shfl_sync(0xffffffffu, acc[q], src);
+      if (update) {
+        const T a = tile[c][r];
+#pragma unroll
+        for (int q = 0; q < NR; ++q) acc[q] = fma(-a, xc[q], acc[q]);
+      }
+    };
     if (warp == w_first) {
       // columns of the first half, in sweep order
-      const int cbeg = FWD ? 0 : min(nr, kTS) - 1;
-      const int cend = FWD ? min(nr, 32) : 32;  // exclusive bound (fwd) / inclusive low (bwd)
       if (FWD) {
-        for (int c = cbeg; c < cend; ++c) {
-#pragma unroll
-          for (int q = 0; q < NR; ++q) {
-            if (!kUnit && lane == c) acc[q] = div_markstein(acc[q], tile[c][c], yrow);
-            const T xc = __shfl_sync(0xffffffffu, acc[q], c);
-            if (r > c && r < nr) acc[q] = fma(-tile[c][r], xc, acc[q]);
-          }
-        }
+        const int cend = min(nr, 32);
+        for (int c = 0; c < cend; ++c) chain_step(c, c, lane == c, r > c && r < nr);
       } else {
-        for (int c = cbeg; c >= cend; --c) {
-#pragma unroll
-          for (int q = 0; q < NR; ++q) {
-            if (!kUnit && r == c) acc[q] = div_markstein(acc[q], tile[c][c], yrow);
-            const T xc = __shfl_sync(0xffffffffu, acc[q], c - 32);
-            if (r < c) acc[q] = fma(-tile[c][r], xc, acc[q]);
-          }
-        }
+        for (int c = min(nr, kTS) - 1; c >= 32; --c) chain_step(c, c - 32, r == c, r < c);
       }
       if (valid)
 #pragma unroll
@@ -305,28 +307,14 @@ solve_sweep_kernel(int64_t n, const T* __restrict__ LU, int64_t lda, const int32
 #pragma unroll
             for (int q = 0; q < NR; ++q) acc[q] = fma(-tile[c][r], sx[c][q], acc[q]);
           }
-          for (int c = 32; c < nr; ++c) {
-#pragma unroll
-            for (int q = 0; q < NR; ++q) {
-              if (!kUnit && r == c) acc[q] = div_markstein(acc[q], tile[c][c], yrow);
-              const T xc = __shfl_sync(0xffffffffu, acc[q], c - 32);
-              if (r > c && r < nr) acc[q] = fma(-tile[c][r], xc, acc[q]);
-            }
-          }
+          for (int c = 32; c < nr; ++c) chain_step(c, c - 32, r == c, r > c && r < nr);
         }
       } else {
         for (int c = nr - 1; c >= 32; --c) {
 #pragma unroll
           for (int q = 0; q < NR; ++q) acc[q] = fma(-tile[c][r], sx[c][q], acc[q]);
         }
-        for (int c = min(nr, 32) - 1; c >= 0; --c) {
-#pragma unroll
-          for (int q = 0; q < NR; ++q) {
-            if (!kUnit && lane == c) acc[q] = div_markstein(acc[q], tile[c][c], yrow);
-            const T xc = __shfl_sync(0xffffffffu, acc[q], c);
-            if (r < c) acc[q] = fma(-tile[c][r], xc, acc[q]);
-          }
-        }
+        for (int c = min(nr, 32) - 1; c >= 0; --c) chain_step(c, c, lane == c, r < c);
       }
     }
   }
