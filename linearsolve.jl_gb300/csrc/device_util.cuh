@@ -69,60 +69,6 @@ __device__ __forceinline__ bool grid_barrier(DevScratch* s, unsigned target) {
   return ok != 0;
 }
 
-// Correctly rounded a / b from y = RN(1/b), following Markstein's division
-// (P. Markstein, IBM J. Res. Develop. 34(1):111-119, 1990): q = RN(a*y) is
-// within one ulp of a/b, the remainder r = a - b*q is exact with one fused
-// multiply-add, and RN(q + r*y) is the correctly rounded quotient.  The
-// sequence needs q, y and r*y clear of underflow and overflow; outside that
-// range (and for zeros, infinities and NaNs) the IEEE division is used.
-template <typename T>
-struct DivRange;
-template <>
-struct DivRange<double> {
-  static constexpr double lo = 0x1p-960, hi = 0x1p+960;
-};
-template <>
-struct DivRange<float> {
-  static constexpr float lo = 0x1p-100f, hi = 0x1p+100f;
-};
-
-template <typename T>
-__device__ __forceinline__ T div_markstein(T a, T b, T y) {
-  const T q = a * y;
-  const T aq = fabs(q), ay = fabs(y);
-  if (!(aq > DivRange<T>::lo && aq < DivRange<T>::hi && ay > DivRange<T>::lo && ay < DivRange<T>::hi))
-    return a / b;
-  const T r = fma(-b, q, a);
-  return fma(r, y, q);
-}
-
-// a[i] / b for N > 1 dividends with one divisor, as N independent chains
-// without branches in the common case (so the compiler can interleave them;
-// with one dividend the plain div_markstein is faster).  A zero
-// dividend gives q = a*y, which is the correctly signed zero a/b; any other
-// operand outside the safe range sends all N through the IEEE division.
-template <typename T, int N>
-__device__ __forceinline__ void div_markstein_n(T (&a)[N], T b, T y) {
-  const T ay = fabs(y);
-  bool bad = !(ay > DivRange<T>::lo && ay < DivRange<T>::hi);
-  T res[N];
-#pragma unroll
-  for (int i = 0; i < N; ++i) {
-    const T q = a[i] * y;
-    const T aq = fabs(q);
-    const bool zero = a[i] == T(0);
-    bad |= !zero && !(aq > DivRange<T>::lo && aq < DivRange<T>::hi);
-    const T r = fma(-b, q, a[i]);
-    res[i] = zero ? q : fma(r, y, q);
-  }
-  if (bad) {
-#pragma unroll
-    for (int i = 0; i < N; ++i) res[i] = a[i] / b;
-  }
-#pragma unroll
-  for (int i = 0; i < N; ++i) a[i] = res[i];
-}
-
 // Pivot candidates are compared by integer keys: the bit pattern of |a|, which
 // orders non-negative floating-point values like the values themselves, with
 // NaN mapped to 0 so it never becomes a candidate (the reference's `v > amax`
@@ -150,6 +96,66 @@ struct PivKey<float> {
   }
   static __device__ __forceinline__ bool nonzero(float x) { return (__float_as_uint(x) << 1) != 0u; }
 };
+
+// Correctly rounded a / b from y = RN(1/b), following Markstein's division
+// (P. Markstein, IBM J. Res. Develop. 34(1):111-119, 1990): q = RN(a*y) is
+// within one ulp of a/b, the remainder r = a - b*q is exact with one fused
+// multiply-add, and RN(q + r*y) is the correctly rounded quotient.  The
+// sequence needs q, y and r*y clear of underflow and overflow; outside that
+// range (and for zeros, infinities and NaNs) the IEEE division is used.
+// The range test is done on the exponent bits with integer arithmetic: on
+// this GPU a floating-point comparison of doubles occupies the FP64 pipe.
+// in_range(x): 2^-960 <= |x| < 2^960 (double), 2^-100 <= |x| < 2^100 (float);
+// zero, subnormals, infinities and NaN are outside.
+template <typename T>
+struct DivRange;
+template <>
+struct DivRange<double> {
+  static __device__ __forceinline__ bool in_range(double x) {
+    const unsigned e = ((unsigned)(__double_as_longlong(x) >> 52)) & 0x7ffu;  // biased exponent
+    return e - (1023u - 960u) < 2u * 960u;  // 1023-960 <= e < 1023+960
+  }
+};
+template <>
+struct DivRange<float> {
+  static __device__ __forceinline__ bool in_range(float x) {
+    const unsigned e = (__float_as_uint(x) >> 23) & 0xffu;
+    return e - (127u - 100u) < 2u * 100u;  // 127-100 <= e < 127+100
+  }
+};
+
+template <typename T>
+__device__ __forceinline__ T div_markstein(T a, T b, T y) {
+  const T q = a * y;
+  if (!(DivRange<T>::in_range(q) && DivRange<T>::in_range(y))) return a / b;
+  const T r = fma(-b, q, a);
+  return fma(r, y, q);
+}
+
+// a[i] / b for N > 1 dividends with one divisor, as N independent chains
+// without branches in the common case (so the compiler can interleave them;
+// with one dividend the plain div_markstein is faster).  A zero
+// dividend gives q = a*y, which is the correctly signed zero a/b; any other
+// operand outside the safe range sends all N through the IEEE division.
+template <typename T, int N>
+__device__ __forceinline__ void div_markstein_n(T (&a)[N], T b, T y) {
+  bool bad = !DivRange<T>::in_range(y);
+  T res[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    const T q = a[i] * y;
+    const bool zero = !PivKey<T>::nonzero(a[i]);
+    bad |= !zero && !DivRange<T>::in_range(q);
+    const T r = fma(-b, q, a[i]);
+    res[i] = zero ? q : fma(r, y, q);
+  }
+  if (bad) {
+#pragma unroll
+    for (int i = 0; i < N; ++i) res[i] = a[i] / b;
+  }
+#pragma unroll
+  for (int i = 0; i < N; ++i) a[i] = res[i];
+}
 
 template <typename T>
 __device__ __forceinline__ T ldcg(const T* p) { return __ldcg(p); }

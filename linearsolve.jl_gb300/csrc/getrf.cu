@@ -45,12 +45,6 @@ __device__ __forceinline__ bool cand_better(T v, int64_t g, T bv, int64_t bg) {
   return (v > bv) || (v == bv && g < bg);
 }
 
-template <typename T>
-__device__ __forceinline__ T absval(T x) { return x < T(0) ? -x : (x == T(0) ? T(0) : x); }
-template <>
-__device__ __forceinline__ double absval<double>(double x) { return fabs(x); }
-template <>
-__device__ __forceinline__ float absval<float>(float x) { return fabsf(x); }
 
 // ---------------------------------------------------------------------------
 // Cooperative panel kernel: getf2 on rows [c0, m) x columns [c0, c0+w).
@@ -65,9 +59,11 @@ panel_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w,
   T* tile = reinterpret_cast<T*>(smem_raw);  // column j at tile + j*R
   __shared__ T pivrow[kPanelMaxW];
   __shared__ T diagrow[kPanelMaxW];
-  __shared__ T red_v[kPanelThreads / 32];
+  using K = typename PivKey<T>::K;  // pivot candidates compared as integer keys of |a|
+  __shared__ K red_v[kPanelThreads / 32];
   __shared__ int64_t red_g[kPanelThreads / 32];
   __shared__ int red_c[kPanelThreads / 32];
+  K* cand_key = reinterpret_cast<K*>(slots.cand_val);
   __shared__ int64_t s_best_g;
   __shared__ int s_best_c;
 
@@ -89,30 +85,30 @@ panel_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w,
     const T* colk = tile + (size_t)k * R;
 
     // 1. local candidate: first row of max |a| among rows >= d (NaN ignored)
-    T bv = T(0);
+    K bv = 0;
     int64_t bg = -1;
     for (int i = tid; i < nloc; i += blockDim.x) {
       int64_t g = base + i;
-      T v = absval(colk[i]);
+      K v = PivKey<T>::of(colk[i]);
       if (g >= d && v > bv) { bv = v; bg = g; }
     }
     for (int off = 16; off; off >>= 1) {
-      T ov = __shfl_down_sync(0xffffffffu, bv, off);
+      K ov = __shfl_down_sync(0xffffffffu, bv, off);
       int64_t og = __shfl_down_sync(0xffffffffu, bg, off);
       if (cand_better(ov, og, bv, bg)) { bv = ov; bg = og; }
     }
     if (lane == 0) { red_v[warp] = bv; red_g[warp] = bg; }
     __syncthreads();
     if (warp == 0) {
-      bv = lane < (kPanelThreads / 32) ? red_v[lane] : T(0);
+      bv = lane < (kPanelThreads / 32) ? red_v[lane] : K(0);
       bg = lane < (kPanelThreads / 32) ? red_g[lane] : -1;
       for (int off = 16; off; off >>= 1) {
-        T ov = __shfl_down_sync(0xffffffffu, bv, off);
+        K ov = __shfl_down_sync(0xffffffffu, bv, off);
         int64_t og = __shfl_down_sync(0xffffffffu, bg, off);
         if (cand_better(ov, og, bv, bg)) { bv = ov; bg = og; }
       }
       if (lane == 0) {
-        stcg(&slots.cand_val[buf * G + cta], bv);
+        stcg(&cand_key[buf * G + cta], bv);
         stcg(&slots.cand_row[buf * G + cta], bg);
         s_best_g = bg;
       }
@@ -129,16 +125,16 @@ panel_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w,
     if (!grid_barrier(scr, (unsigned)(k + 1) * (unsigned)G)) return;
 
     // 3. global winner over the G candidates (same reduction on every CTA)
-    bv = T(0);
+    bv = 0;
     bg = -1;
     int bc = -1;
     for (int c = tid; c < G; c += blockDim.x) {
-      T v = ldcg(&slots.cand_val[buf * G + c]);
+      K v = ldcg(&cand_key[buf * G + c]);
       int64_t g = ldcg(&slots.cand_row[buf * G + c]);
       if (cand_better(v, g, bv, bg)) { bv = v; bg = g; bc = c; }
     }
     for (int off = 16; off; off >>= 1) {
-      T ov = __shfl_down_sync(0xffffffffu, bv, off);
+      K ov = __shfl_down_sync(0xffffffffu, bv, off);
       int64_t og = __shfl_down_sync(0xffffffffu, bg, off);
       int oc = __shfl_down_sync(0xffffffffu, bc, off);
       if (cand_better(ov, og, bv, bg)) { bv = ov; bg = og; bc = oc; }
@@ -146,11 +142,11 @@ panel_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w,
     if (lane == 0) { red_v[warp] = bv; red_g[warp] = bg; red_c[warp] = bc; }
     __syncthreads();
     if (warp == 0) {
-      bv = lane < (kPanelThreads / 32) ? red_v[lane] : T(0);
+      bv = lane < (kPanelThreads / 32) ? red_v[lane] : K(0);
       bg = lane < (kPanelThreads / 32) ? red_g[lane] : -1;
       bc = lane < (kPanelThreads / 32) ? red_c[lane] : -1;
       for (int off = 16; off; off >>= 1) {
-        T ov = __shfl_down_sync(0xffffffffu, bv, off);
+        K ov = __shfl_down_sync(0xffffffffu, bv, off);
         int64_t og = __shfl_down_sync(0xffffffffu, bg, off);
         int oc = __shfl_down_sync(0xffffffffu, bc, off);
         if (cand_better(ov, og, bv, bg)) { bv = ov; bg = og; bc = oc; }
@@ -217,13 +213,14 @@ panel_cluster_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int 
   cg::cluster_group cluster = cg::this_cluster();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* tile = reinterpret_cast<T*>(smem_raw);  // column j at tile + j*R
-  __shared__ T s_cval[2];
+  __shared__ typename PivKey<T>::K s_cval[2];
   __shared__ int64_t s_crow[2];
   __shared__ T s_crowv[2][kPanelMaxW];
   __shared__ T s_diagv[2][kPanelMaxW];
   __shared__ T pivrow[kPanelMaxW];
   __shared__ T diagrow[kPanelMaxW];
-  __shared__ T red_v[kPanelThreads / 32];
+  using K = typename PivKey<T>::K;  // pivot candidates compared as integer keys of |a|
+  __shared__ K red_v[kPanelThreads / 32];
   __shared__ int64_t red_g[kPanelThreads / 32];
   __shared__ int64_t s_best_g;
   __shared__ int s_best_c;
@@ -244,25 +241,25 @@ panel_cluster_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int 
     const int64_t d = c0 + k;
     const int buf = k & 1;
     const T* colk = tile + (size_t)k * R;
-    T bv = T(0);
+    K bv = 0;
     int64_t bg = -1;
     for (int i = tid; i < nloc; i += blockDim.x) {
       int64_t g = base + i;
-      T v = absval(colk[i]);
+      K v = PivKey<T>::of(colk[i]);
       if (g >= d && v > bv) { bv = v; bg = g; }
     }
     for (int off = 16; off; off >>= 1) {
-      T ov = __shfl_down_sync(0xffffffffu, bv, off);
+      K ov = __shfl_down_sync(0xffffffffu, bv, off);
       int64_t og = __shfl_down_sync(0xffffffffu, bg, off);
       if (cand_better(ov, og, bv, bg)) { bv = ov; bg = og; }
     }
     if (lane == 0) { red_v[warp] = bv; red_g[warp] = bg; }
     __syncthreads();
     if (warp == 0) {
-      bv = lane < (kPanelThreads / 32) ? red_v[lane] : T(0);
+      bv = lane < (kPanelThreads / 32) ? red_v[lane] : K(0);
       bg = lane < (kPanelThreads / 32) ? red_g[lane] : -1;
       for (int off = 16; off; off >>= 1) {
-        T ov = __shfl_down_sync(0xffffffffu, bv, off);
+        K ov = __shfl_down_sync(0xffffffffu, bv, off);
         int64_t og = __shfl_down_sync(0xffffffffu, bg, off);
         if (cand_better(ov, og, bv, bg)) { bv = ov; bg = og; }
       }
@@ -276,11 +273,11 @@ panel_cluster_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int 
     cluster.sync();  // publishes the slots of step k (release/acquire across the cluster)
 
     // winner over the G candidates, read through distributed shared memory
-    bv = T(0);
+    bv = 0;
     bg = -1;
     int bc = -1;
     if (tid < G) {
-      const T* rv = cluster.map_shared_rank(&s_cval[buf], tid);
+      const K* rv = cluster.map_shared_rank(&s_cval[buf], tid);
       const int64_t* rr = cluster.map_shared_rank(&s_crow[buf], tid);
       bv = *rv;
       bg = *rr;
@@ -288,7 +285,7 @@ panel_cluster_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int 
     }
     if (warp == 0) {
       for (int off = 16; off; off >>= 1) {
-        T ov = __shfl_down_sync(0xffffffffu, bv, off);
+        K ov = __shfl_down_sync(0xffffffffu, bv, off);
         int64_t og = __shfl_down_sync(0xffffffffu, bg, off);
         int oc = __shfl_down_sync(0xffffffffu, bc, off);
         if (cand_better(ov, og, bv, bg)) { bv = ov; bg = og; bc = oc; }

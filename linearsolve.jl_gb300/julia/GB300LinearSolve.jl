@@ -168,7 +168,12 @@ function SciMLBase.solve!(cache::LinearCache, alg::GB300Algs; kwargs...)
         cache.isfresh = false
     end
     copyto!(cache.u, cache.b)
-    u = cache.u
+    _solve_in_place!(alg, c, cache.u, 'N')
+    return SciMLBase.build_linear_solution(alg, cache.u, nothing, cache; retcode = ReturnCode.Success)
+end
+
+# u := op(A) \ u with the cached device factors (op = 'N' or 'T').
+function _solve_in_place!(alg::GB300Algs, c::GB300LUCache, u::VecOrMat{Float64}, trans::Char)
     nrhs = u isa AbstractVector ? 1 : size(u, 2)
     if alg isa GB300MixedLUFactorization
         opts = RefineOpts(alg.refine === :gmres_ir ? GBLU_REFINE_GMRES : GBLU_REFINE_IR,
@@ -176,14 +181,26 @@ function SciMLBase.solve!(cache::LinearCache, alg::GB300Algs; kwargs...)
         _check(ccall(_syms[:gblu_solve_refined], Int32,
                      (Ptr{Cvoid}, Ptr{Cvoid}, UInt8, Int64, Ptr{Float64}, Int64, Int32,
                       Ref{RefineOpts}, Ref{RefineStats}),
-                     c.ctx, c.factor, UInt8('N'), nrhs, u, max(1, stride(u, ndims(u))),
+                     c.ctx, c.factor, UInt8(trans), nrhs, u, max(1, size(u, 1)),
                      GBLU_HOST, opts, c.stats), c.ctx)
     else
         _check(ccall(_syms[:gblu_getrs], Int32,
                      (Ptr{Cvoid}, Ptr{Cvoid}, UInt8, Int64, Ptr{Float64}, Int64, Int32),
-                     c.ctx, c.factor, UInt8('N'), nrhs, u, size(u, 1), GBLU_HOST), c.ctx)
+                     c.ctx, c.factor, UInt8(trans), nrhs, u, max(1, size(u, 1)), GBLU_HOST), c.ctx)
     end
-    return SciMLBase.build_linear_solution(alg, u, nothing, cache; retcode = ReturnCode.Success)
+    return u
+end
+
+# solve!(cache; adjoint = true) reuses the device factors (src/adjoint_factorization.jl:
+# the algorithm opts into the custom reuse and answers with a transposed getrs).
+LinearSolve._adjoint_factorization_reuse(::Type{<:GB300Algs}) =
+    LinearSolve._CustomAdjointFactorizationReuse()
+LinearSolve._custom_can_reuse_adjoint_factorization(::GB300Algs, c::GB300LUCache) =
+    c.factor != C_NULL && c.info == 0
+function LinearSolve._custom_adjoint_factorization_solve(alg::GB300Algs, c::GB300LUCache, A, b)
+    x = Matrix{Float64}(reshape(b, size(b, 1), :))
+    _solve_in_place!(alg, c, x, 'T')
+    return b isa AbstractVector ? vec(x) : x
 end
 
 end # module
