@@ -408,8 +408,7 @@ panel_reg_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w,
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int64_t base = c0 + (int64_t)cta * R;
   const int nloc = (int)max((int64_t)0, min((int64_t)R, m - base));
-  const int nwr = min(NW, (R + 31) >> 5);  // warps of a CTA that own rows
-  const int ncand = G * nwr;
+  const int ncand = G * NW;
 
   T pr[RPT][W];  // slot j: column (k + j) mod 32 at step k
 #pragma unroll
@@ -448,14 +447,26 @@ panel_reg_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w,
     // 2. warp 0: the winner over every warp of the cluster, the pivot row and,
     //    for the pivot row's CTA, the old diagonal row
     if (warp == 0) {
+      // every warp's slot of every CTA (slot c: CTA c / NW, warp c % NW; warps
+      // without rows hold row -1), all loads issued before any comparison
+      constexpr int QMAX = 16 * NW / 32;
+      K cv[QMAX];
+      int cr[QMAX];
+#pragma unroll
+      for (int q = 0; q < QMAX; ++q) {
+        const int c = lane + 32 * q;
+        cv[q] = 0;
+        cr[q] = -1;
+        if (c < ncand) {
+          cv[q] = *cluster.map_shared_rank(&s_cval[buf][c % NW], c / NW);
+          cr[q] = *cluster.map_shared_rank(&s_crow[buf][c % NW], c / NW);
+        }
+      }
       K v = 0;
       int g = -1, e = -1;
-      for (int c = lane; c < ncand; c += 32) {
-        const int rc = c / nwr, rw = c - rc * nwr;
-        const K cv = *cluster.map_shared_rank(&s_cval[buf][rw], rc);
-        const int cg_ = *cluster.map_shared_rank(&s_crow[buf][rw], rc);
-        if (cand_better(cv, (int64_t)cg_, v, (int64_t)g)) { v = cv; g = cg_; e = c; }
-      }
+#pragma unroll
+      for (int q = 0; q < QMAX; ++q)
+        if (cand_better(cv[q], (int64_t)cr[q], v, (int64_t)g)) { v = cv[q]; g = cr[q]; e = lane + 32 * q; }
       for (int off = 16; off; off >>= 1) {
         const K ov = __shfl_xor_sync(0xffffffffu, v, off);
         const int og = __shfl_xor_sync(0xffffffffu, g, off);
@@ -468,8 +479,7 @@ panel_reg_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w,
       if (p == d) {
         s_piv[lane] = dv;
       } else {
-        const int rc = e / nwr, rw = e - rc * nwr;
-        s_piv[lane] = *cluster.map_shared_rank(&s_crowv[buf][rw][lane], rc);
+        s_piv[lane] = *cluster.map_shared_rank(&s_crowv[buf][e % NW][lane], e / NW);
         if (p >= base && p < base + nloc) s_old[lane] = dv;
       }
       if (lane == 0) s_p = (int)p;
@@ -887,9 +897,9 @@ struct Driver {
   // panel is taller or not launchable.
   bool panel_reg(int64_t c0, int w) {
     const int64_t M = p.m - c0;
-    // FP64: 16 SMs' FP64 pipes bound the updates of a tall leaf; above 4096
+    // FP64: 16 SMs' FP64 pipes bound the updates of a tall leaf; above 2048
     // rows the grid kernel, spread over the whole GPU, is faster
-    if (sizeof(T) == 8 && M > 4096) return false;
+    if (sizeof(T) == 8 && M > 2048) return false;
     const int cs = (int)std::min<int64_t>(16, std::max<int64_t>(1, (M + 127) / 128));
     const int64_t R = (M + cs - 1) / cs;
     if (R <= kRegPanelThreads) return panel_reg_launch<1>(c0, w, cs);
