@@ -95,15 +95,6 @@ struct SysSmem {
   }
 };
 
-// Candidate order: larger key first, then the smaller row; row -1 is no
-// candidate.  A total order, so every reduction tree gives the first row of
-// maximal |value|.
-template <typename K>
-__device__ __forceinline__ bool cand_better(K v, int g, K bv, int bg) {
-  if (g < 0) return false;
-  if (bg < 0) return true;
-  return v > bv || (v == bv && g < bg);
-}
 
 // In-place getrf of one n x n column-major system (ld = n) in global memory,
 // blocked by NB columns (src/blocked_lufact.jl:658-679 order):
@@ -158,10 +149,9 @@ __device__ int64_t factor_system(T* __restrict__ A, int n, int32_t* __restrict__
           if (v > bv) { bv = v; bg = i; }
         }
       }
-      for (int off = 16; off; off >>= 1) {
-        const K ov = __shfl_xor_sync(0xffffffffu, bv, off);
-        const int og = __shfl_xor_sync(0xffffffffu, bg, off);
-        if (cand_better(ov, og, bv, bg)) { bv = ov; bg = og; }
+      {
+        int src;
+        warp_pivot_choice(bv, bg, src);
       }
       if (lane == 0) { sm.cval[buf * NW + warp] = bv; sm.crow[buf * NW + warp] = bg; }
       // the owners publish (row tests, not a computed slot index, so pr stays in registers)
@@ -180,13 +170,8 @@ __device__ int64_t factor_system(T* __restrict__ A, int n, int32_t* __restrict__
       __syncthreads();
       K wv = lane < NW ? sm.cval[buf * NW + lane] : K(0);
       int wg = lane < NW ? sm.crow[buf * NW + lane] : -1;
-      int ww = lane;
-      for (int off = 16; off; off >>= 1) {
-        const K ov = __shfl_xor_sync(0xffffffffu, wv, off);
-        const int og = __shfl_xor_sync(0xffffffffu, wg, off);
-        const int ow = __shfl_xor_sync(0xffffffffu, ww, off);
-        if (cand_better(ov, og, wv, wg)) { wv = ov; wg = og; ww = ow; }
-      }
+      int ww;  // the winning warp (= the lane that held its slot)
+      warp_pivot_choice(wv, wg, ww);
       const int p = wg < 0 ? col : wg;  // kp = k when the column is zero below the diagonal
       const T* src = (p == col) ? sm.diagv + buf * NB : sm.crowv + (buf * NW + ww) * NB;
       const T piv = src[j];

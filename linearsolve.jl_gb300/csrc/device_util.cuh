@@ -97,6 +97,34 @@ struct PivKey<float> {
   static __device__ __forceinline__ bool nonzero(float x) { return (__float_as_uint(x) << 1) != 0u; }
 };
 
+// Warp-wide pivot choice: every lane holds a candidate (key v, row g; g < 0 =
+// none); on return every lane holds the winner (largest key, then smallest
+// row) and `src` = the lane it came from (-1 when no lane has a candidate).
+// 32-bit keys use the warp reduction instructions (one max, one min); 64-bit
+// keys a shuffle tree.  Rows are unique across lanes.
+template <typename K>
+__device__ __forceinline__ void warp_pivot_choice(K& v, int& g, int& src) {
+  const int lane = threadIdx.x & 31;
+  if constexpr (sizeof(K) == 4) {
+    const K mk = __reduce_max_sync(0xffffffffu, (unsigned)v);
+    const bool mine = g >= 0 && v == mk;
+    const unsigned gmin = __reduce_min_sync(0xffffffffu, mine ? (unsigned)g : 0xffffffffu);
+    const unsigned who = __ballot_sync(0xffffffffu, mine && (unsigned)g == gmin);
+    src = who ? __ffs(who) - 1 : -1;
+    v = mk;
+    g = who ? (int)gmin : -1;
+  } else {
+    src = g >= 0 ? lane : -1;
+    for (int off = 16; off; off >>= 1) {
+      const K ov = __shfl_xor_sync(0xffffffffu, v, off);
+      const int og = __shfl_xor_sync(0xffffffffu, g, off);
+      const int os = __shfl_xor_sync(0xffffffffu, src, off);
+      const bool better = og >= 0 && (g < 0 || ov > v || (ov == v && og < g));
+      if (better) { v = ov; g = og; src = os; }
+    }
+  }
+}
+
 // Correctly rounded a / b from y = RN(1/b), following Markstein's division
 // (P. Markstein, IBM J. Res. Develop. 34(1):111-119, 1990): q = RN(a*y) is
 // within one ulp of a/b, the remainder r = a - b*q is exact with one fused

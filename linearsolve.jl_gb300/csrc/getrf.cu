@@ -402,6 +402,7 @@ panel_reg_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w,
   __shared__ K s_cval[2][NW];
   __shared__ int s_crow[2][NW];
   __shared__ int s_p;
+  __shared__ T s_inv;
 
   const int G = (int)cluster.num_blocks();
   const int cta = (int)cluster.block_rank();
@@ -431,10 +432,9 @@ panel_reg_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w,
       const K v = PivKey<T>::of(pr[r][0]);
       if (i < nloc && base + i >= d && v > bv) { bv = v; bg = (int)(base + i); }
     }
-    for (int off = 16; off; off >>= 1) {
-      const K ov = __shfl_xor_sync(0xffffffffu, bv, off);
-      const int og = __shfl_xor_sync(0xffffffffu, bg, off);
-      if (cand_better(ov, (int64_t)og, bv, (int64_t)bg)) { bv = ov; bg = og; }
+    {
+      int src;
+      warp_pivot_choice(bv, bg, src);
     }
     if (lane == 0) { s_cval[buf][warp] = bv; s_crow[buf][warp] = bg; }
 #pragma unroll
@@ -467,11 +467,10 @@ panel_reg_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w,
 #pragma unroll
       for (int q = 0; q < QMAX; ++q)
         if (cand_better(cv[q], (int64_t)cr[q], v, (int64_t)g)) { v = cv[q]; g = cr[q]; e = lane + 32 * q; }
-      for (int off = 16; off; off >>= 1) {
-        const K ov = __shfl_xor_sync(0xffffffffu, v, off);
-        const int og = __shfl_xor_sync(0xffffffffu, g, off);
-        const int oe = __shfl_xor_sync(0xffffffffu, e, off);
-        if (cand_better(ov, (int64_t)og, v, (int64_t)g)) { v = ov; g = og; e = oe; }
+      {
+        int src;
+        warp_pivot_choice(v, g, src);
+        e = __shfl_sync(0xffffffffu, e, src < 0 ? 0 : src);
       }
       const int64_t p = g < 0 ? d : (int64_t)g;  // kp = k when amax == 0
       const int downer = (int)((d - c0) / R);
@@ -482,7 +481,11 @@ panel_reg_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w,
         s_piv[lane] = *cluster.map_shared_rank(&s_crowv[buf][e % NW][lane], e / NW);
         if (p >= base && p < base + nloc) s_old[lane] = dv;
       }
-      if (lane == 0) s_p = (int)p;
+      if (lane == 0) {
+        s_p = (int)p;
+        const T pv = s_piv[0];  // written above by this lane
+        s_inv = PivKey<T>::nonzero(pv) ? T(1) / pv : T(0);
+      }
     }
     __syncthreads();
     const int64_t p = s_p;
@@ -494,7 +497,7 @@ panel_reg_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w,
     }
     // 3. interchange (nonzero pivot only), scale, rank-1 update, rotate
     const bool swap = nz && p != d;
-    const T inv = nz ? T(1) / piv : T(0);
+    const T inv = s_inv;  // 1 / piv, computed once by warp 0
     const int lim = w - k;  // slots 1..lim-1 hold columns k+1..w-1
     T l[RPT];
     bool upd[RPT];
