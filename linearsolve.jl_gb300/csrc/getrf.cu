@@ -514,18 +514,32 @@ panel_reg_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w,
       if (upd[r] && nz) l[r] *= inv;
       if (upd[r]) pr[r][0] = l[r];
     }
+    if constexpr (sizeof(T) == 4) {
+      // FP32: predicated FMAs over all slots (no branches)
 #pragma unroll
-    for (int q = 0; q < W / VT::N; ++q) {
-      const typename VT::V pv = reinterpret_cast<const typename VT::V*>(s_piv)[q];
+      for (int q = 0; q < W / VT::N; ++q) {
+        const typename VT::V pv = reinterpret_cast<const typename VT::V*>(s_piv)[q];
 #pragma unroll
-      for (int e = 0; e < VT::N; ++e) {
-        const int j = q * VT::N + e;
-        if (j >= 1 && j < lim) {
-          const T u = VT::get(pv, e);
+        for (int e = 0; e < VT::N; ++e) {
+          const int j = q * VT::N + e;
+          if (j >= 1 && j < lim) {
+            const T u = VT::get(pv, e);
 #pragma unroll
-          for (int r = 0; r < RPT; ++r)
-            if (upd[r]) pr[r][j] = fma(-l[r], u, pr[r][j]);
+            for (int r = 0; r < RPT; ++r)
+              if (upd[r]) pr[r][j] = fma(-l[r], u, pr[r][j]);
+          }
         }
+      }
+    } else {
+      // FP64: stop at the last live slot with a uniform branch, so the FP64
+      // pipe only sees the FMAs that do work
+#pragma unroll
+      for (int j = 1; j < W; ++j) {
+        if (j >= lim) break;
+        const T u = s_piv[j];
+#pragma unroll
+        for (int r = 0; r < RPT; ++r)
+          if (upd[r]) pr[r][j] = fma(-l[r], u, pr[r][j]);
       }
     }
 #pragma unroll
@@ -900,9 +914,9 @@ struct Driver {
   // panel is taller or not launchable.
   bool panel_reg(int64_t c0, int w) {
     const int64_t M = p.m - c0;
-    // FP64: 16 SMs' FP64 pipes bound the updates of a tall leaf; above 2048
-    // rows the grid kernel, spread over the whole GPU, is faster
-    if (sizeof(T) == 8 && M > 2048) return false;
+    // FP64 leaves above 8192 rows (two rows per thread would not fit the
+    // registers) go to the grid kernel
+    if (sizeof(T) == 8 && M > 8192) return false;
     const int cs = (int)std::min<int64_t>(16, std::max<int64_t>(1, (M + 127) / 128));
     const int64_t R = (M + cs - 1) / cs;
     if (R <= kRegPanelThreads) return panel_reg_launch<1>(c0, w, cs);
