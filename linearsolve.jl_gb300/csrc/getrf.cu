@@ -20,6 +20,8 @@
 // are bit-identical to the reference's blocked LU for any blocking.
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
+#include <cstring>
 #include <mutex>
 #include <type_traits>
 
@@ -822,6 +824,7 @@ struct Driver {
   cudaStream_t s;
   int device;
   cudaError_t err = cudaSuccess;
+  int forced = 0;  // forced_panel_kind()
 
   T* at(int64_t r, int64_t c) const { return p.A + r + c * p.lda; }
 
@@ -955,11 +958,13 @@ struct Driver {
   void panel(int64_t c0, int w) {
     const int64_t M = p.m - c0;
     const DeviceInfo& di = device_info(device);
-    if (p.use_reg_panel && panel_reg(c0, w)) {
+    // forced: 0 automatic, 1 grid kernel only, 2 shared-memory cluster kernel
+    // where it fits, 3 register kernel where it fits (falling back in order)
+    if (forced != 1 && forced != 2 && p.use_reg_panel && panel_reg(c0, w)) {
       laswp(c0, w);
       return;
     }
-    if (p.use_cluster_panel && panel_cluster(c0, w)) {
+    if (forced != 1 && p.use_cluster_panel && panel_cluster(c0, w)) {
       laswp(c0, w);
       return;
     }
@@ -1103,11 +1108,24 @@ void getrf_configure(int device) {
   tc_configure(device);
 }
 
+// GBLU_PANEL=grid|cluster|reg forces one panel kernel (where the panel fits
+// it; the kernels give identical results), so every variant can be tested on
+// small matrices.  Read at each factorization.
+int forced_panel_kind() {
+  const char* e = getenv("GBLU_PANEL");
+  if (!e) return 0;
+  if (!strcmp(e, "grid")) return 1;
+  if (!strcmp(e, "cluster")) return 2;
+  if (!strcmp(e, "reg")) return 3;
+  return 0;
+}
+
 template <typename T>
 cudaError_t getrf_launch(const GetrfPlan<T>& p, cudaStream_t stream) {
   int device = 0;
   cudaGetDevice(&device);
   Driver<T> d{p, stream, device};
+  d.forced = forced_panel_kind();
   const int64_t minmn = std::min(p.m, p.n);
   d.check(cudaMemsetAsync(p.info, 0, sizeof(int64_t), stream));
   if (minmn > 0) {

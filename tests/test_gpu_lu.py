@@ -254,3 +254,22 @@ def test_markstein_division_matches_ieee():
     m64, m32 = ctypes.c_uint64(), ctypes.c_uint64()
     assert lib.gblu_tool_divcheck(1 << 26, 12345, ctypes.byref(m64), ctypes.byref(m32)) == 0
     assert m64.value == 0 and m32.value == 0, (m64.value, m32.value)
+
+
+@pytest.mark.parametrize("kind", ["grid", "cluster", "reg"])
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_every_panel_kernel_bit_exact(ctx, oracle_mod, monkeypatch, kind, prec):
+    # the three getf2 kernels (cooperative grid, shared-memory cluster,
+    # register cluster) give identical factors; GBLU_PANEL forces one of them
+    monkeypatch.setenv("GBLU_PANEL", kind)
+    rng = np.random.default_rng(77)
+    shapes = ((700, 700), (1100, 300), (300, 520)) if prec == "fp64" else ((700, 700), (1300, 1300))
+    for m, n in shapes:
+        A = rng.standard_normal((m, n))
+        dt = np.float32 if prec == "fp32" else np.float64
+        f = ctx.factor(m, n, prec)
+        f.getrf(A.astype(dt).astype(np.float64))
+        LU, ipiv, _ = oracle_mod.getrf(A.astype(dt))
+        assert np.array_equal(f.ipiv(), ipiv), (kind, prec, m, n)
+        assert np.array_equal(f.factors(), LU.astype(np.float64)), (kind, prec, m, n)
+        f.close()
