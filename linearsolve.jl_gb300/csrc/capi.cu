@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <cstdarg>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -352,6 +353,7 @@ int32_t gblu_factor_destroy(gblu_ctx* ctx, gblu_factor* f) {
   std::lock_guard<std::recursive_mutex> lk(ctx->mu);
   DeviceGuard g(ctx->device);
   cudaStreamSynchronize(ctx->stream);
+  if (f->getrf_exec) cudaGraphExecDestroy(f->getrf_exec);
   ctx_free(ctx, f->arena, f->bytes);
   if (f->rhs) ctx_free(ctx, f->rhs, (size_t)f->ld * f->rhs_cols * sizeof(double));
   if (f->fb_arena) ctx_free(ctx, f->fb_arena, f->fb_bytes);
@@ -374,6 +376,40 @@ int32_t upload_matrix(gblu_ctx* ctx, double* dst, int64_t ld_dst, const double* 
   return GBLU_OK;
 }
 
+// Runs the factor's getrf launch sequence: directly on its first two runs
+// (the first also fills the host-side caches the launches consult; a factor
+// refactored only once or twice does not pay for a capture) and while
+// profiling (per-launch events); from the third run on as one replay of a
+// CUDA graph captured from that sequence.  Any capture problem falls back to
+// direct launches for good.  GBLU_GRAPHS=0 disables the replay.
+template <typename Launch>
+cudaError_t run_getrf(gblu_ctx* ctx, gblu_factor* f, Launch&& launch) {
+  static const bool off = [] {
+    const char* e = getenv("GBLU_GRAPHS");
+    return e && e[0] == '0';
+  }();
+  const bool direct = off || f->getrf_graph_failed || ctx->prof.enabled || f->getrf_runs++ < 2;
+  if (direct) return launch();
+  if (!f->getrf_exec) {
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+      const cudaError_t le = launch();
+      e = cudaStreamEndCapture(ctx->stream, &g);
+      if (le != cudaSuccess) e = le;
+    }
+    if (e == cudaSuccess && g) e = cudaGraphInstantiate(&f->getrf_exec, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (e != cudaSuccess || !f->getrf_exec) {
+      cudaGetLastError();  // clear the capture failure, then launch directly
+      f->getrf_exec = nullptr;
+      f->getrf_graph_failed = true;
+      return launch();
+    }
+  }
+  return cudaGraphLaunch(f->getrf_exec, ctx->stream);
+}
+
 int32_t factor_getrf(gblu_ctx* ctx, gblu_factor* f, const double* A, int64_t lda, int32_t a_loc,
                      int64_t* info) {
   f->factored = false;
@@ -382,13 +418,15 @@ int32_t factor_getrf(gblu_ctx* ctx, gblu_factor* f, const double* A, int64_t lda
   if (f->precision == GBLU_FP64) {
     st = upload_matrix(ctx, f->lu64, f->ld, A, lda, f->m, f->n, a_loc);
     if (st) return st;
-    CK(ctx, getrf_launch<double>(f->rf64, ctx->stream), "launching getrf");
+    CK(ctx, run_getrf(ctx, f, [&] { return getrf_launch<double>(f->rf64, ctx->stream); }),
+       "launching getrf");
   } else {
     st = upload_matrix(ctx, f->lu64, f->ld, A, lda, f->m, f->n, a_loc);
     if (st) return st;
     CK(ctx, refine_prepare(f->refine, f->n, f->lu64, f->ld, f->lu32, f->ld, ctx->stream),
        "preparing mixed-precision factorization");
-    CK(ctx, getrf_launch<float>(f->rf32, ctx->stream), "launching getrf");
+    CK(ctx, run_getrf(ctx, f, [&] { return getrf_launch<float>(f->rf32, ctx->stream); }),
+       "launching getrf");
   }
   int64_t hinfo = 0;
   CK(ctx, cudaMemcpyAsync(&hinfo, f->info_dev, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream),

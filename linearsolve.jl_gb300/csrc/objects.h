@@ -52,6 +52,11 @@ struct gblu_factor {
   gblu::GetrsPlan<double> fb_rs;
   bool fb_valid = false;   // fallback factors hold the current A
   bool use_fb = false;     // solves go straight to the fallback factors
+  // the factorization's launch sequence, captured on its second run and
+  // replayed from then on (it depends only on the factor's shape)
+  cudaGraphExec_t getrf_exec = nullptr;
+  int getrf_runs = 0;
+  bool getrf_graph_failed = false;
 };
 
 namespace gblu {

@@ -273,3 +273,20 @@ def test_every_panel_kernel_bit_exact(ctx, oracle_mod, monkeypatch, kind, prec):
         assert np.array_equal(f.ipiv(), ipiv), (kind, prec, m, n)
         assert np.array_equal(f.factors(), LU.astype(np.float64)), (kind, prec, m, n)
         f.close()
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_graph_replayed_getrf_matches_direct(ctx, oracle_mod, prec):
+    # from its third factorization a factor replays its launch sequence from a
+    # captured CUDA graph; new matrices must give the same bit-exact results
+    n = 900
+    rng = np.random.default_rng(88)
+    dt = np.float32 if prec == "fp32" else np.float64
+    f = ctx.factor(n, n, prec)
+    for run in range(5):
+        A = rng.standard_normal((n, n)).astype(dt).astype(np.float64)
+        assert f.getrf(A) == 0
+        LU, ipiv, _ = oracle_mod.getrf(A.astype(dt))
+        assert np.array_equal(f.ipiv(), ipiv), run
+        assert np.array_equal(f.factors(), LU.astype(np.float64)), run
+    f.close()
