@@ -43,6 +43,13 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 EPS64 = float(np.finfo(np.float64).eps)
+# FP64 roofline denominator: NVIDIA's published FP64 rate of a GB300 (no FP64
+# figure is in MEASURED_PEAKS.json; tcgen05 has no FP64 kind, so FP64 runs on
+# the FP64 pipe).  A register-only DFMA probe (reported beside it) tops out
+# near 1.0-1.1 TFLOP/s, below what the DFMA GEMM itself reaches, so it is not
+# used as the denominator.
+FP64_NOMINAL_TFLOPS = 1.25
+FP64_PEAK_SOURCE = "nominal GB300 FP64 1.25 TFLOP/s (register-only DFMA probe in probe_tflops)"
 METRIC = "FP64-accurate solves/s (1 getrf + 16 cached getrs, n=8192, plain FP64 LU)"
 UNIT = "solves/s"
 
@@ -240,6 +247,7 @@ def run_gpu(args, rank, world, local):
     if args.only_suite:  # profiling aid: the suite parts alone, one JSON object
         if args.suite == "auto":
             args.suite = "mixed,batched,serving"
+        args.peak_fp64 = FP64_NOMINAL_TFLOPS
         out = run_suites(pkg, cu, ctx, args)
         if rank == 0:
             print(json.dumps(out))
@@ -320,15 +328,14 @@ def run_gpu(args, rank, world, local):
     dom = max(kinds, key=lambda k: prof[k]["ms"])
     d = prof[dom]
     peaks = measured_peaks()
-    peak_fp64 = peak_fp64_tflops(local) if rank == 0 else None
+    probe_fp64 = peak_fp64_tflops(local) if rank == 0 else None
+    peak_fp64 = FP64_NOMINAL_TFLOPS
     if dom in ("gemm", "panel", "trsm"):
         achieved = d["flops"] / (d["ms"] / 1000.0) / 1e12 if d["ms"] > 0 else 0.0
         peak = peak_fp64
         roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": (achieved / peak) if peak else None,
-                "peak_source": "FP64 FMA throughput measured in this run by a register-only DFMA "
-                               "loop (MEASURED_PEAKS.json has no FP64 figure; tcgen05 has no FP64 "
-                               "kind, so the FP64 update runs on the FP64 pipe)",
+                "peak_source": FP64_PEAK_SOURCE, "probe_tflops": probe_fp64,
                 "kernel": f"{dom} (FP64)", "launches": d["count"],
                 "flops_per_launch": d["flops"] / max(d["count"], 1),
                 "ms_per_launch": d["ms"] / max(d["count"], 1)}
@@ -348,6 +355,25 @@ def run_gpu(args, rank, world, local):
     else:
         roof["traffic"] = None
 
+    # per-phase fractions of the roofline: getrf against the FP64 peak, getrs
+    # against HBM (its algorithmic bytes: both triangles read once per solve)
+    step_ms = {k: prof[k]["ms"] / args.steps for k in kinds}
+    getrf_ms = sum(step_ms.get(k, 0.0) for k in ("gemm", "panel", "laswp", "trsm", "perm"))
+    getrs_ms = step_ms.get("getrs", 0.0)
+    hbm = peaks.get("hbm_gbs")
+    getrf_tf = getrf_flops(n) / (getrf_ms / 1e3) / 1e12 if getrf_ms > 0 else None
+    getrs_gbs = nrhs * (8.0 * n * n + 16.0 * n) / (getrs_ms / 1e3) / 1e9 if getrs_ms > 0 else None
+    args.peak_fp64 = peak_fp64
+    phases = {
+        "getrf": {"achieved": getrf_tf, "unit": "TFLOP/s", "peak": peak_fp64,
+                  "frac": getrf_tf / peak_fp64 if getrf_tf and peak_fp64 else None,
+                  "bound": "FP64 pipe (" + FP64_PEAK_SOURCE + ")", "flops": getrf_flops(n), "ms": getrf_ms},
+        "getrs": {"achieved": getrs_gbs, "unit": "GB/s", "peak": hbm,
+                  "frac": getrs_gbs / hbm if getrs_gbs and hbm else None,
+                  "bound": "HBM (the sweeps are latency-bound wavefronts)",
+                  "bytes_per_solve": 8.0 * n * n + 16.0 * n, "ms": getrs_ms},
+    }
+
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True,
@@ -362,6 +388,7 @@ def run_gpu(args, rank, world, local):
                 "d2h_bytes_per_step": nrhs * 8 * n + 8},
         "gpu_launches": prof["launches"],
         "roofline": roof,
+        "roofline_by_phase": phases,
         "kernel_ms": {k: round(prof[k]["ms"] / args.steps, 3) for k in kinds if prof[k]["count"]},
     }
 
@@ -470,7 +497,8 @@ def run_mixed_suite(pkg, cu, ctx, args):
             X64 = X.copy()
         be = max(pkg_backward_error(A, X[:, j], B[:, j]) for j in range(nrhs))
         out[label] = {"ms_per_solve_set": ms, "solves_per_s": nrhs / (ms / 1000), "backward_error": be,
-                      "forward_error_vs_fp64": _forward_error(X, X64), "stats": st, "kernel_ms": kms}
+                      "forward_error_vs_fp64": _forward_error(X, X64), "stats": st, "kernel_ms": kms,
+                      "getrf_roofline": getrf_phase_roofline(kms, n, prec, args)}
         f.close()
     for label in ("fp32_ir", "bf16_ir", "fp16_ir"):
         out["speedup_%s_vs_fp64" % label] = out[label]["solves_per_s"] / out["fp64_plain"]["solves_per_s"]
@@ -575,10 +603,13 @@ def run_batched_suite(pkg, cu, ctx, args):
             n = int(sizes[i])
             Ai = A[a_off[i]:a_off[i] + n * n].reshape(n, n, order="F")
             worst = max(worst, pkg_backward_error(Ai, X[b_off[i]:b_off[i] + n], b[b_off[i]:b_off[i] + n]) / n)
-        out[label] = {"ms_per_batch": ms, "solves_per_s": len(sizes) / (ms / 1000.0),
-                      "gflops": out["lu_flops"] / (ms / 1000.0) / 1e9,
+        gf = out["lu_flops"] / (ms / 1000.0) / 1e9
+        out[label] = {"ms_per_batch": ms, "solves_per_s": len(sizes) / (ms / 1000.0), "gflops": gf,
                       "max_backward_error_over_n_eps": worst / EPS64,
                       "failed_info": int((info != 0).sum())}
+        pk = getattr(args, "peak_fp64", None)
+        if prec == 0 and pk:
+            out[label]["frac_of_fp64_peak"] = gf / (pk * 1000.0)
         if prec != 0:  # refinement corrections per system; -1 = re-solved by the FP64 kernel
             its = np.zeros(len(sz), dtype=np.int32)
             if lib.gblu_batch_iterations(ctx.handle, h, its.ctypes.data) == 0:
@@ -603,6 +634,29 @@ def run_batched_suite(pkg, cu, ctx, args):
 
 def pkg_lu_flops(n):
     return 2.0 * n ** 3 / 3.0 + 2.0 * n * n
+
+
+def getrf_flops(n):
+    """LAPACK's operation count of a square getrf."""
+    return 2.0 * n ** 3 / 3.0 - n * n / 2.0 - n / 6.0
+
+
+def getrf_phase_roofline(kms, n, prec, args):
+    """Fraction of the peak reached by the factorization phase of a mixed-suite
+    run (its kernel split comes from one extra run with per-launch events)."""
+    ms = sum(kms.get(k, 0.0) for k in ("gemm", "panel", "laswp", "trsm", "perm"))
+    if ms <= 0:
+        return None
+    tf = getrf_flops(n) / (ms / 1e3) / 1e12
+    if prec in ("bf16", "fp16"):
+        peak, src = measured_peaks().get("bf16_tflops"), "MEASURED_PEAKS.json bf16_tflops (tensor, burst)"
+    elif prec == "fp64":
+        peak, src = getattr(args, "peak_fp64", None), FP64_PEAK_SOURCE
+    else:
+        return {"achieved": tf, "unit": "TFLOP/s", "ms": ms, "peak": None,
+                "note": "FP32 SIMT update: no measured FP32 peak"}
+    return {"achieved": tf, "unit": "TFLOP/s", "ms": ms, "peak": peak, "peak_source": src,
+            "frac": tf / peak if peak else None}
 
 
 def run_serving_suite(pkg, cu, ctx, args):

@@ -1,6 +1,8 @@
-// FP64 fused-multiply-add throughput of the device, measured (not assumed):
-// the roofline denominator for the FP64 trailing update, which runs on the
-// FP64 pipe (tcgen05 has no FP64 kind).  Registers only; one store per thread.
+// FP64 fused-multiply-add throughput of a register-only loop, reported beside
+// the FP64 roofline fractions (the FP64 trailing update runs on the FP64 pipe;
+// tcgen05 has no FP64 kind).  On GB300 such loops top out near 1.0-1.1
+// TFLOP/s, below what a DFMA GEMM reaches, so the fractions use the nominal
+// rate.  Registers only; one store per thread.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
