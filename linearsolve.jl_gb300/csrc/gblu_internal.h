@@ -72,7 +72,7 @@ struct GetrfPlan {
   PanelSlots<T> slots{};
   int panel_width = 32;      // leaf width of the recursion
   int panel_ctas = 0;        // CTAs of the cooperative panel kernel (0: auto)
-  int trsm_base = 64;        // base size of the recursive TRSM
+  int trsm_base = 128;       // base size of the recursive TRSM
   bool use_cluster_panel = true;  // DSMEM cluster panel when the panel fits
   bool use_reg_panel = true;      // register-resident cluster panel when the panel fits
   // FP32 working matrix only: trailing updates on tcgen05 with 16-bit operands

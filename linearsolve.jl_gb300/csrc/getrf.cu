@@ -643,39 +643,60 @@ laswp_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t ncols_total
 }
 
 // ---------------------------------------------------------------------------
-// Unit-lower TRSM base case: B[0:k, cols] := L \ B with L = k x k (k <= 64)
-// held in shared memory.  One warp per right-hand-side column: lane l holds
-// rows l and l + 32 in registers; x_kk is broadcast with a shuffle and every
-// row below it is updated, kk ascending (blocked_lufact.jl:146-178 order).
-constexpr int kTrsmMax = 64;
-constexpr int kTrsmWarps = 8;
+// Unit-lower TRSM base case: B[0:k, cols] := L \ B with L = k x k (k <= KM,
+// KM = 64 or 128) held in shared memory.  One warp per right-hand-side
+// column: lane l holds rows l, l + 32, ... in registers; x_kk is broadcast
+// with a shuffle and every row below it is updated, kk ascending
+// (blocked_lufact.jl:146-178 order).  Row blocks of 32 that are already
+// final are skipped with a warp-uniform branch, so finished rows cost no
+// (FP64) instructions.
+constexpr int kTrsmMax = 128;
+// warps per CTA: one CTA holds the L block; the FP32 128-row variant runs
+// more columns per CTA, while FP64 keeps more CTAs (each SM's FP64 pipe is
+// the limit, so the columns should spread over as many SMs as possible)
+template <typename T, int KM>
+__host__ __device__ constexpr int trsm_warps() { return (sizeof(T) == 4 && KM == 128) ? 16 : 8; }
 
-template <typename T>
-__global__ void __launch_bounds__(kTrsmWarps * 32)
+template <typename T, int KM>
+__global__ void __launch_bounds__(trsm_warps<T, KM>() * 32)
 trsm_lunit_kernel(const T* __restrict__ L, int64_t ldl, int k, T* __restrict__ B,
                   int64_t ldb, int64_t ncols) {
-  __shared__ T sL[kTrsmMax][kTrsmMax + 1];  // sL[c][r] = L[r, c]
+  constexpr int RPL = KM / 32;  // rows per lane
+  constexpr int kTrsmWarps = trsm_warps<T, KM>();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T(*sL)[KM + 1] = reinterpret_cast<T(*)[KM + 1]>(smem_raw);  // sL[c][r] = L[r, c]
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int idx = threadIdx.x; idx < k * k; idx += blockDim.x) {
-    int c = idx / k, r = idx - c * k;
-    sL[c][r] = L[r + (int64_t)c * ldl];
-  }
+  for (int c = warp; c < k; c += kTrsmWarps)
+    for (int r = lane; r < k; r += 32) sL[c][r] = L[r + (int64_t)c * ldl];
   __syncthreads();
-  const int r0 = lane, r1 = lane + 32;
   for (int64_t col = (int64_t)blockIdx.x * kTrsmWarps + warp; col < ncols;
        col += (int64_t)gridDim.x * kTrsmWarps) {
     T* b = B + col * ldb;
-    T b0 = r0 < k ? b[r0] : T(0);
-    T b1 = r1 < k ? b[r1] : T(0);
+    T v[RPL];
+#pragma unroll
+    for (int q = 0; q < RPL; ++q) v[q] = lane + 32 * q < k ? b[lane + 32 * q] : T(0);
     for (int kk = 0; kk < k - 1; ++kk) {
-      const T xk = __shfl_sync(0xffffffffu, kk < 32 ? b0 : b1, kk & 31);
-      if (r0 > kk && r0 < k) b0 = fma(-sL[kk][r0], xk, b0);
-      if (r1 > kk && r1 < k) b1 = fma(-sL[kk][r1], xk, b1);
+      const int qk = kk >> 5;
+      T src = v[0];
+#pragma unroll
+      for (int q = 1; q < RPL; ++q)
+        if (qk == q) src = v[q];
+      const T xk = __shfl_sync(0xffffffffu, src, kk & 31);
+#pragma unroll
+      for (int q = 0; q < RPL; ++q) {
+        if (q < qk) continue;  // rows 32q..32q+31 are final
+        const int r = lane + 32 * q;
+        if (r > kk && r < k) v[q] = fma(-sL[kk][r], xk, v[q]);
+      }
     }
-    if (r0 < k) b[r0] = b0;
-    if (r1 < k) b[r1] = b1;
+#pragma unroll
+    for (int q = 0; q < RPL; ++q)
+      if (lane + 32 * q < k) b[lane + 32 * q] = v[q];
   }
 }
+
+template <typename T, int KM>
+constexpr size_t trsm_smem() { return (size_t)KM * (KM + 1) * sizeof(T); }
 
 // ---------------------------------------------------------------------------
 // SIMT GEMM update C -= A * B (column-major), every C element updated by
@@ -1024,7 +1045,9 @@ struct Driver {
             T* C, int64_t ldc) {
     if (M <= 0 || N <= 0 || K <= 0) return;
     if constexpr (std::is_same<T, float>::value) {
-      if (p.tc_mode != 0 && M >= 128 && N >= 128 && K >= 64 &&
+      // the tensor-core path costs two conversion launches besides the GEMM:
+      // updates with fewer than 256 rows or columns stay on the SIMT kernel
+      if (p.tc_mode != 0 && M >= 256 && N >= 256 && K >= 64 &&
           tc_work_bytes(M, N, K) <= p.tc_work_bytes) {
         check(tc_gemm_sub(p.tc_mode, M, N, K, A, lda, B, ldb, C, ldc, p.tc_work, &p.scratch->error, s));
         return;
@@ -1041,11 +1064,15 @@ struct Driver {
     if (k <= 0 || ncols <= 0) return;
     if (k <= p.trsm_base && k <= kTrsmMax) {
       const DeviceInfo& di = device_info(device);
-      unsigned blocks = (unsigned)std::min<int64_t>((ncols + kTrsmWarps - 1) / kTrsmWarps,
-                                                    (int64_t)di.num_sms * 8);
+      const int warps = k <= 64 ? trsm_warps<T, 64>() : trsm_warps<T, 128>();
+      unsigned blocks = (unsigned)std::min<int64_t>((ncols + warps - 1) / warps, (int64_t)di.num_sms * 8);
       LaunchScope ls(K_TRSM, (double)k * (k - 1) * ncols, (2.0 * k * ncols + (double)k * k) * sizeof(T), s);
-      trsm_lunit_kernel<T><<<blocks, kTrsmWarps * 32, 0, s>>>(at(r0, r0), p.lda, (int)k,
-                                                              at(r0, bc0), p.lda, ncols);
+      if (k <= 64)
+        trsm_lunit_kernel<T, 64><<<blocks, warps * 32, trsm_smem<T, 64>(), s>>>(
+            at(r0, r0), p.lda, (int)k, at(r0, bc0), p.lda, ncols);
+      else
+        trsm_lunit_kernel<T, 128><<<blocks, warps * 32, trsm_smem<T, 128>(), s>>>(
+            at(r0, r0), p.lda, (int)k, at(r0, bc0), p.lda, ncols);
       check(cudaGetLastError());
       return;
     }
@@ -1102,6 +1129,10 @@ void getrf_configure(int device) {
   cudaFuncSetAttribute(panel_reg_kernel<double, 1>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
   cudaFuncSetAttribute(panel_reg_kernel<float, 1>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
   cudaFuncSetAttribute(panel_reg_kernel<float, 2>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  cudaFuncSetAttribute(trsm_lunit_kernel<double, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)trsm_smem<double, 128>());
+  cudaFuncSetAttribute(trsm_lunit_kernel<float, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)trsm_smem<float, 128>());
   cudaFuncSetAttribute(perm_from_ipiv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (kPermSmemMax + kPermChunk) * (int)sizeof(int32_t));
   getrs_configure(device);
