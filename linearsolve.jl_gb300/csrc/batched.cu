@@ -182,6 +182,11 @@ __device__ int64_t factor_system(T* __restrict__ A, int n, int32_t* __restrict__
       const T inv = nz ? T(1) / piv : T(0);
 #pragma unroll
       for (int m = 0; m < RPT; ++m) {
+        // row slot m of the CTA holds rows NT*m .. NT*m+NT-1: skip it with a
+        // block-uniform branch when all of them lie above the diagonal row (no
+        // interchange, no update) or outside the system (predicated-off FP64
+        // instructions still occupy the FP64 pipe)
+        if (NT * m + NT - 1 < col || NT * m >= n) continue;
         const int i = tid + NT * m;
         if (swap && i == col) {
 #pragma unroll
@@ -197,8 +202,10 @@ __device__ int64_t factor_system(T* __restrict__ A, int n, int32_t* __restrict__
           if (nz) l *= inv;
           pr[m][j] = l;
 #pragma unroll
-          for (int jj = j + 1; jj < NB; ++jj)
-            if (jj < kb) pr[m][jj] = fma(-l, src[jj], pr[m][jj]);
+          for (int jj = j + 1; jj < NB; ++jj) {
+            if (jj >= kb) break;
+            pr[m][jj] = fma(-l, src[jj], pr[m][jj]);
+          }
         }
       }
     }
@@ -304,10 +311,11 @@ __device__ int64_t factor_system(T* __restrict__ A, int n, int32_t* __restrict__
 #pragma unroll
           for (int q = 0; q < CN; ++q) uv[q] = sm.U[jj * kBatchUStride + cc + q];
 #pragma unroll
-          for (int r = 0; r < RM; ++r)
-            if (r < rg)
+          for (int r = 0; r < RM; ++r) {
+            if (r >= rg) break;  // warp-uniform: row groups below n only
 #pragma unroll
-              for (int q = 0; q < CN; ++q) acc[r][q] = fma(-lv[r], uv[q], acc[r][q]);
+            for (int q = 0; q < CN; ++q) acc[r][q] = fma(-lv[r], uv[q], acc[r][q]);
+          }
         }
 #pragma unroll
         for (int r = 0; r < RM; ++r)
