@@ -504,6 +504,7 @@ batch_mixed_kernel(BatchDev d, const double* __restrict__ A64, float* __restrict
     for (int j = 0; j < n; ++j) {
 #pragma unroll
       for (int m = 0; m < RPT; ++m) {
+        if (NT * m >= n) break;  // block-uniform: no rows in this slot
         const int i = threadIdx.x + NT * m;
         if (i < n) {
           const double a = A[i + (int64_t)j * n];
