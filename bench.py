@@ -719,7 +719,7 @@ def main():
                          "auto = mixed,batched,serving on one GPU, none on several")
     ap.add_argument("--batch-count", type=int, default=20000)
     ap.add_argument("--only-suite", action="store_true")
-    ap.add_argument("--serve-requests", type=int, default=300)
+    ap.add_argument("--serve-requests", type=int, default=1000)
     ap.add_argument("--mixed-n", type=int, default=16384)
     ap.add_argument("--serve-rates", type=float, nargs="*", default=[100.0, 400.0, 0.0])
     args = ap.parse_args()
