@@ -185,17 +185,20 @@ def profile_traffic(kind: str):
 # ---------------------------------------------------------------------------
 # CPU reference arm
 
-def cpu_lapack_steps(A, B, steps: int):
-    """LAPACK getrf + one getrs per RHS column (the cached-solve pattern)."""
+def cpu_lapack_steps(A, B, steps: int, want_x: bool = False):
+    """LAPACK getrf + one getrs per RHS column (the cached-solve pattern);
+    with want_x also the solutions of the last step."""
     import oracle
     times = []
+    X = None
     for _ in range(steps):
         t0 = time.perf_counter()
         LU, ipiv, info = oracle.lapack_getrf(A)
-        for j in range(B.shape[1]):
-            oracle.lapack_getrs(LU, ipiv, B[:, j:j + 1])
+        cols = [oracle.lapack_getrs(LU, ipiv, B[:, j:j + 1]) for j in range(B.shape[1])]
         times.append(time.perf_counter() - t0)
-    return times
+        if want_x:
+            X = np.concatenate([np.asarray(c).reshape(-1, 1) for c in cols], axis=1)
+    return (times, X) if want_x else times
 
 
 def run_reference(args, rank, world):
@@ -399,8 +402,10 @@ def run_gpu(args, rank, world, local):
 
     if rank == 0 and not args.no_cpu:
         # bounded CPU sample of the same workload on this host
-        ts = cpu_lapack_steps(A, B, args.cpu_steps)
+        ts, Xl = cpu_lapack_steps(A, B, args.cpu_steps, want_x=True)
         cv = args.cpu_steps * nrhs / sum(ts)
+        if Xl is not None:  # forward error of the GPU solutions against LAPACK's
+            line["accuracy"]["forward_error_vs_lapack"] = float(np.abs(X - Xl).max() / np.abs(Xl).max())
         line["cpu_baseline"] = {
             "value": cv, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
             "sample": f"{args.cpu_steps} full steps: scipy.linalg.lapack dgetrf + {nrhs} dgetrs (OpenBLAS, "
