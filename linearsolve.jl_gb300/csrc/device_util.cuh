@@ -37,6 +37,16 @@ __device__ __forceinline__ int ld_volatile_i32(const int* p) {
   return *(volatile const int*)p;
 }
 
+// The two halves of a cluster barrier: shared-memory writes made before
+// cluster_arrive() are visible to every CTA of the cluster after its
+// cluster_wait(); work placed between the two overlaps the barrier.
+__device__ __forceinline__ void cluster_arrive() {
+  asm volatile("barrier.cluster.arrive.release;" ::: "memory");
+}
+__device__ __forceinline__ void cluster_wait() {
+  asm volatile("barrier.cluster.wait.acquire;" ::: "memory");
+}
+
 // Grid-wide barrier for cooperative launches.  Arrival counter is
 // s->barrier (zeroed before the launch); `target` = (#barriers so far) * G.
 // Returns false (on every thread of the CTA) when the wait timed out or another
@@ -100,28 +110,33 @@ struct PivKey<float> {
 // Warp-wide pivot choice: every lane holds a candidate (key v, row g; g < 0 =
 // none); on return every lane holds the winner (largest key, then smallest
 // row) and `src` = the lane it came from (-1 when no lane has a candidate).
-// 32-bit keys use the warp reduction instructions (one max, one min); 64-bit
-// keys a shuffle tree.  Rows are unique across lanes.
+// Built from the warp reduction instructions: one max per 32-bit half of the
+// key (the low half compared only among lanes holding the largest high
+// half), one min over the rows holding the largest key, one ballot.  Rows
+// are unique across lanes.
 template <typename K>
 __device__ __forceinline__ void warp_pivot_choice(K& v, int& g, int& src) {
-  const int lane = threadIdx.x & 31;
+  constexpr unsigned kAll = 0xffffffffu;
   if constexpr (sizeof(K) == 4) {
-    const K mk = __reduce_max_sync(0xffffffffu, (unsigned)v);
-    const bool mine = g >= 0 && v == mk;
-    const unsigned gmin = __reduce_min_sync(0xffffffffu, mine ? (unsigned)g : 0xffffffffu);
-    const unsigned who = __ballot_sync(0xffffffffu, mine && (unsigned)g == gmin);
+    const unsigned vm = g >= 0 ? (unsigned)v : 0u;
+    const unsigned mk = __reduce_max_sync(kAll, vm);
+    const bool mine = g >= 0 && vm == mk;
+    const unsigned gmin = __reduce_min_sync(kAll, mine ? (unsigned)g : 0xffffffffu);
+    const unsigned who = __ballot_sync(kAll, mine && (unsigned)g == gmin);
     src = who ? __ffs(who) - 1 : -1;
-    v = mk;
+    v = who ? (K)mk : K(0);
     g = who ? (int)gmin : -1;
   } else {
-    src = g >= 0 ? lane : -1;
-    for (int off = 16; off; off >>= 1) {
-      const K ov = __shfl_xor_sync(0xffffffffu, v, off);
-      const int og = __shfl_xor_sync(0xffffffffu, g, off);
-      const int os = __shfl_xor_sync(0xffffffffu, src, off);
-      const bool better = og >= 0 && (g < 0 || ov > v || (ov == v && og < g));
-      if (better) { v = ov; g = og; src = os; }
-    }
+    const unsigned long long vm = g >= 0 ? (unsigned long long)v : 0ull;
+    const unsigned hi = (unsigned)(vm >> 32), lo = (unsigned)vm;
+    const unsigned mh = __reduce_max_sync(kAll, hi);
+    const unsigned ml = __reduce_max_sync(kAll, hi == mh ? lo : 0u);
+    const bool mine = g >= 0 && hi == mh && lo == ml;
+    const unsigned gmin = __reduce_min_sync(kAll, mine ? (unsigned)g : 0xffffffffu);
+    const unsigned who = __ballot_sync(kAll, mine && (unsigned)g == gmin);
+    src = who ? __ffs(who) - 1 : -1;
+    v = who ? (K)(((unsigned long long)mh << 32) | ml) : K(0);
+    g = who ? (int)gmin : -1;
   }
 }
 

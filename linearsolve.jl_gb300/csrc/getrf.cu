@@ -337,22 +337,6 @@ panel_cluster_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int 
   cluster.sync();  // no CTA leaves while another may still read its shared memory
 }
 
-// ---------------------------------------------------------------------------
-// Register panel kernel: the same getf2 on rows [c0, m) x columns [c0, c0+w)
-// with every panel row held in registers by one thread for the whole leaf
-// (row base + tid + NT * r of CTA `cta`, r < RPT, the CTA holding R rows).
-// The registers rotate by one slot per column, identically in every thread,
-// so the current column is always slot 0 and the column loop is a plain loop
-// with one small body; rows are exchanged in slot order (16-byte shared
-// memory accesses, no index arithmetic).  Per column: each warp reduces its
-// candidate (integer keys of |a|) and the owners publish the candidate row
-// and the diagonal row; one cluster barrier; warp 0 of every CTA reduces all
-// warp candidates of the cluster and fetches the pivot row through
-// distributed shared memory; one CTA barrier; every thread interchanges,
-// scales and updates its own rows.  The per-element arithmetic is
-// panel_kernel's.
-constexpr int kRegPanelThreads = 512;
-
 template <typename T>
 struct Vec16;  // 16-byte vector of T
 template <>
@@ -388,6 +372,63 @@ __device__ __forceinline__ void row_load(T (&dst)[W], const T* src) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Register panel kernel: the same getf2 on rows [c0, m) x columns [c0, c0+w)
+// with every panel row held in registers by one thread for the whole leaf
+// (row base + tid + NT * r of CTA `cta`, r < RPT, the CTA holding R rows).
+// The registers rotate by one slot per column, identically in every thread,
+// so the current column is always slot 0 and the column loop is a plain loop
+// with one small body; rows are exchanged in slot order (16-byte shared
+// memory accesses, no index arithmetic).
+//
+// The step of column k is arranged so that the rank-1 update overlaps the
+// cluster barrier.  After the interchange and scaling of column k, each
+// thread updates only slot 1 (column k+1); each warp reduces its column-k+1
+// candidate and publishes it with the candidate row and the diagonal row in
+// their partly updated form (slot 0 = the multiplier l, slot 1 updated,
+// slots 2.. not yet); the last warp of the CTA to publish reduces the CTA's
+// warp candidates to one; every thread arrives at the cluster barrier and
+// runs the rest of the update (slots 2..) before the wait.  After the wait,
+// warp 0 of every CTA reads the G CTA candidates (one 16-byte load of
+// distributed shared memory per CTA), picks the winner, fetches the pivot row
+// and the diagonal row together and finishes their update itself with the
+// same fma(-l, u, a) on the same operands the owner uses, so the fetched
+// rows are bit-identical to the owners' registers; 1 / pivot is started from
+// the winning key (the bit pattern of |pivot|) while the rows are in flight.
+// One CTA barrier hands the pivot row to every thread.  Warps that hold no
+// rows skip the arithmetic (a predicated-off FP64 instruction still occupies
+// the FP64 pipe).  The per-element arithmetic is panel_kernel's.
+constexpr int kRegPanelThreads = 512;
+
+// A CTA's pivot candidate as one 16-byte word: key, row (-1 = none), warp.
+template <typename K>
+__device__ __forceinline__ int4 cand_pack(K key, int row, int warp) {
+  if constexpr (sizeof(K) == 4) return make_int4((int)key, row, warp, 0);
+  else return make_int4((int)(unsigned)key, (int)(unsigned)(key >> 32), row, warp);
+}
+template <typename K>
+__device__ __forceinline__ void cand_unpack(const int4& c, K& key, int& row, int& warp) {
+  if constexpr (sizeof(K) == 4) { key = (K)(unsigned)c.x; row = c.y; warp = c.z; }
+  else { key = ((K)(unsigned)c.y << 32) | (K)(unsigned)c.x; row = c.z; warp = c.w; }
+}
+
+// The value whose bit pattern is the key (|a| for a key of a)
+template <typename T>
+__device__ __forceinline__ T key_magnitude(typename PivKey<T>::K key) {
+  if constexpr (sizeof(T) == 4) return __uint_as_float(key);
+  else return __longlong_as_double((long long)key);
+}
+
+// x with the sign of s (bit operations only)
+template <typename T>
+__device__ __forceinline__ T with_sign_of(T x, T s) {
+  if constexpr (sizeof(T) == 4)
+    return __uint_as_float(__float_as_uint(x) ^ (__float_as_uint(s) & 0x80000000u));
+  else
+    return __longlong_as_double(__double_as_longlong(x) ^
+                                (__double_as_longlong(s) & (long long)0x8000000000000000ull));
+}
+
 template <typename T, int RPT>
 __global__ void __launch_bounds__(kRegPanelThreads, 1)
 panel_reg_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w,
@@ -395,14 +436,18 @@ panel_reg_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w,
   namespace cg = cooperative_groups;
   using K = typename PivKey<T>::K;
   using VT = Vec16<T>;
+  constexpr unsigned kAll = 0xffffffffu;
   cg::cluster_group cluster = cg::this_cluster();
   constexpr int NT = kRegPanelThreads, NW = NT / 32, W = kPanelMaxW;
-  __shared__ __align__(16) T s_crowv[2][NW][W];  // each warp's candidate row, slot order
-  __shared__ __align__(16) T s_diagv[2][W];      // the diagonal row (owner CTA), slot order
-  __shared__ __align__(16) T s_piv[W];           // the pivot row, slot order
+  // [b]: candidates of column k live in buffer k & 1
+  __shared__ __align__(16) T s_crowv[2][NW][W];  // each warp's candidate row (published form)
+  __shared__ __align__(16) T s_diagv[2][W];      // the diagonal row (owner CTA, published form)
+  __shared__ __align__(16) T s_piv[2][W];        // the pivot row of column k, slot order of step k
   __shared__ __align__(16) T s_old[W];           // the old diagonal row, for the pivot row's owner
+  __shared__ __align__(16) int4 s_cta[2];        // the CTA's candidate (cand_pack)
   __shared__ K s_cval[2][NW];
   __shared__ int s_crow[2][NW];
+  __shared__ unsigned s_cnt[2];                  // warps that published into buffer b
   __shared__ int s_p;
   __shared__ T s_inv;
 
@@ -411,7 +456,7 @@ panel_reg_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w,
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int64_t base = c0 + (int64_t)cta * R;
   const int nloc = (int)max((int64_t)0, min((int64_t)R, m - base));
-  const int ncand = G * NW;
+  const bool warp_rows = warp * 32 < nloc;  // this warp holds at least one row
 
   T pr[RPT][W];  // slot j: column (k + j) mod 32 at step k
 #pragma unroll
@@ -420,84 +465,110 @@ panel_reg_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w,
 #pragma unroll
     for (int j = 0; j < W; ++j) pr[r][j] = (i < nloc && j < w) ? A[(base + i) + (c0 + j) * lda] : T(0);
   }
+  if (tid < 2) s_cnt[tid] = 0;
+  __syncthreads();
   int64_t info_local = 0;
 
-  for (int k = 0; k < w; ++k) {
-    const int64_t d = c0 + k;
-    const int buf = k & 1;
-    // 1. this warp's candidate: first row of max |a| among rows >= d (NaN ignored)
+  // Candidates of the column in slot S among rows >= dn into buffer pb: each
+  // warp's first row of max |a| (NaN ignored) with its row and the diagonal
+  // row dn; the last warp to publish reduces them to the CTA's candidate;
+  // then arrive at the cluster barrier.
+  auto publish = [&](auto slot_c, int64_t dn, int pb) {
+    constexpr int S = decltype(slot_c)::value;
     K bv = 0;
     int bg = -1;
 #pragma unroll
     for (int r = 0; r < RPT; ++r) {
       const int i = tid + NT * r;
-      const K v = PivKey<T>::of(pr[r][0]);
-      if (i < nloc && base + i >= d && v > bv) { bv = v; bg = (int)(base + i); }
+      const K v = PivKey<T>::of(pr[r][S]);
+      if (i < nloc && base + i >= dn && v > bv) { bv = v; bg = (int)(base + i); }
     }
     {
       int src;
       warp_pivot_choice(bv, bg, src);
     }
-    if (lane == 0) { s_cval[buf][warp] = bv; s_crow[buf][warp] = bg; }
 #pragma unroll
     for (int r = 0; r < RPT; ++r) {
       const int64_t g = base + tid + NT * r;
-      if (g == bg) row_store<T, W>(s_crowv[buf][warp], pr[r]);
-      if (g == d && tid + NT * r < nloc) row_store<T, W>(s_diagv[buf], pr[r]);
+      if (g == bg) row_store<T, W>(s_crowv[pb][warp], pr[r]);
+      if (g == dn && tid + NT * r < nloc) row_store<T, W>(s_diagv[pb], pr[r]);
     }
-    cluster.sync();  // publishes every CTA's slots of column k (release/acquire)
-    // 2. warp 0: the winner over every warp of the cluster, the pivot row and,
+    unsigned last = 0;
+    if (lane == 0) {
+      s_cval[pb][warp] = bv;
+      s_crow[pb][warp] = bg;
+      __threadfence_block();
+      last = atomicAdd(&s_cnt[pb], 1u) == NW - 1;
+    }
+    if (__shfl_sync(kAll, last, 0)) {
+      __threadfence_block();
+      K v = lane < NW ? s_cval[pb][lane] : K(0);
+      int g = lane < NW ? s_crow[pb][lane] : -1;
+      int wsrc;
+      warp_pivot_choice(v, g, wsrc);
+      if (lane == 0) {
+        s_cta[pb] = cand_pack<K>(v, g, wsrc);
+        s_cnt[pb] = 0;
+      }
+    }
+    cluster_arrive();
+  };
+
+  publish(std::integral_constant<int, 0>{}, c0, 0);  // column 0: the rows as loaded
+
+  for (int k = 0; k < w; ++k) {
+    const int64_t d = c0 + k;
+    const int buf = k & 1;
+    cluster_wait();  // every CTA's candidate of column k is published
+    // 1. warp 0: the winner over the CTAs of the cluster, the pivot row and,
     //    for the pivot row's CTA, the old diagonal row
     if (warp == 0) {
-      // every warp's slot of every CTA (slot c: CTA c / NW, warp c % NW; warps
-      // without rows hold row -1), all loads issued before any comparison
-      constexpr int QMAX = 16 * NW / 32;
-      K cv[QMAX];
-      int cr[QMAX];
-#pragma unroll
-      for (int q = 0; q < QMAX; ++q) {
-        const int c = lane + 32 * q;
-        cv[q] = 0;
-        cr[q] = -1;
-        if (c < ncand) {
-          cv[q] = *cluster.map_shared_rank(&s_cval[buf][c % NW], c / NW);
-          cr[q] = *cluster.map_shared_rank(&s_crow[buf][c % NW], c / NW);
-        }
-      }
       K v = 0;
-      int g = -1, e = -1;
-#pragma unroll
-      for (int q = 0; q < QMAX; ++q)
-        if (cand_better(cv[q], (int64_t)cr[q], v, (int64_t)g)) { v = cv[q]; g = cr[q]; e = lane + 32 * q; }
-      {
-        int src;
-        warp_pivot_choice(v, g, src);
-        e = __shfl_sync(0xffffffffu, e, src < 0 ? 0 : src);
+      int g = -1, ew = 0;
+      if (lane < G) {
+        const int4 c = *cluster.map_shared_rank(&s_cta[buf], lane);
+        cand_unpack<K>(c, v, g, ew);
       }
+      int ec;  // the winning CTA
+      warp_pivot_choice(v, g, ec);
+      ew = __shfl_sync(kAll, ew, ec < 0 ? 0 : ec);
       const int64_t p = g < 0 ? d : (int64_t)g;  // kp = k when amax == 0
       const int downer = (int)((d - c0) / R);
-      const T dv = *cluster.map_shared_rank(&s_diagv[buf][lane], downer);
-      if (p == d) {
-        s_piv[lane] = dv;
-      } else {
-        s_piv[lane] = *cluster.map_shared_rank(&s_crowv[buf][e % NW][lane], e / NW);
-        if (p >= base && p < base + nloc) s_old[lane] = dv;
+      // published rows are in the slot order of step k-1: lane j takes slot
+      // j + 1 and finishes its step-(k-1) update (slots 2 .. w-k of step k-1)
+      const int js = k > 0 ? ((lane + 1) & (W - 1)) : lane;
+      const T* dsrc = cluster.map_shared_rank(&s_diagv[buf][js], downer);
+      const T* psrc = p != d ? cluster.map_shared_rank(&s_crowv[buf][ew][js], ec) : dsrc;
+      T dv = *dsrc;
+      T pv = *psrc;
+      // |pivot| is the winning key: start 1 / |pivot| while the rows load
+      const T inv_mag = T(1) / key_magnitude<T>(g >= 0 ? v : K(1));
+      if (k > 0) {
+        const T u = s_piv[buf ^ 1][js];
+        const T ld = __shfl_sync(kAll, dv, W - 1);  // slot 0 of step k-1: the multiplier
+        const T lp = __shfl_sync(kAll, pv, W - 1);
+        if (lane >= 1 && lane < w - k) {
+          dv = fma(-ld, u, dv);
+          pv = fma(-lp, u, pv);
+        }
       }
+      s_piv[buf][lane] = pv;
+      if (p != d && p >= base && p < base + nloc) s_old[lane] = dv;
       if (lane == 0) {
         s_p = (int)p;
-        const T pv = s_piv[0];  // written above by this lane
-        s_inv = PivKey<T>::nonzero(pv) ? T(1) / pv : T(0);
+        // no candidate: the pivot is the diagonal entry, zero or NaN
+        s_inv = g >= 0 ? with_sign_of(inv_mag, pv) : (PivKey<T>::nonzero(pv) ? T(1) / pv : T(0));
       }
     }
     __syncthreads();
     const int64_t p = s_p;
-    const T piv = s_piv[0];
+    const T piv = s_piv[buf][0];
     const bool nz = PivKey<T>::nonzero(piv);
     if (cta == 0 && tid == 0) {
       ipiv[d] = p + 1;
       if (!nz && info_local == 0) info_local = d + 1;
     }
-    // 3. interchange (nonzero pivot only), scale, rank-1 update, rotate
+    // 2. interchange (nonzero pivot only) and scale
     const bool swap = nz && p != d;
     const T inv = s_inv;  // 1 / piv, computed once by warp 0
     const int lim = w - k;  // slots 1..lim-1 hold columns k+1..w-1
@@ -509,39 +580,57 @@ panel_reg_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w,
       const int64_t gi = base + i;
       upd[r] = i < nloc && gi > d;
       if (i < nloc && swap) {
-        if (gi == d) row_load<T, W>(pr[r], s_piv);
+        if (gi == d) row_load<T, W>(pr[r], s_piv[buf]);
         else if (gi == p) row_load<T, W>(pr[r], s_old);
       }
       l[r] = pr[r][0];
-      if (upd[r] && nz) l[r] *= inv;
-      if (upd[r]) pr[r][0] = l[r];
     }
-    if constexpr (sizeof(T) == 4) {
-      // FP32: predicated FMAs over all slots (no branches)
+    if (warp_rows) {
 #pragma unroll
-      for (int q = 0; q < W / VT::N; ++q) {
-        const typename VT::V pv = reinterpret_cast<const typename VT::V*>(s_piv)[q];
+      for (int r = 0; r < RPT; ++r) {
+        if (upd[r] && nz) l[r] *= inv;
+        if (upd[r]) pr[r][0] = l[r];
+      }
+    }
+    if (k + 1 < w) {
+      // 3. slot 1 first, publish the candidates of column k + 1, then the
+      //    rest of the rank-1 update while the cluster barrier completes
+      if (warp_rows) {
+        const T u1 = s_piv[buf][1];
 #pragma unroll
-        for (int e = 0; e < VT::N; ++e) {
-          const int j = q * VT::N + e;
-          if (j >= 1 && j < lim) {
-            const T u = VT::get(pv, e);
+        for (int r = 0; r < RPT; ++r)
+          if (upd[r]) pr[r][1] = fma(-l[r], u1, pr[r][1]);
+      }
+      publish(std::integral_constant<int, 1>{}, d + 1, buf ^ 1);
+      if (warp_rows) {
+        if constexpr (sizeof(T) == 4) {
+          // FP32: predicated FMAs over all slots (no branches)
+#pragma unroll
+          for (int q = 0; q < W / VT::N; ++q) {
+            const typename VT::V pv = reinterpret_cast<const typename VT::V*>(s_piv[buf])[q];
+#pragma unroll
+            for (int e = 0; e < VT::N; ++e) {
+              const int j = q * VT::N + e;
+              if (j >= 2 && j < lim) {
+                const T u = VT::get(pv, e);
+#pragma unroll
+                for (int r = 0; r < RPT; ++r)
+                  if (upd[r]) pr[r][j] = fma(-l[r], u, pr[r][j]);
+              }
+            }
+          }
+        } else {
+          // FP64: stop at the last live slot with a uniform branch, so the FP64
+          // pipe only sees the FMAs that do work
+#pragma unroll
+          for (int j = 2; j < W; ++j) {
+            if (j >= lim) break;
+            const T u = s_piv[buf][j];
 #pragma unroll
             for (int r = 0; r < RPT; ++r)
               if (upd[r]) pr[r][j] = fma(-l[r], u, pr[r][j]);
           }
         }
-      }
-    } else {
-      // FP64: stop at the last live slot with a uniform branch, so the FP64
-      // pipe only sees the FMAs that do work
-#pragma unroll
-      for (int j = 1; j < W; ++j) {
-        if (j >= lim) break;
-        const T u = s_piv[j];
-#pragma unroll
-        for (int r = 0; r < RPT; ++r)
-          if (upd[r]) pr[r][j] = fma(-l[r], u, pr[r][j]);
       }
     }
 #pragma unroll
