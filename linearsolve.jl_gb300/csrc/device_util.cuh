@@ -47,6 +47,15 @@ __device__ __forceinline__ void cluster_wait() {
   asm volatile("barrier.cluster.wait.acquire;" ::: "memory");
 }
 
+// Named CTA barrier `id` (1..15) over `nthreads` threads (a multiple of 32):
+// arrive does not wait, sync waits for all nthreads.
+__device__ __forceinline__ void named_bar_arrive(int id, int nthreads) {
+  asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+__device__ __forceinline__ void named_bar_sync(int id, int nthreads) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
 // Grid-wide barrier for cooperative launches.  Arrival counter is
 // s->barrier (zeroed before the launch); `target` = (#barriers so far) * G.
 // Returns false (on every thread of the CTA) when the wait timed out or another

@@ -393,8 +393,9 @@ __device__ __forceinline__ void row_load(T (&dst)[W], const T* src) {
 // distributed shared memory per CTA), picks the winner, fetches the pivot row
 // and the diagonal row together and finishes their update itself with the
 // same fma(-l, u, a) on the same operands the owner uses, so the fetched
-// rows are bit-identical to the owners' registers; 1 / pivot is started from
-// the winning key (the bit pattern of |pivot|) while the rows are in flight.
+// rows are bit-identical to the owners' registers.  Meanwhile warp 1 computes
+// 1 / |candidate| of every CTA candidate from its key (the bit pattern of
+// |a|) and hands the winner's to warp 0 through a named barrier.
 // One CTA barrier hands the pivot row to every thread.  Warps that hold no
 // rows skip the arithmetic (a predicated-off FP64 instruction still occupies
 // the FP64 pipe).  The per-element arithmetic is panel_kernel's.
@@ -448,6 +449,7 @@ panel_reg_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w,
   __shared__ K s_cval[2][NW];
   __shared__ int s_crow[2][NW];
   __shared__ unsigned s_cnt[2];                  // warps that published into buffer b
+  __shared__ T s_rinv[32];                       // 1 / |candidate| of CTA c's candidate
   __shared__ int s_p;
   __shared__ T s_inv;
 
@@ -487,11 +489,25 @@ panel_reg_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w,
       int src;
       warp_pivot_choice(bv, bg, src);
     }
+    // the stores are issued by the owning warp only (a predicated-off store
+    // still occupies the shared-memory pipe)
+    if (bg >= 0) {
+      const int lw = (int)(bg - base);  // the winner's local row
 #pragma unroll
-    for (int r = 0; r < RPT; ++r) {
-      const int64_t g = base + tid + NT * r;
-      if (g == bg) row_store<T, W>(s_crowv[pb][warp], pr[r]);
-      if (g == dn && tid + NT * r < nloc) row_store<T, W>(s_diagv[pb], pr[r]);
+      for (int r = 0; r < RPT; ++r)
+        if (lw >= NT * r && lw < NT * (r + 1)) {
+          if (tid + NT * r == lw) row_store<T, W>(s_crowv[pb][warp], pr[r]);
+        }
+    }
+    {
+      const int64_t ld = dn - base;
+      if (ld >= 0 && ld < nloc && (((int)ld & (NT - 1)) >> 5) == warp) {
+#pragma unroll
+        for (int r = 0; r < RPT; ++r)
+          if (ld >= NT * r && ld < NT * (r + 1)) {
+            if (tid + NT * r == ld) row_store<T, W>(s_diagv[pb], pr[r]);
+          }
+      }
     }
     unsigned last = 0;
     if (lane == 0) {
@@ -541,8 +557,9 @@ panel_reg_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w,
       const T* psrc = p != d ? cluster.map_shared_rank(&s_crowv[buf][ew][js], ec) : dsrc;
       T dv = *dsrc;
       T pv = *psrc;
-      // |pivot| is the winning key: start 1 / |pivot| while the rows load
-      const T inv_mag = T(1) / key_magnitude<T>(g >= 0 ? v : K(1));
+      // 1 / |pivot| from warp 1
+      named_bar_sync(1, 64);
+      const T inv_mag = s_rinv[ec < 0 ? 0 : ec];
       if (k > 0) {
         const T u = s_piv[buf ^ 1][js];
         const T ld = __shfl_sync(kAll, dv, W - 1);  // slot 0 of step k-1: the multiplier
@@ -559,6 +576,19 @@ panel_reg_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w,
         // no candidate: the pivot is the diagonal entry, zero or NaN
         s_inv = g >= 0 ? with_sign_of(inv_mag, pv) : (PivKey<T>::nonzero(pv) ? T(1) / pv : T(0));
       }
+    } else if (warp == 1) {
+      // 1 / |candidate| of every CTA's candidate (its key is the bit pattern
+      // of |a|), beside warp 0's reduction and row loads: the division is a
+      // long dependent sequence
+      K v = 0;
+      int g = -1, ew = 0;
+      if (lane < G) {
+        const int4 c = *cluster.map_shared_rank(&s_cta[buf], lane);
+        cand_unpack<K>(c, v, g, ew);
+      }
+      const T rinv = T(1) / key_magnitude<T>(g >= 0 ? v : K(1));
+      if (lane < G) s_rinv[lane] = rinv;
+      named_bar_arrive(1, 64);
     }
     __syncthreads();
     const int64_t p = s_p;
@@ -574,15 +604,24 @@ panel_reg_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w,
     const int lim = w - k;  // slots 1..lim-1 hold columns k+1..w-1
     T l[RPT];
     bool upd[RPT];
+    if (swap) {
+      // only the warps holding row d or row p load
+      const int64_t ld = d - base, lp = p - base;
+      const bool own_d = ld >= 0 && ld < nloc && (((int)ld & (NT - 1)) >> 5) == warp;
+      const bool own_p = lp >= 0 && lp < nloc && (((int)lp & (NT - 1)) >> 5) == warp;
+      if (own_d || own_p) {
+#pragma unroll
+        for (int r = 0; r < RPT; ++r) {
+          const int64_t gi = base + tid + NT * r;
+          if (gi == d) row_load<T, W>(pr[r], s_piv[buf]);
+          else if (gi == p) row_load<T, W>(pr[r], s_old);
+        }
+      }
+    }
 #pragma unroll
     for (int r = 0; r < RPT; ++r) {
       const int i = tid + NT * r;
-      const int64_t gi = base + i;
-      upd[r] = i < nloc && gi > d;
-      if (i < nloc && swap) {
-        if (gi == d) row_load<T, W>(pr[r], s_piv[buf]);
-        else if (gi == p) row_load<T, W>(pr[r], s_old);
-      }
+      upd[r] = i < nloc && base + i > d;
       l[r] = pr[r][0];
     }
     if (warp_rows) {
