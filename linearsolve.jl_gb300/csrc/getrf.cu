@@ -381,24 +381,31 @@ __device__ __forceinline__ void row_load(T (&dst)[W], const T* src) {
 // with one small body; rows are exchanged in slot order (16-byte shared
 // memory accesses, no index arithmetic).
 //
-// The step of column k is arranged so that the rank-1 update overlaps the
-// cluster barrier.  After the interchange and scaling of column k, each
-// thread updates only slot 1 (column k+1); each warp reduces its column-k+1
-// candidate and publishes it with the candidate row and the diagonal row in
+// The CTAs exchange pivot candidates by pushing them: no cluster barrier per
+// column.  After the interchange and scaling of column k, each thread
+// updates only slot 1 (column k+1); each warp reduces its column-k+1
+// candidate and leaves it, with the candidate row and the diagonal row in
 // their partly updated form (slot 0 = the multiplier l, slot 1 updated,
-// slots 2.. not yet); the last warp of the CTA to publish reduces the CTA's
-// warp candidates to one; every thread arrives at the cluster barrier and
-// runs the rest of the update (slots 2..) before the wait.  After the wait,
-// warp 0 of every CTA reads the G CTA candidates (one 16-byte load of
-// distributed shared memory per CTA), picks the winner, fetches the pivot row
-// and the diagonal row together and finishes their update itself with the
-// same fma(-l, u, a) on the same operands the owner uses, so the fetched
-// rows are bit-identical to the owners' registers.  Meanwhile warp 1 computes
-// 1 / |candidate| of every CTA candidate from its key (the bit pattern of
-// |a|) and hands the winner's to warp 0 through a named barrier.
-// One CTA barrier hands the pivot row to every thread.  Warps that hold no
-// rows skip the arithmetic (a predicated-off FP64 instruction still occupies
-// the FP64 pipe).  The per-element arithmetic is panel_kernel's.
+// slots 2.. not yet), in shared memory; the pushing warp (the last warp)
+// waits for them on a named barrier, reduces them to the CTA's candidate and
+// writes candidate, row and (in the diagonal row's CTA) the diagonal row into
+// every CTA's receive slots with st.async, each store counted by the
+// receiver's mbarrier of that column.  The other warps run the rest of the
+// update (slots 2..) meanwhile.  Warp 0 of every CTA waits on its own
+// mbarrier (a bounded wait), picks the winner among the G received
+// candidates, and finishes the update of the received pivot row and
+// diagonal row itself with the same fma(-l, u, a) on the same operands the
+// owners use, so they are bit-identical to the owners' registers; warp 1
+// computes 1 / |candidate| of every received candidate from its key (the bit
+// pattern of |a|) and hands the winner's to warp 0 through a named barrier.
+// One CTA barrier hands the pivot row to every thread.
+//
+// Receive slots are double-buffered by column parity.  A CTA pushes column
+// k+1 only after it received every CTA's column k, and each CTA pushes
+// column k only after it finished reading its column k-1 slots, so a push
+// never overwrites slots still being read.  Warps that hold no rows skip the
+// arithmetic (a predicated-off FP64 instruction still occupies the FP64
+// pipe).  The per-element arithmetic is panel_kernel's.
 constexpr int kRegPanelThreads = 512;
 
 // A CTA's pivot candidate as one 16-byte word: key, row (-1 = none), warp.
@@ -430,26 +437,77 @@ __device__ __forceinline__ T with_sign_of(T x, T s) {
                                 (__double_as_longlong(s) & (long long)0x8000000000000000ull));
 }
 
+// Shared-memory addresses, cluster mapping, st.async and the mbarrier steps
+// of the panel exchange.
+__device__ __forceinline__ uint32_t pan_saddr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ uint32_t pan_mapa(uint32_t a, int rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ void pan_st_async(uint32_t raddr, int4 v, uint32_t rbar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.b32 [%0], {%1, %2, %3, %4}, [%5];"
+               ::"r"(raddr), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w), "r"(rbar)
+               : "memory");
+}
+__device__ __forceinline__ void pan_bar_init(uint32_t a) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(a) : "memory");
+}
+__device__ __forceinline__ void pan_bar_arm(uint32_t a, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(a), "r"(bytes) : "memory");
+}
+// Bounded wait for the phase of the given parity; false when it gave up
+// (the error word is set).
+__device__ __forceinline__ bool pan_bar_wait(uint32_t a, uint32_t parity, int* err) {
+  unsigned long long t0 = 0;
+  for (uint32_t it = 0;; ++it) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    if ((it & 63u) == 0) {
+      const unsigned long long now = global_ns();
+      if (t0 == 0) t0 = now;
+      else if (now - t0 > kSpinTimeoutNs) {
+        atomicCAS(err, 0, (int)DEV_TIMEOUT_PANEL);
+        return false;
+      }
+    }
+  }
+}
+
 template <typename T, int RPT>
 __global__ void __launch_bounds__(kRegPanelThreads, 1)
 panel_reg_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w,
-                 int64_t* __restrict__ ipiv, int64_t* __restrict__ info_out, int R) {
+                 int64_t* __restrict__ ipiv, int64_t* __restrict__ info_out, int R,
+                 DevScratch* __restrict__ scr) {
   namespace cg = cooperative_groups;
   using K = typename PivKey<T>::K;
   using VT = Vec16<T>;
   constexpr unsigned kAll = 0xffffffffu;
   cg::cluster_group cluster = cg::this_cluster();
   constexpr int NT = kRegPanelThreads, NW = NT / 32, W = kPanelMaxW;
-  // [b]: candidates of column k live in buffer k & 1
+  constexpr int RB = W * (int)sizeof(T) / 16;  // 16-byte chunks per row
+  constexpr int kPusher = NW - 1;              // the warp that pushes the CTA's candidate
+  // [b]: column k uses buffer k & 1
   __shared__ __align__(16) T s_crowv[2][NW][W];  // each warp's candidate row (published form)
   __shared__ __align__(16) T s_diagv[2][W];      // the diagonal row (owner CTA, published form)
   __shared__ __align__(16) T s_piv[2][W];        // the pivot row of column k, slot order of step k
   __shared__ __align__(16) T s_old[W];           // the old diagonal row, for the pivot row's owner
-  __shared__ __align__(16) int4 s_cta[2];        // the CTA's candidate (cand_pack)
+  __shared__ __align__(16) T r_row[2][16][W];    // received: CTA c's candidate row
+  __shared__ __align__(16) T r_diag[2][W];       // received: the diagonal row
+  __shared__ __align__(16) int4 r_cand[2][16];   // received: CTA c's candidate (cand_pack)
+  __shared__ __align__(8) unsigned long long r_bar[2];  // counts the received bytes of a column
   __shared__ K s_cval[2][NW];
   __shared__ int s_crow[2][NW];
-  __shared__ unsigned s_cnt[2];                  // warps that published into buffer b
-  __shared__ T s_rinv[32];                       // 1 / |candidate| of CTA c's candidate
+  __shared__ T s_rinv[16];                       // 1 / |candidate| of CTA c's candidate
   __shared__ int s_p;
   __shared__ T s_inv;
 
@@ -459,6 +517,10 @@ panel_reg_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w,
   const int64_t base = c0 + (int64_t)cta * R;
   const int nloc = (int)max((int64_t)0, min((int64_t)R, m - base));
   const bool warp_rows = warp * 32 < nloc;  // this warp holds at least one row
+  // bytes received per column: G candidates and rows, one diagonal row
+  const uint32_t rx_bytes = (uint32_t)(G * 16 * (1 + RB) + 16 * RB);
+  int* const err = &scr->error;
+  bool bad = false;  // a wait gave up: stop waiting, finish without hanging
 
   T pr[RPT][W];  // slot j: column (k + j) mod 32 at step k
 #pragma unroll
@@ -467,14 +529,20 @@ panel_reg_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w,
 #pragma unroll
     for (int j = 0; j < W; ++j) pr[r][j] = (i < nloc && j < w) ? A[(base + i) + (c0 + j) * lda] : T(0);
   }
-  if (tid < 2) s_cnt[tid] = 0;
-  __syncthreads();
+  if (tid == 0) {
+    pan_bar_init(pan_saddr(&r_bar[0]));
+    pan_bar_init(pan_saddr(&r_bar[1]));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    pan_bar_arm(pan_saddr(&r_bar[0]), rx_bytes);  // column 0
+    pan_bar_arm(pan_saddr(&r_bar[1]), rx_bytes);  // column 1
+  }
+  cluster.sync();  // every CTA's mbarriers exist before the first push
   int64_t info_local = 0;
 
   // Candidates of the column in slot S among rows >= dn into buffer pb: each
-  // warp's first row of max |a| (NaN ignored) with its row and the diagonal
-  // row dn; the last warp to publish reduces them to the CTA's candidate;
-  // then arrive at the cluster barrier.
+  // warp's first row of max |a| (NaN ignored) with its row, and the diagonal
+  // row dn; the pushing warp reduces them to the CTA's candidate and writes
+  // it into every CTA's receive slots.
   auto publish = [&](auto slot_c, int64_t dn, int pb) {
     constexpr int S = decltype(slot_c)::value;
     K bv = 0;
@@ -499,35 +567,45 @@ panel_reg_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w,
           if (tid + NT * r == lw) row_store<T, W>(s_crowv[pb][warp], pr[r]);
         }
     }
-    {
-      const int64_t ld = dn - base;
-      if (ld >= 0 && ld < nloc && (((int)ld & (NT - 1)) >> 5) == warp) {
+    const int64_t ldn = dn - base;
+    const bool own_diag = ldn >= 0 && ldn < nloc;
+    if (own_diag && (((int)ldn & (NT - 1)) >> 5) == warp) {
 #pragma unroll
-        for (int r = 0; r < RPT; ++r)
-          if (ld >= NT * r && ld < NT * (r + 1)) {
-            if (tid + NT * r == ld) row_store<T, W>(s_diagv[pb], pr[r]);
-          }
-      }
+      for (int r = 0; r < RPT; ++r)
+        if (ldn >= NT * r && ldn < NT * (r + 1)) {
+          if (tid + NT * r == ldn) row_store<T, W>(s_diagv[pb], pr[r]);
+        }
     }
-    unsigned last = 0;
-    if (lane == 0) {
-      s_cval[pb][warp] = bv;
-      s_crow[pb][warp] = bg;
-      __threadfence_block();
-      last = atomicAdd(&s_cnt[pb], 1u) == NW - 1;
+    if (lane == 0) { s_cval[pb][warp] = bv; s_crow[pb][warp] = bg; }
+    if (warp != kPusher) {
+      named_bar_arrive(2, NT);
+      return;
     }
-    if (__shfl_sync(kAll, last, 0)) {
-      __threadfence_block();
-      K v = lane < NW ? s_cval[pb][lane] : K(0);
-      int g = lane < NW ? s_crow[pb][lane] : -1;
-      int wsrc;
-      warp_pivot_choice(v, g, wsrc);
-      if (lane == 0) {
-        s_cta[pb] = cand_pack<K>(v, g, wsrc);
-        s_cnt[pb] = 0;
-      }
+    named_bar_sync(2, NT);  // every warp's candidate and rows are in shared memory
+    K v = lane < NW ? s_cval[pb][lane] : K(0);
+    int g = lane < NW ? s_crow[pb][lane] : -1;
+    int wsrc;
+    warp_pivot_choice(v, g, wsrc);
+    const int4 cand = cand_pack<K>(v, g, wsrc);
+    const int4* rsrc = reinterpret_cast<const int4*>(s_crowv[pb][wsrc < 0 ? 0 : wsrc]);
+    const int4* dsrc = reinterpret_cast<const int4*>(s_diagv[pb]);
+    const uint32_t a_cand = pan_saddr(&r_cand[pb][cta]);
+    const uint32_t a_row = pan_saddr(&r_row[pb][cta][0]);
+    const uint32_t a_diag = pan_saddr(&r_diag[pb][0]);
+    const uint32_t a_bar = pan_saddr(&r_bar[pb]);
+    constexpr int C = 1 + RB;  // chunks per receiver: candidate, row
+    const int total = G * C + (own_diag ? G * RB : 0);
+    for (int x = lane; x < total; x += 32) {
+      int dest, ch;
+      if (x < G * C) { dest = x / C; ch = x - dest * C; }
+      else { const int y = x - G * C; dest = y / RB; ch = C + (y - dest * RB); }
+      int4 val;
+      uint32_t la;
+      if (ch == 0) { val = cand; la = a_cand; }
+      else if (ch < C) { val = rsrc[ch - 1]; la = a_row + 16u * (ch - 1); }
+      else { val = dsrc[ch - C]; la = a_diag + 16u * (ch - C); }
+      pan_st_async(pan_mapa(la, dest), val, pan_mapa(a_bar, dest));
     }
-    cluster_arrive();
   };
 
   publish(std::integral_constant<int, 0>{}, c0, 0);  // column 0: the rows as loaded
@@ -535,31 +613,22 @@ panel_reg_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w,
   for (int k = 0; k < w; ++k) {
     const int64_t d = c0 + k;
     const int buf = k & 1;
-    cluster_wait();  // every CTA's candidate of column k is published
     // 1. warp 0: the winner over the CTAs of the cluster, the pivot row and,
     //    for the pivot row's CTA, the old diagonal row
     if (warp == 0) {
+      if (!bad && !pan_bar_wait(pan_saddr(&r_bar[buf]), (uint32_t)(k >> 1) & 1u, err)) bad = true;
+      if (lane == 0 && k + 2 < w) pan_bar_arm(pan_saddr(&r_bar[buf]), rx_bytes);  // column k + 2
       K v = 0;
       int g = -1, ew = 0;
-      if (lane < G) {
-        const int4 c = *cluster.map_shared_rank(&s_cta[buf], lane);
-        cand_unpack<K>(c, v, g, ew);
-      }
+      if (lane < G) cand_unpack<K>(r_cand[buf][lane], v, g, ew);
       int ec;  // the winning CTA
       warp_pivot_choice(v, g, ec);
-      ew = __shfl_sync(kAll, ew, ec < 0 ? 0 : ec);
       const int64_t p = g < 0 ? d : (int64_t)g;  // kp = k when amax == 0
-      const int downer = (int)((d - c0) / R);
-      // published rows are in the slot order of step k-1: lane j takes slot
+      // received rows are in the slot order of step k-1: lane j takes slot
       // j + 1 and finishes its step-(k-1) update (slots 2 .. w-k of step k-1)
       const int js = k > 0 ? ((lane + 1) & (W - 1)) : lane;
-      const T* dsrc = cluster.map_shared_rank(&s_diagv[buf][js], downer);
-      const T* psrc = p != d ? cluster.map_shared_rank(&s_crowv[buf][ew][js], ec) : dsrc;
-      T dv = *dsrc;
-      T pv = *psrc;
-      // 1 / |pivot| from warp 1
-      named_bar_sync(1, 64);
-      const T inv_mag = s_rinv[ec < 0 ? 0 : ec];
+      T dv = r_diag[buf][js];
+      T pv = p != d ? r_row[buf][ec < 0 ? 0 : ec][js] : dv;
       if (k > 0) {
         const T u = s_piv[buf ^ 1][js];
         const T ld = __shfl_sync(kAll, dv, W - 1);  // slot 0 of step k-1: the multiplier
@@ -569,6 +638,9 @@ panel_reg_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w,
           pv = fma(-lp, u, pv);
         }
       }
+      // 1 / |pivot| from warp 1
+      named_bar_sync(1, 64);
+      const T inv_mag = s_rinv[ec < 0 ? 0 : ec];
       s_piv[buf][lane] = pv;
       if (p != d && p >= base && p < base + nloc) s_old[lane] = dv;
       if (lane == 0) {
@@ -577,15 +649,13 @@ panel_reg_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w,
         s_inv = g >= 0 ? with_sign_of(inv_mag, pv) : (PivKey<T>::nonzero(pv) ? T(1) / pv : T(0));
       }
     } else if (warp == 1) {
-      // 1 / |candidate| of every CTA's candidate (its key is the bit pattern
-      // of |a|), beside warp 0's reduction and row loads: the division is a
-      // long dependent sequence
+      // 1 / |candidate| of every received candidate (its key is the bit
+      // pattern of |a|), beside warp 0's reduction: the division is a long
+      // dependent sequence
+      if (!bad && !pan_bar_wait(pan_saddr(&r_bar[buf]), (uint32_t)(k >> 1) & 1u, err)) bad = true;
       K v = 0;
       int g = -1, ew = 0;
-      if (lane < G) {
-        const int4 c = *cluster.map_shared_rank(&s_cta[buf], lane);
-        cand_unpack<K>(c, v, g, ew);
-      }
+      if (lane < G) cand_unpack<K>(r_cand[buf][lane], v, g, ew);
       const T rinv = T(1) / key_magnitude<T>(g >= 0 ? v : K(1));
       if (lane < G) s_rinv[lane] = rinv;
       named_bar_arrive(1, 64);
@@ -633,7 +703,7 @@ panel_reg_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w,
     }
     if (k + 1 < w) {
       // 3. slot 1 first, publish the candidates of column k + 1, then the
-      //    rest of the rank-1 update while the cluster barrier completes
+      //    rest of the rank-1 update while the candidates travel
       if (warp_rows) {
         const T u1 = s_piv[buf][1];
 #pragma unroll
@@ -692,7 +762,7 @@ panel_reg_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w,
       }
   }
   if (cta == 0 && tid == 0 && info_local != 0 && *info_out == 0) *info_out = info_local;
-  cluster.sync();  // no CTA exits while another may still read its shared memory
+  cluster.sync();  // no CTA exits while a push to it may be in flight
 }
 
 // ---------------------------------------------------------------------------
@@ -1057,7 +1127,8 @@ struct Driver {
     double fl = 0;
     for (int k = 0; k < w; ++k) fl += (double)(M - k - 1) * (1.0 + 2.0 * (w - k - 1));
     LaunchScope ls(K_PANEL, fl, 2.0 * M * w * sizeof(T), s);
-    check(cudaLaunchKernelEx(&cfg, panel_reg_kernel<T, RPT>, p.A, p.lda, p.m, c0, w, p.ipiv, p.info, (int)R));
+    check(cudaLaunchKernelEx(&cfg, panel_reg_kernel<T, RPT>, p.A, p.lda, p.m, c0, w, p.ipiv, p.info, (int)R,
+                             p.scratch));
     return true;
   }
 
