@@ -586,25 +586,24 @@ panel_reg_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w,
     int g = lane < NW ? s_crow[pb][lane] : -1;
     int wsrc;
     warp_pivot_choice(v, g, wsrc);
-    const int4 cand = cand_pack<K>(v, g, wsrc);
-    const int4* rsrc = reinterpret_cast<const int4*>(s_crowv[pb][wsrc < 0 ? 0 : wsrc]);
-    const int4* dsrc = reinterpret_cast<const int4*>(s_diagv[pb]);
-    const uint32_t a_cand = pan_saddr(&r_cand[pb][cta]);
-    const uint32_t a_row = pan_saddr(&r_row[pb][cta][0]);
-    const uint32_t a_diag = pan_saddr(&r_diag[pb][0]);
-    const uint32_t a_bar = pan_saddr(&r_bar[pb]);
-    constexpr int C = 1 + RB;  // chunks per receiver: candidate, row
-    const int total = G * C + (own_diag ? G * RB : 0);
-    for (int x = lane; x < total; x += 32) {
-      int dest, ch;
-      if (x < G * C) { dest = x / C; ch = x - dest * C; }
-      else { const int y = x - G * C; dest = y / RB; ch = C + (y - dest * RB); }
-      int4 val;
-      uint32_t la;
-      if (ch == 0) { val = cand; la = a_cand; }
-      else if (ch < C) { val = rsrc[ch - 1]; la = a_row + 16u * (ch - 1); }
-      else { val = dsrc[ch - C]; la = a_diag + 16u * (ch - C); }
-      pan_st_async(pan_mapa(la, dest), val, pan_mapa(a_bar, dest));
+    // lane c writes CTA c's receive slots: the candidate, the candidate row
+    // and, from the diagonal row's CTA, the diagonal row (offsets within
+    // one mapped array stay in that CTA's shared memory window)
+    if (lane < G) {
+      const int4 cand = cand_pack<K>(v, g, wsrc);
+      const int4* rsrc = reinterpret_cast<const int4*>(s_crowv[pb][wsrc < 0 ? 0 : wsrc]);
+      const uint32_t rbar = pan_mapa(pan_saddr(&r_bar[pb]), lane);
+      const uint32_t rc = pan_mapa(pan_saddr(&r_cand[pb][cta]), lane);
+      const uint32_t rr = pan_mapa(pan_saddr(&r_row[pb][cta][0]), lane);
+      pan_st_async(rc, cand, rbar);
+#pragma unroll
+      for (int q = 0; q < RB; ++q) pan_st_async(rr + 16u * q, rsrc[q], rbar);
+      if (own_diag) {
+        const int4* dsrc = reinterpret_cast<const int4*>(s_diagv[pb]);
+        const uint32_t rd = pan_mapa(pan_saddr(&r_diag[pb][0]), lane);
+#pragma unroll
+        for (int q = 0; q < RB; ++q) pan_st_async(rd + 16u * q, dsrc[q], rbar);
+      }
     }
   };
 
@@ -730,14 +729,19 @@ panel_reg_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w,
           }
         } else {
           // FP64: stop at the last live slot with a uniform branch, so the FP64
-          // pipe only sees the FMAs that do work
+          // pipe only sees the FMAs that do work; the pivot row is read two
+          // slots per 16-byte load
 #pragma unroll
-          for (int j = 2; j < W; ++j) {
+          for (int j = 2; j < W; j += 2) {
             if (j >= lim) break;
-            const T u = s_piv[buf][j];
+            const typename VT::V u2 = reinterpret_cast<const typename VT::V*>(s_piv[buf])[j / 2];
 #pragma unroll
             for (int r = 0; r < RPT; ++r)
-              if (upd[r]) pr[r][j] = fma(-l[r], u, pr[r][j]);
+              if (upd[r]) pr[r][j] = fma(-l[r], VT::get(u2, 0), pr[r][j]);
+            if (j + 1 >= lim) break;
+#pragma unroll
+            for (int r = 0; r < RPT; ++r)
+              if (upd[r]) pr[r][j + 1] = fma(-l[r], VT::get(u2, 1), pr[r][j + 1]);
           }
         }
       }
