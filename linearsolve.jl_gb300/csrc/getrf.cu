@@ -902,59 +902,110 @@ constexpr size_t trsm_smem() { return (size_t)KM * (KM + 1) * sizeof(T); }
 
 // ---------------------------------------------------------------------------
 // SIMT GEMM update C -= A * B (column-major), every C element updated by
-// fma(-a_k, b_k, c) for k ascending.  64 x 64 tile, 16-deep k slices,
-// 256 threads with a 4 x 4 register tile each.
-constexpr int kGBM = 64, kGBN = 64, kGBK = 16;
+// fma(-a_k, b_k, c) for k ascending.  BM x BN tile (64 x 64, 32 x 32 or
+// 16 x 16), 16-deep k slices, 256 threads with a (BM/16) x (BN/16) register
+// tile each.  The smaller tiles spread short updates over more SMs: one SM
+// of this GPU retires two FP64 FMA lanes per cycle, so an update covered by
+// a few 64 x 64 tiles would run on a few SMs.
+constexpr int kGBK = 16;
 
-template <typename T>
-__global__ void __launch_bounds__(256)
+template <typename T, int BM, int BN>
+__global__ void __launch_bounds__(256, BM == 64 ? 2 : 4)
 gemm_sub_kernel(int64_t M, int64_t N, int64_t K, const T* __restrict__ A, int64_t lda,
                 const T* __restrict__ B, int64_t ldb, T* __restrict__ C, int64_t ldc) {
-  __shared__ T sA[kGBK][kGBM];
-  __shared__ T sB[kGBK][kGBN + 1];
+  constexpr int TM = BM / 16, TN = BN / 16;
+  __shared__ T sA[kGBK][BM];
+  __shared__ T sB[kGBK][BN + 1];
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-  const int64_t m0 = (int64_t)blockIdx.x * kGBM, n0 = (int64_t)blockIdx.y * kGBN;
-  T c[4][4];
+  const int64_t m0 = (int64_t)blockIdx.x * BM, n0 = (int64_t)blockIdx.y * BN;
+  T c[TM][TN];
 #pragma unroll
-  for (int i = 0; i < 4; ++i)
+  for (int i = 0; i < TM; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
+    for (int j = 0; j < TN; ++j) {
       int64_t r = m0 + tx + 16 * i, cc = n0 + ty + 16 * j;
       c[i][j] = (r < M && cc < N) ? C[r + cc * ldc] : T(0);
     }
   for (int64_t k0 = 0; k0 < K; k0 += kGBK) {
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
+    for (int q = 0; q < (kGBK * BM) / 256; ++q) {
       int idx = tid + 256 * q;
-      int kk = idx >> 6, i = idx & 63;
+      int kk = idx / BM, i = idx % BM;
       int64_t r = m0 + i, kc = k0 + kk;
       sA[kk][i] = (r < M && kc < K) ? A[r + kc * lda] : T(0);
-      int kb = idx & 15, j = idx >> 4;
+    }
+#pragma unroll
+    for (int q = 0; q < (kGBK * BN) / 256; ++q) {
+      int idx = tid + 256 * q;
+      int kb = idx % kGBK, j = idx / kGBK;
       int64_t kr = k0 + kb, cc = n0 + j;
       sB[kb][j] = (kr < K && cc < N) ? B[kr + cc * ldb] : T(0);
     }
     __syncthreads();
     const int kmax = (int)min((int64_t)kGBK, K - k0);
     for (int kk = 0; kk < kmax; ++kk) {
-      T a[4], b[4];
+      T a[TM], b[TN];
 #pragma unroll
-      for (int i = 0; i < 4; ++i) a[i] = sA[kk][tx + 16 * i];
+      for (int i = 0; i < TM; ++i) a[i] = sA[kk][tx + 16 * i];
 #pragma unroll
-      for (int j = 0; j < 4; ++j) b[j] = sB[kk][ty + 16 * j];
+      for (int j = 0; j < TN; ++j) b[j] = sB[kk][ty + 16 * j];
 #pragma unroll
-      for (int i = 0; i < 4; ++i)
+      for (int i = 0; i < TM; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) c[i][j] = fma(-a[i], b[j], c[i][j]);
+        for (int j = 0; j < TN; ++j) c[i][j] = fma(-a[i], b[j], c[i][j]);
     }
     __syncthreads();
   }
 #pragma unroll
-  for (int i = 0; i < 4; ++i)
+  for (int i = 0; i < TM; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
+    for (int j = 0; j < TN; ++j) {
       int64_t r = m0 + tx + 16 * i, cc = n0 + ty + 16 * j;
       if (r < M && cc < N) C[r + cc * ldc] = c[i][j];
     }
+}
+
+// The tile for an M x N update.  FP64: the least work on the busiest SM,
+// ceil(tiles / SMs) x BM x BN, with a small penalty per halving of the tile
+// for its extra loads (one tile per SM already keeps the FP64 pipe busy).
+// FP32: 64 x 64 unless that leaves SMs without a tile, then 32 x 32, then
+// 16 x 16.
+inline int gemm_tile_choice(int64_t M, int64_t N, int sms, int elem_size) {
+  auto tiles = [&](int b) { return ((M + b - 1) / b) * ((N + b - 1) / b); };
+  if (elem_size == 4) {
+    if (tiles(64) >= sms) return 64;
+    if (tiles(32) >= sms) return 32;
+    return 16;
+  }
+  const int bm[3] = {64, 32, 16};
+  const double pen[3] = {1.0, 1.08, 1.25};
+  int best = 64;
+  double bt = 0;
+  for (int q = 0; q < 3; ++q) {
+    const double t = (double)((tiles(bm[q]) + sms - 1) / sms) * bm[q] * bm[q] * pen[q];
+    if (q == 0 || t < bt) { bt = t; best = bm[q]; }
+  }
+  return best;
+}
+
+// GBLU_GEMM_TILE=64|32|16 forces the SIMT update's tile (the tiles give
+// identical results), so each variant can be tested on small matrices.
+int forced_gemm_tile() {
+  const char* e = getenv("GBLU_GEMM_TILE");
+  if (!e) return 0;
+  const int t = atoi(e);
+  return (t == 64 || t == 32 || t == 16) ? t : 0;
+}
+
+// forced: 0 = gemm_tile_choice, else the tile edge (64, 32 or 16)
+template <typename T>
+void gemm_sub_launch(int64_t M, int64_t N, int64_t K, const T* A, int64_t lda, const T* B, int64_t ldb,
+                     T* C, int64_t ldc, int sms, int forced, cudaStream_t s) {
+  const int t = forced ? forced : gemm_tile_choice(M, N, sms, (int)sizeof(T));
+  dim3 grid((unsigned)((M + t - 1) / t), (unsigned)((N + t - 1) / t));
+  if (t == 64) gemm_sub_kernel<T, 64, 64><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc);
+  else if (t == 32) gemm_sub_kernel<T, 32, 32><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc);
+  else gemm_sub_kernel<T, 16, 16><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc);
 }
 
 // ---------------------------------------------------------------------------
@@ -1048,6 +1099,7 @@ struct Driver {
   int device;
   cudaError_t err = cudaSuccess;
   int forced = 0;  // forced_panel_kind()
+  int forced_tile = 0;  // forced_gemm_tile()
 
   T* at(int64_t r, int64_t c) const { return p.A + r + c * p.lda; }
 
@@ -1256,9 +1308,8 @@ struct Driver {
         return;
       }
     }
-    dim3 grid((unsigned)((M + kGBM - 1) / kGBM), (unsigned)((N + kGBN - 1) / kGBN));
     LaunchScope ls(K_GEMM, 2.0 * M * N * K, (2.0 * M * N + (double)M * K + (double)K * N) * sizeof(T), s);
-    gemm_sub_kernel<T><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc);
+    gemm_sub_launch<T>(M, N, K, A, lda, B, ldb, C, ldc, device_info(device).num_sms, forced_tile, s);
     check(cudaGetLastError());
   }
 
@@ -1306,9 +1357,10 @@ struct Driver {
 cudaError_t simt_gemm_sub_f32(int64_t M, int64_t N, int64_t K, const float* A, int64_t lda,
                               const float* B, int64_t ldb, float* C, int64_t ldc, cudaStream_t s) {
   if (M <= 0 || N <= 0 || K <= 0) return cudaSuccess;
-  dim3 grid((unsigned)((M + kGBM - 1) / kGBM), (unsigned)((N + kGBN - 1) / kGBN));
+  int device = 0;
+  cudaGetDevice(&device);
   LaunchScope ls(K_GEMM, 2.0 * M * N * K, (2.0 * M * N + (double)M * K + (double)K * N) * 4.0, s);
-  gemm_sub_kernel<float><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc);
+  gemm_sub_launch<float>(M, N, K, A, lda, B, ldb, C, ldc, device_info(device).num_sms, forced_gemm_tile(), s);
   return cudaGetLastError();
 }
 
@@ -1360,6 +1412,7 @@ cudaError_t getrf_launch(const GetrfPlan<T>& p, cudaStream_t stream) {
   cudaGetDevice(&device);
   Driver<T> d{p, stream, device};
   d.forced = forced_panel_kind();
+  d.forced_tile = forced_gemm_tile();
   const int64_t minmn = std::min(p.m, p.n);
   d.check(cudaMemsetAsync(p.info, 0, sizeof(int64_t), stream));
   if (minmn > 0) {

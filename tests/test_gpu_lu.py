@@ -275,6 +275,25 @@ def test_every_panel_kernel_bit_exact(ctx, oracle_mod, monkeypatch, kind, prec):
         f.close()
 
 
+@pytest.mark.parametrize("tile", ["64", "32", "16"])
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_every_gemm_tile_bit_exact(ctx, oracle_mod, monkeypatch, tile, prec):
+    # the SIMT trailing update picks a 64, 32 or 16 square tile by shape;
+    # GBLU_GEMM_TILE forces one for every update (same per-element order)
+    monkeypatch.setenv("GBLU_GEMM_TILE", tile)
+    rng = np.random.default_rng(79)
+    dt = np.float32 if prec == "fp32" else np.float64
+    shapes = ((1000, 1000), (1200, 700), (500, 900)) if prec == "fp64" else ((1000, 1000), (1300, 1300))
+    for m, n in shapes:
+        A = rng.standard_normal((m, n)).astype(dt).astype(np.float64)
+        f = ctx.factor(m, n, prec)
+        f.getrf(A)
+        LU, ipiv, _ = oracle_mod.getrf(A.astype(dt))
+        assert np.array_equal(f.ipiv(), ipiv), (tile, prec, m, n)
+        assert np.array_equal(f.factors(), LU.astype(np.float64)), (tile, prec, m, n)
+        f.close()
+
+
 @pytest.mark.parametrize("prec", ["fp64", "fp32"])
 def test_graph_replayed_getrf_matches_direct(ctx, oracle_mod, prec):
     # from its third factorization a factor replays its launch sequence from a
