@@ -864,15 +864,28 @@ __global__ void __launch_bounds__(trsm_warps<T, KM>() * 32)
 trsm_lunit_kernel(const T* __restrict__ L, int64_t ldl, int k, T* __restrict__ B,
                   int64_t ldb, int64_t ncols) {
   constexpr int RPL = KM / 32;  // rows per lane
-  constexpr int kTrsmWarps = trsm_warps<T, KM>();
+  // warps (columns in flight) of this CTA: chosen per launch for FP64, fixed
+  // for FP32 (a compile-time stride keeps its short chain steps lean)
+  const int nw = sizeof(T) == 8 ? (int)(blockDim.x >> 5) : trsm_warps<T, KM>();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T(*sL)[KM + 1] = reinterpret_cast<T(*)[KM + 1]>(smem_raw);  // sL[c][r] = L[r, c]
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int c = warp; c < k; c += kTrsmWarps)
-    for (int r = lane; r < k; r += 32) sL[c][r] = L[r + (int64_t)c * ldl];
+  if constexpr (sizeof(T) == 8) {
+    // the strictly lower triangle of L, copied asynchronously (an FP64 CTA
+    // may have a single warp)
+    for (int c = warp; c < k; c += nw)
+      for (int r = c + 1 + lane; r < k; r += 32) {
+        const unsigned d = (unsigned)__cvta_generic_to_shared(&sL[c][r]);
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(L + r + (int64_t)c * ldl)
+                     : "memory");
+      }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+  } else {
+    for (int c = warp; c < k; c += nw)
+      for (int r = lane; r < k; r += 32) sL[c][r] = L[r + (int64_t)c * ldl];
+  }
   __syncthreads();
-  for (int64_t col = (int64_t)blockIdx.x * kTrsmWarps + warp; col < ncols;
-       col += (int64_t)gridDim.x * kTrsmWarps) {
+  for (int64_t col = (int64_t)blockIdx.x * nw + warp; col < ncols; col += (int64_t)gridDim.x * nw) {
     T* b = B + col * ldb;
     T v[RPL];
 #pragma unroll
@@ -887,6 +900,7 @@ trsm_lunit_kernel(const T* __restrict__ L, int64_t ldl, int k, T* __restrict__ B
 #pragma unroll
       for (int q = 0; q < RPL; ++q) {
         if (q < qk) continue;  // rows 32q..32q+31 are final
+        if (sizeof(T) == 8 && 32 * q >= k) break;  // no rows (a predicated-off FP64 FMA still occupies the pipe)
         const int r = lane + 32 * q;
         if (r > kk && r < k) v[q] = fma(-sL[kk][r], xk, v[q]);
       }
@@ -1318,7 +1332,13 @@ struct Driver {
     if (k <= 0 || ncols <= 0) return;
     if (k <= p.trsm_base && k <= kTrsmMax) {
       const DeviceInfo& di = device_info(device);
-      const int warps = k <= 64 ? trsm_warps<T, 64>() : trsm_warps<T, 128>();
+      // one column per warp.  FP64: few columns are spread over the SMs one
+      // or two warps per CTA (each column is a chain of k dependent steps of
+      // 64-cycle FMAs, and the warps of one SM share its FP64 pipe); FP32
+      // chains are short and keep full CTAs.
+      const int maxw = k <= 64 ? trsm_warps<T, 64>() : trsm_warps<T, 128>();
+      const int warps = sizeof(T) == 4 ? maxw
+                                       : (int)std::max<int64_t>(1, std::min<int64_t>(maxw, (ncols + di.num_sms - 1) / di.num_sms));
       unsigned blocks = (unsigned)std::min<int64_t>((ncols + warps - 1) / warps, (int64_t)di.num_sms * 8);
       LaunchScope ls(K_TRSM, (double)k * (k - 1) * ncols, (2.0 * k * ncols + (double)k * k) * sizeof(T), s);
       if (k <= 64)
