@@ -67,8 +67,10 @@ struct SweepBits<double> {
     return v;
   }
   static __device__ __forceinline__ double as_t(U v) { return __longlong_as_double((long long)v); }
+  // NaN -> the canonical quiet NaN, on the integer pipe
   static __device__ __forceinline__ double canon(double v) {
-    return v != v ? __longlong_as_double(0x7ff8000000000000ll) : v;
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    return (b << 1) > 0xffe0000000000000ull ? __longlong_as_double(0x7ff8000000000000ll) : v;
   }
 };
 template <>
@@ -81,7 +83,9 @@ struct SweepBits<float> {
     return v;
   }
   static __device__ __forceinline__ float as_t(U v) { return __uint_as_float(v); }
-  static __device__ __forceinline__ float canon(float v) { return v != v ? __uint_as_float(0x7fc00000u) : v; }
+  static __device__ __forceinline__ float canon(float v) {
+    return (__float_as_uint(v) << 1) > 0xff000000u ? __uint_as_float(0x7fc00000u) : v;
+  }
 };
 
 // Wait for one published value; false on timeout or when another CTA failed.
@@ -153,11 +157,17 @@ solve_sweep_kernel(int64_t n, const T* __restrict__ LU, int64_t lda, const int32
   T(*tiles)[kTS][kTS + 1] = reinterpret_cast<T(*)[kTS][kTS + 1]>(smem_raw);
   __shared__ T sx[kTS][NR];
   __shared__ int s_blk;
+  __shared__ int s_fail;
   constexpr bool kUnit = FWD != TRANS;  // fwd 'N' (L) and bwd 'T' (L^T) have unit diagonals
+  // FP64: rows are published as soon as they are final and the next block
+  // row applies them as they come (its last tile is 64 dependent 64-cycle
+  // FMAs per row); FP32 tiles are cheap, so rows are published at the end.
+  constexpr bool kEarly = sizeof(T) == 8;
   const int nblk = (int)((n + kTS - 1) / kTS);
   if (threadIdx.x == 0) {
     const int t = (int)atomicAdd(&scr->ticket, 1u);
     s_blk = FWD ? t : nblk - 1 - t;
+    s_fail = 0;
   }
   __syncthreads();
   const int blk = s_blk;
@@ -209,13 +219,69 @@ solve_sweep_kernel(int64_t n, const T* __restrict__ LU, int64_t lda, const int32
       pre[k] = (idx < kTS * NR && q < nrhs && c < nc) ? SweepBits<T>::load(src_of(cb, c, q)) : UB(0);
     }
   };
-  if (noff > 0) prefetch(0);
+  // (FP64: the last off-diagonal tile is consumed as it is published)
+  if (noff > (kEarly ? 1 : 0)) prefetch(0);
+  // this row's solution values, to the sweep's output (dependents poll them)
+  auto publish_row = [&]() {
+#pragma unroll
+    for (int q = 0; q < NR; ++q)
+      if (q < nrhs) {
+        const T v = SweepBits<T>::canon(acc[q]);
+        if (FWD) Y[(r0 + r) + q * ldy] = v;
+        else Out[(TRANS ? (int64_t)perm[r0 + r] : r0 + r) + q * ldo] = v;
+      }
+  };
   for (int t = 0; t < ntiles; ++t) {
     if (t + kStages - 1 < ntiles) issue(t + kStages - 1);
     cp_async_commit();
     cp_async_wait<kStages - 1>();
     __syncthreads();
     T(*tile)[kTS + 1] = tiles[t % kStages];
+    if (kEarly && t == noff - 1) {
+      // The tile of the block row just before this one in the sweep: its
+      // rows are published one by one while that block solves its diagonal,
+      // so it is applied CH columns at a time in sweep order, warp 2 polling
+      // the next columns while warps 0-1 apply the previous ones.
+      const int cb = col_block(t);
+      const int nc = (int)min((int64_t)kTS, n - (int64_t)cb * kTS);
+      constexpr int CH = 8, NCH = kTS / CH;
+      for (int ch = 0; ch <= NCH; ++ch) {
+        if (warp == 2 && ch < NCH) {
+          const int cbeg = FWD ? CH * ch : kTS - CH * (ch + 1);
+          for (int idx = lane; idx < CH * NR; idx += 32) {
+            const int c = cbeg + idx / NR, q = idx % NR;
+            T v = T(0);
+            if (q < nrhs && c < nc && !poll_value(src_of(cb, c, q), scr, &v)) s_fail = 1;
+            sx[c][q] = v;
+          }
+        }
+        if (warp < 3) named_bar_sync(1, 96);
+        if (ch > 0 && tid < kTS) {
+          const int pc = ch - 1;
+          if (FWD) {
+#pragma unroll
+            for (int c = CH * pc; c < CH * pc + CH; ++c) {
+              const T l = tile[c][r];
+#pragma unroll
+              for (int q = 0; q < NR; ++q) acc[q] = fma(-l, sx[c][q], acc[q]);
+            }
+          } else {
+#pragma unroll
+            for (int c = kTS - CH * pc - 1; c >= kTS - CH * (pc + 1); --c) {
+              if (c >= nc) continue;
+              const T u = tile[c][r];
+#pragma unroll
+              for (int q = 0; q < NR; ++q) acc[q] = fma(-u, sx[c][q], acc[q]);
+            }
+          }
+        }
+      }
+      if (!__syncthreads_and(s_fail == 0)) {
+        cp_async_wait<0>();  // no copy may land after the CTA has left
+        return;
+      }
+      continue;
+    }
     if (t < noff) {
       const int cb = col_block(t);
       const int64_t c0 = (int64_t)cb * kTS;
@@ -237,7 +303,7 @@ solve_sweep_kernel(int64_t n, const T* __restrict__ LU, int64_t lda, const int32
         cp_async_wait<0>();  // no copy may land after the CTA has left
         return;
       }
-      if (t + 1 < noff) prefetch(t + 1);
+      if (t + 1 < noff - (kEarly ? 1 : 0)) prefetch(t + 1);
       if (tid < kTS) {
         if (FWD) {
 #pragma unroll 8
@@ -265,6 +331,7 @@ solve_sweep_kernel(int64_t n, const T* __restrict__ LU, int64_t lda, const int32
       continue;
     }
     // ---- diagonal block: warp shuffles within each 32-row half ----
+
     // reciprocal of this row's diagonal entry, off the dependency chain
     const T yrow = (!kUnit && valid && tid < kTS) ? T(1) / tile[r][r] : T(1);
     const int w_first = FWD ? 0 : 1, w_second = FWD ? 1 : 0;
@@ -273,7 +340,8 @@ solve_sweep_kernel(int64_t n, const T* __restrict__ LU, int64_t lda, const int32
     // One column of the diagonal chain for all NR right-hand sides: the
     // divisions (lane `src` only, non-unit diagonal), then the broadcasts,
     // then the updates, so the NR chains overlap.
-    auto chain_step = [&](int c, int src, bool divide_here, bool update) {
+    // keep: the owner also leaves its value in sx for the other warp
+    auto chain_step = [&](int c, int src, bool divide_here, bool update, bool keep) {
       if (!kUnit && divide_here) {
         if constexpr (NR == 1) acc[0] = div_markstein(acc[0], tile[c][c], yrow);
         else div_markstein_n<T, NR>(acc, tile[c][c], yrow);
@@ -281,53 +349,57 @@ solve_sweep_kernel(int64_t n, const T* __restrict__ LU, int64_t lda, const int32
       T xc[NR];
 #pragma unroll
       for (int q = 0; q < NR; ++q) xc[q] = __shfl_sync(0xffffffffu, acc[q], src);
+      // row c is final: its dependents may start on it (stored while the
+      // broadcast is in flight)
+      if (kEarly && r == c && valid) {
+        publish_row();
+        if (keep)
+#pragma unroll
+          for (int q = 0; q < NR; ++q) sx[c][q] = acc[q];
+      }
       if (update) {
         const T a = tile[c][r];
 #pragma unroll
         for (int q = 0; q < NR; ++q) acc[q] = fma(-a, xc[q], acc[q]);
       }
     };
+    // FP64: the second warp applies the first half's solutions eight
+    // columns at a time while the first warp is still solving (one named
+    // barrier per group of eight), instead of re-applying all of them as a
+    // chain of 64-cycle FMAs afterwards.
+    const bool prog = kEarly && nr > 32;
+    const int m1 = FWD ? min(nr, 32) : nr - 32;  // columns of the first half
     if (warp == w_first) {
       // columns of the first half, in sweep order
-      if (FWD) {
-        const int cend = min(nr, 32);
-        for (int c = 0; c < cend; ++c) chain_step(c, c, lane == c, r > c && r < nr);
-      } else {
-        for (int c = min(nr, kTS) - 1; c >= 32; --c) chain_step(c, c - 32, r == c, r < c);
+      for (int st = 0; st < m1; ++st) {
+        const int c = FWD ? st : nr - 1 - st;
+        if (FWD) chain_step(c, c, lane == c, r > c && r < nr, prog);
+        else chain_step(c, c - 32, r == c, r < c, prog);
+        if (prog && ((st & 7) == 7 || st == m1 - 1)) named_bar_arrive(2 + (st >> 3), 64);
       }
-      if (valid)
+      if (!prog && valid)
 #pragma unroll
         for (int q = 0; q < NR; ++q) sx[r][q] = acc[q];
     }
-    __syncthreads();
+    if (!prog) __syncthreads();
     if (warp == w_second) {
+      // the first half's columns applied in sweep order, then this half's chain
+      for (int st = 0; st < m1; ++st) {
+        if (prog && (st & 7) == 0) named_bar_sync(2 + (st >> 3), 64);
+        const int c = FWD ? st : nr - 1 - st;
+        if (FWD && nr <= 32) break;
+#pragma unroll
+        for (int q = 0; q < NR; ++q) acc[q] = fma(-tile[c][r], sx[c][q], acc[q]);
+      }
       if (FWD) {
-        if (nr > 32) {
-          for (int c = 0; c < 32; ++c) {
-#pragma unroll
-            for (int q = 0; q < NR; ++q) acc[q] = fma(-tile[c][r], sx[c][q], acc[q]);
-          }
-          for (int c = 32; c < nr; ++c) chain_step(c, c - 32, r == c, r > c && r < nr);
-        }
+        for (int c = 32; c < nr; ++c) chain_step(c, c - 32, r == c, r > c && r < nr, false);
       } else {
-        for (int c = nr - 1; c >= 32; --c) {
-#pragma unroll
-          for (int q = 0; q < NR; ++q) acc[q] = fma(-tile[c][r], sx[c][q], acc[q]);
-        }
-        for (int c = min(nr, 32) - 1; c >= 0; --c) chain_step(c, c, lane == c, r < c);
+        for (int c = min(nr, 32) - 1; c >= 0; --c) chain_step(c, c, lane == c, r < c, false);
       }
     }
   }
   cp_async_wait<0>();
-  if (valid && tid < kTS) {
-#pragma unroll
-    for (int q = 0; q < NR; ++q)
-      if (q < nrhs) {
-        const T v = SweepBits<T>::canon(acc[q]);
-        if (FWD) Y[(r0 + r) + q * ldy] = v;
-        else Out[(TRANS ? (int64_t)perm[r0 + r] : r0 + r) + q * ldo] = v;
-      }
-  }
+  if (!kEarly && valid && tid < kTS) publish_row();
   (void)flags;
 }
 
