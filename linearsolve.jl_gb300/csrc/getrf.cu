@@ -28,6 +28,7 @@
 #include <cooperative_groups.h>
 
 #include "device_util.cuh"
+#include "waits.cuh"
 #include "gblu_internal.h"
 #include "profile.h"
 
@@ -435,52 +436,6 @@ __device__ __forceinline__ T with_sign_of(T x, T s) {
   else
     return __longlong_as_double(__double_as_longlong(x) ^
                                 (__double_as_longlong(s) & (long long)0x8000000000000000ull));
-}
-
-// Shared-memory addresses, cluster mapping, st.async and the mbarrier steps
-// of the panel exchange.
-__device__ __forceinline__ uint32_t pan_saddr(const void* p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ uint32_t pan_mapa(uint32_t a, int rank) {
-  uint32_t r;
-  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
-  return r;
-}
-__device__ __forceinline__ void pan_st_async(uint32_t raddr, int4 v, uint32_t rbar) {
-  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.b32 [%0], {%1, %2, %3, %4}, [%5];"
-               ::"r"(raddr), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w), "r"(rbar)
-               : "memory");
-}
-__device__ __forceinline__ void pan_bar_init(uint32_t a) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(a) : "memory");
-}
-__device__ __forceinline__ void pan_bar_arm(uint32_t a, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(a), "r"(bytes) : "memory");
-}
-// Bounded wait for the phase of the given parity; false when it gave up
-// (the error word is set).
-__device__ __forceinline__ bool pan_bar_wait(uint32_t a, uint32_t parity, int* err) {
-  unsigned long long t0 = 0;
-  for (uint32_t it = 0;; ++it) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(a), "r"(parity)
-        : "memory");
-    if (ok) return true;
-    if ((it & 63u) == 0) {
-      const unsigned long long now = global_ns();
-      if (t0 == 0) t0 = now;
-      else if (now - t0 > kSpinTimeoutNs) {
-        atomicCAS(err, 0, (int)DEV_TIMEOUT_PANEL);
-        return false;
-      }
-    }
-  }
 }
 
 template <typename T, int RPT>

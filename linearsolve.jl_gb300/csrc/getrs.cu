@@ -18,6 +18,7 @@
 #include <algorithm>
 
 #include "device_util.cuh"
+#include "waits.cuh"
 #include "gblu_internal.h"
 #include "profile.h"
 
@@ -48,64 +49,6 @@ __device__ __forceinline__ bool wait_flag(const int32_t* flags, int j, DevScratc
   }
   __syncthreads();
   return ok != 0;
-}
-
-// Published solution values are polled directly: the buffers a sweep's
-// dependents read are filled with an all-ones bit pattern (a NaN no
-// computation produces, outputs are written with canonical NaNs) before the
-// sweep, and each 4/8-byte value is single-copy atomic, so a value that is not
-// the sentinel is final.  This saves the flag round trip per tile.
-template <typename T>
-struct SweepBits;
-template <>
-struct SweepBits<double> {
-  using U = unsigned long long;
-  static constexpr U kSentinel = ~0ull;
-  static __device__ __forceinline__ U load(const double* p) {
-    U v;
-    asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-    return v;
-  }
-  static __device__ __forceinline__ double as_t(U v) { return __longlong_as_double((long long)v); }
-  // NaN -> the canonical quiet NaN, on the integer pipe
-  static __device__ __forceinline__ double canon(double v) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
-    return (b << 1) > 0xffe0000000000000ull ? __longlong_as_double(0x7ff8000000000000ll) : v;
-  }
-};
-template <>
-struct SweepBits<float> {
-  using U = unsigned;
-  static constexpr U kSentinel = ~0u;
-  static __device__ __forceinline__ U load(const float* p) {
-    U v;
-    asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-  }
-  static __device__ __forceinline__ float as_t(U v) { return __uint_as_float(v); }
-  static __device__ __forceinline__ float canon(float v) {
-    return (__float_as_uint(v) << 1) > 0xff000000u ? __uint_as_float(0x7fc00000u) : v;
-  }
-};
-
-// Wait for one published value; false on timeout or when another CTA failed.
-template <typename T>
-__device__ __forceinline__ bool poll_value(const T* p, DevScratch* scr, T* out) {
-  using B = SweepBits<T>;
-  unsigned long long t0 = 0;
-  for (unsigned it = 0;; ++it) {
-    const typename B::U v = B::load(p);
-    if (v != B::kSentinel) { *out = B::as_t(v); return true; }
-    if ((it & 63u) == 63u) {
-      if (ld_volatile_i32(&scr->error) != 0) return false;
-      const unsigned long long now = global_ns();
-      if (t0 == 0) t0 = now;
-      else if (now - t0 > kSpinTimeoutNs) {
-        atomicCAS(&scr->error, 0, (int)DEV_TIMEOUT_SOLVE);
-        return false;
-      }
-    }
-  }
 }
 
 constexpr int kSweepThreads = 128;  // all issue copies; threads 0..63 own one row each
