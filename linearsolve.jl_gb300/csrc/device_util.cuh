@@ -37,16 +37,6 @@ __device__ __forceinline__ int ld_volatile_i32(const int* p) {
   return *(volatile const int*)p;
 }
 
-// The two halves of a cluster barrier: shared-memory writes made before
-// cluster_arrive() are visible to every CTA of the cluster after its
-// cluster_wait(); work placed between the two overlaps the barrier.
-__device__ __forceinline__ void cluster_arrive() {
-  asm volatile("barrier.cluster.arrive.release;" ::: "memory");
-}
-__device__ __forceinline__ void cluster_wait() {
-  asm volatile("barrier.cluster.wait.acquire;" ::: "memory");
-}
-
 // Named CTA barrier `id` (1..15) over `nthreads` threads (a multiple of 32):
 // arrive does not wait, sync waits for all nthreads.
 __device__ __forceinline__ void named_bar_arrive(int id, int nthreads) {
