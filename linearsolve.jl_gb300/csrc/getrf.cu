@@ -934,15 +934,98 @@ gemm_sub_kernel(int64_t M, int64_t N, int64_t K, const T* __restrict__ A, int64_
     }
 }
 
+// FP32 update with a 128 x 128 tile and an 8 x 8 register block per thread
+// (rows tx*4 .. tx*4+3 and 64+tx*4 .. 64+tx*4+3, the same for columns), so
+// each k step reads four float4 from shared memory for 64 FMAs; the next
+// 8-deep k slice is fetched into registers while the current one is used.
+// Every C element is loaded first and updated by fma(-a_k, b_k, c) for k
+// ascending, as in gemm_sub_kernel.
+constexpr int kRbK = 8;
+
+__global__ void __launch_bounds__(256, 2)
+gemm_sub_f32_rb_kernel(int64_t M, int64_t N, int64_t K, const float* __restrict__ A, int64_t lda,
+                       const float* __restrict__ B, int64_t ldb, float* __restrict__ C, int64_t ldc) {
+  constexpr int BM = 128, BN = 128, BK = kRbK;
+  __shared__ __align__(16) float sA[BK][BM];      // sA[k][i] = A[m0 + i, k0 + k]
+  __shared__ __align__(16) float sB[BK][BN + 4];  // sB[k][j] = B[k0 + k, n0 + j] (padded: conflict-free stores)
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const int64_t m0 = (int64_t)blockIdx.x * BM, n0 = (int64_t)blockIdx.y * BN;
+  float c[8][8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int64_t r = m0 + tx * 4 + (i & 3) + (i >> 2) * 64, cc = n0 + ty * 4 + (j & 3) + (j >> 2) * 64;
+      c[i][j] = (r < M && cc < N) ? C[r + cc * ldc] : 0.f;
+    }
+  // this thread's share of a k slice: A elements (kk = idx / 128, i = idx % 128)
+  // and B elements (kb = idx % 8, j = idx / 8) for idx = tid + 256 q, q < 4
+  float pa[4], pb[4];
+  auto fetch = [&](int64_t k0) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int idx = tid + 256 * q;
+      const int kk = idx >> 7, i = idx & 127;
+      const int64_t r = m0 + i, kc = k0 + kk;
+      pa[q] = (r < M && kc < K) ? A[r + kc * lda] : 0.f;
+      const int kb = idx & 7, j = idx >> 3;
+      const int64_t kr = k0 + kb, cc = n0 + j;
+      pb[q] = (kr < K && cc < N) ? B[kr + cc * ldb] : 0.f;
+    }
+  };
+  auto stash = [&]() {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int idx = tid + 256 * q;
+      sA[idx >> 7][idx & 127] = pa[q];
+      sB[idx & 7][idx >> 3] = pb[q];
+    }
+  };
+  fetch(0);
+  stash();
+  __syncthreads();
+  for (int64_t k0 = 0; k0 < K; k0 += BK) {
+    const bool more = k0 + BK < K;
+    if (more) fetch(k0 + BK);  // in flight while this slice is used
+    const int kmax = (int)min((int64_t)BK, K - k0);
+    for (int kk = 0; kk < kmax; ++kk) {
+      const float4 a0 = *reinterpret_cast<const float4*>(&sA[kk][tx * 4]);
+      const float4 a1 = *reinterpret_cast<const float4*>(&sA[kk][64 + tx * 4]);
+      const float4 b0 = *reinterpret_cast<const float4*>(&sB[kk][ty * 4]);
+      const float4 b1 = *reinterpret_cast<const float4*>(&sB[kk][64 + ty * 4]);
+      const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+      const float b[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) c[i][j] = fmaf(-a[i], b[j], c[i][j]);
+    }
+    __syncthreads();
+    if (more) {
+      stash();
+      __syncthreads();
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int64_t r = m0 + tx * 4 + (i & 3) + (i >> 2) * 64, cc = n0 + ty * 4 + (j & 3) + (j >> 2) * 64;
+      if (r < M && cc < N) C[r + cc * ldc] = c[i][j];
+    }
+}
+
 // The tile for an M x N update.  FP64: the least work on the busiest SM,
 // ceil(tiles / SMs) x BM x BN, ties to the larger tile (the FP64 pipe is the
 // bound: timing every update shape of the n = 8192 and 16384 recursions with
 // each tile, this rule came within 0.1 % of the best tile per shape, and the
-// smaller tiles' extra loads cost nothing measurable).  FP32: 64 x 64 unless
-// that leaves SMs without a tile, then 32 x 32, then 16 x 16.
+// smaller tiles' extra loads cost nothing measurable).  FP32: the largest of
+// 128 x 128 (register-blocked kernel), 64 x 64, 32 x 32 whose tiles cover the
+// SMs, else 16 x 16.
 inline int gemm_tile_choice(int64_t M, int64_t N, int sms, int elem_size) {
   auto tiles = [&](int b) { return ((M + b - 1) / b) * ((N + b - 1) / b); };
   if (elem_size == 4) {
+    if (tiles(128) >= sms) return 128;
     if (tiles(64) >= sms) return 64;
     if (tiles(32) >= sms) return 32;
     return 16;
@@ -957,21 +1040,29 @@ inline int gemm_tile_choice(int64_t M, int64_t N, int sms, int elem_size) {
   return best;
 }
 
-// GBLU_GEMM_TILE=64|32|16 forces the SIMT update's tile (the tiles give
+// GBLU_GEMM_TILE=128|64|32|16 forces the SIMT update's tile (128: FP32 only,
+// 64 for FP64; the tiles give
 // identical results), so each variant can be tested on small matrices.
 int forced_gemm_tile() {
   const char* e = getenv("GBLU_GEMM_TILE");
   if (!e) return 0;
   const int t = atoi(e);
-  return (t == 64 || t == 32 || t == 16) ? t : 0;
+  return (t == 128 || t == 64 || t == 32 || t == 16) ? t : 0;
 }
 
 // forced: 0 = gemm_tile_choice, else the tile edge (64, 32 or 16)
 template <typename T>
 void gemm_sub_launch(int64_t M, int64_t N, int64_t K, const T* A, int64_t lda, const T* B, int64_t ldb,
                      T* C, int64_t ldc, int sms, int forced, cudaStream_t s) {
-  const int t = forced ? forced : gemm_tile_choice(M, N, sms, (int)sizeof(T));
+  int t = forced ? forced : gemm_tile_choice(M, N, sms, (int)sizeof(T));
+  if (t == 128 && sizeof(T) != 4) t = 64;
   dim3 grid((unsigned)((M + t - 1) / t), (unsigned)((N + t - 1) / t));
+  if constexpr (std::is_same<T, float>::value) {
+    if (t == 128) {
+      gemm_sub_f32_rb_kernel<<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc);
+      return;
+    }
+  }
   if (t == 64) gemm_sub_kernel<T, 64, 64><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc);
   else if (t == 32) gemm_sub_kernel<T, 32, 32><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc);
   else gemm_sub_kernel<T, 16, 16><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc);

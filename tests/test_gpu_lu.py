@@ -275,11 +275,12 @@ def test_every_panel_kernel_bit_exact(ctx, oracle_mod, monkeypatch, kind, prec):
         f.close()
 
 
-@pytest.mark.parametrize("tile", ["64", "32", "16"])
+@pytest.mark.parametrize("tile", ["128", "64", "32", "16"])
 @pytest.mark.parametrize("prec", ["fp64", "fp32"])
 def test_every_gemm_tile_bit_exact(ctx, oracle_mod, monkeypatch, tile, prec):
-    # the SIMT trailing update picks a 64, 32 or 16 square tile by shape;
-    # GBLU_GEMM_TILE forces one for every update (same per-element order)
+    # the SIMT trailing update picks a 128 (FP32 register-blocked kernel), 64,
+    # 32 or 16 square tile by shape; GBLU_GEMM_TILE forces one for every
+    # update (same per-element order)
     monkeypatch.setenv("GBLU_GEMM_TILE", tile)
     rng = np.random.default_rng(79)
     dt = np.float32 if prec == "fp32" else np.float64
