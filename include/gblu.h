@@ -128,6 +128,13 @@ int32_t gblu_get_ipiv(gblu_ctx* ctx, gblu_factor* f, int64_t* ipiv_host);
 int32_t gblu_get_factors(gblu_ctx* ctx, gblu_factor* f, double* host, int64_t ld);
 /* info of the last getrf on f. */
 int32_t gblu_get_info(gblu_ctx* ctx, gblu_factor* f, int64_t* info);
+/* Pivot growth max_ij |U_ij| / max_ij |A_ij| of the last getrf on a
+ * mixed-precision factor (GBLU_FP32 / BF16 / FP16), computed on the device:
+ * max |A| over the FP64 input as it is converted, max |U| over the
+ * low-precision factors after getrf (0 for GBLU_FP64 factors).  The refined
+ * solve compares it with gblu_refine_opts.growth_limit.  No counterpart in
+ * the reference. */
+int32_t gblu_get_growth(gblu_ctx* ctx, gblu_factor* f, double* growth);
 
 /* ---- mixed precision and iterative refinement --------------------------------
  * A GBLU_FP32 factor holds FP32 L\U factors; solves reach FP64 accuracy by
@@ -150,7 +157,20 @@ typedef struct gblu_refine_opts {
   int32_t fallback;      /* nonzero: FP64 LU when refinement stalls          */
   int32_t gmres_restart; /* GMRES basis size (<= 30)                          */
   double gmres_tol;      /* relative residual target of each GMRES solve     */
+  double growth_limit;   /* pivot growth max|U| / max|A| of the low-precision
+                            factors above which the solve goes to the FP64
+                            LU at once, without refining (<= 0: 1 / u of the
+                            factorization's arithmetic: 2^24 for FP32, 2^11
+                            for FP16 operands, 2^8 for BF16 operands, the
+                            growth at which its rounding errors reach the size
+                            of A's entries)                                   */
 } gblu_refine_opts;
+
+/* Why the FP64 fallback produced an answer (gblu_refine_stats.fallback_reason). */
+#define GBLU_FALLBACK_NONE 0
+#define GBLU_FALLBACK_STALL 1      /* backward error stopped decreasing / max_iter */
+#define GBLU_FALLBACK_GROWTH 2     /* pivot growth above growth_limit             */
+#define GBLU_FALLBACK_ZERO_PIVOT 3 /* exact zero pivot in the low-precision LU    */
 
 typedef struct gblu_refine_stats {
   int32_t iterations;       /* outer iterations taken (max over columns)     */
@@ -158,6 +178,9 @@ typedef struct gblu_refine_stats {
   int32_t converged;        /* 1 if every column met tol                     */
   int32_t fell_back;        /* 1 if the FP64 fallback produced the answer    */
   double backward_error;    /* final max_j ||b-Ax||/(||A|| ||x|| + ||b||), inf-norms */
+  double growth;            /* pivot growth of the factors (gblu_get_growth) */
+  int32_t fallback_reason;  /* GBLU_FALLBACK_*                                */
+  int32_t pad_;
 } gblu_refine_stats;
 
 int32_t gblu_refine_opts_default(gblu_refine_opts* opts);

@@ -50,15 +50,22 @@ class RefineOpts(ctypes.Structure):
     _fields_ = [
         ("mode", ctypes.c_int32), ("max_iter", ctypes.c_int32), ("tol", ctypes.c_double),
         ("fallback", ctypes.c_int32), ("gmres_restart", ctypes.c_int32),
-        ("gmres_tol", ctypes.c_double),
+        ("gmres_tol", ctypes.c_double), ("growth_limit", ctypes.c_double),
     ]
+
+
+GBLU_FALLBACK_NONE = 0
+GBLU_FALLBACK_STALL = 1
+GBLU_FALLBACK_GROWTH = 2
+GBLU_FALLBACK_ZERO_PIVOT = 3
 
 
 class RefineStats(ctypes.Structure):
     _fields_ = [
         ("iterations", ctypes.c_int32), ("inner_iterations", ctypes.c_int32),
         ("converged", ctypes.c_int32), ("fell_back", ctypes.c_int32),
-        ("backward_error", ctypes.c_double),
+        ("backward_error", ctypes.c_double), ("growth", ctypes.c_double),
+        ("fallback_reason", ctypes.c_int32), ("pad_", ctypes.c_int32),
     ]
 
 
@@ -124,6 +131,7 @@ SIGNATURES = {
     "gblu_get_ipiv": (_I32, [_P, _P, _P]),
     "gblu_get_factors": (_I32, [_P, _P, _P, _I64]),
     "gblu_get_info": (_I32, [_P, _P, _PI64]),
+    "gblu_get_growth": (_I32, [_P, _P, ctypes.POINTER(ctypes.c_double)]),
     "gblu_refine_opts_default": (_I32, [ctypes.POINTER(RefineOpts)]),
     "gblu_solve_refined": (_I32, [_P, _P, ctypes.c_char, _I64, _P, _I64, _I32,
                                   ctypes.POINTER(RefineOpts), ctypes.POINTER(RefineStats)]),

@@ -392,12 +392,17 @@ cudaError_t run_getrf(gblu_ctx* ctx, gblu_factor* f, Launch&& launch) {
   if (direct) return launch();
   if (!f->getrf_exec) {
     cudaGraph_t g = nullptr;
+    // the launches counted while capturing are kept with the graph and added
+    // at each replay (a replay does not pass through LaunchScope)
+    const LaunchCounts before = ctx->prof.counts();
     cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
       const cudaError_t le = launch();
       e = cudaStreamEndCapture(ctx->stream, &g);
       if (le != cudaSuccess) e = le;
     }
+    f->getrf_graph_counts = Profiler::diff(before, ctx->prof.counts());
+    ctx->prof.sub(f->getrf_graph_counts);  // counted again below, per launch
     if (e == cudaSuccess && g) e = cudaGraphInstantiate(&f->getrf_exec, g, 0);
     if (g) cudaGraphDestroy(g);
     if (e != cudaSuccess || !f->getrf_exec) {
@@ -407,6 +412,7 @@ cudaError_t run_getrf(gblu_ctx* ctx, gblu_factor* f, Launch&& launch) {
       return launch();
     }
   }
+  ctx->prof.add(f->getrf_graph_counts);
   return cudaGraphLaunch(f->getrf_exec, ctx->stream);
 }
 
@@ -427,15 +433,22 @@ int32_t factor_getrf(gblu_ctx* ctx, gblu_factor* f, const double* A, int64_t lda
        "preparing mixed-precision factorization");
     CK(ctx, run_getrf(ctx, f, [&] { return getrf_launch<float>(f->rf32, ctx->stream); }),
        "launching getrf");
+    CK(ctx, refine_growth_launch(f->refine, f->n, f->lu32, f->ld, ctx->stream), "pivot growth");
   }
   int64_t hinfo = 0;
+  unsigned long long umax_bits = 0;
   CK(ctx, cudaMemcpyAsync(&hinfo, f->info_dev, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream),
      "reading info");
+  if (f->precision != GBLU_FP64)
+    CK(ctx, cudaMemcpyAsync(&umax_bits, f->refine.growth_bits + 1, sizeof(umax_bits),
+                            cudaMemcpyDeviceToHost, ctx->stream),
+       "reading pivot growth");
   CK(ctx, cudaStreamSynchronize(ctx->stream), "getrf");
   st = check_device_errors(ctx, {f->precision == GBLU_FP64 ? f->rf64.scratch : f->rf32.scratch});
   if (st) return st;
   f->info = hinfo;
   f->use_fb = false;
+  f->growth = f->precision == GBLU_FP64 ? 0.0 : refine_growth(f->refine, umax_bits);
   if (f->precision != GBLU_FP64 && hinfo != 0) {
     // An exactly zero pivot in the low-precision factors: decide singularity
     // with the FP64 factorization, which then serves every solve.
@@ -678,6 +691,13 @@ int32_t gblu_get_info(gblu_ctx* ctx, gblu_factor* f, int64_t* info) {
   if (!ctx || !f || !info) return fail(ctx, GBLU_EINVAL, "gblu_get_info: NULL argument");
   if (!f->factored) return fail(ctx, GBLU_ENOTFACTORED, "gblu_get_info: no factorization");
   *info = f->info;
+  return GBLU_OK;
+}
+
+int32_t gblu_get_growth(gblu_ctx* ctx, gblu_factor* f, double* growth) {
+  if (!ctx || !f || !growth) return fail(ctx, GBLU_EINVAL, "gblu_get_growth: NULL argument");
+  if (!f->factored) return fail(ctx, GBLU_ENOTFACTORED, "gblu_get_growth: no factorization");
+  *growth = f->growth;
   return GBLU_OK;
 }
 

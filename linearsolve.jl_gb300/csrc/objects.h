@@ -52,9 +52,11 @@ struct gblu_factor {
   gblu::GetrsPlan<double> fb_rs;
   bool fb_valid = false;   // fallback factors hold the current A
   bool use_fb = false;     // solves go straight to the fallback factors
+  double growth = 0;       // max|U| / max|A| of the last low-precision getrf
   // the factorization's launch sequence, captured on its second run and
   // replayed from then on (it depends only on the factor's shape)
   cudaGraphExec_t getrf_exec = nullptr;
+  gblu::LaunchCounts getrf_graph_counts;  // the captured sequence's launches
   int getrf_runs = 0;
   bool getrf_graph_failed = false;
 };

@@ -23,6 +23,15 @@ enum KernelKind : int {
   K_NKINDS = 9,
 };
 
+// Launch counts and algorithmic work of a launch sequence (a captured graph
+// replays them without passing through a LaunchScope).
+struct LaunchCounts {
+  uint64_t launches = 0;
+  uint64_t count[K_NKINDS] = {};
+  double flops[K_NKINDS] = {};
+  double bytes[K_NKINDS] = {};
+};
+
 struct Profiler {
   bool enabled = false;
   uint64_t launches = 0;
@@ -30,6 +39,29 @@ struct Profiler {
   double ms[K_NKINDS] = {};
   double flops[K_NKINDS] = {};
   double bytes[K_NKINDS] = {};
+
+  LaunchCounts counts() const {
+    LaunchCounts c;
+    c.launches = launches;
+    for (int k = 0; k < K_NKINDS; ++k) c.count[k] = count[k], c.flops[k] = flops[k], c.bytes[k] = bytes[k];
+    return c;
+  }
+  static LaunchCounts diff(const LaunchCounts& a, const LaunchCounts& b) {  // b - a
+    LaunchCounts c;
+    c.launches = b.launches - a.launches;
+    for (int k = 0; k < K_NKINDS; ++k)
+      c.count[k] = b.count[k] - a.count[k], c.flops[k] = b.flops[k] - a.flops[k],
+      c.bytes[k] = b.bytes[k] - a.bytes[k];
+    return c;
+  }
+  void add(const LaunchCounts& c) {
+    launches += c.launches;
+    for (int k = 0; k < K_NKINDS; ++k) count[k] += c.count[k], flops[k] += c.flops[k], bytes[k] += c.bytes[k];
+  }
+  void sub(const LaunchCounts& c) {
+    launches -= c.launches;
+    for (int k = 0; k < K_NKINDS; ++k) count[k] -= c.count[k], flops[k] -= c.flops[k], bytes[k] -= c.bytes[k];
+  }
   struct Pending {
     int kind;
     double flops, bytes;

@@ -28,20 +28,56 @@ constexpr int kMaxW = 8;
 // ---------------------------------------------------------------------------
 // kernels
 
-__global__ void convert_f64_f32_kernel(int64_t rows, int64_t cols, const double* __restrict__ A,
-                                       int64_t lda, float* __restrict__ B, int64_t ldb) {
-  const int64_t total = rows * cols;
-  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
-       idx += (int64_t)gridDim.x * blockDim.x) {
-    int64_t j = idx / rows, i = idx - j * rows;
-    B[i + j * ldb] = (float)A[i + j * lda];
-  }
-}
-
 __device__ __forceinline__ void atomic_max_nonneg(unsigned long long* p, double v) {
   // non-negative doubles order like their bit patterns; NaN maps above +inf
   unsigned long long bits = isnan(v) ? 0x7ff8000000000000ull : (unsigned long long)__double_as_longlong(v);
   atomicMax(p, bits);
+}
+
+// Block-wide max of non-negative v (NaN wins) folded into *p by thread 0.
+__device__ __forceinline__ void block_max_into(double v, unsigned long long* p) {
+  __shared__ double red[32];
+  for (int off = 16; off; off >>= 1) {
+    const double o = __shfl_down_sync(0xffffffffu, v, off);
+    v = (o > v || isnan(o)) ? o : v;
+  }
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double m = 0.0;
+    for (int w = 0; w < (int)((blockDim.x + 31) >> 5); ++w) m = (red[w] > m || isnan(red[w])) ? red[w] : m;
+    atomic_max_nonneg(p, m);
+  }
+}
+
+// B = float(A), and max |A_ij| (the denominator of the pivot growth) into *amax.
+__global__ void convert_f64_f32_kernel(int64_t rows, int64_t cols, const double* __restrict__ A,
+                                       int64_t lda, float* __restrict__ B, int64_t ldb,
+                                       unsigned long long* __restrict__ amax) {
+  const int64_t total = rows * cols;
+  double mx = 0.0;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    int64_t j = idx / rows, i = idx - j * rows;
+    const double a = A[i + j * lda];
+    B[i + j * ldb] = (float)a;
+    const double v = fabs(a);
+    mx = (v > mx || isnan(v)) ? v : mx;
+  }
+  block_max_into(mx, amax);
+}
+
+// max |U_ij| over the upper triangle of the n x n FP32 factors; one CTA per
+// column, rows 0..j.
+__global__ void umax_kernel(int64_t n, const float* __restrict__ LU, int64_t ld,
+                            unsigned long long* __restrict__ umax) {
+  const int64_t j = blockIdx.x;
+  double mx = 0.0;
+  for (int64_t i = threadIdx.x; i <= j; i += blockDim.x) {
+    const double v = fabs((double)LU[i + j * ld]);
+    mx = (v > mx || isnan(v)) ? v : mx;
+  }
+  block_max_into(mx, umax);
 }
 
 // P[s][q][i] = sum_{j in chunk s} op(A)[i, j] * X[j, q]
@@ -234,6 +270,7 @@ size_t refine_bytes(int64_t n, int64_t W) {
   b += align256((size_t)kDotBlocks * (kGmresRestart + 1) * sizeof(double));
   b += align256(4 * sizeof(double) * kMaxW);               // scales
   b += align256(sizeof(double));                           // anorm
+  b += align256(2 * sizeof(unsigned long long));           // growth words
   return b + 256;
 }
 
@@ -255,6 +292,7 @@ void refine_carve(RefineWork& w, char* base, int64_t n, int64_t W) {
   w.colmax = reinterpret_cast<unsigned long long*>(take(4 * W * sizeof(unsigned long long)));
   w.dots = reinterpret_cast<double*>(take((size_t)kDotBlocks * (kGmresRestart + 1) * sizeof(double)));
   w.anorm_dev = reinterpret_cast<double*>(take(4 * sizeof(double) * kMaxW));
+  w.growth_bits = reinterpret_cast<unsigned long long*>(take(2 * sizeof(unsigned long long)));
 }
 
 namespace {
@@ -309,22 +347,49 @@ double bits_to_double(unsigned long long b) {
 
 cudaError_t refine_prepare(RefineWork& w, int64_t n, const double* A, int64_t lda, float* A32,
                            int64_t ld32, cudaStream_t s) {
-  if (n == 0) { w.anorm = 0; return cudaSuccess; }
-  { LaunchScope ls_(K_REFINE, 0.0, 0.0, s);
-  convert_f64_f32_kernel<<<grid_for(n * n), 256, 0, s>>>(n, n, A, lda, A32, ld32);
+  if (n == 0) { w.anorm = 0; w.amax = 0; return cudaSuccess; }
+  cudaError_t e = cudaMemsetAsync(w.growth_bits, 0, 2 * sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return e;
+  { LaunchScope ls_(K_REFINE, 0.0, 12.0 * n * n, s);
+  convert_f64_f32_kernel<<<grid_for(n * n), 256, 0, s>>>(n, n, A, lda, A32, ld32, w.growth_bits);
   }
-  cudaError_t e = cudaGetLastError();
+  e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   // ||A||_inf = max_i sum_j |A[i,j]|
   e = cudaMemsetAsync(w.colmax, 0, sizeof(unsigned long long), s);
   if (e != cudaSuccess) return e;
   e = gemv('N', n, n, A, lda, nullptr, 1, 1, 1.0, nullptr, 1, 0.0, w.w, n, w.partial, w.colmax, s, true);
   if (e != cudaSuccess) return e;
-  unsigned long long bits = 0;
-  e = cudaMemcpyAsync(&bits, w.colmax, sizeof(bits), cudaMemcpyDeviceToHost, s);
+  unsigned long long bits[2] = {0, 0};
+  e = cudaMemcpyAsync(&bits[0], w.colmax, sizeof(bits[0]), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&bits[1], w.growth_bits, sizeof(bits[1]), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  w.anorm = bits_to_double(bits);
+  w.anorm = bits_to_double(bits[0]);
+  w.amax = bits_to_double(bits[1]);
   return e;
+}
+
+cudaError_t refine_growth_launch(RefineWork& w, int64_t n, const float* LU, int64_t ld, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  LaunchScope ls_(K_REFINE, 0.0, 2.0 * n * n, s);
+  umax_kernel<<<(unsigned)n, 256, 0, s>>>(n, LU, ld, w.growth_bits + 1);
+  return cudaGetLastError();
+}
+
+double refine_growth(const RefineWork& w, unsigned long long umax_bits) {
+  const double umax = bits_to_double(umax_bits);
+  if (!(umax <= INFINITY)) return INFINITY;  // NaN in the factors
+  if (w.amax > 0) return umax / w.amax;
+  return umax > 0 ? INFINITY : 1.0;
+}
+
+double growth_limit_default(int32_t precision) {
+  // 1 / u of the arithmetic the factors were computed in: FP32 (u = 2^-24),
+  // or the 16-bit operands of the tensor-core updates (FP16 2^-11, BF16 2^-8)
+  if (precision == GBLU_BF16) return 256.0;
+  if (precision == GBLU_FP16) return 2048.0;
+  return 16777216.0;
 }
 
 gblu_refine_opts refine_default_opts() {
@@ -335,6 +400,7 @@ gblu_refine_opts refine_default_opts() {
   o.fallback = 1;
   o.gmres_restart = kGmresRestart;
   o.gmres_tol = 1e-10;
+  o.growth_limit = 0.0;
   return o;
 }
 
@@ -528,8 +594,18 @@ int32_t refine_solve(gblu_ctx* ctx, gblu_factor* f, char trans, int64_t nrhs, do
   const int W = (int)w.W;
   gblu_refine_stats st_acc{};
   st_acc.converged = 1;
+  st_acc.growth = f->growth;
   Solver S{ctx, f, w, trans, s, n};
   if (stats) *stats = gblu_refine_stats{};
+  // Pivot growth (FP64 ratio of the device-computed maxima): factors whose
+  // rounding errors reach the size of A's entries go straight to the FP64 LU.
+  const double glimit = o.growth_limit > 0 ? o.growth_limit : growth_limit_default(f->precision);
+  const bool growth_fb = !f->use_fb && !(f->growth <= glimit);
+  if (growth_fb && !o.fallback)
+    return fail(ctx, GBLU_ESTALL, "pivot growth %.3e of the low-precision factors exceeds %.3e",
+                f->growth, glimit);
+  const int fb_reason = f->use_fb ? GBLU_FALLBACK_ZERO_PIVOT
+                                  : growth_fb ? GBLU_FALLBACK_GROWTH : GBLU_FALLBACK_STALL;
   for (int64_t c0 = 0; c0 < nrhs; c0 += W) {
     const int nc = (int)std::min<int64_t>(W, nrhs - c0);
     double* Bc = B + c0 * ldb;
@@ -544,7 +620,8 @@ int32_t refine_solve(gblu_ctx* ctx, gblu_factor* f, char trans, int64_t nrhs, do
     std::vector<int> state(nc, ACTIVE), slow(nc, 0), its_q(nc, 0);
     std::vector<double> rn(nc), xn(nc), bn(nc), prev(nc, INFINITY), be_q(nc, INFINITY);
     bool any_fb = false;
-    if (f->use_fb) {
+    const bool direct_fb = f->use_fb || growth_fb;  // no refinement at all
+    if (direct_fb) {
       for (int q = 0; q < nc; ++q) state[q] = STALLED;
     } else {
       GBLU_CK(ctx, cudaMemsetAsync(w.x, 0, (size_t)n * nc * sizeof(double), s), "x0");  // x0 = 0
@@ -610,7 +687,7 @@ int32_t refine_solve(gblu_ctx* ctx, gblu_factor* f, char trans, int64_t nrhs, do
                                        cudaMemcpyDeviceToDevice, s), "fallback column");
       int32_t e = S.residual(nc, rn.data(), xn.data());
       if (e) return e;
-      if (f->use_fb) {  // ||b|| was not measured yet
+      if (direct_fb) {  // ||b|| was not measured yet
         GBLU_CK(ctx, cudaMemsetAsync(w.colmax + 2 * w.W, 0, nc * sizeof(unsigned long long), s), "memset");
         {
           LaunchScope ls_(K_REFINE, 0.0, 0.0, s);
@@ -644,6 +721,7 @@ int32_t refine_solve(gblu_ctx* ctx, gblu_factor* f, char trans, int64_t nrhs, do
     if (e) return e;
     st_acc.iterations = std::max(st_acc.iterations, iters);
     st_acc.fell_back |= fell_back ? 1 : 0;
+    if (fell_back && st_acc.fallback_reason == GBLU_FALLBACK_NONE) st_acc.fallback_reason = fb_reason;
     if (!done) st_acc.converged = fell_back ? st_acc.converged : 0;
     st_acc.backward_error = std::max(st_acc.backward_error, berr_final);
   }

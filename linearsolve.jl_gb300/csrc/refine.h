@@ -26,6 +26,8 @@ struct RefineWork {
   double* dots = nullptr;   // kDotBlocks x (restart + 1)
   double anorm = 0;         // ||A||_inf of the FP64 matrix (host copy)
   double* anorm_dev = nullptr;
+  double amax = 0;          // max |A_ij| of the FP64 matrix (host copy)
+  unsigned long long* growth_bits = nullptr;  // [0] max|A| (FP64 bits), [1] max|U| (FP32 bits)
 };
 
 constexpr int kSplit = 16;       // column chunks of the residual GEMV
@@ -35,9 +37,18 @@ constexpr int kGmresRestart = 30;
 size_t refine_bytes(int64_t n, int64_t W);
 void refine_carve(RefineWork& w, char* base, int64_t n, int64_t W);
 
-// FP64 A (ld) -> FP32 A32 (ld32) and ||A||_inf, before the FP32 getrf.
+// FP64 A (ld) -> FP32 A32 (ld32), ||A||_inf and max |A_ij|, before the FP32 getrf.
 cudaError_t refine_prepare(RefineWork& w, int64_t n, const double* A, int64_t lda, float* A32,
                            int64_t ld32, cudaStream_t s);
+
+// max |U_ij| of the FP32 factors (upper triangle of LU) into w.growth_bits[1];
+// asynchronous, read back with refine_growth after the stream synchronises.
+cudaError_t refine_growth_launch(RefineWork& w, int64_t n, const float* LU, int64_t ld, cudaStream_t s);
+// max|U| / max|A| from the host copy of growth_bits (inf for a non-finite max|U|).
+double refine_growth(const RefineWork& w, unsigned long long umax_bits);
+
+// The default growth_limit of a factor precision (GBLU_FP32 / BF16 / FP16).
+double growth_limit_default(int32_t precision);
 
 gblu_refine_opts refine_default_opts();
 

@@ -1,6 +1,6 @@
 """Python handles over the C ABI: a context (device + stream + HBM budget) and
 device-resident factorizations.  This is the layer LinearCache drives; it is
-the Python twin of the Julia binding shown in INTEGRATION.md.
+the Python twin of the Julia binding in julia/GB300LinearSolve.jl.
 """
 from __future__ import annotations
 
@@ -147,7 +147,7 @@ class Factorization:
 
     def solve_refined(self, B, trans: str = "N", mode: str = "ir", max_iter: int = 30,
                       tol: float = 0.0, fallback: bool = True, gmres_restart: int = 30,
-                      gmres_tol: float = 1e-10):
+                      gmres_tol: float = 1e-10, growth_limit: float = 0.0):
         """Refined solve; returns (X, stats dict)."""
         o = RefineOpts()
         check(self.lib.gblu_refine_opts_default(ctypes.byref(o)), None)
@@ -157,6 +157,7 @@ class Factorization:
         o.fallback = 1 if fallback else 0
         o.gmres_restart = int(gmres_restart)
         o.gmres_tol = float(gmres_tol)
+        o.growth_limit = float(growth_limit)
         s = RefineStats()
         if isinstance(B, DeviceMatrix):
             check(self.lib.gblu_solve_refined(self.ctx.handle, self.handle, trans.encode(), B.cols,
@@ -172,8 +173,14 @@ class Factorization:
                                               _lib.GBLU_HOST, ctypes.byref(o), ctypes.byref(s)),
                   self.ctx.handle)
             X = X[:, 0].copy() if vec else X
-        stats = {k: getattr(s, k) for k, _ in RefineStats._fields_}
+        stats = {k: getattr(s, k) for k, _ in RefineStats._fields_ if k != "pad_"}
         return X, stats
+
+    def growth(self) -> float:
+        """Pivot growth max|U| / max|A| of the last getrf (mixed precisions)."""
+        g = ctypes.c_double()
+        check(self.lib.gblu_get_growth(self.ctx.handle, self.handle, ctypes.byref(g)), self.ctx.handle)
+        return float(g.value)
 
     # -- inspection ------------------------------------------------------------
     def ipiv(self) -> np.ndarray:

@@ -35,6 +35,97 @@ def test_ill_conditioned(ctx, oracle_mod, pkg, mode):
     f.close()
 
 
+@pytest.fixture(scope="module")
+def kappa_1e6_n4096(pkg):
+    # A = Q1 diag(s) Q2^T, s log-spaced 1..1e6 (the hard mixed configuration
+    # at a quarter of its size), generated with FP64 QR on the GPU
+    return pkg.workloads.svd_conditioned_gpu(4096, 4, cond=1e6, seed=21)
+
+
+@pytest.fixture(scope="module")
+def kappa_1e6_fp64_solution(ctx, kappa_1e6_n4096):
+    A, B = kappa_1e6_n4096
+    f = ctx.factor(4096, 4096, "fp64")
+    assert f.getrf(A) == 0
+    X = f.getrs(B)
+    f.close()
+    return X
+
+
+@pytest.mark.parametrize("mode", ["ir", "gmres_ir"])
+def test_kappa_1e6_n4096(ctx, oracle_mod, kappa_1e6_n4096, kappa_1e6_fp64_solution, mode):
+    """FP32 LU + FP64 IR / GMRES-IR on a cond = 1e6 matrix of n = 4096 meets
+    the 10 n eps64 backward-error bound; GMRES-IR needs no fallback; a column
+    the fallback produced is the plain FP64 LU's answer bit for bit."""
+    A, B = kappa_1e6_n4096
+    n = A.shape[0]
+    f = ctx.factor(n, n, "fp32")
+    assert f.getrf(A) == 0
+    X, st = f.solve_refined(B, mode=mode)
+    be = oracle_mod.backward_error(A, X, B)
+    assert be <= 10 * n * EPS64, (be, st)
+    if mode == "gmres_ir":
+        assert st["fell_back"] == 0 and st["converged"] == 1, st
+    if st["fell_back"]:
+        X64 = kappa_1e6_fp64_solution
+        for j in range(B.shape[1]):
+            ok = np.array_equal(X[:, j], X64[:, j])
+            assert ok or oracle_mod.backward_error(A, X[:, j], B[:, j]) <= n * EPS64
+    f.close()
+
+
+def test_kappa_1e6_n4096_forced_fallback_bit_exact(ctx, kappa_1e6_n4096, kappa_1e6_fp64_solution):
+    """With no refinement allowed every column falls back, and the answer is
+    the plain FP64 LU's, bit for bit."""
+    A, B = kappa_1e6_n4096
+    n = A.shape[0]
+    f = ctx.factor(n, n, "fp32")
+    assert f.getrf(A) == 0
+    X, st = f.solve_refined(B, max_iter=0)
+    assert st["fell_back"] == 1
+    assert np.array_equal(X, kappa_1e6_fp64_solution)
+    f.close()
+
+
+@pytest.mark.parametrize("prec", ["fp32", "bf16", "fp16"])
+def test_pivot_growth_goes_to_fp64_at_once(ctx, oracle_mod, pkg, prec):
+    """Wilkinson's matrix (growth 2^(n-1) under partial pivoting): the device
+    computes the growth at getrf, the solve skips refinement and answers with
+    the plain FP64 LU, bit for bit; without fallback it is GBLU_ESTALL."""
+    n = 60
+    A, B = pkg.workloads.growth_matrix(n, 2, seed=1)
+    f = ctx.factor(n, n, prec)
+    assert f.getrf(A) == 0
+    assert f.growth() == 2.0 ** (n - 1)
+    X, st = f.solve_refined(B)
+    assert st["fell_back"] == 1 and st["fallback_reason"] == pkg._lib.GBLU_FALLBACK_GROWTH, st
+    assert st["iterations"] == 0 and st["growth"] == 2.0 ** (n - 1)
+    LU, ipiv, _ = oracle_mod.getrf(A)
+    assert np.array_equal(X, oracle_mod.getrs(LU, ipiv, B))
+    with pytest.raises(pkg.GBLUError) as ei:
+        f.solve_refined(B, fallback=False)
+    assert ei.value.status == 6  # GBLU_ESTALL
+    f.close()
+
+
+def test_growth_limit_option(ctx, oracle_mod, pkg):
+    """A benign matrix has growth O(1) and refines; a growth_limit below its
+    growth sends the same solve to the FP64 LU."""
+    n = 500
+    A, B = pkg.workloads.shifted(n, 2, seed=31)
+    f = ctx.factor(n, n, "fp32")
+    assert f.getrf(A) == 0
+    g = f.growth()
+    assert 0.5 <= g <= 2.0, g
+    X, st = f.solve_refined(B)
+    assert st["fell_back"] == 0 and st["fallback_reason"] == 0 and st["growth"] == g
+    X2, st2 = f.solve_refined(B, growth_limit=0.25)
+    assert st2["fell_back"] == 1 and st2["fallback_reason"] == pkg._lib.GBLU_FALLBACK_GROWTH
+    LU, ipiv, _ = oracle_mod.getrf(A)
+    assert np.array_equal(X2, oracle_mod.getrs(LU, ipiv, B))
+    f.close()
+
+
 def test_transposed_refined(ctx, oracle_mod, pkg):
     n = 300
     A, B = pkg.workloads.shifted(n, 2, seed=5)
