@@ -808,6 +808,52 @@ def run_serving_suite(pkg, cu, ctx, args):
     return out
 
 
+KERNEL_CASES = ("gemm_bf16", "gemm_fp16", "gemm_fp32", "refine", "perm")
+
+
+def run_kernel_case(args) -> int:
+    """One small invocation of a group of kernels, for ncu (no timing, no
+    JSON line): operands larger than L2 so DRAM counters mean something.
+      gemm_bf16 / gemm_fp16  C -= A B, M = N = K = 4096 through gblu_gemm_update
+                             (conv_a / col_scale / conv_b + tc_gemm_kernel)
+      gemm_fp32              the same on the FP32 SIMT path (gemm_sub_f32_rb_kernel)
+      refine                 FP32 factor of n = 6144 (convert_f64_f32, umax) and refined
+                             solves of 4 RHS, IR then GMRES-IR (gemv partial / reduce,
+                             colmax, pow2_scales, scale_to_f32, update_from_f32, axpby)
+      perm                   LAPACK-shaped dgetrs with host factors and pivots, n = 8192
+                             (upload_ipiv_check_kernel, perm_from_ipiv_kernel)"""
+    pkg = load_pkg()
+    _, _, local = dist_env()
+    ctx = pkg.Context(local)
+    rng = np.random.default_rng(5)
+    case = args.kernel_case
+    if case.startswith("gemm_"):
+        m = n = k = 4096
+        A = rng.uniform(-1, 1, size=(m, k)).astype(np.float32)
+        B = rng.standard_normal((k, n)).astype(np.float32)
+        C = rng.standard_normal((m, n)).astype(np.float32)
+        for _ in range(2):
+            ctx.gemm_update(C, A, B, case.split("_")[1])
+    elif case == "refine":
+        n = 6144
+        A, B = pkg.workloads.shifted(n, 4, seed=3)
+        f = ctx.factor(n, n, "fp32")
+        f.getrf(A)
+        f.solve_refined(B, mode="ir")
+        f.solve_refined(B, mode="gmres_ir")
+        f.close()
+    elif case == "perm":
+        n = 8192
+        A, B = pkg.workloads.plain(n, 1, seed=4)
+        LU, ipiv, _ = pkg.dgetrf(A)
+        pkg.dgetrs(LU, ipiv, B)
+    else:
+        raise SystemExit(f"unknown kernel case {case!r}; one of {KERNEL_CASES}")
+    ctx.close()
+    print(f"kernel case {case} done")
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -826,8 +872,12 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=1000)
     ap.add_argument("--mixed-n", type=int, default=16384)
     ap.add_argument("--serve-rates", type=float, nargs="*", default=[100.0, 400.0, 0.0])
+    ap.add_argument("--kernel-case", choices=KERNEL_CASES, default=None,
+                    help="run one small case of a kernel group once (for ncu) and exit")
     args = ap.parse_args()
     rank, world, local = dist_env()
+    if args.kernel_case:
+        return run_kernel_case(args)
     if args.impl == "reference":
         return run_reference(args, rank, world)
     return run_gpu(args, rank, world, local)

@@ -191,6 +191,23 @@ int32_t gblu_solve_refined(gblu_ctx* ctx, gblu_factor* f, char trans, int64_t nr
                            int64_t ldb, int32_t b_loc, const gblu_refine_opts* opts,
                            gblu_refine_stats* stats);
 
+/* ---- a-posteriori residual check ---------------------------------------------
+ * res_norm = ||B - op(A) X||_F and b_norm = ||B||_F (the 2-norms for one
+ * column), computed in FP64 on the device from the FP64 matrix of f's last
+ * getrf, with a fixed summation order.  A mixed-precision factor keeps that
+ * matrix anyway; a GBLU_FP64 factor factors A in place, so it keeps a copy
+ * only after gblu_factor_keep_matrix(ctx, f, 1) (the copy is taken at each
+ * later getrf; keep = 0 frees it).  X and B are n x nrhs (ldx, ldb) in host
+ * or device memory (loc).  A caller compares res_norm with
+ * abstol + reltol * b_norm.
+ * Replaces: _check_residual_safety (src/factorization.jl:127-156: mul!, axpy!
+ * and norm on the backed-up A), which solve!(cache, ::LUFactorization) runs
+ * after each refactorization when residualsafety = true (:647-651, :729-732). */
+int32_t gblu_factor_keep_matrix(gblu_ctx* ctx, gblu_factor* f, int32_t keep);
+int32_t gblu_residual_norm(gblu_ctx* ctx, gblu_factor* f, char trans, int64_t nrhs,
+                           const double* X, int64_t ldx, const double* B, int64_t ldb,
+                           int32_t loc, double* res_norm, double* b_norm);
+
 /* The trailing-update contraction of the mixed-precision getrf on its own:
  * C (m x n, FP32) -= A (m x k) * B (k x n), all column-major FP32 in memory.
  * precision GBLU_BF16 / GBLU_FP16: operands rounded to 16 bits (FP16 with a

@@ -18,7 +18,7 @@ from ._lib import GBLUError, load as load_library  # noqa: F401
 from .device import Context, Factorization, default_context, dgetrf, dgetrs  # noqa: F401
 from .linear import (  # noqa: F401
     DefaultAlgorithmChoice, DefaultLinearSolver, GB300LUFactorization, GB300MixedLUFactorization,
-    LinearAliasSpecifier, LinearCache, LinearProblem, LinearSolution, OperatorAssumptions,
+    GB300RFLUFactorization, LinearAliasSpecifier, RFLUCacheval, LinearCache, LinearProblem, LinearSolution, OperatorAssumptions,
     OperatorCondition, ReturnCode, defaultalg, init, reinit, solve, solve_bang, successful_retcode,
 )
 from ._cuda import DeviceMatrix, Event, PinnedArray  # noqa: F401

@@ -132,6 +132,9 @@ SIGNATURES = {
     "gblu_get_factors": (_I32, [_P, _P, _P, _I64]),
     "gblu_get_info": (_I32, [_P, _P, _PI64]),
     "gblu_get_growth": (_I32, [_P, _P, ctypes.POINTER(ctypes.c_double)]),
+    "gblu_factor_keep_matrix": (_I32, [_P, _P, _I32]),
+    "gblu_residual_norm": (_I32, [_P, _P, ctypes.c_char, _I64, _P, _I64, _P, _I64, _I32,
+                                  ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     "gblu_refine_opts_default": (_I32, [ctypes.POINTER(RefineOpts)]),
     "gblu_solve_refined": (_I32, [_P, _P, ctypes.c_char, _I64, _P, _I64, _I32,
                                   ctypes.POINTER(RefineOpts), ctypes.POINTER(RefineStats)]),

@@ -357,7 +357,30 @@ int32_t gblu_factor_destroy(gblu_ctx* ctx, gblu_factor* f) {
   ctx_free(ctx, f->arena, f->bytes);
   if (f->rhs) ctx_free(ctx, f->rhs, (size_t)f->ld * f->rhs_cols * sizeof(double));
   if (f->fb_arena) ctx_free(ctx, f->fb_arena, f->fb_bytes);
+  if (f->a_keep) ctx_free(ctx, f->a_keep, std::max<size_t>((size_t)f->ld * f->n * sizeof(double), 256));
+  if (f->chk_arena) ctx_free(ctx, f->chk_arena, f->chk_bytes);
   delete f;
+  return GBLU_OK;
+}
+
+int32_t gblu_factor_keep_matrix(gblu_ctx* ctx, gblu_factor* f, int32_t keep) {
+  if (!ctx || !f) return fail(ctx, GBLU_EINVAL, "gblu_factor_keep_matrix: NULL argument");
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  DeviceGuard g(ctx->device);
+  if (f->precision != GBLU_FP64) return GBLU_OK;  // mixed factors keep A anyway
+  const size_t bytes = (size_t)f->ld * f->n * sizeof(double);
+  if (keep && !f->a_keep) {
+    void* p = nullptr;
+    int32_t st = ctx_alloc(ctx, std::max<size_t>(bytes, 256), &p);
+    if (st) return st;
+    f->a_keep = reinterpret_cast<double*>(p);
+    f->a_keep_valid = false;
+  } else if (!keep && f->a_keep) {
+    cudaStreamSynchronize(ctx->stream);
+    ctx_free(ctx, f->a_keep, std::max<size_t>(bytes, 256));
+    f->a_keep = nullptr;
+    f->a_keep_valid = false;
+  }
   return GBLU_OK;
 }
 
@@ -424,6 +447,13 @@ int32_t factor_getrf(gblu_ctx* ctx, gblu_factor* f, const double* A, int64_t lda
   if (f->precision == GBLU_FP64) {
     st = upload_matrix(ctx, f->lu64, f->ld, A, lda, f->m, f->n, a_loc);
     if (st) return st;
+    f->a_keep_valid = false;
+    if (f->a_keep) {  // the copy residual checks read (gblu_factor_keep_matrix)
+      CK(ctx, cudaMemcpyAsync(f->a_keep, f->lu64, (size_t)f->ld * f->n * sizeof(double),
+                              cudaMemcpyDeviceToDevice, ctx->stream),
+         "keeping A");
+      f->a_keep_valid = true;
+    }
     CK(ctx, run_getrf(ctx, f, [&] { return getrf_launch<double>(f->rf64, ctx->stream); }),
        "launching getrf");
   } else {

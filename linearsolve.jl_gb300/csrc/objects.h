@@ -53,6 +53,12 @@ struct gblu_factor {
   bool fb_valid = false;   // fallback factors hold the current A
   bool use_fb = false;     // solves go straight to the fallback factors
   double growth = 0;       // max|U| / max|A| of the last low-precision getrf
+  // FP64 copy of A kept by a GBLU_FP64 factor for residual checks
+  double* a_keep = nullptr;
+  bool a_keep_valid = false;  // a_keep holds the matrix of the last getrf
+  // residual-check buffers (allocated on the first gblu_residual_norm)
+  void* chk_arena = nullptr;
+  uint64_t chk_bytes = 0;
   // the factorization's launch sequence, captured on its second run and
   // replayed from then on (it depends only on the factor's shape)
   cudaGraphExec_t getrf_exec = nullptr;

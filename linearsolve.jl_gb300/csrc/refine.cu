@@ -246,6 +246,39 @@ __global__ void update_from_f32_kernel(int64_t n, int W, double* __restrict__ X,
   }
 }
 
+// Sum of squares of each of W columns, in two fixed-order passes: block b of
+// column q sums rows b, b + kSumBlocks*256, ... (strided per thread, then a
+// shuffle / shared-memory tree) into part[q][b]; sumsq_final adds part[q][*]
+// in index order.  The result does not depend on scheduling.
+constexpr int kSumBlocks = 64;
+
+__global__ void __launch_bounds__(256)
+sumsq_partial_kernel(int64_t n, const double* __restrict__ X, int64_t ldx, double* __restrict__ part) {
+  __shared__ double red[8];
+  const int q = blockIdx.y;
+  double acc = 0.0;
+  for (int64_t i = blockIdx.x * 256 + threadIdx.x; i < n; i += (int64_t)kSumBlocks * 256) {
+    const double v = X[i + q * ldx];
+    acc = fma(v, v, acc);
+  }
+  for (int off = 16; off; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < 8; ++w) s += red[w];
+    part[q * kSumBlocks + blockIdx.x] = s;
+  }
+}
+
+__global__ void sumsq_final_kernel(int W, const double* __restrict__ part, double* __restrict__ out) {
+  const int q = threadIdx.x;
+  if (q >= W) return;
+  double s = 0.0;
+  for (int b = 0; b < kSumBlocks; ++b) s += part[q * kSumBlocks + b];
+  out[q] = s;
+}
+
 // Y = a*X + b*Y
 __global__ void axpby_kernel(int64_t n, double a, const double* __restrict__ X, double b,
                              double* __restrict__ Y) {
@@ -729,6 +762,75 @@ int32_t refine_solve(gblu_ctx* ctx, gblu_factor* f, char trans, int64_t nrhs, do
   return GBLU_OK;
 }
 
+// ||B - op(A) X||_F and ||B||_F with the FP64 matrix the factor keeps; up to
+// kMaxW columns at a time through a lazily allocated work arena.
+int32_t residual_norm(gblu_ctx* ctx, gblu_factor* f, char trans, int64_t nrhs, const double* X,
+                      int64_t ldx, const double* B, int64_t ldb, int32_t loc, double* res_norm,
+                      double* b_norm) {
+  const int64_t n = f->n;
+  const double* A = f->precision == GBLU_FP64 ? (f->a_keep_valid ? f->a_keep : nullptr) : f->lu64;
+  if (!A) return fail(ctx, GBLU_EINVAL, "gblu_residual_norm: the factor keeps no copy of A "
+                                        "(gblu_factor_keep_matrix before getrf)");
+  cudaStream_t s = ctx->stream;
+  const int64_t W = kMaxW;
+  const size_t vec = align256((size_t)n * W * sizeof(double));
+  const size_t pbytes = align256((size_t)kSplit * n * W * sizeof(double));
+  const size_t sbytes = align256((size_t)2 * kSumBlocks * W * sizeof(double)) + align256(2 * W * sizeof(double));
+  const size_t need = 3 * vec + pbytes + sbytes;
+  if (f->chk_bytes < need) {
+    if (f->chk_arena) {
+      GBLU_CK(ctx, cudaStreamSynchronize(s), "residual check");
+      ctx_free(ctx, f->chk_arena, f->chk_bytes);
+      f->chk_arena = nullptr;
+      f->chk_bytes = 0;
+    }
+    int32_t st = ctx_alloc(ctx, need, &f->chk_arena);
+    if (st) return st;
+    f->chk_bytes = need;
+  }
+  char* c = reinterpret_cast<char*>(f->chk_arena);
+  double* Xd = reinterpret_cast<double*>(c);
+  double* Bd = reinterpret_cast<double*>(c + vec);
+  double* R = reinterpret_cast<double*>(c + 2 * vec);
+  double* P = reinterpret_cast<double*>(c + 3 * vec);
+  double* part = reinterpret_cast<double*>(c + 3 * vec + pbytes);
+  double* sums = part + 2 * kSumBlocks * W;
+  const cudaMemcpyKind kind = loc == GBLU_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  const char op = (trans == 'N' || trans == 'n') ? 'N' : 'T';
+  double rr = 0.0, bb = 0.0;
+  for (int64_t c0 = 0; c0 < nrhs; c0 += W) {
+    const int nc = (int)std::min<int64_t>(W, nrhs - c0);
+    GBLU_CK(ctx, cudaMemcpy2DAsync(Xd, n * sizeof(double), X + c0 * ldx, ldx * sizeof(double),
+                                   n * sizeof(double), nc, kind, s), "copying X");
+    GBLU_CK(ctx, cudaMemcpy2DAsync(Bd, n * sizeof(double), B + c0 * ldb, ldb * sizeof(double),
+                                   n * sizeof(double), nc, kind, s), "copying B");
+    GBLU_CK(ctx, gemv(op, n, n, A, f->ld, Xd, n, nc, -1.0, Bd, n, 1.0, R, n, P, nullptr, s), "residual");
+    {
+      LaunchScope ls_(K_REFINE, 0.0, 8.0 * n * nc, s);
+      sumsq_partial_kernel<<<dim3(kSumBlocks, nc), 256, 0, s>>>(n, R, n, part);
+    }
+    {
+      LaunchScope ls_(K_REFINE, 0.0, 8.0 * n * nc, s);
+      sumsq_partial_kernel<<<dim3(kSumBlocks, nc), 256, 0, s>>>(n, Bd, n, part + kSumBlocks * W);
+    }
+    {
+      LaunchScope ls_(K_REFINE, 0.0, 0.0, s);
+      sumsq_final_kernel<<<1, 2 * W, 0, s>>>(2 * W, part, sums);
+    }
+    GBLU_CK(ctx, cudaGetLastError(), "residual norms");
+    double h[2 * kMaxW];
+    GBLU_CK(ctx, cudaMemcpyAsync(h, sums, 2 * W * sizeof(double), cudaMemcpyDeviceToHost, s), "reading norms");
+    GBLU_CK(ctx, cudaStreamSynchronize(s), "residual check");
+    for (int q = 0; q < nc; ++q) {
+      rr += h[q];
+      bb += h[W + q];
+    }
+  }
+  *res_norm = std::sqrt(rr);
+  *b_norm = std::sqrt(bb);
+  return GBLU_OK;
+}
+
 }  // namespace gblu
 
 extern "C" {
@@ -737,6 +839,29 @@ int32_t gblu_refine_opts_default(gblu_refine_opts* opts) {
   if (!opts) return GBLU_EINVAL;
   *opts = gblu::refine_default_opts();
   return GBLU_OK;
+}
+
+int32_t gblu_residual_norm(gblu_ctx* ctx, gblu_factor* f, char trans, int64_t nrhs, const double* X,
+                           int64_t ldx, const double* B, int64_t ldb, int32_t loc, double* res_norm,
+                           double* b_norm) {
+  using namespace gblu;
+  if (!ctx || !f || !res_norm || !b_norm) return fail(ctx, GBLU_EINVAL, "gblu_residual_norm: NULL argument");
+  if (!(trans == 'N' || trans == 'n' || trans == 'T' || trans == 't' || trans == 'C' || trans == 'c'))
+    return fail(ctx, GBLU_EINVAL, "gblu_residual_norm: trans must be 'N' or 'T'");
+  if (f->m != f->n) return fail(ctx, GBLU_EINVAL, "gblu_residual_norm: factor is not square");
+  if (nrhs < 0) return fail(ctx, GBLU_EINVAL, "gblu_residual_norm: nrhs < 0");
+  if (ldx < std::max<int64_t>(1, f->n) || ldb < std::max<int64_t>(1, f->n))
+    return fail(ctx, GBLU_EINVAL, "gblu_residual_norm: leading dimension < n");
+  if (loc != GBLU_HOST && loc != GBLU_DEVICE) return fail(ctx, GBLU_EINVAL, "gblu_residual_norm: bad loc");
+  if (!f->factored) return fail(ctx, GBLU_ENOTFACTORED, "gblu_residual_norm: no factorization");
+  *res_norm = 0.0;
+  *b_norm = 0.0;
+  if (nrhs == 0 || f->n == 0) return GBLU_OK;
+  if (!X || !B) return fail(ctx, GBLU_EINVAL, "gblu_residual_norm: X or B is NULL");
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  DeviceGuard g(ctx->device);
+  ActiveProfiler ap(&ctx->prof);
+  return residual_norm(ctx, f, trans, nrhs, X, ldx, B, ldb, loc, res_norm, b_norm);
 }
 
 }  // extern "C"

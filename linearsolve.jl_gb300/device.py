@@ -176,6 +176,30 @@ class Factorization:
         stats = {k: getattr(s, k) for k, _ in RefineStats._fields_ if k != "pad_"}
         return X, stats
 
+    def keep_matrix(self, keep: bool = True) -> None:
+        """FP64 factors: keep a device copy of A from the next getrf on, for
+        residual_norm (mixed factors keep A anyway)."""
+        check(self.lib.gblu_factor_keep_matrix(self.ctx.handle, self.handle, 1 if keep else 0),
+              self.ctx.handle)
+
+    def residual_norm(self, X, B, trans: str = "N") -> tuple[float, float]:
+        """(||B - op(A) X||_F, ||B||_F) computed on the device with the kept A."""
+        r, bn = ctypes.c_double(), ctypes.c_double()
+        if isinstance(X, DeviceMatrix) and isinstance(B, DeviceMatrix):
+            st = self.lib.gblu_residual_norm(self.ctx.handle, self.handle, trans.encode(), X.cols, X.ptr,
+                                             X.ld, B.ptr, B.ld, _lib.GBLU_DEVICE, ctypes.byref(r),
+                                             ctypes.byref(bn))
+        else:
+            X = X.to_host() if isinstance(X, DeviceMatrix) else X
+            B = B.to_host() if isinstance(B, DeviceMatrix) else B
+            Xf = np.asfortranarray(np.asarray(X, dtype=np.float64).reshape(self.n, -1))
+            Bf = np.asfortranarray(np.asarray(B, dtype=np.float64).reshape(self.n, -1))
+            st = self.lib.gblu_residual_norm(self.ctx.handle, self.handle, trans.encode(), Xf.shape[1],
+                                             Xf.ctypes.data, max(self.n, 1), Bf.ctypes.data, max(self.n, 1),
+                                             _lib.GBLU_HOST, ctypes.byref(r), ctypes.byref(bn))
+        check(st, self.ctx.handle)
+        return float(r.value), float(bn.value)
+
     def growth(self) -> float:
         """Pivot growth max|U| / max|A| of the last getrf (mixed precisions)."""
         g = ctypes.c_double()

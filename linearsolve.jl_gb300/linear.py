@@ -107,6 +107,58 @@ class GB300LUFactorization(AbstractDenseFactorization):
         return f"GB300LUFactorization(residualsafety={self.residualsafety})"
 
 
+class GB300RFLUFactorization(GB300LUFactorization):
+    """The drop-in for RFLUFactorization(; pivot = Val(true), thread =
+    Val(true)) (src/extension_algs.jl:524-537, solve! in
+    ext/LinearSolveRecursiveFactorizationExt.jl:15-42): the same recursive,
+    partial-pivot FP64 LU (RecursiveFactorization's lu! is recursive; so is
+    this library's getrf) and the same forward / back substitution, on the
+    GB300.  Its cacheval has RFLU's (LU, ipiv) shape.
+
+    pivot: True (RecursiveFactorization's Val(true)); the pivot-free
+           Val(false) variant is not provided (ValueError).  On matrices whose
+           column maxima sit on the diagonal (the diagonally dominant ones the
+           reference tests with) the two factorizations coincide.
+    thread: accepted and ignored (the GPU is the thread pool)."""
+
+    def __init__(self, pivot: bool = True, thread: bool = True, residualsafety: bool = False,
+                 device: int = 0):
+        if not bool(pivot):
+            raise ValueError("GB300RFLUFactorization: pivot=False (RecursiveFactorization's pivot-free "
+                             "lu!) is not provided; partial pivoting only")
+        super().__init__(residualsafety=residualsafety, device=device)
+        self.pivot = True
+        self.thread = bool(thread)
+
+    def __repr__(self):
+        return f"GB300RFLUFactorization(pivot=True, thread={self.thread}, residualsafety={self.residualsafety})"
+
+
+class RFLUCacheval:
+    """RFLUFactorization's cacheval shape, (LU, ipiv) (src/factorization.jl:
+    232-255): unpacks as (factorization, ipiv) with ipiv the 1-based int64
+    pivots of the last getrf; every other attribute is the device-resident
+    factorization's."""
+
+    def __init__(self, fact):
+        object.__setattr__(self, "fact", fact)
+
+    def _pair(self):
+        return (self.fact, self.fact.ipiv())
+
+    def __iter__(self):
+        return iter(self._pair())
+
+    def __len__(self):
+        return 2
+
+    def __getitem__(self, i):
+        return self._pair()[i]
+
+    def __getattr__(self, name):
+        return getattr(object.__getattribute__(self, "fact"), name)
+
+
 class GB300MixedLUFactorization(AbstractDenseFactorization):
     """Mixed precision: FP32 LU, FP64 accuracy by refinement.
 
@@ -115,14 +167,19 @@ class GB300MixedLUFactorization(AbstractDenseFactorization):
                               cores (tcgen05) with 16-bit operands
     refine:  "ir" | "gmres_ir" (classic IR, or GMRES-IR preconditioned by the LU)
     maxiters, tol: outer refinement limits (tol None: n * eps64)
-    fallback: FP64 LU when refinement stalls.
+    fallback: FP64 LU when refinement stalls, or at once when the pivot
+              growth of the low-precision factors exceeds growth_limit
+              (None: 1 / u of the factorization's arithmetic)
+    residualsafety: the a-posteriori residual check of the reference
+              (src/factorization.jl:127-156), run on the device.
 
     Unlike the reference's CUDAOffload32MixedLUFactorization
     (ext/LinearSolveCUDAExt.jl:211-242) the result is FP64-accurate."""
 
     def __init__(self, factor: str = "fp32", refine: str = "ir", maxiters: int = 30,
                  tol: Optional[float] = None, fallback: bool = True, gmres_restart: int = 30,
-                 gmres_tol: float = 1e-10, device: int = 0):
+                 gmres_tol: float = 1e-10, growth_limit: Optional[float] = None,
+                 residualsafety: bool = False, device: int = 0):
         if factor not in ("fp32", "bf16", "fp16"):
             raise ValueError(f"unsupported factor precision {factor!r}")
         if refine not in ("ir", "gmres_ir"):
@@ -134,6 +191,8 @@ class GB300MixedLUFactorization(AbstractDenseFactorization):
         self.fallback = bool(fallback)
         self.gmres_restart = int(gmres_restart)
         self.gmres_tol = float(gmres_tol)
+        self.growth_limit = growth_limit
+        self.residualsafety = bool(residualsafety)
         self.device = int(device)
 
     def __repr__(self):
@@ -299,7 +358,10 @@ def init(prob: LinearProblem, alg=None, alias: Optional[LinearAliasSpecifier] = 
     cache = LinearCache(A, b, u, alg, d_abs if abstol is None else abstol,
                         d_rel if reltol is None else reltol, verbose, alias_A, alias_b, ctx)
     # init_cacheval: the device-resident factorization object, allocated once
-    cache.cacheval = ctx.factor(m, n, alg.factor_precision())
+    fact = ctx.factor(m, n, alg.factor_precision())
+    if alg.residualsafety:
+        fact.keep_matrix(True)  # the FP64 copy of A the residual check reads (A_backup)
+    cache.cacheval = RFLUCacheval(fact) if isinstance(alg, GB300RFLUFactorization) else fact
     cache.default = default
     return cache
 
@@ -314,11 +376,13 @@ def _solve_into(cache: LinearCache, fact, b, trans: str = "N"):
             device_synchronize()
             X, stats = fact.solve_refined(out, trans=trans, mode=alg.refine, max_iter=alg.maxiters,
                                           tol=alg.tol or 0.0, fallback=alg.fallback,
-                                          gmres_restart=alg.gmres_restart, gmres_tol=alg.gmres_tol)
+                                          gmres_restart=alg.gmres_restart, gmres_tol=alg.gmres_tol,
+                                          growth_limit=alg.growth_limit or 0.0)
             return out, stats
         X, stats = fact.solve_refined(b, trans=trans, mode=alg.refine, max_iter=alg.maxiters,
                                       tol=alg.tol or 0.0, fallback=alg.fallback,
-                                      gmres_restart=alg.gmres_restart, gmres_tol=alg.gmres_tol)
+                                      gmres_restart=alg.gmres_restart, gmres_tol=alg.gmres_tol,
+                                      growth_limit=alg.growth_limit or 0.0)
         return X, stats
     if isinstance(b, DeviceMatrix):
         out = cache.u if isinstance(cache.u, DeviceMatrix) else DeviceMatrix(b.rows, b.cols)
@@ -374,6 +438,9 @@ def _solve_bang(cache: LinearCache) -> LinearSolution:
     """solve!(cache, alg) for the GB300 algorithms (factorization.jl:643-736 shape)."""
     alg = cache.alg
     fact = cache.cacheval
+    # the reference checks the residual after the solves that refactored
+    # (check_safety = alg.residualsafety && cache.isfresh, factorization.jl:647)
+    check_safety = bool(getattr(alg, "residualsafety", False)) and cache.isfresh
     if cache.isfresh:
         A_now = cache.A
         info = fact.getrf(A_now)
@@ -387,12 +454,14 @@ def _solve_bang(cache: LinearCache) -> LinearSolution:
     u, stats = _solve_into(cache, fact, cache.b)
     _store_u(cache, u)
     cache.stats = stats
-    if getattr(alg, "residualsafety", False) and not isinstance(cache.A, DeviceMatrix):
-        # _check_residual_safety (factorization.jl:127-156), 2-norms as the reference
-        A = np.asarray(cache.A, dtype=np.float64)
-        bb = np.asarray(cache.b, dtype=np.float64)
-        res = np.linalg.norm(A @ cache.u - bb)
-        tol = cache.abstol + cache.reltol * np.linalg.norm(bb)
+    if check_safety:
+        # _check_residual_safety (factorization.jl:127-156): ||A u - b|| against
+        # abstol + reltol ||b||, 2-norms as the reference, computed on the
+        # device from the FP64 A the factorization kept
+        res, bnorm = fact.residual_norm(cache.u, cache.b)
+        tol = cache.abstol + cache.reltol * bnorm
+        stats = dict(stats, residual_norm=res, residual_tol=tol)
+        cache.stats = stats
         if res > tol:
             return LinearSolution(cache.u, None, alg, ReturnCode.APosterioriSafetyFailure,
                                   cache=cache, stats=stats)

@@ -37,6 +37,15 @@ def test_python_binding_covers_header(pkg):
     assert sorted(lib_mod.SIGNATURES) == declared
 
 
+def test_julia_binding_symbols_are_declared():
+    """Every symbol the Julia binding resolves with dlsym is in gblu.h."""
+    src = open(os.path.join(ROOT, "linearsolve.jl_gb300", "julia", "GB300LinearSolve.jl")).read()
+    used = set(re.findall(r":(gblu_[a-z0-9_]+)", src))
+    assert used, "no symbols parsed"
+    missing = sorted(used - set(declared_functions()))
+    assert not missing, f"the Julia binding resolves undeclared symbols: {missing}"
+
+
 def test_library_loads_without_gpu(pkg):
     lib = pkg.load_library()
     assert lib.gblu_version() >> 16 == 1

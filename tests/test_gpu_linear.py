@@ -100,6 +100,90 @@ def test_residual_safety(pkg):
     B = rng.random((n, 3))
     sol = pkg.solve(pkg.LinearProblem(A, B), pkg.GB300LUFactorization(residualsafety=True))
     assert pkg.successful_retcode(sol)
+    assert sol.stats["residual_norm"] <= sol.stats["residual_tol"]
+
+
+@pytest.mark.parametrize("mk", [lambda pkg: pkg.GB300LUFactorization(residualsafety=True),
+                                lambda pkg: pkg.GB300MixedLUFactorization(residualsafety=True)])
+def test_residual_safety_failure_only_after_refactor(pkg, mk):
+    """_check_residual_safety (src/factorization.jl:127-156): with abstol =
+    reltol = 0 any nonzero residual fails the check, as
+    APosterioriSafetyFailure; the check runs only on solves that refactored
+    (check_safety = residualsafety && isfresh)."""
+    rng = np.random.default_rng(27)
+    n = 200
+    A = rng.standard_normal((n, n)) + 2 * np.sqrt(n) * np.eye(n)
+    b = rng.standard_normal(n)
+    cache = pkg.init(pkg.LinearProblem(A, b), mk(pkg), abstol=0.0, reltol=0.0)
+    sol = pkg.solve_bang(cache)
+    assert sol.retcode == pkg.ReturnCode.APosterioriSafetyFailure
+    res = np.linalg.norm(A @ sol.u - b)
+    assert res > 0 and sol.stats["residual_norm"] > 0
+    cache.b = rng.standard_normal(n)  # no refactorization: no check
+    assert pkg.solve_bang(cache).retcode == pkg.ReturnCode.Success
+    cache.A = A.copy()  # refactorization: checked again
+    assert pkg.solve_bang(cache).retcode == pkg.ReturnCode.APosterioriSafetyFailure
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("where", ["host", "device"])
+def test_residual_norm_on_device(ctx, pkg, prec, where):
+    """The device residual ||B - A X||_F and ||B||_F against numpy, for a
+    perturbed X (residual well above rounding level), N and T."""
+    rng = np.random.default_rng(28)
+    n, k = 333, 3
+    A = rng.standard_normal((n, n)) + 2 * np.sqrt(n) * np.eye(n)
+    B = rng.standard_normal((n, k))
+    X = np.asfortranarray(rng.standard_normal((n, k)) * 1e-3)
+    f = ctx.factor(n, n, prec)
+    f.keep_matrix(True)
+    assert f.getrf(A) == 0
+    for trans, M in (("N", A), ("T", A.T)):
+        if where == "device":
+            dX, dB = pkg.DeviceMatrix.from_host(X), pkg.DeviceMatrix.from_host(B)
+            r, bn = f.residual_norm(dX, dB, trans=trans)
+            dX.free(); dB.free()
+        else:
+            r, bn = f.residual_norm(X, B, trans=trans)
+        assert abs(r - np.linalg.norm(B - M @ X)) <= 1e-12 * r
+        assert abs(bn - np.linalg.norm(B)) <= 1e-13 * bn
+    f.close()
+
+
+def test_residual_norm_needs_kept_matrix(ctx, pkg):
+    n = 64
+    A, B = pkg.workloads.plain(n, 1, seed=3)
+    f = ctx.factor(n, n, "fp64")
+    f.getrf(A)
+    with pytest.raises(pkg.GBLUError):
+        f.residual_norm(B, B)
+    f.close()
+
+
+@pytest.mark.parametrize("n,nrhs", [(8, 1), (8, 3), (40, 1), (40, 3)])
+def test_rflu_dropin(pkg, oracle_mod, n, nrhs):
+    """RFLUFactorization multi-RHS and cache reuse (test/Core/basictests.jl
+    "RFLUFactorization multi-RHS") with GB300RFLUFactorization swapped in; the
+    cacheval unpacks as RFLU's (LU, ipiv)."""
+    rng = np.random.default_rng(7 + n + nrhs)
+    Ar = rng.random((n, n)) + n * np.eye(n)
+    Br = rng.random((n, nrhs))
+    alg = pkg.GB300RFLUFactorization()
+    sol = pkg.solve(pkg.LinearProblem(Ar.copy(), Br.copy()), alg)
+    np.testing.assert_allclose(sol.u, np.linalg.solve(Ar, Br), rtol=1e-12)
+    cache = pkg.init(pkg.LinearProblem(Ar.copy(), Br.copy()), alg)
+    np.testing.assert_allclose(pkg.solve_bang(cache).u, np.linalg.solve(Ar, Br), rtol=1e-12)
+    fact, ipiv = cache.cacheval
+    LU, ipiv_ref, _ = oracle_mod.getrf(Ar)
+    assert np.array_equal(ipiv, ipiv_ref) and np.array_equal(fact.factors(), LU)
+    A2 = Ar + np.eye(n)
+    cache.A = A2.copy()
+    np.testing.assert_allclose(pkg.solve_bang(cache).u, np.linalg.solve(A2, Br), rtol=1e-12)
+
+
+def test_rflu_pivot_false_is_refused(pkg):
+    with pytest.raises(ValueError):
+        pkg.GB300RFLUFactorization(pivot=False)
 
 
 def test_device_resident_inputs(pkg, oracle_mod):
