@@ -355,6 +355,42 @@ def run_gpu(args, rank, world, local):
     ctx.profile_enable(False)
     profiled_ms = p0.elapsed_ms(p1) / args.steps
 
+    # ---- the same step with the fast getrs (inverted diagonal blocks) ----
+    fast = None
+    if rank == 0:
+        ff = ctx.factor(n, n, "fp64")
+        ff.set_solve("fast")
+        dBf = pkg.DeviceMatrix(n, nrhs)
+        colsf = [cu.DeviceColumn(dBf, j) for j in range(nrhs)]
+
+        def step_fast():
+            dBf.copy_from(dB0, stream)
+            ff.getrf(dA)
+            for c in colsf:
+                ff.getrs(c)
+
+        for _ in range(max(3, args.warmup)):
+            step_fast()
+        f0, f1 = cu.Event(), cu.Event()
+        f0.record(stream)
+        for _ in range(args.steps):
+            step_fast()
+        f1.record(stream)
+        f1.synchronize()
+        ms_fast = f0.elapsed_ms(f1) / args.steps
+        ctx.profile_enable(True)
+        step_fast()
+        pf = ctx.profile_read(reset=True)
+        ctx.profile_enable(False)
+        Xf = dBf.to_host()
+        fast = {"solve": "fast (64 x 64 diagonal blocks of L and U inverted after getrf)",
+                "value": nrhs / (ms_fast / 1e3), "unit": UNIT, "ms_per_step": ms_fast,
+                "getrs_ms_per_solve": pf["getrs"]["ms"] / nrhs,
+                "backward_error": max(pkg_backward_error(A, Xf[:, j], B[:, j]) for j in range(nrhs)),
+                "forward_error_vs_exact": _forward_error(Xf, X)}
+        dBf.free()
+        ff.close()
+
     # ---- end to end through the public interface, pinned host buffers ----
     pA = cu.PinnedArray((n, n))
     pA.array[...] = A
@@ -451,6 +487,8 @@ def run_gpu(args, rank, world, local):
         "roofline_by_phase": phases,
         "kernel_ms": {k: round(prof[k]["ms"] / args.steps, 3) for k in kinds if prof[k]["count"]},
     }
+    if fast is not None:
+        line["getrs_fast"] = fast
 
     if args.suite == "auto":
         args.suite = ",".join(SUITES) if world == 1 else ""
@@ -611,9 +649,13 @@ def run_mixed_suite(pkg, cu, ctx, args):
     dB = pkg.DeviceMatrix(n, nrhs)
     out = {"n": n, "nrhs": nrhs, "A": "G + 4 sqrt(n) I"}
     X64 = None
-    for label, prec in (("fp64_plain", "fp64"), ("fp32_ir", "fp32"), ("bf16_ir", "bf16"),
-                        ("fp16_ir", "fp16")):
+    variants = (("fp64_plain", "fp64", "exact"), ("fp32_ir", "fp32", "exact"), ("bf16_ir", "bf16", "exact"),
+                ("fp16_ir", "fp16", "exact"), ("fp32_ir_fast_solve", "fp32", "fast"),
+                ("bf16_ir_fast_solve", "bf16", "fast"), ("fp16_ir_fast_solve", "fp16", "fast"))
+    for label, prec, solve in variants:
         f = ctx.factor(n, n, prec)
+        if solve != "exact":
+            f.set_solve(solve)  # the low-precision correction solve
         # the FP64 solve set takes seconds: one warm-up and one timed run
         ms, st, kms = _timed_solve(pkg, cu, ctx, f, dA, dB0, dB, prec, 1 if prec == "fp64" else 3,
                                    warm=1 if prec == "fp64" else 3)
@@ -625,7 +667,7 @@ def run_mixed_suite(pkg, cu, ctx, args):
                       "forward_error_vs_fp64": _forward_error(X, X64), "stats": st, "kernel_ms": kms,
                       "getrf_roofline": getrf_phase_roofline(kms, n, prec, args)}
         f.close()
-    for label in ("fp32_ir", "bf16_ir", "fp16_ir"):
+    for label, _, _ in variants[1:]:
         out["speedup_%s_vs_fp64" % label] = out[label]["solves_per_s"] / out["fp64_plain"]["solves_per_s"]
     out["bound"] = 10 * n * EPS64
     dA.free(); dB0.free(); dB.free()
@@ -644,11 +686,16 @@ def run_mixed_hard_suite(pkg, cu, ctx, args):
     dB = pkg.DeviceMatrix(n, nrhs)
     out = {"n": n, "nrhs": nrhs, "A": "Q1 diag(s) Q2^T, s log-spaced 1..1e6", "input_generation_s": gen_s}
     X64 = None
-    for label, prec, mode, kw in (("fp64_plain", "fp64", "ir", {}),
-                                  ("fp32_gmres_ir", "fp32", "gmres_ir", {}),
-                                  ("fp32_gmres_ir_inner_tol_1e-6", "fp32", "gmres_ir", {"gmres_tol": 1e-6}),
-                                  ("fp32_ir", "fp32", "ir", {})):
+    variants = (("fp64_plain", "fp64", "ir", {}),
+                ("fp32_gmres_ir", "fp32", "gmres_ir", {}),
+                ("fp32_gmres_ir_inner_tol_1e-6", "fp32", "gmres_ir", {"gmres_tol": 1e-6}),
+                ("fp32_ir", "fp32", "ir", {}),
+                ("fp32_gmres_ir_fast_solve", "fp32", "gmres_ir", {"solve": "fast"}))
+    for label, prec, mode, kw in variants:
         f = ctx.factor(n, n, prec)
+        kw = dict(kw)
+        if kw.pop("solve", "exact") == "fast":
+            f.set_solve("fast")  # the low-precision preconditioner solve
         ms, st, kms = _timed_solve(pkg, cu, ctx, f, dA, dB0, dB, prec, 1 if prec == "fp64" else 2,
                                    mode=mode, warm=1 if prec == "fp64" else 3, **kw)
         X = dB.to_host()
@@ -658,7 +705,7 @@ def run_mixed_hard_suite(pkg, cu, ctx, args):
         out[label] = {"ms_per_solve_set": ms, "solves_per_s": nrhs / (ms / 1000), "backward_error": be,
                       "forward_error_vs_fp64": _forward_error(X, X64), "stats": st, "kernel_ms": kms}
         f.close()
-    for label in ("fp32_gmres_ir", "fp32_gmres_ir_inner_tol_1e-6", "fp32_ir"):
+    for label, _, _, _ in variants[1:]:
         out["speedup_%s_vs_fp64" % label] = out[label]["solves_per_s"] / out["fp64_plain"]["solves_per_s"]
     out["bound"] = 10 * n * EPS64
     dA.free(); dB0.free(); dB.free()

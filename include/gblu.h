@@ -114,6 +114,21 @@ int32_t gblu_factor_destroy(gblu_ctx* ctx, gblu_factor* f);
 int32_t gblu_getrf(gblu_ctx* ctx, gblu_factor* f, const double* A, int64_t lda,
                    int32_t a_loc, int64_t* info);
 
+/* How getrs applies the triangular factors (gblu_factor_set_solve).
+ * GBLU_SOLVE_EXACT (default): each row of the two sweeps accumulates its
+ *   updates in the reference back-solve's order (src/factorization.jl:433-457),
+ *   bit-identical to it; a chain of n dependent steps per sweep.
+ * GBLU_SOLVE_FAST: the same two sweeps with the 64 x 64 diagonal blocks of L
+ *   and U inverted once after each getrf and applied as matrix-vector
+ *   products, and independent partial sums elsewhere; backward-error accurate
+ *   (not bit-identical), several times shorter critical path.  For a mixed
+ *   factor it selects the low-precision solve inside refinement; the FP64
+ *   fallback solve stays exact.  Allocates n x 128 elements of the factor's
+ *   precision on first use. */
+#define GBLU_SOLVE_EXACT 0
+#define GBLU_SOLVE_FAST 1
+int32_t gblu_factor_set_solve(gblu_ctx* ctx, gblu_factor* f, int32_t mode);
+
 /* getrs: solve op(A) X = B in place for nrhs columns of B (ldb), with
  * trans = 'N' or 'T'.  For a GBLU_FP32 factor this is the refined solve
  * (gblu_solve_refined with default options), so the result is FP64-accurate.

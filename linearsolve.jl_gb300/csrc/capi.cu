@@ -359,7 +359,32 @@ int32_t gblu_factor_destroy(gblu_ctx* ctx, gblu_factor* f) {
   if (f->fb_arena) ctx_free(ctx, f->fb_arena, f->fb_bytes);
   if (f->a_keep) ctx_free(ctx, f->a_keep, std::max<size_t>((size_t)f->ld * f->n * sizeof(double), 256));
   if (f->chk_arena) ctx_free(ctx, f->chk_arena, f->chk_bytes);
+  if (f->inv_arena) ctx_free(ctx, f->inv_arena, f->inv_bytes);
   delete f;
+  return GBLU_OK;
+}
+
+int32_t gblu_factor_set_solve(gblu_ctx* ctx, gblu_factor* f, int32_t mode) {
+  if (!ctx || !f) return fail(ctx, GBLU_EINVAL, "gblu_factor_set_solve: NULL argument");
+  if (mode != GBLU_SOLVE_EXACT && mode != GBLU_SOLVE_FAST)
+    return fail(ctx, GBLU_EINVAL, "gblu_factor_set_solve: unknown mode %d", mode);
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  DeviceGuard g(ctx->device);
+  const bool fast = mode == GBLU_SOLVE_FAST;
+  if (fast && !f->inv_arena && f->m == f->n) {
+    const size_t bytes = getrs_inverse_bytes(f->n, f->precision == GBLU_FP64 ? 8 : 4);
+    int32_t st = ctx_alloc(ctx, bytes, &f->inv_arena);
+    if (st) return st;
+    f->inv_bytes = bytes;
+    f->inv_valid = false;
+  }
+  if (f->precision == GBLU_FP64) {
+    f->rs64.fast = fast && f->inv_arena;
+    f->rs64.inv = reinterpret_cast<double*>(f->inv_arena);
+  } else {
+    f->rs32.fast = fast && f->inv_arena;
+    f->rs32.inv = reinterpret_cast<float*>(f->inv_arena);
+  }
   return GBLU_OK;
 }
 
@@ -439,10 +464,24 @@ cudaError_t run_getrf(gblu_ctx* ctx, gblu_factor* f, Launch&& launch) {
   return cudaGraphLaunch(f->getrf_exec, ctx->stream);
 }
 
+int32_t ensure_inverse(gblu_ctx* ctx, gblu_factor* f) {
+  if (f->inv_valid) return GBLU_OK;
+  if (f->precision == GBLU_FP64) {
+    if (!f->rs64.fast) return GBLU_OK;
+    CK(ctx, getrs_invert_launch<double>(f->rs64, ctx->stream), "inverting diagonal blocks");
+  } else {
+    if (!f->rs32.fast) return GBLU_OK;
+    CK(ctx, getrs_invert_launch<float>(f->rs32, ctx->stream), "inverting diagonal blocks");
+  }
+  f->inv_valid = true;
+  return GBLU_OK;
+}
+
 int32_t factor_getrf(gblu_ctx* ctx, gblu_factor* f, const double* A, int64_t lda, int32_t a_loc,
                      int64_t* info) {
   f->factored = false;
   f->fb_valid = false;
+  f->inv_valid = false;
   int32_t st;
   if (f->precision == GBLU_FP64) {
     st = upload_matrix(ctx, f->lu64, f->ld, A, lda, f->m, f->n, a_loc);
@@ -521,6 +560,8 @@ int32_t factor_fp64_fallback(gblu_ctx* ctx, gblu_factor* f, int64_t* info_out) {
 
 int32_t factor_getrs_plain(gblu_ctx* ctx, gblu_factor* f, char trans, int64_t nrhs, double* dB,
                            int64_t ldb) {
+  int32_t st = ensure_inverse(ctx, f);
+  if (st) return st;
   CK(ctx, getrs_launch<double>(f->rs64, trans, nrhs, dB, ldb, nullptr, ctx->stream),
      "launching getrs");
   return GBLU_OK;
@@ -900,6 +941,7 @@ int32_t factor_getrs_f64_host(gblu_ctx* ctx, gblu_factor* f, char trans, int64_t
   f->factored = true;
   f->info = 0;
   f->fb_valid = false;
+  f->inv_valid = false;
   return gblu_getrs(ctx, f, trans, nrhs, B, ldb, GBLU_HOST);
 }
 

@@ -117,7 +117,17 @@ struct GetrsPlan {
   int32_t* flags = nullptr;  // 2 * nblocks
   T* work = nullptr;         // n * nrhs_chunk
   int64_t work_cols = 0;
+  // fast mode: diagonal blocks applied through their inverses (not the
+  // reference's per-row order; backward-error accurate, not bit-exact)
+  bool fast = false;
+  T* inv = nullptr;          // getrs_inverse_bytes(n): [block][L, U][64 x 64]
 };
+
+// Device bytes of the inverted 64 x 64 diagonal blocks of L and U (fast getrs).
+size_t getrs_inverse_bytes(int64_t n, int elem_size);
+// Invert the diagonal blocks of the factors of p into p.inv (after each getrf).
+template <typename T>
+cudaError_t getrs_invert_launch(const GetrsPlan<T>& p, cudaStream_t stream);
 
 // In-place solve op(A) X = B for nrhs columns of B (ldb), trans 'N' or 'T'.
 template <typename T>

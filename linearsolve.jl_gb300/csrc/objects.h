@@ -59,6 +59,10 @@ struct gblu_factor {
   // residual-check buffers (allocated on the first gblu_residual_norm)
   void* chk_arena = nullptr;
   uint64_t chk_bytes = 0;
+  // fast getrs: inverted diagonal blocks of the factors (rs64 or rs32 .inv)
+  void* inv_arena = nullptr;
+  uint64_t inv_bytes = 0;
+  bool inv_valid = false;  // inverses belong to the current factors
   // the factorization's launch sequence, captured on its second run and
   // replayed from then on (it depends only on the factor's shape)
   cudaGraphExec_t getrf_exec = nullptr;
@@ -79,6 +83,9 @@ int32_t upload_matrix(gblu_ctx* ctx, double* dst, int64_t ld_dst, const double* 
 int32_t ensure_rhs(gblu_ctx* ctx, gblu_factor* f, int64_t cols);
 // FP64 factorization of the FP64 copy of A of a mixed factor (fb_* fields).
 int32_t factor_fp64_fallback(gblu_ctx* ctx, gblu_factor* f, int64_t* info_out);
+// Fast getrs: invert the factors' diagonal blocks if the current factors'
+// inverses are not there yet (asynchronous on the context stream).
+int32_t ensure_inverse(gblu_ctx* ctx, gblu_factor* f);
 
 inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 

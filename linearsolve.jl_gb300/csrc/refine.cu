@@ -50,34 +50,52 @@ __device__ __forceinline__ void block_max_into(double v, unsigned long long* p) 
   }
 }
 
-// B = float(A), and max |A_ij| (the denominator of the pivot growth) into *amax.
-__global__ void convert_f64_f32_kernel(int64_t rows, int64_t cols, const double* __restrict__ A,
-                                       int64_t lda, float* __restrict__ B, int64_t ldb,
-                                       unsigned long long* __restrict__ amax) {
-  const int64_t total = rows * cols;
-  double mx = 0.0;
-  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
-       idx += (int64_t)gridDim.x * blockDim.x) {
-    int64_t j = idx / rows, i = idx - j * rows;
-    const double a = A[i + j * lda];
-    B[i + j * ldb] = (float)a;
-    const double v = fabs(a);
-    mx = (v > mx || isnan(v)) ? v : mx;
+// One pass over the FP64 matrix before the low-precision getrf: B = float(A),
+// P[s][i] = sum of |A_ij| over the columns j of chunk s (j ascending; the
+// chunks of gemv_n_partial_kernel, so ||A||_inf is reduced by
+// gemv_reduce_kernel exactly as the residual norms are), and max |A_ij| into
+// *amax.  Grid (rows / 256, kSplit); consecutive threads read consecutive
+// rows of a column.
+__global__ void __launch_bounds__(256)
+prepare_kernel(int64_t n, const double* __restrict__ A, int64_t lda, float* __restrict__ B, int64_t ldb,
+               double* __restrict__ P, unsigned long long* __restrict__ amax) {
+  const int s = blockIdx.y;
+  const int64_t cs = (n + kSplit - 1) / kSplit;
+  const int64_t j0 = s * cs, j1 = min(n, j0 + cs);
+  const int64_t i = (int64_t)blockIdx.x * 256 + threadIdx.x;
+  double acc = 0.0, mx = 0.0;
+  if (i < n) {
+    const double* a = A + i;
+    float* b = B + i;
+#pragma unroll 4
+    for (int64_t j = j0; j < j1; ++j) {
+      const double v = a[j * lda];
+      b[j * ldb] = (float)v;
+      const double av = fabs(v);
+      acc += av;
+      mx = (av > mx || isnan(av)) ? av : mx;
+    }
+    P[(size_t)s * n + i] = acc;
   }
   block_max_into(mx, amax);
 }
 
-// max |U_ij| over the upper triangle of the n x n FP32 factors; one CTA per
-// column, rows 0..j.
-__global__ void umax_kernel(int64_t n, const float* __restrict__ LU, int64_t ld,
-                            unsigned long long* __restrict__ umax) {
-  const int64_t j = blockIdx.x;
-  double mx = 0.0;
-  for (int64_t i = threadIdx.x; i <= j; i += blockDim.x) {
-    const double v = fabs((double)LU[i + j * ld]);
-    mx = (v > mx || isnan(v)) ? v : mx;
+// max |U_ij| over the upper triangle of the n x n FP32 factors: one warp per
+// column (rows 0..j, 32 consecutive rows per load), eight columns per CTA.
+__global__ void __launch_bounds__(256)
+umax_kernel(int64_t n, const float* __restrict__ LU, int64_t ld, unsigned long long* __restrict__ umax) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t j = (int64_t)blockIdx.x * 8 + warp;
+  float mx = 0.f;
+  if (j < n) {
+    const float* col = LU + j * ld;
+#pragma unroll 4
+    for (int64_t i = lane; i <= j; i += 32) {
+      const float v = fabsf(col[i]);
+      mx = (v > mx || isnan(v)) ? v : mx;
+    }
   }
-  block_max_into(mx, umax);
+  block_max_into((double)mx, umax);
 }
 
 // P[s][q][i] = sum_{j in chunk s} op(A)[i, j] * X[j, q]
@@ -383,15 +401,23 @@ cudaError_t refine_prepare(RefineWork& w, int64_t n, const double* A, int64_t ld
   if (n == 0) { w.anorm = 0; w.amax = 0; return cudaSuccess; }
   cudaError_t e = cudaMemsetAsync(w.growth_bits, 0, 2 * sizeof(unsigned long long), s);
   if (e != cudaSuccess) return e;
-  { LaunchScope ls_(K_REFINE, 0.0, 12.0 * n * n, s);
-  convert_f64_f32_kernel<<<grid_for(n * n), 256, 0, s>>>(n, n, A, lda, A32, ld32, w.growth_bits);
+  e = cudaMemsetAsync(w.colmax, 0, sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return e;
+  // FP32 copy, row sums of |A| and max |A| in one pass over A; then
+  // ||A||_inf = max_i sum_j |A[i,j]| from the row sums
+  {
+    LaunchScope ls_(K_REFINE, (double)n * n, 12.0 * n * n, s);
+    dim3 grid((unsigned)((n + 255) / 256), kSplit);
+    prepare_kernel<<<grid, 256, 0, s>>>(n, A, lda, A32, ld32, w.partial, w.growth_bits);
   }
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  // ||A||_inf = max_i sum_j |A[i,j]|
-  e = cudaMemsetAsync(w.colmax, 0, sizeof(unsigned long long), s);
-  if (e != cudaSuccess) return e;
-  e = gemv('N', n, n, A, lda, nullptr, 1, 1, 1.0, nullptr, 1, 0.0, w.w, n, w.partial, w.colmax, s, true);
+  {
+    LaunchScope ls_(K_REFINE, 0.0, 8.0 * kSplit * n, s);
+    gemv_reduce_kernel<<<grid_for(n), 256, 0, s>>>(n, 1, 1, w.partial, 1.0, nullptr, 1, 0.0, w.w, n,
+                                                   w.colmax);
+  }
+  e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   unsigned long long bits[2] = {0, 0};
   e = cudaMemcpyAsync(&bits[0], w.colmax, sizeof(bits[0]), cudaMemcpyDeviceToHost, s);
@@ -406,7 +432,7 @@ cudaError_t refine_prepare(RefineWork& w, int64_t n, const double* A, int64_t ld
 cudaError_t refine_growth_launch(RefineWork& w, int64_t n, const float* LU, int64_t ld, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
   LaunchScope ls_(K_REFINE, 0.0, 2.0 * n * n, s);
-  umax_kernel<<<(unsigned)n, 256, 0, s>>>(n, LU, ld, w.growth_bits + 1);
+  umax_kernel<<<(unsigned)((n + 7) / 8), 256, 0, s>>>(n, LU, ld, w.growth_bits + 1);
   return cudaGetLastError();
 }
 
@@ -625,6 +651,10 @@ int32_t refine_solve(gblu_ctx* ctx, gblu_factor* f, char trans, int64_t nrhs, do
   trans = (trans == 'n') ? 'N' : (trans == 't' || trans == 'c' || trans == 'C') ? 'T' : trans;
   const double tol = o.tol > 0 ? o.tol : (double)std::max<int64_t>(n, 1) * 2.220446049250313e-16;
   const int W = (int)w.W;
+  {
+    int32_t e = ensure_inverse(ctx, f);  // fast low-precision solves
+    if (e) return e;
+  }
   gblu_refine_stats st_acc{};
   st_acc.converged = 1;
   st_acc.growth = f->growth;

@@ -176,6 +176,17 @@ class Factorization:
         stats = {k: getattr(s, k) for k, _ in RefineStats._fields_ if k != "pad_"}
         return X, stats
 
+    def set_solve(self, mode: str = "exact") -> None:
+        """getrs mode: "exact" (the reference back-solve's per-row order,
+        bit-identical) or "fast" (inverted 64 x 64 diagonal blocks; backward-
+        error accurate).  For mixed factors: the low-precision solve inside
+        refinement."""
+        modes = {"exact": _lib.GBLU_SOLVE_EXACT, "fast": _lib.GBLU_SOLVE_FAST}
+        if mode not in modes:
+            raise ValueError("solve mode must be 'exact' or 'fast'")
+        check(self.lib.gblu_factor_set_solve(self.ctx.handle, self.handle, modes[mode]), self.ctx.handle)
+        self.solve_mode = mode
+
     def keep_matrix(self, keep: bool = True) -> None:
         """FP64 factors: keep a device copy of A from the next getrf on, for
         residual_norm (mixed factors keep A anyway)."""

@@ -85,6 +85,7 @@ class AbstractDenseFactorization:
     default_alias_b = False
     precision = "fp64"
     residualsafety = False
+    solve = "exact"
 
     def factor_precision(self) -> str:
         return self.precision
@@ -97,10 +98,18 @@ class GB300LUFactorization(AbstractDenseFactorization):
     CudaOffloadLUFactorization (src/extension_algs.jl:344-356).  Factors and
     ipiv are bit-identical to the reference's blocked LU
     (src/blocked_lufact.jl), and the solve to its back-solve
-    (src/factorization.jl:433-457)."""
+    (src/factorization.jl:433-457).
 
-    def __init__(self, residualsafety: bool = False, device: int = 0):
+    solve: "exact" (that back-solve order, bit for bit) or "fast" (the 64 x 64
+    diagonal blocks of L and U inverted once per factorization and applied as
+    matrix-vector products: a shorter critical path, backward-error accurate
+    but not bit-identical)."""
+
+    def __init__(self, residualsafety: bool = False, solve: str = "exact", device: int = 0):
+        if solve not in ("exact", "fast"):
+            raise ValueError("solve must be 'exact' or 'fast'")
         self.residualsafety = bool(residualsafety)
+        self.solve = solve
         self.device = int(device)
 
     def __repr__(self):
@@ -172,6 +181,8 @@ class GB300MixedLUFactorization(AbstractDenseFactorization):
               (None: 1 / u of the factorization's arithmetic)
     residualsafety: the a-posteriori residual check of the reference
               (src/factorization.jl:127-156), run on the device.
+    solve:    the low-precision correction solve, "exact" or "fast" (see
+              GB300LUFactorization); refinement makes either FP64-accurate.
 
     Unlike the reference's CUDAOffload32MixedLUFactorization
     (ext/LinearSolveCUDAExt.jl:211-242) the result is FP64-accurate."""
@@ -179,11 +190,14 @@ class GB300MixedLUFactorization(AbstractDenseFactorization):
     def __init__(self, factor: str = "fp32", refine: str = "ir", maxiters: int = 30,
                  tol: Optional[float] = None, fallback: bool = True, gmres_restart: int = 30,
                  gmres_tol: float = 1e-10, growth_limit: Optional[float] = None,
-                 residualsafety: bool = False, device: int = 0):
+                 residualsafety: bool = False, solve: str = "exact", device: int = 0):
         if factor not in ("fp32", "bf16", "fp16"):
             raise ValueError(f"unsupported factor precision {factor!r}")
         if refine not in ("ir", "gmres_ir"):
             raise ValueError("refine must be 'ir' or 'gmres_ir'")
+        if solve not in ("exact", "fast"):
+            raise ValueError("solve must be 'exact' or 'fast'")
+        self.solve = solve
         self.precision = factor
         self.refine = refine
         self.maxiters = int(maxiters)
@@ -359,6 +373,8 @@ def init(prob: LinearProblem, alg=None, alias: Optional[LinearAliasSpecifier] = 
                         d_rel if reltol is None else reltol, verbose, alias_A, alias_b, ctx)
     # init_cacheval: the device-resident factorization object, allocated once
     fact = ctx.factor(m, n, alg.factor_precision())
+    if alg.solve != "exact":
+        fact.set_solve(alg.solve)
     if alg.residualsafety:
         fact.keep_matrix(True)  # the FP64 copy of A the residual check reads (A_backup)
     cache.cacheval = RFLUCacheval(fact) if isinstance(alg, GB300RFLUFactorization) else fact

@@ -310,3 +310,72 @@ def test_graph_replayed_getrf_matches_direct(ctx, oracle_mod, prec):
         assert np.array_equal(f.ipiv(), ipiv), run
         assert np.array_equal(f.factors(), LU.astype(np.float64)), run
     f.close()
+
+
+# ---- fast getrs: inverted diagonal blocks (backward-error accurate) ----
+
+@pytest.mark.parametrize("n", [1, 63, 64, 65, 200, 1000, 2049])
+@pytest.mark.parametrize("nrhs", [1, 3, 11])
+@pytest.mark.parametrize("trans", ["N", "T"])
+def test_fast_getrs_backward_error(ctx, oracle_mod, n, nrhs, trans):
+    """GBLU_SOLVE_FAST on FP64 factors: backward error within 10 n eps64 of
+    op(A) and a solution close to the exact mode's, for ragged last blocks,
+    several right-hand sides (more than one 8-column pass) and both
+    orientations."""
+    rng = np.random.default_rng(100 * n + nrhs)
+    A = np.asfortranarray(rng.standard_normal((n, n)))
+    B = np.asfortranarray(rng.standard_normal((n, nrhs)))
+    f = ctx.factor(n, n, "fp64")
+    assert f.getrf(A) == 0
+    Xe = f.getrs(B, trans=trans)
+    f.set_solve("fast")
+    X = f.getrs(B, trans=trans)
+    M = A if trans == "N" else A.T
+    assert oracle_mod.backward_error(M, X, B) <= 10 * max(n, 1) * EPS64
+    assert oracle_mod.forward_error(X, Xe) < 1e-8
+    f.close()
+
+
+def test_fast_getrs_follows_refactorization(ctx, oracle_mod):
+    """The inverses are recomputed after each getrf: a new matrix in the same
+    factor solves correctly, and exact mode can be switched back on."""
+    n = 700
+    f = ctx.factor(n, n, "fp64")
+    f.set_solve("fast")
+    for seed in (1, 2, 3):
+        A = np.asfortranarray(np.random.default_rng(seed).standard_normal((n, n)))
+        B = np.random.default_rng(seed + 10).standard_normal((n, 2))
+        assert f.getrf(A) == 0
+        assert oracle_mod.backward_error(A, f.getrs(B), B) <= 10 * n * EPS64
+    f.set_solve("exact")
+    LU, ipiv, _ = oracle_mod.getrf(A)
+    assert np.array_equal(f.getrs(B), oracle_mod.getrs(LU, ipiv, B))
+    f.close()
+
+
+@pytest.mark.parametrize("prec", ["fp32", "bf16"])
+def test_fast_inner_solve_of_mixed_factors(ctx, oracle_mod, pkg, prec):
+    n = 1500
+    A, B = pkg.workloads.shifted(n, 4, seed=41)
+    f = ctx.factor(n, n, prec)
+    f.set_solve("fast")
+    assert f.getrf(A) == 0
+    for mode in ("ir", "gmres_ir"):
+        X, st = f.solve_refined(B, mode=mode)
+        assert oracle_mod.backward_error(A, X, B) <= 10 * n * EPS64, st
+        assert st["fell_back"] == 0
+    f.close()
+
+
+def test_fast_getrs_through_the_interface(pkg, oracle_mod):
+    rng = np.random.default_rng(43)
+    n = 900
+    A = rng.standard_normal((n, n))
+    b = rng.standard_normal(n)
+    cache = pkg.init(pkg.LinearProblem(A, b), pkg.GB300LUFactorization(solve="fast"))
+    sol = pkg.solve_bang(cache)
+    assert sol.retcode == pkg.ReturnCode.Success
+    assert oracle_mod.backward_error(A, sol.u, b) <= 10 * n * EPS64
+    cache.b = rng.standard_normal(n)
+    sol = pkg.solve_bang(cache)
+    assert oracle_mod.backward_error(A, sol.u, cache.b) <= 10 * n * EPS64
