@@ -855,7 +855,7 @@ def run_serving_suite(pkg, cu, ctx, args):
     return out
 
 
-KERNEL_CASES = ("gemm_bf16", "gemm_fp16", "gemm_fp32", "refine", "perm")
+KERNEL_CASES = ("gemm_bf16", "gemm_fp16", "gemm_fp32", "refine", "perm", "mixed_bf16", "step_fp64")
 
 
 def run_kernel_case(args) -> int:
@@ -868,7 +868,10 @@ def run_kernel_case(args) -> int:
                              solves of 4 RHS, IR then GMRES-IR (gemv partial / reduce,
                              colmax, pow2_scales, scale_to_f32, update_from_f32, axpby)
       perm                   LAPACK-shaped dgetrs with host factors and pivots, n = 8192
-                             (upload_ipiv_check_kernel, perm_from_ipiv_kernel)"""
+                             (upload_ipiv_check_kernel, perm_from_ipiv_kernel)
+      mixed_bf16             the mixed suite's BF16 solve set, n = 16384, 4 RHS, run twice
+                             (launch lists: every kernel of getrf + refined solve)
+      step_fp64              two steps of the headline workload (n = 8192, 1 getrf + 16 getrs)"""
     pkg = load_pkg()
     _, _, local = dist_env()
     ctx = pkg.Context(local)
@@ -894,6 +897,27 @@ def run_kernel_case(args) -> int:
         A, B = pkg.workloads.plain(n, 1, seed=4)
         LU, ipiv, _ = pkg.dgetrf(A)
         pkg.dgetrs(LU, ipiv, B)
+    elif case == "mixed_bf16":
+        n = args.mixed_n
+        A, B = pkg.workloads.shifted(n, 4, seed=1)
+        dA = pkg.DeviceMatrix.from_host(A)
+        dB = pkg.DeviceMatrix.from_host(B)
+        f = ctx.factor(n, n, "bf16")
+        for _ in range(2):
+            dB.copy_from(pkg.DeviceMatrix.from_host(B))
+            f.getrf(dA)
+            f.solve_refined(dB)
+        f.close()
+    elif case == "step_fp64":
+        n, nrhs = args.n, args.nrhs
+        A, B = pkg.workloads.plain(n, nrhs, seed=0)
+        dA = pkg.DeviceMatrix.from_host(A)
+        f = ctx.factor(n, n, "fp64")
+        for _ in range(2):
+            f.getrf(dA)
+            for j in range(nrhs):
+                f.getrs(pkg.DeviceMatrix.from_host(B[:, j:j + 1]))
+        f.close()
     else:
         raise SystemExit(f"unknown kernel case {case!r}; one of {KERNEL_CASES}")
     ctx.close()

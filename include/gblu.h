@@ -285,6 +285,14 @@ typedef struct gblu_serve_config {
   int32_t refine_mode;       /* GBLU_REFINE_IR / GBLU_REFINE_GMRES (mixed precisions) */
   uint64_t hbm_budget_bytes; /* resident factorizations (0: no limit)             */
   int32_t max_rhs_batch;     /* solve-only requests merged per key                 */
+  int32_t small_n;           /* requests with n <= small_n (<= 256; 0: none) go to
+                                the small-system lane: whatever of them is queued,
+                                across keys, is factored and solved in one launch
+                                of the batched kernels (the key keeps its matrix
+                                in host memory, not its factors)                   */
+  int32_t solve_mode;        /* GBLU_SOLVE_EXACT / GBLU_SOLVE_FAST for the factors
+                                the server creates                                 */
+  int32_t max_small_batch;   /* systems per small-lane launch                      */
 } gblu_serve_config;
 typedef struct gblu_request {
   uint64_t key;      /* factorization key                                        */
@@ -309,6 +317,9 @@ typedef struct gblu_serve_stats {
   int64_t submitted, completed, failed, factorizations, solves, merged_solves, evictions;
   int64_t resident_factors, queued, in_flight;
   uint64_t resident_bytes;
+  int64_t small_launches;   /* launches of the small-system lane                */
+  int64_t small_systems;    /* requests solved by it                             */
+  int64_t admission_waits;  /* times a request waited for memory to be admitted  */
 } gblu_serve_stats;
 int32_t gblu_serve_config_default(gblu_serve_config* cfg);
 int32_t gblu_serve_create(gblu_ctx* ctx, const gblu_serve_config* cfg, gblu_server** out);

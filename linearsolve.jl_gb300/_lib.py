@@ -89,7 +89,8 @@ class Profile(ctypes.Structure):
 class ServeConfig(ctypes.Structure):
     _fields_ = [("workers", ctypes.c_int32), ("precision", ctypes.c_int32),
                 ("refine_mode", ctypes.c_int32), ("hbm_budget_bytes", ctypes.c_uint64),
-                ("max_rhs_batch", ctypes.c_int32)]
+                ("max_rhs_batch", ctypes.c_int32), ("small_n", ctypes.c_int32),
+                ("solve_mode", ctypes.c_int32), ("max_small_batch", ctypes.c_int32)]
 
 
 class Request(ctypes.Structure):
@@ -107,7 +108,8 @@ class Completion(ctypes.Structure):
 class ServeStats(ctypes.Structure):
     _fields_ = [(k, ctypes.c_int64) for k in (
         "submitted", "completed", "failed", "factorizations", "solves", "merged_solves",
-        "evictions", "resident_factors", "queued", "in_flight")] + [("resident_bytes", ctypes.c_uint64)]
+        "evictions", "resident_factors", "queued", "in_flight")] + [("resident_bytes", ctypes.c_uint64)] + [
+        (k, ctypes.c_int64) for k in ("small_launches", "small_systems", "admission_waits")]
 
 
 _P = ctypes.c_void_p

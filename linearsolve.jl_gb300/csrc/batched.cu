@@ -20,6 +20,9 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
+#include <mutex>
+#include <new>
 #include <vector>
 
 #include "device_util.cuh"
@@ -723,6 +726,50 @@ void default_buckets(gblu_batch* b, std::vector<BatchBucket>& out, const int32_t
   (void)b;
 }
 
+// The device arena of a batch holding up to `count` systems with a_total / b_total
+// packed elements (sets b->arena, b->bytes and the device views).
+int32_t batch_alloc(gblu_ctx* ctx, gblu_batch* b, int64_t count, int64_t a_total, int64_t b_total,
+                    int32_t precision) {
+  const int nbuckets_max = 8;
+  size_t bytes = 0;
+  auto add = [&](size_t x) { size_t o = bytes; bytes += align256(x); return o; };
+  size_t o_sizes = add(count * 4 + 4), o_order = add(count * 4 + 4), o_aoff = add(count * 8 + 8),
+         o_boff = add(count * 8 + 8), o_info = add(count * 8 + 8), o_flag = add(count * 4 + 4),
+         o_iters = add(count * 4 + 4),
+         o_q = add(2 * nbuckets_max * 4), o_A = add(a_total * 8 + 8), o_X = add(b_total * 8 + 8),
+         o_ipiv = add(b_total * 4 + 4);
+  size_t o_A32 = 0, o_B = 0, o_Aw = 0;
+  if (precision != GBLU_FP64) {
+    o_A32 = add(a_total * 4 + 4);
+    o_B = add(b_total * 8 + 8);
+    o_Aw = add(a_total * 8 + 8);
+  }
+  int32_t st = ctx_alloc(ctx, bytes, &b->arena);
+  if (st) return st;
+  b->bytes = bytes;
+  char* base = reinterpret_cast<char*>(b->arena);
+  b->d_sizes = reinterpret_cast<int32_t*>(base + o_sizes);
+  b->d_order = reinterpret_cast<int32_t*>(base + o_order);
+  b->d_aoff = reinterpret_cast<int64_t*>(base + o_aoff);
+  b->d_boff = reinterpret_cast<int64_t*>(base + o_boff);
+  b->d_info = reinterpret_cast<int64_t*>(base + o_info);
+  b->d_flag = reinterpret_cast<int32_t*>(base + o_flag);
+  b->d_iters = reinterpret_cast<int32_t*>(base + o_iters);
+  b->d_queues = reinterpret_cast<unsigned*>(base + o_q);
+  b->d_A = reinterpret_cast<double*>(base + o_A);
+  b->d_X = reinterpret_cast<double*>(base + o_X);
+  b->d_ipiv = reinterpret_cast<int32_t*>(base + o_ipiv);
+  b->d_A32 = nullptr;
+  b->d_B = nullptr;
+  b->d_Awork = nullptr;
+  if (precision != GBLU_FP64) {
+    b->d_A32 = reinterpret_cast<float*>(base + o_A32);
+    b->d_B = reinterpret_cast<double*>(base + o_B);
+    b->d_Awork = reinterpret_cast<double*>(base + o_Aw);
+  }
+  return GBLU_OK;
+}
+
 int32_t build_graph(gblu_ctx* ctx, gblu_batch* b) {
   if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
   if (b->graph) { cudaGraphDestroy(b->graph); b->graph = nullptr; }
@@ -812,40 +859,9 @@ int32_t gblu_batch_create(gblu_ctx* ctx, int64_t count, const int64_t* sizes, in
     b->a_total += sizes[i] * sizes[i];
     b->b_total += sizes[i];
   }
-  const int nbuckets_max = 8;
-  size_t bytes = 0;
-  auto add = [&](size_t x) { size_t o = bytes; bytes += align256(x); return o; };
-  size_t o_sizes = add(count * 4 + 4), o_order = add(count * 4 + 4), o_aoff = add(count * 8 + 8),
-         o_boff = add(count * 8 + 8), o_info = add(count * 8 + 8), o_flag = add(count * 4 + 4),
-         o_iters = add(count * 4 + 4),
-         o_q = add(2 * nbuckets_max * 4), o_A = add(b->a_total * 8 + 8), o_X = add(b->b_total * 8 + 8),
-         o_ipiv = add(b->b_total * 4 + 4);
-  size_t o_A32 = 0, o_B = 0, o_Aw = 0;
-  if (precision != GBLU_FP64) {
-    o_A32 = add(b->a_total * 4 + 4);
-    o_B = add(b->b_total * 8 + 8);
-    o_Aw = add(b->a_total * 8 + 8);
-  }
-  int32_t st = ctx_alloc(ctx, bytes, &b->arena);
+  int32_t st = batch_alloc(ctx, b, count, b->a_total, b->b_total, precision);
   if (st) { delete b; return st; }
-  b->bytes = bytes;
-  char* base = reinterpret_cast<char*>(b->arena);
-  b->d_sizes = reinterpret_cast<int32_t*>(base + o_sizes);
-  b->d_order = reinterpret_cast<int32_t*>(base + o_order);
-  b->d_aoff = reinterpret_cast<int64_t*>(base + o_aoff);
-  b->d_boff = reinterpret_cast<int64_t*>(base + o_boff);
-  b->d_info = reinterpret_cast<int64_t*>(base + o_info);
-  b->d_flag = reinterpret_cast<int32_t*>(base + o_flag);
-  b->d_iters = reinterpret_cast<int32_t*>(base + o_iters);
-  b->d_queues = reinterpret_cast<unsigned*>(base + o_q);
-  b->d_A = reinterpret_cast<double*>(base + o_A);
-  b->d_X = reinterpret_cast<double*>(base + o_X);
-  b->d_ipiv = reinterpret_cast<int32_t*>(base + o_ipiv);
-  if (precision != GBLU_FP64) {
-    b->d_A32 = reinterpret_cast<float*>(base + o_A32);
-    b->d_B = reinterpret_cast<double*>(base + o_B);
-    b->d_Awork = reinterpret_cast<double*>(base + o_Aw);
-  }
+  const size_t bytes = b->bytes;
   cudaError_t e = cudaMemsetAsync(b->arena, 0, bytes, ctx->stream);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(b->d_sizes, b->sizes.data(), count * 4, cudaMemcpyHostToDevice, ctx->stream);
@@ -974,3 +990,160 @@ int32_t gblu_batch_destroy(gblu_ctx* ctx, gblu_batch* b) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Lane: batches whose system list changes at every call (the serving loop's
+// small-system lane).  One bucket [1, 256] of 128-thread CTAs with 8-column
+// panels, direct launches instead of a captured graph, device arena and
+// pinned staging grown to the largest call and then reused.
+
+namespace gblu {
+
+struct BatchLane {
+  gblu_batch b;
+  int64_t cap_count = 0, cap_a = 0, cap_b = 0;
+  int32_t precision = -1;
+  double* hA = nullptr;  // pinned: packed A
+  double* hX = nullptr;  // pinned: packed b in, x out
+  char* hmeta = nullptr; // pinned: sizes, order, a_off, b_off, info, iters
+  size_t hA_cap = 0, hX_cap = 0, hmeta_cap = 0;
+};
+
+BatchLane* batch_lane_create() { return new (std::nothrow) BatchLane(); }
+
+void batch_lane_destroy(gblu_ctx* ctx, BatchLane* lane) {
+  if (!lane) return;
+  if (ctx) {
+    DeviceGuard g(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    if (lane->b.arena) ctx_free(ctx, lane->b.arena, lane->b.bytes);
+  }
+  if (lane->hA) cudaFreeHost(lane->hA);
+  if (lane->hX) cudaFreeHost(lane->hX);
+  if (lane->hmeta) cudaFreeHost(lane->hmeta);
+  delete lane;
+}
+
+namespace {
+int32_t grow_pinned(gblu_ctx* ctx, void** p, size_t* cap, size_t need) {
+  if (*cap >= need) return GBLU_OK;
+  if (*p) cudaFreeHost(*p);
+  *p = nullptr;
+  *cap = 0;
+  const size_t sz = std::max<size_t>(need + need / 2, 4096);
+  GBLU_CK(ctx, cudaMallocHost(p, sz), "pinned lane staging");
+  *cap = sz;
+  return GBLU_OK;
+}
+}  // namespace
+
+int32_t batch_lane_solve(gblu_ctx* ctx, BatchLane* lane, int32_t precision, int count, const int32_t* sizes,
+                         const double* const* A, const double* const* bvec, double* const* x, int64_t* info,
+                         int32_t* iters) {
+  if (count <= 0) return GBLU_OK;
+  DeviceGuard g(ctx->device);
+  {
+    static std::mutex mu;
+    static bool done[64] = {false};
+    std::lock_guard<std::mutex> l2(mu);
+    if (ctx->device < 64 && !done[ctx->device]) { batch_configure(ctx->device); done[ctx->device] = true; }
+  }
+  cudaStream_t s = ctx->stream;
+  int64_t a_total = 0, b_total = 0;
+  for (int i = 0; i < count; ++i) {
+    if (sizes[i] < 1 || sizes[i] > kBatchMaxN)
+      return fail(ctx, GBLU_EUNSUPPORTED, "batch lane: n = %d outside 1..%d", sizes[i], kBatchMaxN);
+    a_total += (int64_t)sizes[i] * sizes[i];
+    b_total += sizes[i];
+  }
+  const bool mixed = precision != GBLU_FP64;
+  gblu_batch& b = lane->b;
+  if (lane->cap_count < count || lane->cap_a < a_total || lane->cap_b < b_total ||
+      (mixed && lane->precision == GBLU_FP64) || lane->precision < 0) {
+    GBLU_CK(ctx, cudaStreamSynchronize(s), "batch lane");
+    if (b.arena) ctx_free(ctx, b.arena, b.bytes);
+    b.arena = nullptr;
+    const int64_t cc = std::max<int64_t>(count, 2 * lane->cap_count);
+    const int64_t ca = std::max<int64_t>(a_total, 2 * lane->cap_a);
+    const int64_t cb = std::max<int64_t>(b_total, 2 * lane->cap_b);
+    const int32_t prec = mixed ? GBLU_FP32 : GBLU_FP64;
+    int32_t st = batch_alloc(ctx, &b, cc, ca, cb, prec);
+    if (st) { lane->cap_count = lane->cap_a = lane->cap_b = 0; lane->precision = -1; return st; }
+    GBLU_CK(ctx, cudaMemsetAsync(b.arena, 0, b.bytes, s), "batch lane clear");
+    lane->cap_count = cc;
+    lane->cap_a = ca;
+    lane->cap_b = cb;
+    lane->precision = prec;
+  }
+  const size_t meta = (size_t)count * (4 + 4 + 8 + 8 + 8 + 4) + 64;
+  int32_t st = grow_pinned(ctx, reinterpret_cast<void**>(&lane->hA), &lane->hA_cap, (size_t)a_total * 8);
+  if (!st) st = grow_pinned(ctx, reinterpret_cast<void**>(&lane->hX), &lane->hX_cap, (size_t)b_total * 8);
+  if (!st) st = grow_pinned(ctx, reinterpret_cast<void**>(&lane->hmeta), &lane->hmeta_cap, meta);
+  if (st) return st;
+  int64_t* h_aoff = reinterpret_cast<int64_t*>(lane->hmeta);
+  int64_t* h_boff = h_aoff + count;
+  int64_t* h_info = h_boff + count;
+  int32_t* h_sizes = reinterpret_cast<int32_t*>(h_info + count);
+  int32_t* h_order = h_sizes + count;
+  int32_t* h_iters = h_order + count;
+  int64_t ao = 0, bo = 0;
+  for (int i = 0; i < count; ++i) {
+    const int n = sizes[i];
+    h_sizes[i] = n;
+    h_aoff[i] = ao;
+    h_boff[i] = bo;
+    std::memcpy(lane->hA + ao, A[i], (size_t)n * n * sizeof(double));
+    std::memcpy(lane->hX + bo, bvec[i], (size_t)n * sizeof(double));
+    ao += (int64_t)n * n;
+    bo += n;
+    h_order[i] = i;
+  }
+  std::stable_sort(h_order, h_order + count, [&](int32_t p, int32_t q) { return h_sizes[p] > h_sizes[q]; });
+  GBLU_CK(ctx, cudaMemcpyAsync(b.d_sizes, h_sizes, count * 4, cudaMemcpyHostToDevice, s), "lane sizes");
+  GBLU_CK(ctx, cudaMemcpyAsync(b.d_order, h_order, count * 4, cudaMemcpyHostToDevice, s), "lane order");
+  GBLU_CK(ctx, cudaMemcpyAsync(b.d_aoff, h_aoff, count * 8, cudaMemcpyHostToDevice, s), "lane offsets");
+  GBLU_CK(ctx, cudaMemcpyAsync(b.d_boff, h_boff, count * 8, cudaMemcpyHostToDevice, s), "lane offsets");
+  GBLU_CK(ctx, cudaMemcpyAsync(b.d_A, lane->hA, a_total * 8, cudaMemcpyHostToDevice, s), "lane A");
+  GBLU_CK(ctx, cudaMemcpyAsync(b.d_X, lane->hX, b_total * 8, cudaMemcpyHostToDevice, s), "lane b");
+  if (mixed)
+    GBLU_CK(ctx, cudaMemcpyAsync(b.d_B, b.d_X, b_total * 8, cudaMemcpyDeviceToDevice, s), "lane b copy");
+  GBLU_CK(ctx, cudaMemsetAsync(b.d_queues, 0, 2 * sizeof(unsigned), s), "lane queues");
+  GBLU_CK(ctx, cudaMemsetAsync(b.d_flag, 0, count * 4, s), "lane flags");
+  GBLU_CK(ctx, cudaMemsetAsync(b.d_iters, 0, count * 4, s), "lane iterations");
+  b.precision = mixed ? GBLU_FP32 : GBLU_FP64;
+  b.count = count;
+  BatchDev d;
+  d.order = b.d_order;
+  d.sizes = b.d_sizes;
+  d.a_off = b.d_aoff;
+  d.b_off = b.d_boff;
+  d.count = count;
+  d.queue = b.d_queues;
+  d.info = b.d_info;
+  d.flag = b.d_flag;
+  d.iters = b.d_iters;
+  const int ctas = std::max(1, std::min(count, device_info(ctx->device).num_sms * 4));
+  cudaError_t e;
+  if (!mixed) {
+    e = launch_fp64<128, 8>(d, ctas, &b, b.d_A, 0, s);
+  } else {
+    e = launch_mixed<128, 8>(d, ctas, &b, s);
+    if (e == cudaSuccess) {
+      d.queue = b.d_queues + 1;  // FP64 re-solve of the systems refinement flagged
+      e = launch_fp64<128, 8>(d, ctas, &b, b.d_Awork, 1, s);
+    }
+  }
+  GBLU_CK(ctx, e, "batch lane launch");
+  GBLU_CK(ctx, cudaMemcpyAsync(lane->hX, b.d_X, b_total * 8, cudaMemcpyDeviceToHost, s), "lane x");
+  GBLU_CK(ctx, cudaMemcpyAsync(h_info, b.d_info, count * 8, cudaMemcpyDeviceToHost, s), "lane info");
+  GBLU_CK(ctx, cudaMemcpyAsync(h_iters, b.d_iters, count * 4, cudaMemcpyDeviceToHost, s), "lane iterations");
+  GBLU_CK(ctx, cudaStreamSynchronize(s), "batch lane");
+  for (int i = 0; i < count; ++i) {
+    std::memcpy(x[i], lane->hX + h_boff[i], (size_t)sizes[i] * sizeof(double));
+    if (info) info[i] = h_info[i];
+    if (iters) iters[i] = h_iters[i];
+  }
+  return GBLU_OK;
+}
+
+}  // namespace gblu

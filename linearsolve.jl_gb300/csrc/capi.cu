@@ -360,6 +360,7 @@ int32_t gblu_factor_destroy(gblu_ctx* ctx, gblu_factor* f) {
   if (f->a_keep) ctx_free(ctx, f->a_keep, std::max<size_t>((size_t)f->ld * f->n * sizeof(double), 256));
   if (f->chk_arena) ctx_free(ctx, f->chk_arena, f->chk_bytes);
   if (f->inv_arena) ctx_free(ctx, f->inv_arena, f->inv_bytes);
+  if (f->refine.gflags_host) cudaFreeHost(f->refine.gflags_host);
   delete f;
   return GBLU_OK;
 }

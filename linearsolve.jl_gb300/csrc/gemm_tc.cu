@@ -35,12 +35,12 @@
 namespace gblu {
 namespace tc {
 
-constexpr int BM = 128, BN = 128, BK = 64, STAGES = 3, THREADS = 192;
+constexpr int BM = 128, BN = 128, BK = 64, STAGES = 6, THREADS = 192;
 constexpr int UMMA_K = 16;
 constexpr uint32_t A_BYTES = BM * BK * 2;
 constexpr uint32_t B_BYTES = BN * BK * 2;
 constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
-constexpr uint32_t TMEM_COLS = 128;
+constexpr uint32_t TMEM_COLS = 2 * BN;  // two accumulators: one drains while the other fills
 constexpr size_t SMEM_BYTES = (size_t)STAGES * STAGE_BYTES + 1024 + 256;
 
 __device__ __forceinline__ uint32_t saddr(const void* p) {
@@ -48,6 +48,9 @@ __device__ __forceinline__ uint32_t saddr(const void* p) {
 }
 __device__ __forceinline__ void mbar_init(uint32_t a, uint32_t cnt) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(cnt) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t a) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(a) : "memory");
 }
 __device__ __forceinline__ void mbar_expect_tx(uint32_t a, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(a), "r"(bytes) : "memory");
@@ -149,8 +152,15 @@ __host__ __device__ constexpr uint32_t idesc_f16(uint32_t fmt) {
          ((uint32_t)(BM >> 4) << 24);
 }
 
+// Persistent: one CTA per SM walks the output tiles t = blockIdx.x,
+// blockIdx.x + gridDim.x, ... (row-tile index fastest, so the CTAs of a wave
+// share their B tiles in L2).  The producer's TMA ring runs across tile
+// boundaries; the MMA issuer fills TMEM accumulator (i & 1) of the CTA's i-th
+// tile while the epilogue warps drain the other one.
+//   full[s] / empty[s]      smem stage s loaded / consumed (ring of STAGES)
+//   tfull[b] / tempty[b]    accumulator b complete / drained (4 epilogue warps)
 template <uint32_t FMT>
-__global__ void __launch_bounds__(THREADS, 2)
+__global__ void __launch_bounds__(THREADS, 1)
 tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                float* __restrict__ C, int64_t ldc, int M, int N, int K,
                const float* __restrict__ inv_scale, int* __restrict__ err) {
@@ -160,19 +170,24 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);
   uint64_t* full = bars;
   uint64_t* empty = bars + STAGES;
-  uint64_t* tfull = bars + 2 * STAGES;
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 1);
+  uint64_t* tfull = bars + 2 * STAGES;       // [2]
+  uint64_t* tempty = bars + 2 * STAGES + 2;  // [2]
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 4);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
   const int kblocks = (K + BK - 1) / BK;
+  const int tiles_m = (M + BM - 1) / BM;
+  const int tiles = tiles_m * ((N + BN - 1) / BN);
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
       mbar_init(saddr(&full[s]), 1);
       mbar_init(saddr(&empty[s]), 1);
     }
-    mbar_init(saddr(tfull), 1);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(saddr(&tfull[b]), 1);
+      mbar_init(saddr(&tempty[b]), 4);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
@@ -185,40 +200,57 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
   const uint32_t tbase = *tslot;
 
   if (warp == 0 && lane == 0) {
-    // TMA producer
-    for (int kb = 0; kb < kblocks; ++kb) {
-      const int s = kb % STAGES;
-      if (kb >= STAGES && !mbar_wait(saddr(&empty[s]), ((kb / STAGES) & 1) ^ 1, err)) break;
-      const uint32_t a_dst = saddr(smem + s * STAGE_BYTES);
-      const uint32_t b_dst = a_dst + A_BYTES;
-      mbar_expect_tx(saddr(&full[s]), STAGE_BYTES);
-      tma_load_2d(a_dst, &tmA, kb * BK, m0, saddr(&full[s]));
-      tma_load_2d(b_dst, &tmB, kb * BK, n0, saddr(&full[s]));
+    // TMA producer: k-blocks of every tile of this CTA, one ring
+    int it = 0;
+    bool ok = true;
+    for (int t = blockIdx.x; t < tiles && ok; t += gridDim.x) {
+      const int m0 = (t % tiles_m) * BM, n0 = (t / tiles_m) * BN;
+      for (int kb = 0; kb < kblocks; ++kb, ++it) {
+        const int s = it % STAGES;
+        if (it >= STAGES && !mbar_wait(saddr(&empty[s]), ((it / STAGES) & 1) ^ 1, err)) { ok = false; break; }
+        const uint32_t a_dst = saddr(smem + s * STAGE_BYTES);
+        const uint32_t b_dst = a_dst + A_BYTES;
+        mbar_expect_tx(saddr(&full[s]), STAGE_BYTES);
+        tma_load_2d(a_dst, &tmA, kb * BK, m0, saddr(&full[s]));
+        tma_load_2d(b_dst, &tmB, kb * BK, n0, saddr(&full[s]));
+      }
     }
   } else if (warp == 1 && lane == 0) {
     // MMA issuer
     constexpr uint32_t idesc = idesc_f16(FMT);
+    int it = 0, i = 0;
     bool ok = true;
-    for (int kb = 0; kb < kblocks && ok; ++kb) {
-      const int s = kb % STAGES;
-      if (!mbar_wait(saddr(&full[s]), (kb / STAGES) & 1, err)) { ok = false; break; }
+    for (int t = blockIdx.x; t < tiles && ok; t += gridDim.x, ++i) {
+      const int b = i & 1;
+      // accumulator b is free once the epilogue drained its previous tile
+      if (i >= 2 && !mbar_wait(saddr(&tempty[b]), ((i >> 1) & 1) ^ 1, err)) break;
       tc_fence_after();
-      const uint32_t a_base = saddr(smem + s * STAGE_BYTES);
-      const uint32_t b_base = a_base + A_BYTES;
+      const uint32_t acc = tbase + (uint32_t)(b * BN);
+      for (int kb = 0; kb < kblocks; ++kb, ++it) {
+        const int s = it % STAGES;
+        if (!mbar_wait(saddr(&full[s]), (it / STAGES) & 1, err)) { ok = false; break; }
+        tc_fence_after();
+        const uint32_t a_base = saddr(smem + s * STAGE_BYTES);
+        const uint32_t b_base = a_base + A_BYTES;
 #pragma unroll
-      for (int k = 0; k < BK / UMMA_K; ++k) {
-        const uint64_t ad = sdesc_k128(a_base + k * UMMA_K * 2);
-        const uint64_t bd = sdesc_k128(b_base + k * UMMA_K * 2);
-        tc_mma(tbase, ad, bd, idesc, (kb > 0 || k > 0) ? 1u : 0u);
+        for (int k = 0; k < BK / UMMA_K; ++k) {
+          const uint64_t ad = sdesc_k128(a_base + k * UMMA_K * 2);
+          const uint64_t bd = sdesc_k128(b_base + k * UMMA_K * 2);
+          tc_mma(acc, ad, bd, idesc, (kb > 0 || k > 0) ? 1u : 0u);
+        }
+        tc_commit(saddr(&empty[s]));  // stage s is free once these MMAs have read it
       }
-      tc_commit(saddr(&empty[s]));  // stage s is free once these MMAs have read it
+      tc_commit(saddr(&tfull[b]));  // accumulator b complete (or abandoned)
     }
-    tc_commit(saddr(tfull));  // accumulator complete (or abandoned)
   } else if (warp >= 2) {
     // epilogue: TMEM lanes [32*(warp%4), +32) are this warp's rows
     const int q = warp & 3;
-    if (mbar_wait(saddr(tfull), 0, err)) {
+    int i = 0;
+    for (int t = blockIdx.x; t < tiles; t += gridDim.x, ++i) {
+      const int b = i & 1;
+      if (!mbar_wait(saddr(&tfull[b]), (i >> 1) & 1, err)) break;
       tc_fence_after();
+      const int m0 = (t % tiles_m) * BM, n0 = (t / tiles_m) * BN;
       const int row = m0 + q * 32 + lane;
 #pragma unroll 1
       for (int c0 = 0; c0 < BN; c0 += 32) {
@@ -230,7 +262,7 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
         for (int j = 0; j < 32; ++j)
           cv[j] = (row < M && n0 + c0 + j < N) ? crow[(int64_t)j * ldc] : 0.f;
         uint32_t v[32];
-        tmem_ld_32cols(tbase + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, v);
+        tmem_ld_32cols(tbase + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * BN + c0), v);
         if (row < M) {
           float* cw = C + (int64_t)row + (int64_t)(n0 + c0) * ldc;
 #pragma unroll
@@ -244,6 +276,10 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
           }
         }
       }
+      // this warp's reads of accumulator b are complete (tcgen05.wait::ld)
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(saddr(&tempty[b]));
     }
   }
   tc_fence_before();
@@ -407,7 +443,12 @@ cudaError_t tc_gemm_sub(int mode, int64_t M, int64_t N, int64_t K, const float* 
   if (!tc::make_map(&ta, Ah, (uint64_t)K, (uint64_t)M, (uint64_t)Kp * 2, bf16) ||
       !tc::make_map(&tb, Bh, (uint64_t)K, (uint64_t)N, (uint64_t)Kp * 2, bf16))
     return cudaErrorInvalidValue;
-  dim3 grid((unsigned)((M + tc::BM - 1) / tc::BM), (unsigned)((N + tc::BN - 1) / tc::BN));
+  // persistent: at most one CTA per SM, each walking its share of the tiles
+  int device = 0;
+  cudaGetDevice(&device);
+  const int64_t tiles = ((M + tc::BM - 1) / tc::BM) * ((N + tc::BN - 1) / tc::BN);
+  if (tiles > INT32_MAX) return cudaErrorInvalidValue;
+  dim3 grid((unsigned)std::min<int64_t>(tiles, device_info(device).num_sms));
   LaunchScope ls(K_GEMM, 2.0 * M * N * K, (2.0 * M * N + (double)(M + N) * K / 2.0) * 4.0, s);
   if (bf16)
     tc::tc_gemm_kernel<1><<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(ta, tb, C, ldc, (int)M, (int)N, (int)K,

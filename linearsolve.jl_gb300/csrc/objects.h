@@ -87,6 +87,19 @@ int32_t factor_fp64_fallback(gblu_ctx* ctx, gblu_factor* f, int64_t* info_out);
 // inverses are not there yet (asynchronous on the context stream).
 int32_t ensure_inverse(gblu_ctx* ctx, gblu_factor* f);
 
+// Small uneven systems (n <= 256) solved together by one launch of the
+// batched kernels, for a system list that changes at every call (batched.cu;
+// the serving loop's small-system lane).  Device and pinned buffers grow to
+// the largest call and are reused.  System i: A[i] (n_i x n_i, column-major,
+// host) x = b[i] (host), x written to x[i]; info[i] its getrf info; iters[i]
+// (mixed precision) its refinement corrections, -1 if re-solved in FP64.
+struct BatchLane;
+BatchLane* batch_lane_create();
+void batch_lane_destroy(gblu_ctx* ctx, BatchLane* lane);
+int32_t batch_lane_solve(gblu_ctx* ctx, BatchLane* lane, int32_t precision, int count, const int32_t* sizes,
+                         const double* const* A, const double* const* b, double* const* x, int64_t* info,
+                         int32_t* iters);
+
 inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
 struct DeviceGuard {

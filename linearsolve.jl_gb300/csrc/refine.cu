@@ -297,6 +297,110 @@ __global__ void sumsq_final_kernel(int W, const double* __restrict__ part, doubl
   out[q] = s;
 }
 
+// ---- GMRES(m) bookkeeping on the device, one thread per RHS column ----
+// State of column q: gm + q * kGmStride (H, rotations, g, y, beta, 1/norm of
+// the newest basis vector); flags gflags[2q] = still extending its basis,
+// gflags[2q + 1] = basis size k.  A column that stopped keeps its state and
+// gets 1/norm = 0, so its later basis vectors are zero and stay finite.
+
+// beta_q = ||z_q||_2 from the squared norm in hn2[q] (columns outside run_mask
+// do not step), g = beta e_1.
+__global__ void gmres_begin_kernel(int nc, unsigned run_mask, const double* __restrict__ hn2,
+                                   double* __restrict__ gm, int* __restrict__ gflags) {
+  const int q = threadIdx.x;
+  if (q >= nc) return;
+  double* st = gm + (size_t)q * kGmStride;
+  int* fl = gflags + 2 * q;
+  const double beta = ((run_mask >> q) & 1u) ? sqrt(hn2[q]) : 0.0;
+  const bool step = beta > 0 && isfinite(beta);
+  for (int i = 0; i <= kGmresRestart; ++i) {
+    st[kGmG + i] = 0.0;
+    st[kGmY + i] = 0.0;
+  }
+  st[kGmG] = beta;
+  st[kGmBeta] = beta;
+  st[kGmInv] = step ? 1.0 / beta : 0.0;
+  fl[0] = step ? 1 : 0;
+  fl[1] = 0;
+}
+
+// V_q(:, j) *= 1/norm_q for the nc bases (column q's basis starts at V + q * ldV).
+__global__ void gmres_scale_kernel(int64_t n, int nc, double* __restrict__ V, int64_t ldV, int j,
+                                   const double* __restrict__ gm) {
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < n * nc;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int q = (int)(idx / n);
+    const int64_t i = idx - (int64_t)q * n;
+    double* v = V + (size_t)q * ldV + (size_t)j * n + i;
+    *v = gm[(size_t)q * kGmStride + kGmInv] * *v;
+  }
+}
+
+// Step j of each stepping column: Hessenberg column from the two projection
+// passes and the norm (h: [q][pass 0, 1, norm^2][m + 1]), the previous Givens
+// rotations, the new rotation, g, the stopping test |g_{j+1}| <= rtol beta.
+__global__ void gmres_step_kernel(int nc, int j, int m, const double* __restrict__ h, double rtol,
+                                  double* __restrict__ gm, int* __restrict__ gflags) {
+  const int q = threadIdx.x;
+  if (q >= nc) return;
+  double* st = gm + (size_t)q * kGmStride;
+  int* fl = gflags + 2 * q;
+  if (!fl[0]) {
+    st[kGmInv] = 0.0;
+    return;
+  }
+  const int hs = kGmresRestart + 1;
+  const double* h1 = h + (size_t)(q * 3) * hs;
+  const double* h2 = h1 + hs;
+  const double hn = sqrt(h1[2 * hs]);
+  double* Hj = st + kGmH + (size_t)j * (m + 1);
+  double* cs = st + kGmCs;
+  double* sn = st + kGmSn;
+  double* g = st + kGmG;
+  for (int i = 0; i <= j; ++i) Hj[i] = h1[i] + h2[i];
+  Hj[j + 1] = hn;
+  for (int i = 0; i < j; ++i) {
+    const double a = Hj[i], b = Hj[i + 1];
+    Hj[i] = cs[i] * a + sn[i] * b;
+    Hj[i + 1] = -sn[i] * a + cs[i] * b;
+  }
+  const double a = Hj[j], b = Hj[j + 1];
+  const double rr = hypot(a, b);
+  cs[j] = rr > 0 ? a / rr : 1.0;
+  sn[j] = rr > 0 ? b / rr : 0.0;
+  Hj[j] = rr;
+  Hj[j + 1] = 0.0;
+  g[j + 1] = -sn[j] * g[j];
+  g[j] = cs[j] * g[j];
+  fl[1] = j + 1;
+  if (fabs(g[j + 1]) <= rtol * st[kGmBeta] || !(hn > 0) || !isfinite(hn)) {
+    fl[0] = 0;
+    st[kGmInv] = 0.0;
+  } else {
+    st[kGmInv] = 1.0 / hn;
+  }
+}
+
+// y_q = H_q(1:k, 1:k) \ g_q(1:k) by back substitution, into y_out + q * hs.
+__global__ void gmres_finish_kernel(int nc, int m, const double* __restrict__ gm,
+                                    const int* __restrict__ gflags, double* __restrict__ y_out) {
+  const int q = threadIdx.x;
+  if (q >= nc) return;
+  const int hs = kGmresRestart + 1;
+  const double* st = gm + (size_t)q * kGmStride;
+  const double* H = st + kGmH;
+  const double* g = st + kGmG;
+  const int k = gflags[2 * q + 1];
+  double* y = y_out + (size_t)q * hs;
+  for (int i = 0; i < hs; ++i) y[i] = 0.0;
+  for (int i = k - 1; i >= 0; --i) {
+    double acc = g[i];
+    for (int jj = i + 1; jj < k; ++jj) acc -= H[(size_t)jj * (m + 1) + i] * y[jj];
+    const double d = H[(size_t)i * (m + 1) + i];
+    y[i] = d != 0 ? acc / d : 0.0;
+  }
+}
+
 // Y = a*X + b*Y
 __global__ void axpby_kernel(int64_t n, double a, const double* __restrict__ X, double b,
                              double* __restrict__ Y) {
@@ -322,6 +426,8 @@ size_t refine_bytes(int64_t n, int64_t W) {
   b += align256(4 * sizeof(double) * kMaxW);               // scales
   b += align256(sizeof(double));                           // anorm
   b += align256(2 * sizeof(unsigned long long));           // growth words
+  b += align256((size_t)W * kGmStride * sizeof(double));   // GMRES state
+  b += align256((size_t)W * 2 * sizeof(int));              // GMRES flags
   return b + 256;
 }
 
@@ -344,6 +450,8 @@ void refine_carve(RefineWork& w, char* base, int64_t n, int64_t W) {
   w.dots = reinterpret_cast<double*>(take((size_t)kDotBlocks * (kGmresRestart + 1) * sizeof(double)));
   w.anorm_dev = reinterpret_cast<double*>(take(4 * sizeof(double) * kMaxW));
   w.growth_bits = reinterpret_cast<unsigned long long*>(take(2 * sizeof(unsigned long long)));
+  w.gm = reinterpret_cast<double*>(take((size_t)W * kGmStride * sizeof(double)));
+  w.gflags = reinterpret_cast<int*>(take((size_t)W * 2 * sizeof(int)));
 }
 
 namespace {
@@ -526,114 +634,113 @@ struct Solver {
 
   // GMRES(m) on op(A) d = r[:,q], left-preconditioned by the FP32 LU, for the
   // columns q < nc with run[q] set, in lockstep: each inner step does one
-  // nc-column matvec and one nc-column preconditioner solve, while every
-  // column keeps its own basis V_q, Hessenberg matrix, rotations and stopping
-  // step, so its result is the one it would have alone.  Adds d_q into x[:,q];
-  // its[q] receives the column's inner iterations.
+  // nc-column matvec, one nc-column preconditioner solve and the two
+  // Gram-Schmidt passes of every column, while every column keeps its own
+  // basis V_q, Hessenberg matrix, rotations and stopping step (device state,
+  // gmres_*_kernel), so its result is the one it would have alone.  The host
+  // never waits inside a step: it reads the stepping flags of step j - 1 while
+  // step j is already queued, and stops when no column steps (a step queued
+  // after every column stopped changes nothing).  Adds d_q into x[:,q]; its[q]
+  // receives the column's inner iterations.
   int32_t gmres_block(int nc, const std::vector<int>& run, int restart, double rtol, std::vector<int>& its) {
     const int m = std::max(1, std::min(restart, (int)kGmresRestart));
     const int64_t ldV = (int64_t)(kGmresRestart + 1) * n;  // stride between the columns' bases
     const int hs = kGmresRestart + 1;
     double* V = w.V;
     auto Vq = [&](int q, int j) { return V + (size_t)q * ldV + (size_t)j * n; };
+    if (!w.gflags_host) {
+      void* p = nullptr;
+      GBLU_CK(ctx, cudaMallocHost(&p, 4 * kMaxW * sizeof(int)), "pinned GMRES flags");
+      w.gflags_host = reinterpret_cast<int*>(p);
+    }
     int32_t st = precond(w.r, n, V, ldV, nc);
     if (st) return st;
-    // beta_q = ||z_q||_2
-    std::vector<double> hb((size_t)3 * hs * nc);
+    unsigned mask = 0;
     for (int q = 0; q < nc; ++q)
-      if (run[q])
+      if (run[q]) {
+        mask |= 1u << q;
         GBLU_CK(ctx, gemv('T', n, 1, Vq(q, 0), n, Vq(q, 0), n, 1, 1.0, nullptr, 1, 0.0, w.h + q, 1,
                           w.partial, nullptr, s), "norm");
-    std::vector<double> beta(nc, 0.0);
-    GBLU_CK(ctx, cudaMemcpyAsync(beta.data(), w.h, nc * sizeof(double), cudaMemcpyDeviceToHost, s), "norm");
-    GBLU_CK(ctx, cudaStreamSynchronize(s), "norm");
-    std::vector<int> step(nc, 0);  // 1 = still extending its basis
-    std::vector<int> k(nc, 0);
-    for (int q = 0; q < nc; ++q) {
-      its[q] = 0;
-      if (!run[q]) continue;
-      beta[q] = std::sqrt(beta[q]);
-      if (!(beta[q] > 0) || !std::isfinite(beta[q])) continue;
-      step[q] = 1;
+      }
+    {
       LaunchScope ls_(K_REFINE, 0.0, 0.0, s);
-      axpby_kernel<<<grid_for(n), 256, 0, s>>>(n, 1.0 / beta[q], Vq(q, 0), 0.0, Vq(q, 0));
+      gmres_begin_kernel<<<1, 32, 0, s>>>(nc, mask, w.h, w.gm, w.gflags);
     }
-    std::vector<std::vector<double>> H(nc, std::vector<double>((size_t)(m + 1) * m, 0.0));
-    std::vector<std::vector<double>> cs(nc, std::vector<double>(m)), sn(nc, std::vector<double>(m));
-    std::vector<std::vector<double>> g(nc, std::vector<double>(m + 1, 0.0));
-    for (int q = 0; q < nc; ++q) g[q][0] = beta[q];
-    for (int j = 0; j < m; ++j) {
-      bool any = false;
-      for (int q = 0; q < nc; ++q) any |= step[q] != 0;
-      if (!any) break;
+    {
+      LaunchScope ls_(K_REFINE, 0.0, 16.0 * n * nc, s);
+      gmres_scale_kernel<<<grid_for(n * nc), 256, 0, s>>>(n, nc, V, ldV, 0, w.gm);
+    }
+    GBLU_CK(ctx, cudaGetLastError(), "GMRES start");
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    for (auto& e : ev) GBLU_CK(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
+    auto release = [&]() {
+      for (auto& e : ev)
+        if (e) cudaEventDestroy(e);
+    };
+    int32_t rc = GBLU_OK;
+    for (int j = 0; j < m && mask && rc == GBLU_OK; ++j) {
       // w = op(A) v_j ; z = M^{-1} w  (all nc columns at once)
-      GBLU_CK(ctx, gemv(trans == 'N' ? 'N' : 'T', n, n, f->lu64, f->ld, Vq(0, j), ldV, nc, 1.0, nullptr, 1,
-                        0.0, w.w, n, w.partial, nullptr, s), "matvec");
-      st = precond(w.w, n, Vq(0, j + 1), ldV, nc);
-      if (st) return st;
-      // classical Gram-Schmidt, twice, and the norm, per stepping column
-      for (int q = 0; q < nc; ++q) {
-        if (!step[q]) continue;
+      cudaError_t ce = gemv(trans == 'N' ? 'N' : 'T', n, n, f->lu64, f->ld, Vq(0, j), ldV, nc, 1.0, nullptr,
+                            1, 0.0, w.w, n, w.partial, nullptr, s);
+      if (ce != cudaSuccess) { rc = cuda_fail(ctx, ce, "matvec"); break; }
+      rc = precond(w.w, n, Vq(0, j + 1), ldV, nc);
+      if (rc) break;
+      // classical Gram-Schmidt, twice, and the norm, for every column
+      for (int q = 0; q < nc && ce == cudaSuccess; ++q) {
         double* z = Vq(q, j + 1);
-        for (int pass = 0; pass < 2; ++pass) {
+        for (int pass = 0; pass < 2 && ce == cudaSuccess; ++pass) {
           double* hq = w.h + (size_t)(q * 3 + pass) * hs;
-          GBLU_CK(ctx, gemv('T', n, j + 1, Vq(q, 0), n, z, n, 1, 1.0, nullptr, 1, 0.0, hq, 1, w.partial,
-                            nullptr, s), "project");
-          GBLU_CK(ctx, gemv('N', n, j + 1, Vq(q, 0), n, hq, j + 1, 1, -1.0, z, n, 1.0, z, n, w.partial,
-                            nullptr, s), "orthogonalise");
+          ce = gemv('T', n, j + 1, Vq(q, 0), n, z, n, 1, 1.0, nullptr, 1, 0.0, hq, 1, w.partial, nullptr, s);
+          if (ce == cudaSuccess)
+            ce = gemv('N', n, j + 1, Vq(q, 0), n, hq, j + 1, 1, -1.0, z, n, 1.0, z, n, w.partial, nullptr, s);
         }
-        GBLU_CK(ctx, gemv('T', n, 1, z, n, z, n, 1, 1.0, nullptr, 1, 0.0, w.h + (size_t)(q * 3 + 2) * hs, 1,
-                          w.partial, nullptr, s), "norm");
+        if (ce == cudaSuccess)
+          ce = gemv('T', n, 1, z, n, z, n, 1, 1.0, nullptr, 1, 0.0, w.h + (size_t)(q * 3 + 2) * hs, 1, w.partial,
+                    nullptr, s);
       }
-      GBLU_CK(ctx, cudaMemcpyAsync(hb.data(), w.h, (size_t)3 * hs * nc * sizeof(double), cudaMemcpyDeviceToHost,
-                                   s), "readback");
-      GBLU_CK(ctx, cudaStreamSynchronize(s), "gmres step");
-      for (int q = 0; q < nc; ++q) {
-        if (!step[q]) continue;
-        const double* h1 = hb.data() + (size_t)(q * 3) * hs;
-        const double* h2 = h1 + hs;
-        const double hn = std::sqrt(h1[2 * hs]);
-        std::vector<double>& Hq = H[q];
-        for (int i = 0; i <= j; ++i) Hq[(size_t)j * (m + 1) + i] = h1[i] + h2[i];
-        Hq[(size_t)j * (m + 1) + j + 1] = hn;
-        for (int i = 0; i < j; ++i) {  // previous rotations
-          const double a = Hq[(size_t)j * (m + 1) + i], b = Hq[(size_t)j * (m + 1) + i + 1];
-          Hq[(size_t)j * (m + 1) + i] = cs[q][i] * a + sn[q][i] * b;
-          Hq[(size_t)j * (m + 1) + i + 1] = -sn[q][i] * a + cs[q][i] * b;
-        }
-        const double a = Hq[(size_t)j * (m + 1) + j], b = Hq[(size_t)j * (m + 1) + j + 1];
-        const double rr = std::hypot(a, b);
-        cs[q][j] = rr > 0 ? a / rr : 1.0;
-        sn[q][j] = rr > 0 ? b / rr : 0.0;
-        Hq[(size_t)j * (m + 1) + j] = rr;
-        Hq[(size_t)j * (m + 1) + j + 1] = 0.0;
-        g[q][j + 1] = -sn[q][j] * g[q][j];
-        g[q][j] = cs[q][j] * g[q][j];
-        k[q] = j + 1;
-        if (std::fabs(g[q][j + 1]) <= rtol * beta[q] || !(hn > 0) || !std::isfinite(hn)) {
-          step[q] = 0;
-        } else {
-          LaunchScope ls_(K_REFINE, 0.0, 0.0, s);
-          axpby_kernel<<<grid_for(n), 256, 0, s>>>(n, 1.0 / hn, Vq(q, j + 1), 0.0, Vq(q, j + 1));
+      if (ce != cudaSuccess) { rc = cuda_fail(ctx, ce, "Gram-Schmidt"); break; }
+      {
+        LaunchScope ls_(K_REFINE, 0.0, 0.0, s);
+        gmres_step_kernel<<<1, 32, 0, s>>>(nc, j, m, w.h, rtol, w.gm, w.gflags);
+      }
+      {
+        LaunchScope ls_(K_REFINE, 0.0, 16.0 * n * nc, s);
+        gmres_scale_kernel<<<grid_for(n * nc), 256, 0, s>>>(n, nc, V, ldV, j + 1, w.gm);
+      }
+      ce = cudaGetLastError();
+      // pinned slot j & 1 of 2 * kMaxW ints receives this step's flags
+      if (ce == cudaSuccess)
+        ce = cudaMemcpyAsync(w.gflags_host + (j & 1) * 2 * kMaxW, w.gflags, 2 * nc * sizeof(int),
+                             cudaMemcpyDeviceToHost, s);
+      if (ce == cudaSuccess) ce = cudaEventRecord(ev[j & 1], s);
+      if (ce == cudaSuccess && j >= 1) {
+        ce = cudaEventSynchronize(ev[(j - 1) & 1]);
+        if (ce == cudaSuccess) {
+          const int* fl = w.gflags_host + ((j - 1) & 1) * 2 * kMaxW;
+          bool any = false;
+          for (int q = 0; q < nc; ++q) any |= fl[2 * q] != 0;
+          if (!any) mask = 0;
         }
       }
+      if (ce != cudaSuccess) rc = cuda_fail(ctx, ce, "GMRES step");
     }
+    release();
+    if (rc) return rc;
     // y_q = H_q(1:k,1:k) \ g_q(1:k); x[:,q] += V_q(:,1:k) y_q
-    std::vector<double> y((size_t)hs * nc, 0.0);
-    for (int q = 0; q < nc; ++q) {
-      its[q] = k[q];
-      for (int i = k[q] - 1; i >= 0; --i) {
-        double acc = g[q][i];
-        for (int jj = i + 1; jj < k[q]; ++jj) acc -= H[q][(size_t)jj * (m + 1) + i] * y[(size_t)q * hs + jj];
-        const double d = H[q][(size_t)i * (m + 1) + i];
-        y[(size_t)q * hs + i] = d != 0 ? acc / d : 0.0;
-      }
+    {
+      LaunchScope ls_(K_REFINE, 0.0, 0.0, s);
+      gmres_finish_kernel<<<1, 32, 0, s>>>(nc, m, w.gm, w.gflags, w.h);
     }
-    GBLU_CK(ctx, cudaMemcpyAsync(w.h, y.data(), y.size() * sizeof(double), cudaMemcpyHostToDevice, s), "y");
+    GBLU_CK(ctx, cudaGetLastError(), "GMRES finish");
+    std::vector<int> fl(2 * nc);
+    GBLU_CK(ctx, cudaMemcpyAsync(fl.data(), w.gflags, 2 * nc * sizeof(int), cudaMemcpyDeviceToHost, s),
+            "reading GMRES steps");
+    GBLU_CK(ctx, cudaStreamSynchronize(s), "GMRES");
     for (int q = 0; q < nc; ++q) {
-      if (k[q] == 0) continue;
+      its[q] = fl[2 * q + 1];
+      if (its[q] == 0) continue;
       double* xq = w.x + (size_t)q * n;
-      GBLU_CK(ctx, gemv('N', n, k[q], Vq(q, 0), n, w.h + (size_t)q * hs, k[q], 1, 1.0, xq, n, 1.0, xq, n,
+      GBLU_CK(ctx, gemv('N', n, its[q], Vq(q, 0), n, w.h + (size_t)q * hs, its[q], 1, 1.0, xq, n, 1.0, xq, n,
                         w.partial, nullptr, s), "update");
     }
     return GBLU_OK;

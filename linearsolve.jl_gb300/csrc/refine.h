@@ -28,11 +28,26 @@ struct RefineWork {
   double* anorm_dev = nullptr;
   double amax = 0;          // max |A_ij| of the FP64 matrix (host copy)
   unsigned long long* growth_bits = nullptr;  // [0] max|A| (FP64 bits), [1] max|U| (FP32 bits)
+  // GMRES state on the device, per column: Hessenberg matrix, rotations,
+  // right-hand side g, solution y, and scalars (beta, 1/norm) / flags
+  double* gm = nullptr;     // W x kGmStride doubles
+  int* gflags = nullptr;    // W x 2 ints: stepping, basis size k
+  int* gflags_host = nullptr;  // pinned: 2 slots x 2 x 8 ints, flags read one step behind
 };
 
 constexpr int kSplit = 16;       // column chunks of the residual GEMV
 constexpr int kDotBlocks = 64;   // blocks of the deterministic dot products
 constexpr int kGmresRestart = 30;
+// per-column GMRES state: H ((m+1) x m), cs (m), sn (m), g (m+1), y (m+1),
+// beta, 1/norm of the newest basis vector
+constexpr int kGmH = 0;
+constexpr int kGmCs = kGmH + (kGmresRestart + 1) * kGmresRestart;
+constexpr int kGmSn = kGmCs + kGmresRestart;
+constexpr int kGmG = kGmSn + kGmresRestart;
+constexpr int kGmY = kGmG + kGmresRestart + 1;
+constexpr int kGmBeta = kGmY + kGmresRestart + 1;
+constexpr int kGmInv = kGmBeta + 1;
+constexpr int kGmStride = kGmInv + 1;
 
 size_t refine_bytes(int64_t n, int64_t W);
 void refine_carve(RefineWork& w, char* base, int64_t n, int64_t W);

@@ -39,6 +39,7 @@ struct Pending {
   gblu_request req;
   Clock::time_point t_submit;
   uint64_t seq;
+  bool waited = false;  // counted once in admission_waits
 };
 
 struct Resident {
@@ -49,6 +50,7 @@ struct Resident {
   bool busy = false;
   bool valid = false;  // holds a successful factorization
   uint64_t last_use = 0;
+  std::vector<double> a_small;  // small-lane key: its current matrix (host)
 };
 
 }  // namespace
@@ -58,6 +60,8 @@ struct gblu_server {
   gblu_serve_config cfg{};
   std::vector<gblu_ctx*> wctx;
   std::vector<std::thread> threads;
+  gblu_ctx* small_ctx = nullptr;  // the small-system lane's context and buffers
+  gblu::BatchLane* lane = nullptr;
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
   std::deque<Pending> queue;
@@ -85,16 +89,24 @@ uint64_t factor_bytes_estimate(gblu_server* s, gblu_ctx* c, int64_t n) {
 }
 
 // Evict least recently used idle factorizations until `need` more bytes fit.
-bool admit(gblu_server* s, uint64_t need) {
+// The evicted objects are handed back in `victims` and destroyed by the
+// caller after it released s->mu (destroying synchronises the owner's stream).
+bool admit(gblu_server* s, uint64_t need, std::vector<std::pair<gblu_ctx*, gblu_factor*>>& victims) {
   const uint64_t budget = s->cfg.hbm_budget_bytes;
   if (budget == 0) return true;
+  // would evicting every idle object be enough?  Otherwise evict nothing.
+  uint64_t idle = 0;
+  for (auto& kv : s->cache)
+    if (!kv.second.busy) idle += kv.second.bytes;
+  if (s->bytes_resident - std::min(s->bytes_resident, idle) + need > budget) return false;
   while (s->bytes_resident + need > budget) {
     auto victim = s->cache.end();
     for (auto it = s->cache.begin(); it != s->cache.end(); ++it)
-      if (!it->second.busy && (victim == s->cache.end() || it->second.last_use < victim->second.last_use))
+      if (!it->second.busy && it->second.bytes > 0 &&  // small-lane keys hold no HBM
+          (victim == s->cache.end() || it->second.last_use < victim->second.last_use))
         victim = it;
     if (victim == s->cache.end()) return false;  // everything resident is in use: wait
-    gblu_factor_destroy(victim->second.owner, victim->second.f);
+    if (victim->second.f) victims.emplace_back(victim->second.owner, victim->second.f);
     s->bytes_resident -= std::min(s->bytes_resident, victim->second.bytes);
     s->cache.erase(victim);
     s->stats.evictions++;
@@ -128,6 +140,7 @@ void worker(gblu_server* s, int wi) {
     Resident* res = nullptr;
     bool need_new = false;
     uint64_t need_bytes = 0;
+    std::vector<std::pair<gblu_ctx*, gblu_factor*>> victims;  // destroyed outside the lock
     {
       std::unique_lock<std::mutex> lk(s->mu);
       for (;;) {
@@ -139,18 +152,25 @@ void worker(gblu_server* s, int wi) {
           for (auto jt = s->queue.begin(); jt != it; ++jt)
             if (jt->req.key == it->req.key) { earlier_same_key = true; break; }
           if (earlier_same_key) continue;  // keep per-key order
+          if (s->cfg.small_n > 0 && it->req.n <= s->cfg.small_n) continue;  // the small lane's
           auto c = s->cache.find(it->req.key);
           if (c != s->cache.end()) key_busy = c->second.busy;
           if (key_busy) continue;
-          const bool has_obj = c != s->cache.end() && c->second.n == it->req.n;
+          const bool has_obj = c != s->cache.end() && c->second.f && c->second.n == it->req.n;
           if (it->req.A && !has_obj) {
             uint64_t nb = factor_bytes_estimate(s, ctx, it->req.n);
             if (c != s->cache.end() && !c->second.busy) {  // resize: free the old object first
-              gblu_factor_destroy(c->second.owner, c->second.f);
+              if (c->second.f) victims.emplace_back(c->second.owner, c->second.f);
               s->bytes_resident -= std::min(s->bytes_resident, c->second.bytes);
               s->cache.erase(c);
             }
-            if (!admit(s, nb)) continue;
+            if (!admit(s, nb, victims)) {
+              if (!it->waited) {
+                it->waited = true;
+                s->stats.admission_waits++;
+              }
+              continue;
+            }
             need_new = true;
             need_bytes = nb;
           } else {
@@ -187,9 +207,12 @@ void worker(gblu_server* s, int wi) {
           break;
         }
         if (s->stopping && s->queue.empty()) return;
+        if (!victims.empty()) break;  // release evicted objects before waiting
         s->cv_work.wait_for(lk, std::chrono::milliseconds(50));
       }
     }
+    for (auto& v : victims) gblu_factor_destroy(v.first, v.second);
+    if (batch.empty()) continue;
     const auto t_start = Clock::now();
     const Pending& head = batch[0];
     const int64_t n = head.req.n;
@@ -200,8 +223,9 @@ void worker(gblu_server* s, int wi) {
     if (need_new) {
       gblu_factor* f = nullptr;
       st = gblu_factor_create(ctx, n, n, s->cfg.precision, &f);
+      if (st == GBLU_OK) st = gblu_factor_set_solve(ctx, f, s->cfg.solve_mode);
       res->f = f;
-      if (st == GBLU_OK) res->owner = ctx;
+      if (f) res->owner = ctx;
     }
     if (st == GBLU_OK && head.req.A) {
       st = gblu_getrf(ctx, res->f, head.req.A, n, GBLU_HOST, &info);
@@ -253,6 +277,147 @@ void worker(gblu_server* s, int wi) {
   }
 }
 
+// The small-system lane: takes every queued request with n <= small_n whose
+// key is idle (per key, the requests up to its first one it cannot take, so a
+// key's requests keep their order), and factors + solves all of them in one
+// launch of the batched kernels.  A request bringing a matrix uses it (and it
+// becomes the key's matrix, copied to host memory); a solve-only request uses
+// the key's matrix.  Each system's arithmetic is its own (the batched kernels
+// give every system the same result whatever else is in the launch).
+void small_worker(gblu_server* s) {
+  gblu_ctx* ctx = s->small_ctx;
+  const int maxb = std::max(1, s->cfg.max_small_batch);
+  std::vector<Pending> batch;
+  std::vector<const double*> Ap, bp;
+  std::vector<double*> xp;
+  std::vector<int32_t> sizes, iters, sys_of;  // sys_of[j]: system of request j (-1: none)
+  std::vector<int64_t> info;
+  std::vector<std::pair<gblu_ctx*, gblu_factor*>> victims;
+  for (;;) {
+    batch.clear();
+    victims.clear();
+    {
+      std::unique_lock<std::mutex> lk(s->mu);
+      for (;;) {
+        if (s->stopping && s->queue.empty()) return;
+        std::vector<uint64_t> blocked;  // keys with an earlier request left in the queue
+        auto is_blocked = [&](uint64_t k) { return std::find(blocked.begin(), blocked.end(), k) != blocked.end(); };
+        for (auto it = s->queue.begin(); it != s->queue.end() && (int)batch.size() < maxb;) {
+          const uint64_t key = it->req.key;
+          if (is_blocked(key)) { ++it; continue; }
+          auto c = s->cache.find(key);
+          const bool small = it->req.n <= s->cfg.small_n;
+          const bool taken_before = std::any_of(batch.begin(), batch.end(),
+                                                [&](const Pending& p) { return p.req.key == key; });
+          if (!small || (c != s->cache.end() && c->second.busy && !taken_before)) {
+            blocked.push_back(key);
+            ++it;
+            continue;
+          }
+          if (!taken_before) {
+            if (c == s->cache.end()) {
+              c = s->cache.emplace(key, Resident{}).first;
+            } else if (c->second.f) {  // the key held a large factorization: release it
+              victims.emplace_back(c->second.owner, c->second.f);
+              s->bytes_resident -= std::min(s->bytes_resident, c->second.bytes);
+              c->second.f = nullptr;
+              c->second.bytes = 0;
+              c->second.valid = false;
+              c->second.n = 0;
+            }
+            c->second.busy = true;
+            c->second.last_use = ++s->use_clock;
+          }
+          batch.push_back(*it);
+          it = s->queue.erase(it);
+        }
+        if (!batch.empty()) {
+          s->in_flight += (int64_t)batch.size();
+          break;
+        }
+        if (!victims.empty()) break;
+        s->cv_work.wait_for(lk, std::chrono::milliseconds(50));
+      }
+    }
+    for (auto& v : victims) gblu_factor_destroy(v.first, v.second);
+    if (batch.empty()) continue;
+    const auto t_start = Clock::now();
+    // systems: each request's matrix is its own, or its key's latest one
+    const size_t k = batch.size();
+    Ap.clear(); bp.clear(); xp.clear(); sizes.clear();
+    sys_of.assign(k, -1);
+    {
+      std::lock_guard<std::mutex> lk(s->mu);  // the keys' host matrices
+      for (size_t j = 0; j < k; ++j) {
+        const gblu_request& r = batch[j].req;
+        const double* A = r.A;
+        if (!A) {
+          for (size_t i = j; i-- > 0;)  // an earlier request of this launch brought one
+            if (batch[i].req.key == r.key && batch[i].req.A) {
+              A = batch[i].req.n == r.n ? batch[i].req.A : nullptr;
+              goto found;
+            }
+          {
+            const Resident& res = s->cache[r.key];
+            if (res.valid && res.n == r.n && !res.a_small.empty()) A = res.a_small.data();
+          }
+        found:;
+        }
+        if (!A) continue;  // no matrix for this key: not factored
+        sys_of[j] = (int32_t)sizes.size();
+        sizes.push_back((int32_t)r.n);
+        Ap.push_back(A);
+        bp.push_back(r.b);
+        xp.push_back(r.x);
+      }
+    }
+    info.assign(sizes.size(), 0);
+    iters.assign(sizes.size(), 0);
+    int32_t st = sizes.empty() ? GBLU_OK
+                               : batch_lane_solve(ctx, s->lane, s->cfg.precision, (int)sizes.size(), sizes.data(),
+                                                  Ap.data(), bp.data(), xp.data(), info.data(), iters.data());
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      for (size_t j = 0; j < k; ++j) {
+        const gblu_request& r = batch[j].req;
+        Resident& res = s->cache[r.key];
+        const int sy = sys_of[j];
+        if (r.A && st == GBLU_OK && sy >= 0) {  // the key's matrix from now on
+          res.a_small.assign(r.A, r.A + (size_t)r.n * r.n);
+          res.n = r.n;
+          res.valid = info[sy] == 0;
+        }
+        gblu_refine_stats rs{};
+        rs.backward_error = -1;
+        rs.converged = 1;
+        int32_t rst = st;
+        int64_t rinfo = 0;
+        if (sy < 0) {
+          rst = GBLU_ENOTFACTORED;
+        } else if (st == GBLU_OK) {
+          rinfo = info[sy];
+          rs.iterations = std::max(0, iters[sy]);
+          rs.fell_back = iters[sy] < 0 ? 1 : 0;
+          if (rinfo != 0) rst = GBLU_EINVAL;  // singular matrix for this key
+        }
+        complete(s, batch[j], rst, rinfo, r.A ? 1 : 0, rs, t_start);
+        if (r.A && rst == GBLU_OK) s->stats.factorizations++;
+      }
+      for (size_t j = 0; j < k; ++j) {
+        Resident& res = s->cache[batch[j].req.key];
+        res.busy = false;
+        res.last_use = ++s->use_clock;
+      }
+      s->in_flight -= (int64_t)k;
+      s->stats.solves += (int64_t)k;
+      s->stats.small_launches += sizes.empty() ? 0 : 1;
+      s->stats.small_systems += (int64_t)sizes.size();
+    }
+    s->cv_done.notify_all();
+    s->cv_work.notify_all();
+  }
+}
+
 }  // namespace
 }  // namespace gblu
 
@@ -267,6 +432,9 @@ int32_t gblu_serve_config_default(gblu_serve_config* cfg) {
   cfg->refine_mode = GBLU_REFINE_IR;
   cfg->hbm_budget_bytes = 120ull << 30;
   cfg->max_rhs_batch = 8;
+  cfg->small_n = 256;
+  cfg->solve_mode = GBLU_SOLVE_FAST;
+  cfg->max_small_batch = 1024;
   return GBLU_OK;
 }
 
@@ -281,20 +449,38 @@ int32_t gblu_serve_create(gblu_ctx* ctx, const gblu_serve_config* cfg, gblu_serv
     return fail(ctx, GBLU_EINVAL, "gblu_serve_create: bad precision");
   if (c.refine_mode != GBLU_REFINE_IR && c.refine_mode != GBLU_REFINE_GMRES)
     return fail(ctx, GBLU_EINVAL, "gblu_serve_create: bad refine mode");
+  if (c.small_n < 0 || c.small_n > 256) return fail(ctx, GBLU_EINVAL, "gblu_serve_create: small_n in 0..256");
+  if (c.solve_mode != GBLU_SOLVE_EXACT && c.solve_mode != GBLU_SOLVE_FAST)
+    return fail(ctx, GBLU_EINVAL, "gblu_serve_create: bad solve mode");
+  if (c.small_n > 0 && c.max_small_batch < 1)
+    return fail(ctx, GBLU_EINVAL, "gblu_serve_create: max_small_batch < 1");
   gblu_server* s = new gblu_server();
   s->parent = ctx;
   s->cfg = c;
+  auto undo = [&]() {
+    for (auto* x : s->wctx) gblu_destroy(x);
+    if (s->small_ctx) gblu_destroy(s->small_ctx);
+    delete s;
+  };
   for (int i = 0; i < c.workers; ++i) {
     gblu_ctx* w = nullptr;
     int32_t st = gblu_create(&w, ctx->device, 0);
     if (st) {
-      for (auto* x : s->wctx) gblu_destroy(x);
-      delete s;
+      undo();
       return fail(ctx, st, "gblu_serve_create: worker context: %s", gblu_last_error(nullptr));
     }
     s->wctx.push_back(w);
   }
+  if (c.small_n > 0) {
+    int32_t st = gblu_create(&s->small_ctx, ctx->device, 0);
+    if (st == GBLU_OK && !(s->lane = batch_lane_create())) st = GBLU_ENOMEM;
+    if (st) {
+      undo();
+      return fail(ctx, st, "gblu_serve_create: small-system lane: %s", gblu_last_error(nullptr));
+    }
+  }
   for (int i = 0; i < c.workers; ++i) s->threads.emplace_back(worker, s, i);
+  if (c.small_n > 0) s->threads.emplace_back(small_worker, s);
   *out = s;
   return GBLU_OK;
 }
@@ -312,7 +498,7 @@ int32_t gblu_serve_submit(gblu_server* s, const gblu_request* r) {
     s->queue.push_back(p);
     s->stats.submitted++;
   }
-  s->cv_work.notify_one();
+  s->cv_work.notify_all();  // the small lane and the workers wait on the same condition
   return GBLU_OK;
 }
 
@@ -354,6 +540,10 @@ int32_t gblu_serve_destroy(gblu_server* s) {
     if (kv.second.f) gblu_factor_destroy(kv.second.owner, kv.second.f);
   s->cache.clear();
   for (auto* w : s->wctx) gblu_destroy(w);
+  if (s->small_ctx) {
+    batch_lane_destroy(s->small_ctx, s->lane);
+    gblu_destroy(s->small_ctx);
+  }
   delete s;
   return GBLU_OK;
 }

@@ -18,7 +18,8 @@ PRECISIONS = {"fp64": _lib.GBLU_FP64, "fp32": _lib.GBLU_FP32, "bf16": _lib.GBLU_
 
 class Server:
     def __init__(self, ctx, workers: int = 4, precision: str = "fp32", refine: str = "ir",
-                 hbm_budget_bytes: int = 120 << 30, max_rhs_batch: int = 8):
+                 hbm_budget_bytes: int = 120 << 30, max_rhs_batch: int = 8, small_n: int = 256,
+                 solve: str = "fast", max_small_batch: int = 1024):
         self.ctx, self.lib = ctx, ctx.lib
         cfg = _lib.ServeConfig()
         check(self.lib.gblu_serve_config_default(ctypes.byref(cfg)), None)
@@ -27,6 +28,9 @@ class Server:
         cfg.refine_mode = _lib.GBLU_REFINE_GMRES if refine == "gmres_ir" else _lib.GBLU_REFINE_IR
         cfg.hbm_budget_bytes = hbm_budget_bytes
         cfg.max_rhs_batch = max_rhs_batch
+        cfg.small_n = small_n
+        cfg.solve_mode = _lib.GBLU_SOLVE_FAST if solve == "fast" else _lib.GBLU_SOLVE_EXACT
+        cfg.max_small_batch = max_small_batch
         h = ctypes.c_void_p()
         check(self.lib.gblu_serve_create(ctx.handle, ctypes.byref(cfg), ctypes.byref(h)), ctx.handle)
         self.h = h

@@ -66,7 +66,9 @@ def test_serving_budget_evicts_and_reports(ctx, pkg):
     rng = np.random.default_rng(5)
     n = 256
     # a budget that holds about two FP32 factorizations of n = 256
-    srv = serving.Server(ctx, workers=2, precision="fp32", hbm_budget_bytes=3 * (1 << 20) + 1_500_000)
+    # (n = 256 would go to the small-system lane, which holds no factorizations)
+    srv = serving.Server(ctx, workers=2, precision="fp32", hbm_budget_bytes=3 * (1 << 20) + 1_500_000,
+                         small_n=0)
     A = [pkg.workloads.shifted(n, 1, seed=k)[0] for k in range(4)]
     for k in range(4):
         srv.submit(k, k, rng.standard_normal(n), A[k])
@@ -108,3 +110,92 @@ def test_serving_merges_rhs_on_one_key(ctx, pkg):
         assert np.linalg.norm(A @ sol[1 + i] - b, np.inf) <= 10 * n * 2.2e-16 * (
             np.abs(A).sum(1).max() * np.abs(sol[1 + i]).max() + np.abs(b).max())
     srv.close()
+
+
+def _serve_all(pkg, ctx, reqs, **kw):
+    """Submit everything at once (or, with one_by_one, each after the
+    previous completed); return completions by tag and the server stats."""
+    from importlib import import_module
+    serving = import_module(pkg.__name__ + ".serving")
+    one = kw.pop("one_by_one", False)
+    srv = serving.Server(ctx, **kw)
+    done = []
+    if one:
+        for i, r in enumerate(reqs):
+            srv.submit(i, r["key"], r["b"], r.get("A"))
+            got = []
+            while not got:
+                got = srv.poll(16, wait_ms=50)
+            done += got
+    else:
+        for i, r in enumerate(reqs):
+            srv.submit(i, r["key"], r["b"], r.get("A"))
+        while len(done) < len(reqs):
+            done += srv.poll(256, wait_ms=50)
+    st = srv.stats()
+    srv.close()
+    return {d["tag"]: d for d in done}, st
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_small_lane_batches_across_keys(ctx, oracle_mod, pkg, precision):
+    """Requests with n <= 256 of many keys are factored and solved together
+    (one launch of the batched kernels per group of queued requests); each
+    answer meets the bound and equals the answer of the request run alone."""
+    rng = np.random.default_rng(11)
+    nkeys = 40
+    sizes = rng.integers(8, 257, size=nkeys)
+    reqs = []
+    for k in range(nkeys):
+        A = pkg.workloads.shifted(int(sizes[k]), 1, seed=2000 + k)[0]
+        reqs.append({"key": k, "A": A, "b": rng.standard_normal(sizes[k]), "Aeff": A})
+    for _ in range(3 * nkeys):
+        k = int(rng.integers(nkeys))
+        reqs.append({"key": k, "A": None, "b": rng.standard_normal(sizes[k]), "Aeff": reqs[k]["A"]})
+    mixed, st = _serve_all(pkg, ctx, reqs, workers=2, precision=precision)
+    alone, st1 = _serve_all(pkg, ctx, reqs, workers=1, precision=precision, one_by_one=True)
+    assert st["small_systems"] == len(reqs)
+    assert st["small_launches"] < len(reqs) and st1["small_launches"] == len(reqs)
+    for i, r in enumerate(reqs):
+        assert mixed[i]["status"] == 0 and alone[i]["status"] == 0
+        n = len(r["b"])
+        assert oracle_mod.backward_error(r["Aeff"], mixed[i]["x"], r["b"]) <= 10 * n * EPS64
+        assert np.array_equal(mixed[i]["x"], alone[i]["x"]), i
+
+
+def test_small_lane_keeps_per_key_order(ctx, oracle_mod, pkg):
+    """A key's requests keep their order inside one launch: a solve after a
+    new matrix uses that matrix, a solve before it the previous one."""
+    rng = np.random.default_rng(12)
+    n = 100
+    A1 = pkg.workloads.shifted(n, 1, seed=1)[0]
+    A2 = pkg.workloads.shifted(n, 1, seed=2)[0]
+    b = [rng.standard_normal(n) for _ in range(4)]
+    reqs = [{"key": 5, "A": A1, "b": b[0]}, {"key": 5, "A": None, "b": b[1]},
+            {"key": 5, "A": A2, "b": b[2]}, {"key": 5, "A": None, "b": b[3]}]
+    done, _ = _serve_all(pkg, ctx, reqs, workers=1, precision="fp64")
+    for i, A in enumerate((A1, A1, A2, A2)):
+        assert done[i]["status"] == 0
+        assert oracle_mod.backward_error(A, done[i]["x"], b[i]) <= 10 * n * EPS64
+
+
+def test_small_lane_unknown_key_not_factored(ctx, pkg):
+    rng = np.random.default_rng(13)
+    done, _ = _serve_all(pkg, ctx, [{"key": 99, "A": None, "b": rng.standard_normal(50)}], workers=1,
+                         precision="fp64")
+    assert done[0]["status"] == 5  # GBLU_ENOTFACTORED
+
+
+def test_admission_waits_for_memory(ctx, pkg):
+    """A budget that holds one n = 700 FP32 factorization: two new matrices
+    at once, the second waits for the first to go idle, then evicts it."""
+    rng = np.random.default_rng(14)
+    n = 700
+    ld = 704
+    one = ld * n * 4 + ld * n * 8 + 64 * n * 8 + (1 << 20)
+    reqs = [{"key": k, "A": pkg.workloads.shifted(n, 1, seed=30 + k)[0], "b": rng.standard_normal(n)}
+            for k in range(3)]
+    done, st = _serve_all(pkg, ctx, reqs, workers=3, precision="fp32", hbm_budget_bytes=one + one // 2)
+    assert all(done[i]["status"] == 0 for i in range(3))
+    assert st["evictions"] >= 2 and st["admission_waits"] >= 1
+    assert st["resident_bytes"] <= one + one // 2
