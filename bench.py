@@ -490,6 +490,11 @@ def run_gpu(args, rank, world, local):
     if fast is not None:
         line["getrs_fast"] = fast
 
+    if world > 1:  # the batched workload sharded over the ranks' GPUs (every rank takes part)
+        sharded = run_batched_sharded(pkg, cu, ctx, args, dist, rank, world)
+        if rank == 0:
+            line["batched_sharded"] = sharded
+
     if args.suite == "auto":
         args.suite = ",".join(SUITES) if world == 1 else ""
     if args.suite and rank == 0:
@@ -654,8 +659,7 @@ def run_mixed_suite(pkg, cu, ctx, args):
                 ("bf16_ir_fast_solve", "bf16", "fast"), ("fp16_ir_fast_solve", "fp16", "fast"))
     for label, prec, solve in variants:
         f = ctx.factor(n, n, prec)
-        if solve != "exact":
-            f.set_solve(solve)  # the low-precision correction solve
+        f.set_solve(solve)  # the low-precision correction solve (mixed factors default to fast)
         # the FP64 solve set takes seconds: one warm-up and one timed run
         ms, st, kms = _timed_solve(pkg, cu, ctx, f, dA, dB0, dB, prec, 1 if prec == "fp64" else 3,
                                    warm=1 if prec == "fp64" else 3)
@@ -671,6 +675,22 @@ def run_mixed_suite(pkg, cu, ctx, args):
         out["speedup_%s_vs_fp64" % label] = out[label]["solves_per_s"] / out["fp64_plain"]["solves_per_s"]
     out["bound"] = 10 * n * EPS64
     dA.free(); dB0.free(); dB.free()
+    if not args.no_cpu:
+        # the reference's CPU path on this host: LAPACK dgetrf + dgetrs (4 RHS), one
+        # warm-up and two timed runs (a bounded sample: seconds per run at this n)
+        import oracle
+        oracle.lapack_solve(A, B)
+        ts = []
+        for _ in range(2):
+            t0 = time.perf_counter()
+            Xc, _ = oracle.lapack_solve(A, B)
+            ts.append(time.perf_counter() - t0)
+        cms = 1e3 * statistics.median(ts)
+        out["cpu_baseline"] = {"ms_per_solve_set": cms, "solves_per_s": nrhs / (cms / 1e3), "kind": "port",
+                               "impl": "scipy.linalg.lapack dgetrf + dgetrs (OpenBLAS)", "cores": os.cpu_count(),
+                               "cpu_model": cpu_model(), "runs": len(ts),
+                               "backward_error": max(pkg_backward_error(A, np.asarray(Xc)[:, j], B[:, j])
+                                                     for j in range(nrhs))}
     return out
 
 
@@ -687,15 +707,16 @@ def run_mixed_hard_suite(pkg, cu, ctx, args):
     out = {"n": n, "nrhs": nrhs, "A": "Q1 diag(s) Q2^T, s log-spaced 1..1e6", "input_generation_s": gen_s}
     X64 = None
     variants = (("fp64_plain", "fp64", "ir", {}),
-                ("fp32_gmres_ir", "fp32", "gmres_ir", {}),
-                ("fp32_gmres_ir_inner_tol_1e-6", "fp32", "gmres_ir", {"gmres_tol": 1e-6}),
-                ("fp32_ir", "fp32", "ir", {}),
-                ("fp32_gmres_ir_fast_solve", "fp32", "gmres_ir", {"solve": "fast"}))
+                ("fp32_gmres_ir", "fp32", "gmres_ir", {"solve": "exact"}),
+                ("fp32_gmres_ir_inner_tol_1e-6", "fp32", "gmres_ir", {"gmres_tol": 1e-6, "solve": "exact"}),
+                ("fp32_ir", "fp32", "ir", {"solve": "exact"}),
+                ("fp32_gmres_ir_fast_solve", "fp32", "gmres_ir", {"solve": "fast"}),
+                ("fp32_gmres_ir_fast_solve_inner_tol_1e-6", "fp32", "gmres_ir", {"gmres_tol": 1e-6, "solve": "fast"}),
+                ("fp32_ir_fast_solve", "fp32", "ir", {"solve": "fast"}))
     for label, prec, mode, kw in variants:
         f = ctx.factor(n, n, prec)
         kw = dict(kw)
-        if kw.pop("solve", "exact") == "fast":
-            f.set_solve("fast")  # the low-precision preconditioner solve
+        f.set_solve(kw.pop("solve", "exact"))  # the low-precision preconditioner solve
         ms, st, kms = _timed_solve(pkg, cu, ctx, f, dA, dB0, dB, prec, 1 if prec == "fp64" else 2,
                                    mode=mode, warm=1 if prec == "fp64" else 3, **kw)
         X = dB.to_host()
@@ -783,6 +804,67 @@ def run_batched_suite(pkg, cu, ctx, args):
     return out
 
 
+def run_batched_sharded(pkg, cu, ctx, args, dist, rank, world):
+    """The 20,000 uneven systems split over the N ranks (greedy balance of
+    sum n^3, no exchange on the data path): each rank solves its shard with
+    the batched kernels of its own GPU; timing is the max over ranks of the
+    event-timed solves (strong scaling: the total work is fixed); the shards'
+    solutions are gathered on rank 0 afterwards and sampled for accuracy."""
+    import torch.distributed as td
+    from importlib import import_module
+    sh = import_module(pkg.__name__ + ".sharding")
+    sizes, A, b, _ = pkg.workloads.batch(args.batch_count, seed=0)
+    parts = sh.shard_systems(sizes, world)
+    idx = parts[rank]
+    ss, As, bs = sh.pack(sizes, A, b, idx)
+    bt = pkg.Batch(ctx, ss, "fp64")
+    dA = pkg.DeviceMatrix.from_host(As.reshape(-1, 1))
+    dB0 = pkg.DeviceMatrix.from_host(bs.reshape(-1, 1))
+    dB = pkg.DeviceMatrix(len(bs), 1)
+
+    def once():
+        dB.copy_from(dB0, ctx.stream)
+        bt.solve(dA, dB)
+
+    once()
+    reps = 3
+    dist.barrier()
+    cu.device_synchronize()
+    e0, e1 = cu.Event(), cu.Event()
+    e0.record(ctx.stream)
+    for _ in range(reps):
+        once()
+    e1.record(ctx.stream)
+    e1.synchronize()
+    ms = dist.max(e0.elapsed_ms(e1) / reps)
+    x_sub = dB.to_host()[:, 0]
+    gathered = [None] * world
+    td.all_gather_object(gathered, (idx, x_sub))
+    bt.close()
+    dA.free(); dB0.free(); dB.free()
+    if rank != 0:
+        return None
+    a_off, b_off = pkg.workloads.offsets(sizes)
+    x = np.empty(len(b))
+    for ridx, rx in gathered:
+        pos = 0
+        for i in ridx:
+            n = int(sizes[i])
+            x[b_off[i]:b_off[i] + n] = rx[pos:pos + n]
+            pos += n
+    worst = 0.0
+    rng = np.random.default_rng(1)
+    for i in rng.choice(len(sizes), size=min(200, len(sizes)), replace=False):
+        n = int(sizes[i])
+        Ai = A[a_off[i]:a_off[i] + n * n].reshape(n, n, order="F")
+        worst = max(worst, pkg_backward_error(Ai, x[b_off[i]:b_off[i] + n], b[b_off[i]:b_off[i] + n]) / n)
+    loads = [float((sizes[p].astype(float) ** 3).sum()) for p in parts]
+    return {"count": int(len(sizes)), "ranks": world, "scaling": "strong (fixed 20,000 systems split over the ranks)",
+            "ms_per_batch": ms, "solves_per_s": len(sizes) / (ms / 1e3), "precision": "fp64",
+            "load_balance_max_over_min": max(loads) / max(min(loads), 1.0),
+            "max_backward_error_over_n_eps": worst / EPS64}
+
+
 def pkg_lu_flops(n):
     return 2.0 * n ** 3 / 3.0 + 2.0 * n * n
 
@@ -810,36 +892,59 @@ def getrf_phase_roofline(kms, n, prec, args):
             "frac": tf / peak if peak else None}
 
 
-def run_serving_suite(pkg, cu, ctx, args):
-    """Poisson stream: n log-uniform in [64, 4096], 30% new A (G + 4 sqrt(n) I),
-    70% new b on a resident factorization; mixed FP32 factors with FP64
-    refinement; budget 120 GB; p50/p99 latency at swept rates."""
-    from importlib import import_module
-    serving = import_module(pkg.__name__ + ".serving")
-    rng = np.random.default_rng(0)
-    nkeys = 24
+def serving_workload(pkg, nkeys: int, nreq: int, seed: int = 0):
+    """The served stream's requests: every key gets its own size, n
+    log-uniform in [64, 4096] (so the stream holds hundreds of distinct
+    sizes), and starts with its matrix; then 30% new A (A = G + 4 sqrt(n) I,
+    G iid N(0,1)) and 70% a new b against the key's current matrix.  The
+    Gaussian parts are n x n windows at random offsets of one seeded
+    8192 x 8192 pool, so building a thousand requests is a copy."""
+    rng = np.random.default_rng(seed)
     sizes = np.exp(rng.uniform(np.log(64), np.log(4096), size=nkeys)).astype(int)
-    pool = {k: [pkg.workloads.shifted(int(sizes[k]), 1, seed=100 * k + v)[0] for v in range(2)]
-            for k in range(nkeys)}
-    nreq = args.serve_requests
-    reqs, eff = [], []
-    cur = {k: 0 for k in range(nkeys)}
-    for k in range(nkeys):  # every key starts with its matrix
-        reqs.append({"key": k, "A": pool[k][0], "b": rng.standard_normal(sizes[k])})
-        eff.append(pool[k][0])
+    pool = rng.standard_normal((8192, 8192))
+
+    def matrix(n):
+        r0, c0 = (int(v) for v in rng.integers(0, 8192 - n + 1, size=2))
+        A = np.asfortranarray(pool[r0:r0 + n, c0:c0 + n])
+        A[np.diag_indices(n)] += 4.0 * np.sqrt(n)
+        return A
+
+    cur = {}
+    reqs = []
+    for k in range(nkeys):
+        cur[k] = matrix(int(sizes[k]))
+        reqs.append({"key": k, "A": cur[k], "b": rng.standard_normal(sizes[k]), "Aeff": cur[k]})
     for _ in range(nreq):
         k = int(rng.integers(nkeys))
         if rng.random() < 0.3:
-            cur[k] ^= 1
-            reqs.append({"key": k, "A": pool[k][cur[k]], "b": rng.standard_normal(sizes[k])})
+            cur[k] = matrix(int(sizes[k]))
+            reqs.append({"key": k, "A": cur[k], "b": rng.standard_normal(sizes[k]), "Aeff": cur[k]})
         else:
-            reqs.append({"key": k, "A": None, "b": rng.standard_normal(sizes[k])})
-        eff.append(pool[k][cur[k]])
-    out = {"keys": nkeys, "requests": len(reqs), "n_range": [int(sizes.min()), int(sizes.max())],
-           "new_A_fraction": 0.3, "budget_gb": 120, "precision": "fp32 factors + FP64 IR", "rates": []}
-    for rate in args.serve_rates:
-        srv = serving.Server(ctx, workers=4, precision="fp32", hbm_budget_bytes=120 << 30)
-        done, wall = serving.run_stream(srv, reqs, rate_hz=rate, seed=int(rate))
+            reqs.append({"key": k, "A": None, "b": rng.standard_normal(sizes[k]), "Aeff": cur[k]})
+    del pool
+    return sizes, reqs
+
+
+def run_serving_suite(pkg, cu, ctx, args):
+    """Poisson stream: n log-uniform in [64, 4096], one size per key, 30% new
+    A, 70% new b on a resident factorization; mixed FP32 factors with FP64
+    refinement (fast inner solve), systems with n <= 256 batched across keys
+    through the batched kernels; budget 120 GB at the swept rates, and one
+    rate with a budget small enough that admission waits and evictions
+    happen (a solve on an evicted key is sent again with its matrix)."""
+    from importlib import import_module
+    serving = import_module(pkg.__name__ + ".serving")
+    nkeys = args.serve_keys
+    sizes, reqs = serving_workload(pkg, nkeys, args.serve_requests, seed=0)
+    out = {"keys": nkeys, "distinct_sizes": int(len(np.unique(sizes))), "requests": len(reqs),
+           "n_range": [int(sizes.min()), int(sizes.max())], "new_A_fraction": 0.3,
+           "precision": "fp32 factors + FP64 IR (fast inner solve); n <= 256 on the batched lane",
+           "target": "p99 <= 35 ms at 400 Hz, backward error <= 10 n eps64", "rates": []}
+    runs = [(r, 120 << 30) for r in args.serve_rates] + [(400.0, args.serve_small_budget_gb << 30)]
+    for rate, budget in runs:
+        srv = serving.Server(ctx, workers=4, precision="fp32", hbm_budget_bytes=budget)
+        small = budget < (120 << 30)
+        done, wall = serving.run_stream(srv, reqs, rate_hz=rate, seed=int(rate), resubmit_missing=small)
         st = srv.stats()
         srv.close()
         summ = serving.latency_summary(done, wall)
@@ -848,9 +953,12 @@ def run_serving_suite(pkg, cu, ctx, args):
             if d["status"] == 0 and d["tag"] % 7 == 0:
                 i = d["tag"]
                 n = len(reqs[i]["b"])
-                worst = max(worst, pkg_backward_error(eff[i], d["x"], reqs[i]["b"]) / (n * EPS64))
-        summ.update({"offered_rate_hz": rate, "max_backward_error_over_n_eps": worst,
-                     "merged_solves": st["merged_solves"], "factorizations": st["factorizations"]})
+                worst = max(worst, pkg_backward_error(reqs[i]["Aeff"], d["x"], reqs[i]["b"]) / (n * EPS64))
+        summ.update({"offered_rate_hz": rate, "budget_gb": budget / 2 ** 30,
+                     "max_backward_error_over_n_eps": worst, "merged_solves": st["merged_solves"],
+                     "factorizations": st["factorizations"], "evictions": st["evictions"],
+                     "admission_waits": st["admission_waits"], "small_launches": st["small_launches"],
+                     "small_systems": st["small_systems"]})
         out["rates"].append(summ)
     return out
 
@@ -943,6 +1051,8 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=1000)
     ap.add_argument("--mixed-n", type=int, default=16384)
     ap.add_argument("--serve-rates", type=float, nargs="*", default=[100.0, 400.0, 0.0])
+    ap.add_argument("--serve-keys", type=int, default=300)
+    ap.add_argument("--serve-small-budget-gb", type=int, default=4)
     ap.add_argument("--kernel-case", choices=KERNEL_CASES, default=None,
                     help="run one small case of a kernel group once (for ncu) and exit")
     args = ap.parse_args()

@@ -122,9 +122,10 @@ int32_t gblu_getrf(gblu_ctx* ctx, gblu_factor* f, const double* A, int64_t lda,
  *   and U inverted once after each getrf and applied as matrix-vector
  *   products, and independent partial sums elsewhere; backward-error accurate
  *   (not bit-identical), several times shorter critical path.  For a mixed
- *   factor it selects the low-precision solve inside refinement; the FP64
- *   fallback solve stays exact.  Allocates n x 128 elements of the factor's
- *   precision on first use. */
+ *   factor it selects the low-precision solve inside refinement (the
+ *   default for mixed factors: refinement makes either FP64-accurate); the
+ *   FP64 fallback solve stays exact.  An FP64 factor allocates n x 128
+ *   doubles on its first switch to GBLU_SOLVE_FAST. */
 #define GBLU_SOLVE_EXACT 0
 #define GBLU_SOLVE_FAST 1
 int32_t gblu_factor_set_solve(gblu_ctx* ctx, gblu_factor* f, int32_t mode);
@@ -353,9 +354,11 @@ void gblu_sgetrs_(const char* trans, const int64_t* n, const int64_t* nrhs,
 /* ---- allocation-free solve -------------------------------------------------
  * No counterpart in the reference.  For callers that must not allocate device
  * memory: per-step solver loops (e.g. Newton iterations inside an ODE
- * integrator) where cudaMalloc/cudaFree would synchronise the device, threads
- * running while a global-mode stream capture is open elsewhere (cudaMalloc is
- * an error then), and hosts that committed all device memory to a budget.
+ * integrator) where cudaMalloc/cudaFree would synchronise the device, and
+ * hosts that committed all device memory to a budget.  (It is meant for a
+ * non-blocking caller stream; with stream NULL it runs on the legacy default
+ * stream, and it reads one error word back with a synchronising copy, so it
+ * is not meant for use while a global-mode stream capture is open.)
  * Solves op(A) X = B in place with factors dLU (lda) and 1-based int64 pivots
  * d_ipiv from getrf, all three in device memory, on `stream` (NULL: the
  * default stream); returns when the solve has finished.  It allocates
@@ -365,7 +368,9 @@ void gblu_sgetrs_(const char* trans, const int64_t* n, const int64_t* nrhs,
  * call on a device looks up that array's address; make that call before any
  * stream capture.  All calls share the one array, so calls that overlap on
  * the GPU (different streams or threads at once) race; serialise them.
- * Errors are reported through gblu_last_error(NULL). */
+ * Errors are reported through gblu_last_error(NULL).  An invalid pivot is
+ * detected on the device after the solve was queued, so after a non-OK
+ * return the contents of dB are unspecified. */
 int32_t gblu_dgetrs_noalloc(char trans, int64_t n, int64_t nrhs, const double* dLU, int64_t lda,
                             const int64_t* d_ipiv, double* dB, int64_t ldb, void* stream);
 

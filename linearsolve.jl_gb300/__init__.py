@@ -15,7 +15,7 @@ The directory name is not a Python identifier; load it as a package with
 ``__graft_entry__.load_package()`` (it registers it as ``linearsolve_gb300``).
 """
 from ._lib import GBLUError, load as load_library  # noqa: F401
-from .device import Context, Factorization, default_context, dgetrf, dgetrs  # noqa: F401
+from .device import Batch, Context, Factorization, default_context, dgetrf, dgetrs  # noqa: F401
 from .linear import (  # noqa: F401
     DefaultAlgorithmChoice, DefaultLinearSolver, GB300LUFactorization, GB300MixedLUFactorization,
     GB300RFLUFactorization, LinearAliasSpecifier, RFLUCacheval, LinearCache, LinearProblem, LinearSolution, OperatorAssumptions,

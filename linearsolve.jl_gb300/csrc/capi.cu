@@ -311,6 +311,7 @@ int32_t gblu_factor_create(gblu_ctx* ctx, int64_t m, int64_t n, int32_t precisio
       tc_bytes = align256(tc_work_bytes(n, n / 2 + 64, n / 2 + 64));
       bytes += tc_bytes;
     }
+    if (m == n && n > 0) bytes += align256(getrs_inverse_bytes(n, sizeof(float)));
   }
   int32_t st = ctx_alloc(ctx, bytes, &f->arena);
   if (st) {
@@ -334,6 +335,15 @@ int32_t gblu_factor_create(gblu_ctx* ctx, int64_t m, int64_t n, int32_t precisio
       f->rf32.tc_work = c;
       f->rf32.tc_work_bytes = tc_bytes;
       c += tc_bytes;
+    }
+    // the low-precision solve of a mixed factor is refinement's correction
+    // solve: fast (inverted diagonal blocks) by default
+    if (m == n && n > 0) {
+      f->inv_bytes = getrs_inverse_bytes(n, sizeof(float));
+      f->inv_arena = c;
+      f->rs32.fast = true;
+      f->rs32.inv = reinterpret_cast<float*>(c);
+      c += align256(f->inv_bytes);
     }
   }
   cudaError_t e = cudaMemsetAsync(f->arena, 0, bytes, ctx->stream);
@@ -359,7 +369,7 @@ int32_t gblu_factor_destroy(gblu_ctx* ctx, gblu_factor* f) {
   if (f->fb_arena) ctx_free(ctx, f->fb_arena, f->fb_bytes);
   if (f->a_keep) ctx_free(ctx, f->a_keep, std::max<size_t>((size_t)f->ld * f->n * sizeof(double), 256));
   if (f->chk_arena) ctx_free(ctx, f->chk_arena, f->chk_bytes);
-  if (f->inv_arena) ctx_free(ctx, f->inv_arena, f->inv_bytes);
+  if (f->inv_arena && f->inv_owned) ctx_free(ctx, f->inv_arena, f->inv_bytes);
   if (f->refine.gflags_host) cudaFreeHost(f->refine.gflags_host);
   delete f;
   return GBLU_OK;
@@ -377,6 +387,7 @@ int32_t gblu_factor_set_solve(gblu_ctx* ctx, gblu_factor* f, int32_t mode) {
     int32_t st = ctx_alloc(ctx, bytes, &f->inv_arena);
     if (st) return st;
     f->inv_bytes = bytes;
+    f->inv_owned = true;
     f->inv_valid = false;
   }
   if (f->precision == GBLU_FP64) {

@@ -107,6 +107,14 @@ size_t getrf_scratch_bytes(int64_t m, int64_t n, int elem_size, int panel_width,
 template <typename T>
 void getrf_carve(GetrfPlan<T>& p, void* base, size_t bytes, int device);
 
+// Block-row height (and tile width) of the getrs sweeps, and the per-block-row
+// flag words they use for an n-row solve (callers that lay out getrs scratch
+// themselves size it from these).
+constexpr int kGetrsTile = 64;
+constexpr size_t getrs_flag_bytes(int64_t n) {
+  return 2 * (size_t)((n + kGetrsTile - 1) / kGetrsTile) * sizeof(int32_t);
+}
+
 template <typename T>
 struct GetrsPlan {
   int64_t n = 0, lda = 0;

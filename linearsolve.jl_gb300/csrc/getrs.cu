@@ -24,7 +24,7 @@
 
 namespace gblu {
 
-constexpr int kTS = 64;  // block-row height == tile width
+constexpr int kTS = kGetrsTile;  // block-row height == tile width
 
 // Wait until flags[j] != 0; returns false on timeout/abort (all threads).
 __device__ __forceinline__ bool wait_flag(const int32_t* flags, int j, DevScratch* scr) {

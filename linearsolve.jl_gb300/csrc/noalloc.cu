@@ -5,8 +5,6 @@
 //    inside an ODE integrator are the typical LinearSolve.jl caller): a
 //    cudaMalloc/cudaFree there synchronises the whole device and stalls the
 //    loop, and such callers are held to zero-allocation budgets;
-//  * a thread that runs while another thread has a stream capture open in
-//    global mode, where cudaMalloc is an error;
 //  * a host that has committed all device memory to a fixed budget up front.
 // They already own the factors, pivots and right-hand sides in device memory
 // and need the solve to touch no allocator at all.
@@ -29,12 +27,18 @@ namespace gblu {
 namespace {
 
 constexpr int64_t kNoAllocMaxN = 16384;      // largest n accepted
-constexpr int64_t kNoAllocCols = 8;          // right-hand sides per pass
-constexpr int64_t kNoAllocBlk = 64;          // block-row height of the sweeps
+constexpr int64_t kNoAllocCols = 8;          // right-hand sides per pass (getrs_launch's chunk)
 constexpr size_t kOffFlags = 256;
-constexpr size_t kOffPerm = kOffFlags + 2 * ((kNoAllocMaxN + kNoAllocBlk - 1) / kNoAllocBlk) * 4;
+constexpr size_t kOffPerm = kOffFlags + getrs_flag_bytes(kNoAllocMaxN);
 constexpr size_t kOffWork = (kOffPerm + kNoAllocMaxN * 4 + 255) & ~size_t(255);
 constexpr size_t kScratchBytes = kOffWork + kNoAllocMaxN * kNoAllocCols * sizeof(double);
+// the carve below must hold what the sweeps use: the error / ticket words,
+// the block-row flags of kGetrsTile-row blocks, the permutation, and one
+// n x kNoAllocCols block of intermediate values
+static_assert(sizeof(DevScratch) <= kOffFlags, "scratch words overlap the flags");
+static_assert(kOffPerm - kOffFlags >= getrs_flag_bytes(kNoAllocMaxN), "flag area too small");
+static_assert(kScratchBytes - kOffWork >= (size_t)kNoAllocMaxN * kNoAllocCols * sizeof(double),
+              "intermediate block too small");
 
 // ~1.1 MB on every device that loads the library, for the life of the process.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];

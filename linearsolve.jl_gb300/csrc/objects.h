@@ -62,6 +62,7 @@ struct gblu_factor {
   // fast getrs: inverted diagonal blocks of the factors (rs64 or rs32 .inv)
   void* inv_arena = nullptr;
   uint64_t inv_bytes = 0;
+  bool inv_owned = false;  // allocated on its own (else a view into the factor arena)
   bool inv_valid = false;  // inverses belong to the current factors
   // the factorization's launch sequence, captured on its second run and
   // replayed from then on (it depends only on the factor's shape)

@@ -51,33 +51,56 @@ __device__ __forceinline__ void block_max_into(double v, unsigned long long* p) 
 }
 
 // One pass over the FP64 matrix before the low-precision getrf: B = float(A),
-// P[s][i] = sum of |A_ij| over the columns j of chunk s (j ascending; the
-// chunks of gemv_n_partial_kernel, so ||A||_inf is reduced by
-// gemv_reduce_kernel exactly as the residual norms are), and max |A_ij| into
-// *amax.  Grid (rows / 256, kSplit); consecutive threads read consecutive
-// rows of a column.
+// P[s][i] = sum of |A_ij| over the columns j of chunk s (kPrepChunks column
+// chunks, j ascending), and max |A_ij| into *amax.  A CTA covers 1024
+// consecutive rows (4 per thread, 8 KB of a column per step) of one chunk,
+// so every column step is one long contiguous read; prepare_reduce_kernel
+// adds the chunks in index order.
+constexpr int kPrepChunks = 64;
+constexpr int kPrepRows = 1024;
+
 __global__ void __launch_bounds__(256)
 prepare_kernel(int64_t n, const double* __restrict__ A, int64_t lda, float* __restrict__ B, int64_t ldb,
                double* __restrict__ P, unsigned long long* __restrict__ amax) {
   const int s = blockIdx.y;
-  const int64_t cs = (n + kSplit - 1) / kSplit;
+  const int64_t cs = (n + kPrepChunks - 1) / kPrepChunks;
   const int64_t j0 = s * cs, j1 = min(n, j0 + cs);
-  const int64_t i = (int64_t)blockIdx.x * 256 + threadIdx.x;
-  double acc = 0.0, mx = 0.0;
-  if (i < n) {
-    const double* a = A + i;
-    float* b = B + i;
-#pragma unroll 4
-    for (int64_t j = j0; j < j1; ++j) {
-      const double v = a[j * lda];
-      b[j * ldb] = (float)v;
-      const double av = fabs(v);
-      acc += av;
+  const int64_t i0 = (int64_t)blockIdx.x * kPrepRows + threadIdx.x;
+  double acc[4] = {0.0, 0.0, 0.0, 0.0}, mx = 0.0;
+  bool ok[4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r) ok[r] = i0 + 256 * r < n;
+#pragma unroll 2
+  for (int64_t j = j0; j < j1; ++j) {
+    const double* a = A + i0 + j * lda;
+    float* b = B + i0 + j * ldb;
+    double v[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) v[r] = ok[r] ? a[256 * r] : 0.0;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      if (ok[r]) b[256 * r] = (float)v[r];
+      const double av = fabs(v[r]);
+      acc[r] += av;
       mx = (av > mx || isnan(av)) ? av : mx;
     }
-    P[(size_t)s * n + i] = acc;
   }
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+    if (ok[r]) P[(size_t)s * n + i0 + 256 * r] = acc[r];
   block_max_into(mx, amax);
+}
+
+// ||A||_inf = max_i sum_s P[s][i] (chunks added in index order) into *anorm.
+__global__ void __launch_bounds__(256)
+prepare_reduce_kernel(int64_t n, const double* __restrict__ P, unsigned long long* __restrict__ anorm) {
+  double mx = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double sum = 0.0;
+    for (int s = 0; s < kPrepChunks; ++s) sum += P[(size_t)s * n + i];
+    mx = (sum > mx || isnan(sum)) ? sum : mx;
+  }
+  block_max_into(mx, anorm);
 }
 
 // max |U_ij| over the upper triangle of the n x n FP32 factors: one warp per
@@ -515,15 +538,14 @@ cudaError_t refine_prepare(RefineWork& w, int64_t n, const double* A, int64_t ld
   // ||A||_inf = max_i sum_j |A[i,j]| from the row sums
   {
     LaunchScope ls_(K_REFINE, (double)n * n, 12.0 * n * n, s);
-    dim3 grid((unsigned)((n + 255) / 256), kSplit);
+    dim3 grid((unsigned)((n + kPrepRows - 1) / kPrepRows), kPrepChunks);
     prepare_kernel<<<grid, 256, 0, s>>>(n, A, lda, A32, ld32, w.partial, w.growth_bits);
   }
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   {
-    LaunchScope ls_(K_REFINE, 0.0, 8.0 * kSplit * n, s);
-    gemv_reduce_kernel<<<grid_for(n), 256, 0, s>>>(n, 1, 1, w.partial, 1.0, nullptr, 1, 0.0, w.w, n,
-                                                   w.colmax);
+    LaunchScope ls_(K_REFINE, 0.0, 8.0 * kPrepChunks * n, s);
+    prepare_reduce_kernel<<<grid_for(n), 256, 0, s>>>(n, w.partial, w.colmax);
   }
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;

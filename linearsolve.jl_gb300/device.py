@@ -241,6 +241,52 @@ class Factorization:
             pass
 
 
+class Batch:
+    """A gblu_batch: `len(sizes)` independent square systems (n_i <= 256)
+    packed back to back, solved by one graph launch (gblu_batch_*)."""
+
+    def __init__(self, ctx: Context, sizes, precision: str = "fp64"):
+        if precision not in ("fp64", "fp32"):
+            raise ValueError("batched precision must be 'fp64' or 'fp32'")
+        self.ctx, self.lib = ctx, ctx.lib
+        self.sizes = np.ascontiguousarray(sizes, dtype=np.int64)
+        h = ctypes.c_void_p()
+        check(self.lib.gblu_batch_create(ctx.handle, len(self.sizes), self.sizes.ctypes.data,
+                                         PRECISIONS[precision], ctypes.byref(h)), ctx.handle)
+        self.handle = h
+        self.info = np.zeros(len(self.sizes), dtype=np.int64)
+
+    def solve(self, A, b):
+        """Host arrays: A packed column-major systems, b packed right-hand
+        sides; returns the packed solutions (new array).  DeviceMatrix
+        arguments: solved in place of b."""
+        if isinstance(A, DeviceMatrix):
+            check(self.lib.gblu_batch_solve(self.ctx.handle, self.handle, A.ptr, b.ptr, _lib.GBLU_DEVICE,
+                                            self.info.ctypes.data), self.ctx.handle)
+            return b
+        A = np.ascontiguousarray(A, dtype=np.float64)
+        x = np.array(b, dtype=np.float64, copy=True)
+        check(self.lib.gblu_batch_solve(self.ctx.handle, self.handle, A.ctypes.data, x.ctypes.data,
+                                        _lib.GBLU_HOST, self.info.ctypes.data), self.ctx.handle)
+        return x
+
+    def iterations(self) -> np.ndarray:
+        its = np.zeros(len(self.sizes), dtype=np.int32)
+        check(self.lib.gblu_batch_iterations(self.ctx.handle, self.handle, its.ctypes.data), self.ctx.handle)
+        return its
+
+    def close(self) -> None:
+        if getattr(self, "handle", None) and self.ctx.handle:
+            self.lib.gblu_batch_destroy(self.ctx.handle, self.handle)
+        self.handle = None
+
+    def __del__(self):  # pragma: no cover
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 # -- LAPACK-shaped convenience wrappers (host buffers, default context) -------
 
 def dgetrf(A: np.ndarray):

@@ -181,8 +181,8 @@ class GB300MixedLUFactorization(AbstractDenseFactorization):
               (None: 1 / u of the factorization's arithmetic)
     residualsafety: the a-posteriori residual check of the reference
               (src/factorization.jl:127-156), run on the device.
-    solve:    the low-precision correction solve, "exact" or "fast" (see
-              GB300LUFactorization); refinement makes either FP64-accurate.
+    solve:    the low-precision correction solve, "fast" (default) or "exact"
+              (see GB300LUFactorization); refinement makes either FP64-accurate.
 
     Unlike the reference's CUDAOffload32MixedLUFactorization
     (ext/LinearSolveCUDAExt.jl:211-242) the result is FP64-accurate."""
@@ -190,7 +190,7 @@ class GB300MixedLUFactorization(AbstractDenseFactorization):
     def __init__(self, factor: str = "fp32", refine: str = "ir", maxiters: int = 30,
                  tol: Optional[float] = None, fallback: bool = True, gmres_restart: int = 30,
                  gmres_tol: float = 1e-10, growth_limit: Optional[float] = None,
-                 residualsafety: bool = False, solve: str = "exact", device: int = 0):
+                 residualsafety: bool = False, solve: str = "fast", device: int = 0):
         if factor not in ("fp32", "bf16", "fp16"):
             raise ValueError(f"unsupported factor precision {factor!r}")
         if refine not in ("ir", "gmres_ir"):
@@ -373,7 +373,7 @@ def init(prob: LinearProblem, alg=None, alias: Optional[LinearAliasSpecifier] = 
                         d_rel if reltol is None else reltol, verbose, alias_A, alias_b, ctx)
     # init_cacheval: the device-resident factorization object, allocated once
     fact = ctx.factor(m, n, alg.factor_precision())
-    if alg.solve != "exact":
+    if m == n:
         fact.set_solve(alg.solve)
     if alg.residualsafety:
         fact.keep_matrix(True)  # the FP64 copy of A the residual check reads (A_backup)

@@ -74,17 +74,44 @@ class Server:
             self.h = None
 
 
-def run_stream(server: Server, requests, rate_hz: float, seed: int = 0, timeout_s: float = 300.0):
-    """Submit `requests` (list of dicts: key, b, A or None) with Poisson
-    arrivals at `rate_hz`; return completions and the wall time."""
+GBLU_ENOTFACTORED = 5
+
+
+def run_stream(server: Server, requests, rate_hz: float, seed: int = 0, timeout_s: float = 300.0,
+               resubmit_missing: bool = False):
+    """Submit `requests` (list of dicts: key, b, A or None; with
+    resubmit_missing also Aeff, the key's current matrix) with Poisson
+    arrivals at `rate_hz`; return completions and the wall time.
+
+    resubmit_missing: a solve-only request whose key's factorization was
+    evicted completes with GBLU_ENOTFACTORED; the client sends it again with
+    the key's matrix (a factor + solve).  The completion then carries
+    "resubmitted": 1 and "client_latency_us", the time from the first
+    submission to the final completion."""
     rng = np.random.default_rng(seed)
     gaps = rng.exponential(1.0 / rate_hz, size=len(requests)) if rate_hz > 0 else np.zeros(len(requests))
     done = []
     finished = threading.Event()
+    t_first = {}
+    lock = threading.Lock()
 
     def collector():
         while len(done) < len(requests):
-            done.extend(server.poll(256, wait_ms=20))
+            got = server.poll(256, wait_ms=20)
+            now = time.perf_counter()
+            for d in got:
+                i = d["tag"]
+                if (resubmit_missing and d["status"] == GBLU_ENOTFACTORED and requests[i].get("A") is None
+                        and not d.get("resubmitted")):
+                    rq = requests[i]
+                    server.submit(i, rq["key"], rq["b"], rq["Aeff"])
+                    with lock:
+                        t_first.setdefault(("resub", i), True)
+                    continue
+                with lock:
+                    d["resubmitted"] = 1 if ("resub", i) in t_first else 0
+                    d["client_latency_us"] = (now - t_first[i]) * 1e6 if i in t_first else None
+                done.append(d)
         finished.set()
 
     th = threading.Thread(target=collector, daemon=True)
@@ -96,6 +123,8 @@ def run_stream(server: Server, requests, rate_hz: float, seed: int = 0, timeout_
         now = time.perf_counter()
         if t_next > now:
             time.sleep(t_next - now)
+        with lock:
+            t_first[i] = time.perf_counter()
         server.submit(i, rq["key"], rq["b"], rq.get("A"))
     finished.wait(timeout_s)
     wall = time.perf_counter() - t0
@@ -105,7 +134,7 @@ def run_stream(server: Server, requests, rate_hz: float, seed: int = 0, timeout_
 def latency_summary(done, wall: float) -> dict:
     lat = np.array([d["latency_us"] for d in done if d["status"] == 0]) / 1000.0
     ok = int((np.array([d["status"] for d in done]) == 0).sum()) if done else 0
-    return {
+    out = {
         "completed": ok, "failed": len(done) - ok,
         "p50_ms": float(np.percentile(lat, 50)) if len(lat) else None,
         "p99_ms": float(np.percentile(lat, 99)) if len(lat) else None,
@@ -113,3 +142,9 @@ def latency_summary(done, wall: float) -> dict:
         "solves_per_s": ok / wall if wall > 0 else None,
         "wall_s": wall,
     }
+    cl = np.array([d["client_latency_us"] for d in done
+                   if d["status"] == 0 and d.get("client_latency_us") is not None]) / 1000.0
+    if len(cl):
+        out.update({"client_p50_ms": float(np.percentile(cl, 50)), "client_p99_ms": float(np.percentile(cl, 99)),
+                    "resubmitted": int(sum(d.get("resubmitted", 0) for d in done))})
+    return out

@@ -3,7 +3,9 @@
 Batched systems and served requests are independent, so N GPUs take disjoint
 shards with no exchange on the data path; only the host gathers results.
 Systems are assigned greedily, largest first, to the rank with the least LU
-work so far (work ~ n^3), which balances uneven sizes.
+work so far (work ~ n^3), which balances uneven sizes; serving keys are
+assigned the same way by their size (affinity: a key's factorization lives
+on one GPU).
 """
 from __future__ import annotations
 
@@ -35,6 +37,36 @@ def pack(sizes, A, b, idx):
     A_sub = np.concatenate([A[a_off[i]:a_off[i] + sizes[i] ** 2] for i in idx]) if len(idx) else np.zeros(0)
     b_sub = np.concatenate([b[b_off[i]:b_off[i] + sizes[i]] for i in idx]) if len(idx) else np.zeros(0)
     return sub_sizes, A_sub, b_sub
+
+
+def gpu_solve_fn(ctx, precision: str = "fp64"):
+    """solve_fn for solve_distributed: the shard through the batched kernels
+    of this rank's GPU (one graph launch)."""
+    from .device import Batch
+
+    def solve(ss, As, bs):
+        bt = Batch(ctx, ss, precision)
+        try:
+            x = bt.solve(As, bs)
+            if (bt.info != 0).any():
+                raise RuntimeError("singular system in the shard")
+            return x
+        finally:
+            bt.close()
+    return solve
+
+
+def shard_keys(key_sizes, world: int):
+    """Serving affinity: key -> rank, balancing sum n^3 over the ranks
+    (largest keys first), so each key's factorization lives on one GPU."""
+    order = sorted(range(len(key_sizes)), key=lambda k: -int(key_sizes[k]))
+    load = [0.0] * world
+    owner = [0] * len(key_sizes)
+    for k in order:
+        r = min(range(world), key=lambda i: load[i])
+        owner[k] = r
+        load[r] += float(key_sizes[k]) ** 3
+    return owner
 
 
 def solve_distributed(sizes, A, b, rank: int, world: int, solve_fn, group=None):

@@ -68,3 +68,16 @@ def test_two_rank_gloo_solve_matches_single():
         p.join(timeout=60)
         assert p.exitcode == 0
     assert sorted(res) == [(0, True), (1, True)]
+
+
+def test_key_affinity_balances_work():
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    from importlib import import_module
+    sh = import_module(pkg.__name__ + ".sharding")
+    rng = np.random.default_rng(3)
+    ks = np.exp(rng.uniform(np.log(64), np.log(4096), size=300)).astype(int)
+    owner = sh.shard_keys(ks, 4)
+    loads = [sum(float(ks[k]) ** 3 for k in range(len(ks)) if owner[k] == r) for r in range(4)]
+    assert set(owner) == {0, 1, 2, 3}
+    assert max(loads) / min(loads) < 1.2
