@@ -309,7 +309,7 @@ int32_t gblu_factor_create(gblu_ctx* ctx, int64_t m, int64_t n, int32_t precisio
     bytes += refine_bytes(m, kWorkCols);
     if (precision == GBLU_BF16 || precision == GBLU_FP16) {
       tc_bytes = align256(tc_work_bytes(n, n / 2 + 64, n / 2 + 64));
-      bytes += tc_bytes;
+      bytes += tc_bytes + align256(tslu_work_bytes());
     }
     if (m == n && n > 0) bytes += align256(getrs_inverse_bytes(n, sizeof(float)));
   }
@@ -335,6 +335,12 @@ int32_t gblu_factor_create(gblu_ctx* ctx, int64_t m, int64_t n, int32_t precisio
       f->rf32.tc_work = c;
       f->rf32.tc_work_bytes = tc_bytes;
       c += tc_bytes;
+      // 16-bit-operand factors are a preconditioner only: tournament pivoting
+      // for their tall leaves (GBLU_PANEL=partial keeps partial pivoting)
+      const char* pe = getenv("GBLU_PANEL");
+      f->rf32.tslu = !(pe && !strcmp(pe, "partial"));
+      f->rf32.tslu_work = c;
+      c += align256(tslu_work_bytes());
     }
     // the low-precision solve of a mixed factor is refinement's correction
     // solve: fast (inverted diagonal blocks) by default

@@ -79,7 +79,18 @@ struct GetrfPlan {
   int tc_mode = 0;           // 0 SIMT FP32, 1 BF16 operands, 2 FP16 operands (scaled)
   void* tc_work = nullptr;   // conversion buffers for the operands
   size_t tc_work_bytes = 0;
+  // FP32 working matrix only: tournament pivoting for leaves taller than
+  // 512 rows (tslu.cu), instead of partial pivoting
+  bool tslu = false;
+  void* tslu_work = nullptr; // tslu_work_bytes()
 };
+
+// Tournament-pivoting panel of the low-precision getrf (tslu.cu).
+size_t tslu_work_bytes();
+bool tslu_fits(int64_t rows, int w);
+void tslu_configure(int device);
+cudaError_t tslu_panel_launch(float* A, int64_t lda, int64_t m, int64_t c0, int w, int64_t* ipiv,
+                              int64_t* info, void* work, DevScratch* scr, cudaStream_t s);
 
 // FP32 SIMT update C -= A * B in the reference's per-element order (getrf.cu).
 cudaError_t simt_gemm_sub_f32(int64_t M, int64_t N, int64_t K, const float* A, int64_t lda,

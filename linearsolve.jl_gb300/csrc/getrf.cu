@@ -1294,6 +1294,14 @@ struct Driver {
   void panel(int64_t c0, int w) {
     const int64_t M = p.m - c0;
     const DeviceInfo& di = device_info(device);
+    if constexpr (std::is_same<T, float>::value) {
+      // low-precision factors: tournament pivoting for the tall leaves
+      if (p.tslu && p.tslu_work && M > 512 && tslu_fits(M, w)) {
+        check(tslu_panel_launch(p.A, p.lda, p.m, c0, w, p.ipiv, p.info, p.tslu_work, p.scratch, s));
+        laswp(c0, w);
+        return;
+      }
+    }
     // forced: 0 automatic, 1 grid kernel only, 2 shared-memory cluster kernel
     // where it fits, 3 register kernel where it fits (falling back in order)
     if (forced != 1 && forced != 2 && p.use_reg_panel && panel_reg(c0, w)) {
@@ -1458,6 +1466,7 @@ void getrf_configure(int device) {
                        (kPermSmemMax + kPermChunk) * (int)sizeof(int32_t));
   getrs_configure(device);
   tc_configure(device);
+  tslu_configure(device);
 }
 
 // GBLU_PANEL=grid|cluster|reg forces one panel kernel (where the panel fits

@@ -228,10 +228,59 @@ def test_tensor_core_lu_reaches_fp64(ctx, oracle_mod, pkg, prec, mode, n):
     be = oracle_mod.backward_error(A, X, B)
     assert be <= 10 * n * EPS64, (be, st)
     assert st["fell_back"] == 0, st
-    # the 16-bit-operand factors are close to, not equal to, the FP32 ones
-    LU32, ipiv32, _ = oracle_mod.getrf(A.astype(np.float32))
+    # the 16-bit-operand factors (tournament pivoting for leaves taller than
+    # 512 rows) factor A: P A = L U up to the 16-bit operand rounding
+    _check_factorization(A, f.factors(), f.ipiv(), 0.05)
+    f.close()
+
+
+def _check_factorization(A, F, ipiv, tol):
+    """ipiv is a valid 1-based interchange sequence and P A = L U within tol
+    (relative to max |A|)."""
+    n = A.shape[0]
+    assert all(k + 1 <= int(p) <= n for k, p in enumerate(ipiv))
+    PA = np.array(A, dtype=np.float64, copy=True)
+    for k, p in enumerate(ipiv):
+        if p - 1 != k:
+            PA[[k, p - 1], :] = PA[[p - 1, k], :]
+    L = np.tril(F, -1) + np.eye(n)
+    U = np.triu(F)
+    err = np.abs(PA - L @ U).max() / np.abs(A).max()
+    assert err < tol, err
+    return err
+
+
+@pytest.mark.parametrize("prec", ["bf16", "fp16"])
+def test_tournament_panel_factors_and_refines(ctx, oracle_mod, pkg, prec):
+    """Leaves taller than 512 rows pick their pivots by tournament (chunk
+    factorizations, then one over the nominated rows): the factors still
+    satisfy P A = L U to operand precision, the multipliers stay bounded, and
+    refinement reaches the FP64 bound on shifted and on plain Gaussian
+    matrices."""
+    for A, B in (pkg.workloads.shifted(3000, 2, seed=71), pkg.workloads.plain(2500, 2, seed=72)):
+        n = A.shape[0]
+        f = ctx.factor(n, n, prec)
+        assert f.getrf(A) == 0
+        F = f.factors()
+        _check_factorization(A, F, f.ipiv(), 0.1)
+        assert np.abs(np.tril(F, -1)).max() < 16.0  # partial pivoting keeps |l_ij| <= 1
+        X, st = f.solve_refined(B, mode="gmres_ir")
+        assert oracle_mod.backward_error(A, X, B) <= 10 * n * EPS64, st
+        f.close()
+
+
+def test_tournament_panel_off_switch(ctx, oracle_mod, pkg, monkeypatch):
+    """GBLU_PANEL=partial at factor creation keeps partial pivoting for the
+    16-bit-operand factors: every multiplier is then at most 1."""
+    monkeypatch.setenv("GBLU_PANEL", "partial")
+    n = 1500
+    A, B = pkg.workloads.plain(n, 1, seed=73)
+    f = ctx.factor(n, n, "bf16")
+    assert f.getrf(A) == 0
     F = f.factors()
-    assert np.abs(F - LU32).max() < 0.05 * np.abs(LU32).max()
+    assert np.abs(np.tril(F, -1)).max() <= 1.0
+    X, st = f.solve_refined(B, mode="gmres_ir")
+    assert oracle_mod.backward_error(A, X, B) <= 10 * n * EPS64, st
     f.close()
 
 
