@@ -309,8 +309,9 @@ int32_t gblu_factor_create(gblu_ctx* ctx, int64_t m, int64_t n, int32_t precisio
     bytes += refine_bytes(m, kWorkCols);
     if (precision == GBLU_BF16 || precision == GBLU_FP16) {
       tc_bytes = align256(tc_work_bytes(n, n / 2 + 64, n / 2 + 64));
-      bytes += tc_bytes + align256(tslu_work_bytes());
+      bytes += tc_bytes;
     }
+    bytes += align256(tslu_work_bytes());
     if (m == n && n > 0) bytes += align256(getrs_inverse_bytes(n, sizeof(float)));
   }
   int32_t st = ctx_alloc(ctx, bytes, &f->arena);
@@ -335,10 +336,16 @@ int32_t gblu_factor_create(gblu_ctx* ctx, int64_t m, int64_t n, int32_t precisio
       f->rf32.tc_work = c;
       f->rf32.tc_work_bytes = tc_bytes;
       c += tc_bytes;
-      // 16-bit-operand factors are a preconditioner only: tournament pivoting
-      // for their tall leaves (GBLU_PANEL=partial keeps partial pivoting)
+    }
+    // Panel pivoting of the low-precision factors, a preconditioner only:
+    // tournament for the tall leaves of 16-bit-operand factors, partial
+    // pivoting (the reference's order, bit-identical to the FP32 restatement)
+    // for FP32 ones.  GBLU_PANEL=partial / tournament at creation overrides.
+    {
       const char* pe = getenv("GBLU_PANEL");
-      f->rf32.tslu = !(pe && !strcmp(pe, "partial"));
+      const bool force_partial = pe && !strcmp(pe, "partial");
+      const bool force_tournament = pe && !strcmp(pe, "tournament");
+      f->rf32.tslu = force_tournament || (tc_bytes && !force_partial);
       f->rf32.tslu_work = c;
       c += align256(tslu_work_bytes());
     }

@@ -8,13 +8,14 @@
 //   1. conversion kernels write A (M x K) and B (K x N) as K-major 16-bit
 //      copies (FP16: each column of B scaled by an exact power of two so that
 //      its largest entry lies in [2^14, 2^15); |L21| <= 1 needs no scale);
-//   2. tc_gemm_kernel: per 128 x 128 output tile, one warp issues TMA loads
-//      (128-byte swizzled 128 x 64 boxes, 3-stage mbarrier ring, two CTAs per SM so
-//      one CTA's epilogue overlaps the other's main loop), one thread
-//      issues tcgen05.mma (M=128, N=128, K=16 per instruction) into a
-//      128-column FP32 accumulator in TMEM, and four warps read the
+//   2. tc_gemm_kernel, persistent (one CTA per SM walking 128 x 128 output
+//      tiles): one warp issues TMA loads (128-byte swizzled 128 x 64 boxes,
+//      6-stage mbarrier ring running across tile boundaries), one thread
+//      issues tcgen05.mma (M=128, N=128, K=16 per instruction) into one of two
+//      128-column FP32 accumulators in TMEM, and four warps read the other
 //      accumulator back with tcgen05.ld and apply C -= acc * 2^-s in the
-//      epilogue (coalesced along the column-major C).
+//      epilogue (coalesced along the column-major C), so a tile's epilogue
+//      overlaps the next tile's MMAs.
 //
 // All mbarrier waits are bounded (globaltimer, 2 s); an expired wait records
 // DEV_TIMEOUT_GEMM, every CTA then skips to its teardown and frees TMEM.
@@ -290,44 +291,72 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
   }
 }
 
-// A (M x K, column-major, lda) -> Ah (M rows of K, row-major, ldh): 32 x 32
-// tiles through shared memory so both sides are coalesced.
+// Four FP32 values rounded to 16 bits, packed into 8 bytes (element 0 lowest).
 template <typename H>
-__global__ void conv_a_kernel(int M, int K, const float* __restrict__ A, int64_t lda,
-                              H* __restrict__ Ah, int64_t ldh) {
-  __shared__ float t[32][33];
-  const int k0 = blockIdx.x * 32, m0 = blockIdx.y * 32;
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
-  for (int i = ty; i < 32; i += 8) {
-    const int k = k0 + i, m = m0 + tx;
-    t[i][tx] = (k < K && m < M) ? A[(int64_t)m + (int64_t)k * lda] : 0.f;
+__device__ __forceinline__ uint2 pack4(float a, float b, float c, float d) {
+  uint32_t lo, hi;
+  if constexpr (std::is_same<H, __nv_bfloat16>::value) {
+    const __nv_bfloat162 x = __floats2bfloat162_rn(a, b), y = __floats2bfloat162_rn(c, d);
+    lo = *reinterpret_cast<const uint32_t*>(&x);
+    hi = *reinterpret_cast<const uint32_t*>(&y);
+  } else {
+    const __half2 x = __floats2half2_rn(a, b), y = __floats2half2_rn(c, d);
+    lo = *reinterpret_cast<const uint32_t*>(&x);
+    hi = *reinterpret_cast<const uint32_t*>(&y);
+  }
+  return make_uint2(lo, hi);
+}
+
+// A (M x K, column-major, lda) -> Ah (M rows of K, row-major, ldh, ldh a
+// multiple of 8): 64 x 64 tiles through shared memory; a warp reads 64
+// consecutive rows of a column and each thread writes 4 consecutive k of a
+// row as one 8-byte store.
+template <typename H>
+__global__ void __launch_bounds__(256)
+conv_a_kernel(int M, int K, const float* __restrict__ A, int64_t lda, H* __restrict__ Ah, int64_t ldh) {
+  __shared__ float t[64][65];  // t[k][m]
+  const int k0 = blockIdx.x * 64, m0 = blockIdx.y * 64;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int kk = warp; kk < 64; kk += 8) {
+    const int k = k0 + kk, m = m0 + 2 * lane;
+    float v0 = 0.f, v1 = 0.f;
+    if (k < K) {
+      const float* src = A + (int64_t)k * lda;
+      if (m < M) v0 = src[m];
+      if (m + 1 < M) v1 = src[m + 1];
+    }
+    t[kk][2 * lane] = v0;
+    t[kk][2 * lane + 1] = v1;
   }
   __syncthreads();
-  for (int i = ty; i < 32; i += 8) {
-    const int m = m0 + i, k = k0 + tx;
-    if (m < M && k < ldh) {
-      const float v = (k < K) ? t[tx][i] : 0.f;
-      if constexpr (sizeof(H) == 2 && std::is_same<H, __nv_bfloat16>::value)
-        Ah[(int64_t)m * ldh + k] = __float2bfloat16_rn(v);
-      else
-        Ah[(int64_t)m * ldh + k] = __float2half_rn(v);
+  for (int idx = threadIdx.x; idx < 64 * 16; idx += 256) {
+    const int mm = idx >> 4, q = idx & 15;  // row of the tile, pack of 4 k
+    const int m = m0 + mm, k = k0 + 4 * q;
+    if (m < M && k < ldh) {  // k < ldh implies k + 4 <= ldh (both multiples of 4)
+      float v[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) v[i] = (k + i < K) ? t[4 * q + i][mm] : 0.f;
+      *reinterpret_cast<uint2*>(Ah + (int64_t)m * ldh + k) = pack4<H>(v[0], v[1], v[2], v[3]);
     }
   }
 }
 
-// B (K x N, column-major, ldb) -> Bh (N rows of K, ldh), row n scaled by scale[n].
+// B (K x N, column-major, ldb) -> Bh (N rows of K, ldh a multiple of 8), row n
+// scaled by scale[n]: a column of B is a row of Bh, so each thread converts
+// 4 consecutive k with one 8-byte store; 4 columns per CTA.
 template <typename H>
-__global__ void conv_b_kernel(int K, int N, const float* __restrict__ B, int64_t ldb,
-                              H* __restrict__ Bh, int64_t ldh, const float* __restrict__ scale) {
-  const int n = blockIdx.x;
+__global__ void __launch_bounds__(256)
+conv_b_kernel(int K, int N, const float* __restrict__ B, int64_t ldb, H* __restrict__ Bh, int64_t ldh,
+              const float* __restrict__ scale) {
+  const int n = blockIdx.x * 4 + (threadIdx.x >> 6);
   if (n >= N) return;
   const float s = scale ? scale[n] : 1.f;
-  for (int k = threadIdx.x; k < ldh; k += blockDim.x) {
-    const float v = (k < K) ? B[(int64_t)k + (int64_t)n * ldb] * s : 0.f;
-    if constexpr (std::is_same<H, __nv_bfloat16>::value)
-      Bh[(int64_t)n * ldh + k] = __float2bfloat16_rn(v);
-    else
-      Bh[(int64_t)n * ldh + k] = __float2half_rn(v);
+  const float* col = B + (int64_t)n * ldb;
+  for (int64_t k = 4 * (threadIdx.x & 63); k < ldh; k += 256) {
+    float v[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) v[i] = (k + i < K) ? col[k + i] * s : 0.f;
+    *reinterpret_cast<uint2*>(Bh + (int64_t)n * ldh + k) = pack4<H>(v[0], v[1], v[2], v[3]);
   }
 }
 
@@ -417,7 +446,7 @@ cudaError_t tc_gemm_sub(int mode, int64_t M, int64_t N, int64_t K, const float* 
   float* inv_scale = scale + N;
   {
     LaunchScope ls(K_GEMM, 0.0, (double)(M * K + K * N) * 6.0, s);
-    dim3 ga((unsigned)((Kp + 31) / 32), (unsigned)((M + 31) / 32));
+    dim3 ga((unsigned)((Kp + 63) / 64), (unsigned)((M + 63) / 64));
     if (bf16)
       tc::conv_a_kernel<__nv_bfloat16><<<ga, 256, 0, s>>>((int)M, (int)K, A, lda,
                                                           reinterpret_cast<__nv_bfloat16*>(Ah), Kp);
@@ -429,11 +458,11 @@ cudaError_t tc_gemm_sub(int mode, int64_t M, int64_t N, int64_t K, const float* 
   {
     LaunchScope ls(K_GEMM, 0.0, (double)(K * N) * 6.0, s);
     if (bf16) {
-      tc::conv_b_kernel<__nv_bfloat16><<<(unsigned)N, 256, 0, s>>>(
+      tc::conv_b_kernel<__nv_bfloat16><<<(unsigned)((N + 3) / 4), 256, 0, s>>>(
           (int)K, (int)N, B, ldb, reinterpret_cast<__nv_bfloat16*>(Bh), Kp, nullptr);
     } else {
       tc::col_scale_kernel<<<(unsigned)N, 256, 0, s>>>((int)K, (int)N, B, ldb, scale, inv_scale);
-      tc::conv_b_kernel<__half><<<(unsigned)N, 256, 0, s>>>((int)K, (int)N, B, ldb,
+      tc::conv_b_kernel<__half><<<(unsigned)((N + 3) / 4), 256, 0, s>>>((int)K, (int)N, B, ldb,
                                                              reinterpret_cast<__half*>(Bh), Kp, scale);
     }
   }

@@ -250,20 +250,48 @@ def _check_factorization(A, F, ipiv, tol):
     return err
 
 
+def _factor_error(ctx, monkeypatch, A, prec, panel):
+    monkeypatch.setenv("GBLU_PANEL", panel)  # read when the factor is created
+    n = A.shape[0]
+    f = ctx.factor(n, n, prec)
+    monkeypatch.delenv("GBLU_PANEL")
+    assert f.getrf(A) == 0
+    F, ipiv = f.factors(), f.ipiv()
+    f.close()
+    return _check_factorization(A, F, ipiv, 1.0), np.abs(np.tril(F, -1)).max(), ipiv
+
+
+def test_tournament_panel_fp32_factors(ctx, pkg, monkeypatch):
+    """The tournament panel on FP32 factors (GBLU_PANEL=tournament), where
+    the factorization error is at FP32 level: P A = L U as accurately as with
+    partial pivoting, valid interchanges that do move rows, bounded
+    multipliers -- the row moves and L21 = A21 U11^-1 are checked exactly
+    enough to expose any misplaced row."""
+    A, _ = pkg.workloads.plain(2500, 1, seed=72)
+    e_t, lmax_t, ipiv_t = _factor_error(ctx, monkeypatch, A, "fp32", "tournament")
+    e_p, lmax_p, ipiv_p = _factor_error(ctx, monkeypatch, A, "fp32", "partial")
+    assert lmax_p <= 1.0 and lmax_t < 16.0
+    assert (ipiv_t != np.arange(1, 2501)).sum() > 1000  # pivots move rows
+    assert not np.array_equal(ipiv_t, ipiv_p)           # and differ from partial pivoting's
+    assert e_t < 10 * e_p + 1e-6, (e_t, e_p)
+    assert e_t < 1e-4, e_t
+
+
 @pytest.mark.parametrize("prec", ["bf16", "fp16"])
-def test_tournament_panel_factors_and_refines(ctx, oracle_mod, pkg, prec):
-    """Leaves taller than 512 rows pick their pivots by tournament (chunk
-    factorizations, then one over the nominated rows): the factors still
-    satisfy P A = L U to operand precision, the multipliers stay bounded, and
-    refinement reaches the FP64 bound on shifted and on plain Gaussian
-    matrices."""
+def test_tournament_panel_factors_and_refines(ctx, oracle_mod, pkg, monkeypatch, prec):
+    """Leaves taller than 512 rows of the 16-bit-operand factors pick their
+    pivots by tournament (chunk factorizations, then one over the nominated
+    rows): the factors are as accurate as partial pivoting's at the same
+    operand precision, and refinement reaches the FP64 bound on shifted and
+    on plain Gaussian matrices."""
     for A, B in (pkg.workloads.shifted(3000, 2, seed=71), pkg.workloads.plain(2500, 2, seed=72)):
         n = A.shape[0]
-        f = ctx.factor(n, n, prec)
+        e_t, lmax_t, _ = _factor_error(ctx, monkeypatch, A, prec, "tournament")
+        e_p, _, _ = _factor_error(ctx, monkeypatch, A, prec, "partial")
+        assert e_t < 3 * e_p + 1e-3, (e_t, e_p)
+        assert lmax_t < 16.0
+        f = ctx.factor(n, n, prec)  # the default: tournament for these precisions
         assert f.getrf(A) == 0
-        F = f.factors()
-        _check_factorization(A, F, f.ipiv(), 0.1)
-        assert np.abs(np.tril(F, -1)).max() < 16.0  # partial pivoting keeps |l_ij| <= 1
         X, st = f.solve_refined(B, mode="gmres_ir")
         assert oracle_mod.backward_error(A, X, B) <= 10 * n * EPS64, st
         f.close()
