@@ -310,6 +310,7 @@ int32_t gblu_factor_create(gblu_ctx* ctx, int64_t m, int64_t n, int32_t precisio
     if (precision == GBLU_BF16 || precision == GBLU_FP16) {
       tc_bytes = align256(tc_work_bytes(n, n / 2 + 64, n / 2 + 64));
       bytes += tc_bytes;
+      bytes += align256(trsm_inv_bytes(n));
     }
     bytes += align256(tslu_work_bytes());
     if (m == n && n > 0) bytes += align256(getrs_inverse_bytes(n, sizeof(float)));
@@ -336,16 +337,23 @@ int32_t gblu_factor_create(gblu_ctx* ctx, int64_t m, int64_t n, int32_t precisio
       f->rf32.tc_work = c;
       f->rf32.tc_work_bytes = tc_bytes;
       c += tc_bytes;
+      // TRSM base blocks through cached inverses of L's diagonal blocks
+      // (GBLU_TRSM=exact at creation keeps the substitution chain)
+      const char* te = getenv("GBLU_TRSM");
+      if (!(te && !strcmp(te, "exact"))) {
+        f->rf32.trsm_inv = reinterpret_cast<float*>(c);
+        f->rf32.trsm_inv_slots = trsm_inv_slot_count(n);
+      }
+      c += align256(trsm_inv_bytes(n));
     }
-    // Panel pivoting of the low-precision factors, a preconditioner only:
-    // tournament for the tall leaves of 16-bit-operand factors, partial
-    // pivoting (the reference's order, bit-identical to the FP32 restatement)
-    // for FP32 ones.  GBLU_PANEL=partial / tournament at creation overrides.
+    // Panel pivoting of the low-precision factors: partial pivoting (the
+    // reference's order) by default; GBLU_PANEL=tournament at creation
+    // selects tournament pivoting for leaves taller than 512 rows (slower
+    // on this GPU than the register cluster panel: two dependent getf2
+    // passes per leaf against one).
     {
       const char* pe = getenv("GBLU_PANEL");
-      const bool force_partial = pe && !strcmp(pe, "partial");
-      const bool force_tournament = pe && !strcmp(pe, "tournament");
-      f->rf32.tslu = force_tournament || (tc_bytes && !force_partial);
+      f->rf32.tslu = pe && !strcmp(pe, "tournament");
       f->rf32.tslu_work = c;
       c += align256(tslu_work_bytes());
     }

@@ -83,7 +83,16 @@ struct GetrfPlan {
   // 512 rows (tslu.cu), instead of partial pivoting
   bool tslu = false;
   void* tslu_work = nullptr; // tslu_work_bytes()
+  // FP32 working matrix of the 16-bit-operand factors only: TRSM base blocks
+  // of 65..128 rows solved through inverses of L's diagonal blocks, each
+  // computed once per getrf and kept in one of these 128 x 128 slots
+  float* trsm_inv = nullptr;
+  int trsm_inv_slots = 0;
 };
+
+// Slots and bytes of the TRSM inverse cache of an n-column factorization.
+int trsm_inv_slot_count(int64_t n);
+size_t trsm_inv_bytes(int64_t n);
 
 // Tournament-pivoting panel of the low-precision getrf (tslu.cu).
 size_t tslu_work_bytes();

@@ -24,6 +24,7 @@
 #include <cstring>
 #include <mutex>
 #include <type_traits>
+#include <vector>
 
 #include <cooperative_groups.h>
 
@@ -836,8 +837,20 @@ trsm_lunit_kernel(const T* __restrict__ L, int64_t ldl, int k, T* __restrict__ B
       }
     asm volatile("cp.async.wait_all;" ::: "memory");
   } else {
-    for (int c = warp; c < k; c += nw)
-      for (int r = lane; r < k; r += 32) sL[c][r] = L[r + (int64_t)c * ldl];
+    // asynchronous copies, all in flight at once (a load-store loop waits
+    // out one global latency per element); a fixed thread count keeps the
+    // index arithmetic compile-time
+    constexpr int NT = trsm_warps<T, KM>() * 32;
+#pragma unroll
+    for (int e = 0; e < KM * KM / NT; ++e) {
+      const int idx = e * NT + (int)threadIdx.x, c = idx / KM, r = idx % KM;
+      if (c < k && r > c && r < k) {
+        const unsigned d = (unsigned)__cvta_generic_to_shared(&sL[c][r]);
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(L + r + (int64_t)c * ldl)
+                     : "memory");
+      }
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");
   }
   __syncthreads();
   for (int64_t col = (int64_t)blockIdx.x * nw + warp; col < ncols; col += (int64_t)gridDim.x * nw) {
@@ -868,6 +881,112 @@ trsm_lunit_kernel(const T* __restrict__ L, int64_t ldl, int k, T* __restrict__ B
 
 template <typename T, int KM>
 constexpr size_t trsm_smem() { return (size_t)KM * (KM + 1) * sizeof(T); }
+
+// ---------------------------------------------------------------------------
+// TRSM base blocks of the 16-bit-operand factors (FP32 working matrix; the
+// factors are refinement's preconditioner, not the reference's bit pattern):
+// X = L^-1 of a unit-lower k x k diagonal block (64 < k <= 128) once per
+// getrf, then B := X B as a product, with no dependent chain.
+constexpr int kTinvLd = 128;       // leading dimension of a cached inverse
+constexpr int kTinvApCols = 32;    // B columns per CTA of the product
+constexpr int kTinvApLdB = kTinvLd + 1;
+
+// Warp w of CTA b solves L x = e_j, j = 16 b + w (the TRSM chain, starting
+// at row j: the inverse is lower triangular); column j of X, ld 128.
+__global__ void __launch_bounds__(512)
+trsm_inv_kernel(const float* __restrict__ L, int64_t ldl, int k, float* __restrict__ X) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float(*sL)[kTinvLd + 1] = reinterpret_cast<float(*)[kTinvLd + 1]>(smem_raw);  // sL[c][r] = L[r, c]
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int e = 0; e < kTinvLd * kTinvLd / 512; ++e) {
+    const int idx = e * 512 + (int)threadIdx.x, c = idx / kTinvLd, r = idx % kTinvLd;
+    if (c < k && r > c && r < k) {
+      const unsigned d = (unsigned)__cvta_generic_to_shared(&sL[c][r]);
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(L + r + (int64_t)c * ldl) : "memory");
+    }
+  }
+  asm volatile("cp.async.wait_all;" ::: "memory");
+  __syncthreads();
+  const int j = blockIdx.x * 16 + warp;
+  if (j >= k) return;
+  float v[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) v[q] = lane + 32 * q == j ? 1.f : 0.f;
+  for (int kk = j; kk < k - 1; ++kk) {
+    const int qk = kk >> 5;
+    float src = v[0];
+#pragma unroll
+    for (int q = 1; q < 4; ++q)
+      if (qk == q) src = v[q];
+    const float xk = __shfl_sync(0xffffffffu, src, kk & 31);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      if (q < qk) continue;
+      const int r = lane + 32 * q;
+      if (r > kk && r < k) v[q] = fmaf(-sL[kk][r], xk, v[q]);
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < 4; ++q) X[lane + 32 * q + (int64_t)j * kTinvLd] = lane + 32 * q < k ? v[q] : 0.f;
+}
+
+// B (k x ncols, ldb) := X B with X the cached k x k inverse (ld 128), k a
+// multiple of 4.  CTA: 128 rows x 32 columns; thread (ty, tx) = 4 rows x 4
+// columns, accumulating over the columns kk <= its last row (X is lower
+// triangular).  Each CTA reads its columns of B whole before writing them.
+__global__ void __launch_bounds__(256)
+trsm_inv_apply_kernel(const float* __restrict__ X, int k, float* __restrict__ B, int64_t ldb, int64_t ncols) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float* sX = reinterpret_cast<float*>(smem_raw);  // sX[kk * 128 + r] = X[r, kk]
+  float* sB = sX + kTinvLd * kTinvLd;             // sB[c * 129 + kk] = B[kk, cb + c]
+  const int tid = threadIdx.x, ty = tid >> 3, tx = tid & 7;
+  const int64_t cb = (int64_t)blockIdx.x * kTinvApCols;
+  const int nc = (int)min((int64_t)kTinvApCols, ncols - cb);
+  for (int i = tid; i < k * (kTinvLd / 4); i += 256) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(sX + 4 * i);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(X + 4 * i) : "memory");
+  }
+  for (int i = tid; i < k * nc; i += 256) {
+    const int c = i / k, kk = i % k;
+    const unsigned d = (unsigned)__cvta_generic_to_shared(sB + c * kTinvApLdB + kk);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(B + kk + (cb + c) * ldb) : "memory");
+  }
+  asm volatile("cp.async.wait_all;" ::: "memory");
+  __syncthreads();
+  float acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) acc[i][c] = 0.f;
+  const int kend = min(k, 4 * ty + 4);
+  const float* bcol = sB + (4 * tx) * kTinvApLdB;
+  for (int kk = 0; kk < kend; ++kk) {
+    const float4 x0 = *reinterpret_cast<const float4*>(sX + kk * kTinvLd + 4 * ty);
+    const float xr[4] = {x0.x, x0.y, x0.z, x0.w};
+    float bv[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) bv[c] = bcol[c * kTinvApLdB + kk];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) acc[i][c] = fmaf(xr[i], bv[c], acc[i][c]);
+  }
+  if (4 * ty >= k) return;
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    if (4 * tx + c >= nc) break;
+    float* dst = B + 4 * ty + (cb + 4 * tx + c) * ldb;
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+      if (4 * ty + i < k) dst[i] = acc[i][c];
+  }
+}
+
+constexpr size_t trsm_inv_smem() { return (size_t)kTinvLd * (kTinvLd + 1) * sizeof(float); }
+constexpr size_t trsm_inv_apply_smem() {
+  return (size_t)kTinvLd * kTinvLd * sizeof(float) + (size_t)kTinvApCols * kTinvApLdB * sizeof(float);
+}
 
 // ---------------------------------------------------------------------------
 // SIMT GEMM update C -= A * B (column-major), every C element updated by
@@ -1160,6 +1279,10 @@ struct Driver {
   cudaError_t err = cudaSuccess;
   int forced = 0;  // forced_panel_kind()
   int forced_tile = 0;  // forced_gemm_tile()
+  // the TRSM inverse cache of this getrf: slot and order of the inverse kept
+  // for the diagonal block starting at row 32 i (-1: none yet)
+  std::vector<int> inv_slot, inv_k;
+  int inv_next = 0;
 
   T* at(int64_t r, int64_t c) const { return p.A + r + c * p.lda; }
 
@@ -1381,9 +1504,50 @@ struct Driver {
     check(cudaGetLastError());
   }
 
+  // The cached inverse of the k x k diagonal block of L at row r0 (r0 a
+  // multiple of 32): computed on first use in this getrf (the block is final
+  // once the leaves covering it are done; a later getrf starts a new cache),
+  // reused for any order up to k (the leading block of an inverse is the
+  // inverse of the leading block).  Returns the slot, or -1 when full.
+  int inverse_slot(int64_t r0, int64_t k) {
+    if (inv_slot.empty()) {
+      inv_slot.assign((size_t)(p.m / 32 + 2), -1);
+      inv_k.assign(inv_slot.size(), 0);
+    }
+    const size_t key = (size_t)(r0 / 32);
+    if (key >= inv_slot.size()) return -1;
+    if (inv_slot[key] >= 0 && inv_k[key] >= k) return inv_slot[key];
+    int slot = inv_slot[key];
+    if (slot < 0) {
+      if (inv_next >= p.trsm_inv_slots) return -1;
+      slot = inv_next++;
+    }
+    float* X = p.trsm_inv + (size_t)slot * kTinvLd * kTinvLd;
+    LaunchScope ls(K_TRSM, (double)k * k * k / 3.0, ((double)k * k / 2 + (double)k * kTinvLd) * 4.0, s);
+    trsm_inv_kernel<<<(unsigned)((k + 15) / 16), 512, trsm_inv_smem(), s>>>(
+        reinterpret_cast<const float*>(at(r0, r0)), p.lda, (int)k, X);
+    check(cudaGetLastError());
+    inv_slot[key] = slot;
+    inv_k[key] = (int)k;
+    return slot;
+  }
+
   // B (k x ncols at (r0, bc0)) := L \ B, L unit lower at (r0, r0) of size k.
   void trsm(int64_t r0, int64_t k, int64_t bc0, int64_t ncols) {
     if (k <= 0 || ncols <= 0) return;
+    if constexpr (std::is_same<T, float>::value) {
+      if (p.trsm_inv && k > 64 && k <= kTinvLd && k % 4 == 0 && r0 % 32 == 0) {
+        const int slot = inverse_slot(r0, k);
+        if (slot >= 0) {
+          LaunchScope ls(K_TRSM, 2.0 * k * k * ncols / 2.0, (2.0 * k * ncols + (double)k * k) * 4.0, s);
+          trsm_inv_apply_kernel<<<(unsigned)((ncols + kTinvApCols - 1) / kTinvApCols), 256,
+                                  trsm_inv_apply_smem(), s>>>(p.trsm_inv + (size_t)slot * kTinvLd * kTinvLd,
+                                                              (int)k, at(r0, bc0), p.lda, ncols);
+          check(cudaGetLastError());
+          return;
+        }
+      }
+    }
     if (k <= p.trsm_base && k <= kTrsmMax) {
       const DeviceInfo& di = device_info(device);
       // one column per warp.  FP64: few columns are spread over the SMs one
@@ -1405,6 +1569,10 @@ struct Driver {
       return;
     }
     int64_t k1 = k / 2;
+    if (p.trsm_inv) {  // halves on 32-row boundaries, so cached blocks recur
+      const int64_t a = (k1 + 31) / 32 * 32;
+      if (a < k) k1 = a;
+    }
     trsm(r0, k1, bc0, ncols);
     gemm(k - k1, ncols, k1, at(r0 + k1, r0), p.lda, at(r0, bc0), p.lda, at(r0 + k1, bc0), p.lda);
     trsm(r0 + k1, k - k1, bc0, ncols);
@@ -1446,7 +1614,15 @@ cudaError_t perm_build_launch(const int64_t* ipiv, int64_t kmax, int64_t m, int3
   return cudaGetLastError();
 }
 
+int trsm_inv_slot_count(int64_t n) { return (int)(n / 64 + 8); }
+size_t trsm_inv_bytes(int64_t n) {
+  return (size_t)trsm_inv_slot_count(n) * kTinvLd * kTinvLd * sizeof(float);
+}
+
 void getrf_configure(int device) {
+  cudaFuncSetAttribute(trsm_inv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)trsm_inv_smem());
+  cudaFuncSetAttribute(trsm_inv_apply_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)trsm_inv_apply_smem());
   const DeviceInfo& di = device_info(device);
   const int cap = (int)std::min<size_t>(di.smem_optin, 200 * 1024);
   cudaFuncSetAttribute(panel_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);

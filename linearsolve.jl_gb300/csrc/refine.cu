@@ -125,11 +125,13 @@ umax_kernel(int64_t n, const float* __restrict__ LU, int64_t ld, unsigned long l
 //   'N': op(A)[i,j] = A[i + j*lda], A is rows x cols, i < rows
 //   'T': op(A)[i,j] = A[j + i*lda], i < cols (one warp per output row)
 // Chunks are fixed by (cols or rows) and kSplit, so the sum order is fixed.
-template <int W>
+// ABS (|A| x, for the backward error's denominator) is a compile-time
+// switch: on this GPU a predicated-off FP64 instruction still occupies the
+// FP64 pipe, so a runtime flag would cost the plain residual a fifth more.
+template <int W, bool ABS>
 __global__ void __launch_bounds__(kRowsPerCta)
 gemv_n_partial_kernel(int64_t rows, int64_t cols, const double* __restrict__ A, int64_t lda,
-                      const double* __restrict__ X, int64_t ldx, int wreal, double* __restrict__ P,
-                      int absval) {
+                      const double* __restrict__ X, int64_t ldx, int wreal, double* __restrict__ P) {
   __shared__ double sx[kXTile][W];
   const int s = blockIdx.y;
   const int64_t cs = (cols + kSplit - 1) / kSplit;
@@ -151,7 +153,7 @@ gemv_n_partial_kernel(int64_t rows, int64_t cols, const double* __restrict__ A, 
 #pragma unroll 4
       for (int jj = 0; jj < nt; ++jj) {
         double v = a[jj * lda];
-        if (absval) v = fabs(v);
+        if constexpr (ABS) v = fabs(v);
 #pragma unroll
         for (int q = 0; q < W; ++q) acc[q] = fma(v, sx[jj][q], acc[q]);
       }
@@ -496,11 +498,17 @@ cudaError_t gemv(char op, int64_t rows, int64_t cols, const double* A, int64_t l
     len = rows;
     dim3 grid((unsigned)((rows + kRowsPerCta - 1) / kRowsPerCta), kSplit);
     LaunchScope ls_(K_REFINE, 2.0 * rows * cols * W, 8.0 * rows * cols, s);
-    const int ab = absval ? 1 : 0;
-    if (Wp == 1 || X == nullptr) gemv_n_partial_kernel<1><<<grid, kRowsPerCta, 0, s>>>(rows, cols, A, lda, X, ldx, W, P, ab);
-    else if (Wp == 2) gemv_n_partial_kernel<2><<<grid, kRowsPerCta, 0, s>>>(rows, cols, A, lda, X, ldx, W, P, ab);
-    else if (Wp == 4) gemv_n_partial_kernel<4><<<grid, kRowsPerCta, 0, s>>>(rows, cols, A, lda, X, ldx, W, P, ab);
-    else gemv_n_partial_kernel<8><<<grid, kRowsPerCta, 0, s>>>(rows, cols, A, lda, X, ldx, W, P, ab);
+    if (absval) {
+      if (Wp == 1 || X == nullptr) gemv_n_partial_kernel<1, true><<<grid, kRowsPerCta, 0, s>>>(rows, cols, A, lda, X, ldx, W, P);
+      else if (Wp == 2) gemv_n_partial_kernel<2, true><<<grid, kRowsPerCta, 0, s>>>(rows, cols, A, lda, X, ldx, W, P);
+      else if (Wp == 4) gemv_n_partial_kernel<4, true><<<grid, kRowsPerCta, 0, s>>>(rows, cols, A, lda, X, ldx, W, P);
+      else gemv_n_partial_kernel<8, true><<<grid, kRowsPerCta, 0, s>>>(rows, cols, A, lda, X, ldx, W, P);
+    } else {
+      if (Wp == 1 || X == nullptr) gemv_n_partial_kernel<1, false><<<grid, kRowsPerCta, 0, s>>>(rows, cols, A, lda, X, ldx, W, P);
+      else if (Wp == 2) gemv_n_partial_kernel<2, false><<<grid, kRowsPerCta, 0, s>>>(rows, cols, A, lda, X, ldx, W, P);
+      else if (Wp == 4) gemv_n_partial_kernel<4, false><<<grid, kRowsPerCta, 0, s>>>(rows, cols, A, lda, X, ldx, W, P);
+      else gemv_n_partial_kernel<8, false><<<grid, kRowsPerCta, 0, s>>>(rows, cols, A, lda, X, ldx, W, P);
+    }
   } else {
     len = cols;
     dim3 grid((unsigned)((cols + 7) / 8), kSplit);

@@ -2,19 +2,27 @@
 // trailing updates): the panel of a 32-column leaf picks its pivots in two
 // local factorizations instead of one cross-CTA exchange per column.
 //
-//   1. tslu_local_kernel: the panel rows are cut into P chunks of R rows; one
-//      CTA per chunk runs getf2 with partial pivoting on its chunk in shared
-//      memory and nominates the chunk's w pivot rows.
-//   2. tslu_tree_kernel: one CTA runs getf2 with partial pivoting on the P*w
-//      nominated rows (their original values) and keeps the first w: the
-//      panel's pivot rows in order, and the packed L11 \ U11 of those rows.
-//   3. tslu_moves_kernel: the pivot order as the LAPACK interchange sequence
-//      ipiv[c0 .. c0+w) and the at most 2w row moves it implies, with the
-//      moved rows' panel values staged.
-//   4. tslu_apply_kernel: rows c0 .. c0+w-1 receive L11 \ U11; every other
-//      panel row receives l = a U11^{-1} (a: its value after the moves).
+//   1. tslu_select_kernel, every CTA: the panel rows are cut into P <= 32
+//      chunks of R rows; one CTA per chunk runs getf2 with partial pivoting
+//      on its chunk, rows held in registers, and nominates the chunk's w
+//      pivot rows (their original values go to the candidate buffer).
+//   2. the same kernel, the CTA that finishes last: getf2 with partial
+//      pivoting on the P*w nominated rows keeps the first w -- the panel's
+//      pivot rows in order and the packed L11 \ U11 of those rows -- while
+//      one warp turns the pivot order into the LAPACK interchange
+//      sequence ipiv[c0 .. c0+w) and the at most 2w row moves it implies,
+//      and the moved rows' panel values are staged.
+//   3. tslu_apply_kernel: rows c0 .. c0+w-1 receive L11 \ U11; every other
+//      panel row receives l solving l U11 = a (a: its value after the
+//      moves), by substitution in registers.
 // The interchanges reach the other columns through the leaf's laswp, as for
 // the partial-pivoting panels.
+//
+// The getf2 keeps each row in registers, with the columns rotating down one
+// register per step (the live column is always register 0, so the step loop
+// is not unrolled); no row is ever moved: the pivot row of a step leaves the
+// active set.  Every warp publishes its best row whole, so one barrier per
+// column suffices (double-buffered by column parity).
 //
 // This is communication-avoiding LU's tall-skinny panel (Grigori, Demmel and
 // Xiang, SIAM J. Matrix Anal. Appl. 32(4), 2011), one reduction level.  Its
@@ -25,6 +33,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 
 #include "device_util.cuh"
 #include "gblu_internal.h"
@@ -35,226 +44,275 @@ namespace gblu {
 
 namespace {
 
-constexpr int kTsW = 32;          // panel width
-constexpr int kTsMaxCand = 1024;  // nominated rows the tree factors at once
-constexpr int kTsLocalThreads = 512;
-constexpr int kTsTreeThreads = 1024;
+constexpr int kTsW = 32;                        // panel width
+constexpr int kTsThreads = 512;                 // threads of a selection CTA
+constexpr int kTsWarps = kTsThreads / 32;
+constexpr int kTsMaxChunks = 32;                // chunks (CTAs) per panel
+constexpr int kTsMaxCand = kTsMaxChunks * kTsW; // nominated rows the tree factors
+constexpr int kTsTreeRpt = kTsMaxCand / kTsThreads;
 
-// |a| as an ordered integer key; NaN is never a pivot (key -1).
+// |a| as an ordered integer key for an active row (NaN ranks with zero);
+// -1 marks a row that is no longer a candidate.
 __device__ __forceinline__ int piv_key(float a) {
   const float v = fabsf(a);
-  return isnan(v) ? -1 : __float_as_int(v);
+  return isnan(v) ? 0 : __float_as_int(v);
 }
 
-// Block-wide (key max, then smallest index) over one candidate per thread.
-// Returns the winning index (or -1 when no key >= 0) in every thread.
-template <int NT>
-__device__ __forceinline__ int block_argmax(int key, int idx, int* s_key, int* s_idx) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-  for (int off = 16; off; off >>= 1) {
-    const int ok = __shfl_xor_sync(0xffffffffu, key, off);
-    const int oi = __shfl_xor_sync(0xffffffffu, idx, off);
-    if (ok > key || (ok == key && oi < idx)) { key = ok; idx = oi; }
-  }
-  if (lane == 0) { s_key[warp] = key; s_idx[warp] = idx; }
-  __syncthreads();
-  if (warp == 0) {
-    key = lane < NT / 32 ? s_key[lane] : -1;
-    idx = lane < NT / 32 ? s_idx[lane] : 0x7fffffff;
-#pragma unroll
-    for (int off = 16; off; off >>= 1) {
-      const int ok = __shfl_xor_sync(0xffffffffu, key, off);
-      const int oi = __shfl_xor_sync(0xffffffffu, idx, off);
-      if (ok > key || (ok == key && oi < idx)) { key = ok; idx = oi; }
-    }
-    if (lane == 0) s_idx[32] = key >= 0 ? idx : -1;
-  }
-  __syncthreads();
-  const int r = s_idx[32];
-  __syncthreads();  // s_key / s_idx are reused by the next call
-  return r;
-}
-
-// getf2 with partial pivoting on rows [0, nr) x columns [0, w) of the shared
-// matrix s (row stride kTsW + 1), rows tid, tid + NT, ...; row indices in sidx
-// follow the swaps (rows whose index is negative are padding, never pivots).
-// Returns the first column with no usable pivot (-1: none).
-template <int NT, int RPT>
-__device__ int smem_getf2(float* s, int* sidx, int nr, int w, int* s_key, int* s_idx) {
-  constexpr int LD = kTsW + 1;
-  int zero_col = -1;
-  for (int k = 0; k < w && k < nr; ++k) {
-    int key = -1, idx = 0x7fffffff;
-#pragma unroll
-    for (int t = 0; t < RPT; ++t) {
-      const int i = threadIdx.x + NT * t;
-      if (i >= k && i < nr && sidx[i] >= 0) {
-        const int kk = piv_key(s[i * LD + k]);
-        if (kk > key || (kk == key && i < idx)) { key = kk; idx = i; }
-      }
-    }
-    int piv = block_argmax<NT>(key, idx, s_key, s_idx);
-    const bool usable = piv >= 0 && s[piv * LD + k] != 0.f;
-    if (!usable) {
-      if (zero_col < 0) zero_col = k;
-      piv = k;
-    }
-    if (piv != k && threadIdx.x < w) {  // interchange rows k and piv
-      const int j = threadIdx.x;
-      const float t = s[k * LD + j];
-      s[k * LD + j] = s[piv * LD + j];
-      s[piv * LD + j] = t;
-      if (j == 0) {
-        const int ti = sidx[k];
-        sidx[k] = sidx[piv];
-        sidx[piv] = ti;
-      }
-    }
-    __syncthreads();
-    if (usable) {
-      const float rp = 1.0f / s[k * LD + k];
-#pragma unroll
-      for (int t = 0; t < RPT; ++t) {
-        const int i = threadIdx.x + NT * t;
-        if (i > k && i < nr) {
-          float* row = s + i * LD;
-          const float l = row[k] * rp;
-          row[k] = l;
-          for (int j = k + 1; j < w; ++j) row[j] = fmaf(-l, s[k * LD + j], row[j]);
-        }
-      }
-    }
-    __syncthreads();
-  }
-  return zero_col;
-}
-
-// 1. one CTA per chunk of R rows (R <= RPT * NT): nominate the chunk's pivot rows.
 template <int RPT>
-__global__ void __launch_bounds__(kTsLocalThreads)
-tslu_local_kernel(const float* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w, int R,
-                  int32_t* __restrict__ cand_rows, float* __restrict__ cand_vals) {
+__device__ __forceinline__ float pick(const float (&a)[RPT][kTsW], int q, int j) {
+  float v = a[0][j];
+#pragma unroll
+  for (int t = 1; t < RPT; ++t)
+    if (q == t) v = a[t][j];
+  return v;
+}
+
+struct StepShared {
+  float cand[2][kTsWarps][kTsW];  // each warp's best row, by column parity
+  int key[2][kTsWarps];
+  int slot[2][kTsWarps];
+  int piv[kTsW];                  // slot of the pivot row of each step
+  float U[kTsW][kTsW];            // tree: U row k, shifted (U[k][j] = u_{k,k+j})
+};
+
+// getf2 with partial pivoting over the rows in registers: thread t holds
+// slots t*RPT + q (q < RPT), a[q][j] = the row's column k + j at step k.
+// Records the pivot slot of every step; Tree also keeps the multipliers
+// (sl[k * kTsMaxCand + slot]) and the U rows.  Returns the first column with
+// no nonzero pivot, or -1.
+template <int RPT, bool Tree>
+__device__ int reg_getf2(float (&a)[RPT][kTsW], bool (&act)[RPT], int w, StepShared& sh, float* sl) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  int zc = -1;
+#pragma unroll 1
+  for (int k = 0; k < w; ++k) {
+    const int buf = k & 1;
+    int key = -1, qb = 0;
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) {
+      const int kq = act[q] ? piv_key(a[q][0]) : -1;
+      if (kq > key) { key = kq; qb = q; }
+    }
+    const int wmax = __reduce_max_sync(0xffffffffu, key);
+    const int wl = __ffs(__ballot_sync(0xffffffffu, key == wmax)) - 1;
+    if (lane == wl) {
+      float4* dst = reinterpret_cast<float4*>(&sh.cand[buf][warp][0]);
+#pragma unroll
+      for (int j = 0; j < kTsW; j += 4)
+        dst[j / 4] = make_float4(pick<RPT>(a, qb, j), pick<RPT>(a, qb, j + 1), pick<RPT>(a, qb, j + 2),
+                                 pick<RPT>(a, qb, j + 3));
+      sh.key[buf][warp] = wmax;
+      sh.slot[buf][warp] = tid * RPT + qb;
+    }
+    __syncthreads();
+    const int kk = lane < kTsWarps ? sh.key[buf][lane] : INT_MIN;
+    const int bmax = __reduce_max_sync(0xffffffffu, kk);
+    const int ww = __ffs(__ballot_sync(0xffffffffu, kk == bmax)) - 1;
+    const int pslot = sh.slot[buf][ww];
+    const float4* u4 = reinterpret_cast<const float4*>(&sh.cand[buf][ww][0]);
+    if (tid == 0) sh.piv[k] = pslot;
+    if (pslot / RPT == tid) {  // the pivot row leaves the active set
+      const int pq = pslot - tid * RPT;
+#pragma unroll
+      for (int q = 0; q < RPT; ++q)
+        if (q == pq) act[q] = false;
+      if constexpr (Tree) {
+#pragma unroll
+        for (int j = 0; j < kTsW; ++j) sh.U[k][j] = pick<RPT>(a, pq, j);
+      }
+    }
+    const bool usable = bmax > 0;  // a nonzero, non-NaN pivot
+    if (!usable && zc < 0) zc = k;
+    float u[kTsW];
+#pragma unroll
+    for (int j = 0; j < kTsW; j += 4) {
+      const float4 v = u4[j / 4];
+      u[j] = v.x; u[j + 1] = v.y; u[j + 2] = v.z; u[j + 3] = v.w;
+    }
+    const float rp = usable ? 1.0f / u[0] : 0.0f;
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) {
+      if (!act[q]) continue;
+      const float l = a[q][0] * rp;
+      if constexpr (Tree) sl[k * kTsMaxCand + tid * RPT + q] = l;
+#pragma unroll
+      for (int j = 0; j < kTsW - 1; ++j) a[q][j] = fmaf(-l, u[j + 1], a[q][j + 1]);
+      a[q][kTsW - 1] = 0.f;
+    }
+  }
+  __syncthreads();
+  return zc;
+}
+
+// Steps 1 and 2.  Dynamic shared memory (last CTA only uses it): the tree's
+// multipliers, kTsW x kTsMaxCand floats, and the candidates' row numbers.
+template <int RPT>
+__global__ void __launch_bounds__(kTsThreads, 1)
+tslu_select_kernel(const float* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w, int R,
+                   int32_t* __restrict__ cand_rows, float* __restrict__ cand_vals,
+                   unsigned* __restrict__ ticket, float* __restrict__ lu11,
+                   int32_t* __restrict__ moves, float* __restrict__ staged, int64_t* __restrict__ ipiv,
+                   int64_t* __restrict__ info, DevScratch* __restrict__ scr) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  float* s = reinterpret_cast<float*>(smem_raw);
-  int* sidx = reinterpret_cast<int*>(s + (size_t)R * (kTsW + 1));
-  __shared__ int s_key[32], s_idx[33];
+  float* sl = reinterpret_cast<float*>(smem_raw);
+  int* srows = reinterpret_cast<int*>(sl + (size_t)kTsW * kTsMaxCand);
+  __shared__ __align__(16) StepShared sh;
+  __shared__ int pos_s[2 * kTsW], row_s[2 * kTsW], cnt_s;
+  __shared__ bool last_s;
+  const int tid = threadIdx.x;
+  const int P = gridDim.x;
   const int p = blockIdx.x;
   const int64_t r0 = c0 + (int64_t)p * R;
   const int nr = (int)min((int64_t)R, m - r0);
-  for (int j = 0; j < w; ++j)
-    for (int i = threadIdx.x; i < nr; i += kTsLocalThreads) s[i * (kTsW + 1) + j] = A[(r0 + i) + (c0 + j) * lda];
-  for (int i = threadIdx.x; i < nr; i += kTsLocalThreads) sidx[i] = (int)(r0 + i);
-  __syncthreads();
-  smem_getf2<kTsLocalThreads, RPT>(s, sidx, nr, w, s_key, s_idx);
-  // nominated rows and their original panel values
-  const int cw = min(w, nr);
-  for (int idx = threadIdx.x; idx < kTsW * kTsW; idx += kTsLocalThreads) {
-    const int k = idx / kTsW, j = idx % kTsW;
-    float v = 0.f;
-    if (k < cw && j < w) v = A[(int64_t)sidx[k] + (c0 + j) * lda];
-    cand_vals[((size_t)p * kTsW + k) * kTsW + j] = v;
-  }
-  if (threadIdx.x < kTsW) cand_rows[p * kTsW + threadIdx.x] = threadIdx.x < cw ? sidx[threadIdx.x] : -1;
-}
 
-// 2. one CTA: the panel's pivot rows from the nominated ones, and L11 \ U11.
-__global__ void __launch_bounds__(kTsTreeThreads)
-tslu_tree_kernel(int ncand, int w, int64_t c0, const int32_t* __restrict__ cand_rows,
-                 const float* __restrict__ cand_vals, int32_t* __restrict__ piv_rows,
-                 float* __restrict__ lu11, int64_t* __restrict__ info) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  float* s = reinterpret_cast<float*>(smem_raw);
-  int* sidx = reinterpret_cast<int*>(s + (size_t)kTsMaxCand * (kTsW + 1));
-  __shared__ int s_key[32], s_idx[33];
-  for (int idx = threadIdx.x; idx < ncand * kTsW; idx += kTsTreeThreads) {
-    const int k = idx / kTsW, j = idx % kTsW;
-    s[k * (kTsW + 1) + j] = cand_vals[idx];
+  // ---- 1. this chunk's nominations
+  {
+    float a[RPT][kTsW];
+    bool act[RPT];
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) {
+      const int i = tid * RPT + q;
+      act[q] = i < nr;
+#pragma unroll
+      for (int j = 0; j < kTsW; ++j) a[q][j] = (act[q] && j < w) ? A[(r0 + i) + (c0 + j) * lda] : 0.f;
+    }
+    const int cw = min(w, nr);
+    reg_getf2<RPT, false>(a, act, cw, sh, nullptr);
+    for (int idx = tid; idx < kTsW * kTsW; idx += kTsThreads) {
+      const int k = idx / kTsW, j = idx % kTsW;
+      float v = 0.f;
+      if (k < cw && j < w) v = A[(r0 + sh.piv[k]) + (c0 + j) * lda];
+      cand_vals[((size_t)p * kTsW + k) * kTsW + j] = v;
+    }
+    if (tid < kTsW) cand_rows[p * kTsW + tid] = tid < cw ? (int32_t)(r0 + sh.piv[tid]) : -1;
   }
-  for (int i = threadIdx.x; i < ncand; i += kTsTreeThreads) sidx[i] = cand_rows[i];
+  // ---- the last CTA to finish runs the tree (no CTA waits for another)
+  __threadfence();
   __syncthreads();
-  const int zc = smem_getf2<kTsTreeThreads, 1>(s, sidx, ncand, w, s_key, s_idx);
-  if (threadIdx.x < kTsW) piv_rows[threadIdx.x] = threadIdx.x < w ? sidx[threadIdx.x] : -1;
-  for (int idx = threadIdx.x; idx < kTsW * kTsW; idx += kTsTreeThreads) {
-    const int k = idx / kTsW, j = idx % kTsW;
-    lu11[idx] = (k < w && j < w) ? s[k * (kTsW + 1) + j] : 0.f;
+  if (tid == 0) last_s = atomicAdd(ticket, 1u) == (unsigned)(P - 1);
+  __syncthreads();
+  if (!last_s) return;
+  __threadfence();
+  if (tid == 0) *ticket = 0u;  // ready for the next panel
+
+  // ---- 2. the pivot rows among the nominated ones
+  const int ncand = P * kTsW;
+  int zc;
+  {
+    float a[kTsTreeRpt][kTsW];
+    bool act[kTsTreeRpt];
+#pragma unroll
+    for (int q = 0; q < kTsTreeRpt; ++q) {
+      const int c = tid * kTsTreeRpt + q;
+      const int row = c < ncand ? __ldcg(cand_rows + c) : -1;
+      act[q] = row >= 0;
+      srows[c] = row;
+      const float4* src = reinterpret_cast<const float4*>(cand_vals + (size_t)c * kTsW);
+#pragma unroll
+      for (int j = 0; j < kTsW; j += 4) {
+        const float4 v = act[q] ? __ldcg(src + j / 4) : make_float4(0.f, 0.f, 0.f, 0.f);
+        a[q][j] = v.x; a[q][j + 1] = v.y; a[q][j + 2] = v.z; a[q][j + 3] = v.w;
+      }
+    }
+    __syncthreads();
+    zc = reg_getf2<kTsTreeRpt, true>(a, act, w, sh, sl);
   }
-  if (threadIdx.x == 0 && zc >= 0)
+  if (tid == 0 && zc >= 0)
     atomicCAS(reinterpret_cast<unsigned long long*>(info), 0ull, (unsigned long long)(c0 + zc + 1));
-}
-
-// 3. one thread: ipiv[c0 + k] (1-based) from the pivot rows, and the row moves
-// "position dst receives original row src"; all threads then stage the moved
-// rows' panel values.
-__global__ void tslu_moves_kernel(const float* __restrict__ A, int64_t lda, int64_t c0, int w,
-                                  const int32_t* __restrict__ piv_rows, int64_t* __restrict__ ipiv,
-                                  int32_t* __restrict__ moves, float* __restrict__ staged,
-                                  DevScratch* __restrict__ scr) {
-  __shared__ int pos_s[2 * kTsW], row_s[2 * kTsW];  // touched positions and the row each holds
-  __shared__ int cnt_s;
-  if (threadIdx.x == 0) {
+  // the interchange sequence: warp 0, one pivot at a time; position c0 + k
+  // receives row g_k, which sits at a touched position or at its own.
+  // The other warps write the packed L11 \ U11 of the pivot rows meanwhile.
+  if ((tid >> 5) != 0) {
+    for (int idx = tid - 32; idx < kTsW * kTsW; idx += kTsThreads - 32) {
+      const int k = idx / kTsW, j = idx % kTsW;
+      float v = 0.f;
+      if (k < w && j < w) v = j < k ? sl[j * kTsMaxCand + sh.piv[k]] : sh.U[k][j - k];
+      lu11[idx] = v;
+    }
+  } else {
+    const int lane = tid & 31;
     int cnt = 0;
     bool bad = false;
     for (int k = 0; k < w; ++k) {
-      const int g = piv_rows[k];
-      if (g < c0) { bad = true; break; }
-      // where row g sits now: a touched position holding it, or its own
-      int q = g;
-      for (int t = 0; t < cnt; ++t)
-        if (row_s[t] == g) { q = pos_s[t]; break; }
+      const int g = srows[sh.piv[k]];
+      if (g < c0 || g >= m) { bad = true; break; }
       const int target = (int)(c0 + k);
-      ipiv[target] = (int64_t)q + 1;
-      if (q == target) continue;
-      int tt = -1, tq = -1;
-      for (int t = 0; t < cnt; ++t) {
-        if (pos_s[t] == target) tt = t;
-        if (pos_s[t] == q) tq = t;
+      // entries lane and lane + 32 of the touched list
+      const int pa = lane < cnt ? pos_s[lane] : -1, ra = lane < cnt ? row_s[lane] : -1;
+      const int pb = lane + 32 < cnt ? pos_s[lane + 32] : -1, rb = lane + 32 < cnt ? row_s[lane + 32] : -1;
+      const unsigned ha = __ballot_sync(0xffffffffu, ra == g), hb = __ballot_sync(0xffffffffu, rb == g);
+      int q = g;
+      if (ha) q = __shfl_sync(0xffffffffu, pa, __ffs(ha) - 1);
+      else if (hb) q = __shfl_sync(0xffffffffu, pb, __ffs(hb) - 1);
+      if (lane == 0) ipiv[target] = (int64_t)q + 1;
+      if (q != target) {
+        const unsigned ta = __ballot_sync(0xffffffffu, pa == target), tb = __ballot_sync(0xffffffffu, pb == target);
+        const unsigned qa = __ballot_sync(0xffffffffu, pa == q), qb = __ballot_sync(0xffffffffu, pb == q);
+        const int tt = ta ? __ffs(ta) - 1 : (tb ? __ffs(tb) - 1 + 32 : -1);
+        const int tq = qa ? __ffs(qa) - 1 : (qb ? __ffs(qb) - 1 + 32 : -1);
+        // the row now at the target position (the one g displaces)
+        const int rta = __shfl_sync(0xffffffffu, ra, tt & 31), rtb = __shfl_sync(0xffffffffu, rb, tt & 31);
+        const int rt = tt < 0 ? target : (tt < 32 ? rta : rtb);
+        if (lane == 0) {
+          int c2 = cnt, t1 = tt, t2 = tq;
+          if (t1 < 0) { t1 = c2++; pos_s[t1] = target; }
+          row_s[t1] = g;
+          if (t2 < 0) { t2 = c2++; pos_s[t2] = q; }
+          row_s[t2] = rt;
+          cnt = c2;
+        }
+        cnt = __shfl_sync(0xffffffffu, cnt, 0);
+        __syncwarp();
       }
-      const int row_at_target = tt >= 0 ? row_s[tt] : target;
-      if (tt < 0) { tt = cnt++; pos_s[tt] = target; }
-      row_s[tt] = g;
-      if (tq < 0) { tq = cnt++; pos_s[tq] = q; }
-      row_s[tq] = row_at_target;
     }
     if (bad) {
-      atomicCAS(&scr->error, 0, (int)DEV_BAD_PIVOT_INDEX);
+      if (lane == 0) atomicCAS(&scr->error, 0, (int)DEV_BAD_PIVOT_INDEX);
       cnt = 0;
     }
-    cnt_s = cnt;
+    if (lane == 0) cnt_s = cnt;
   }
   __syncthreads();
   const int cnt = cnt_s;
-  for (int t = threadIdx.x; t < 2 * kTsW; t += blockDim.x) {
+  for (int t = tid; t < 2 * kTsW; t += kTsThreads) {
     moves[1 + 2 * t] = t < cnt ? pos_s[t] : -1;
     moves[2 + 2 * t] = t < cnt ? row_s[t] : -1;
   }
-  if (threadIdx.x == 0) moves[0] = cnt;
-  for (int idx = threadIdx.x; idx < cnt * kTsW; idx += blockDim.x) {
+  if (tid == 0) moves[0] = cnt;
+  for (int idx = tid; idx < cnt * kTsW; idx += kTsThreads) {
     const int t = idx / kTsW, j = idx % kTsW;
     staged[idx] = j < w ? A[(int64_t)row_s[t] + (c0 + j) * lda] : 0.f;
   }
 }
 
-// 4. every panel row: L11 \ U11 on top, l = a U11^{-1} below.
-__global__ void __launch_bounds__(256)
+// 3. every panel row: L11 \ U11 on top; below, l with l U11 = a, by
+// right-looking substitution (a zero pivot, singular panel with info set,
+// divides by 1).
+constexpr int kTsApplyThreads = 128;
+__global__ void __launch_bounds__(kTsApplyThreads)
 tslu_apply_kernel(float* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w,
                   const float* __restrict__ lu11, const int32_t* __restrict__ moves,
                   const float* __restrict__ staged) {
-  __shared__ float su[kTsW][kTsW + 1];
+  __shared__ __align__(16) float su[kTsW][kTsW];  // U11, row-major, zero below the diagonal
   __shared__ float rdiag[kTsW];
   __shared__ int mdst[2 * kTsW];
   __shared__ int ncnt;
-  for (int idx = threadIdx.x; idx < kTsW * kTsW; idx += blockDim.x) su[idx / kTsW][idx % kTsW] = lu11[idx];
+  for (int idx = threadIdx.x; idx < kTsW * kTsW; idx += blockDim.x) {
+    const int i = idx / kTsW, j = idx % kTsW;
+    su[i][j] = j >= i ? lu11[idx] : 0.f;
+  }
   if (threadIdx.x == 0) ncnt = moves[0];
   __syncthreads();
   for (int t = threadIdx.x; t < 2 * kTsW; t += blockDim.x) mdst[t] = t < ncnt ? moves[1 + 2 * t] : -1;
-  if (threadIdx.x < kTsW) rdiag[threadIdx.x] = 1.0f / su[threadIdx.x][threadIdx.x];
+  if (threadIdx.x < kTsW) {
+    const float d = su[threadIdx.x][threadIdx.x];
+    rdiag[threadIdx.x] = d != 0.f ? 1.0f / d : 1.0f;
+  }
   __syncthreads();
   const int64_t p = c0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= m) return;
   if (p < c0 + w) {
     const int k = (int)(p - c0);
-    for (int j = 0; j < w; ++j) A[p + (c0 + j) * lda] = su[k][j];
+    for (int j = 0; j < w; ++j) A[p + (c0 + j) * lda] = lu11[k * kTsW + j];
     return;
   }
   int mi = -1;
@@ -265,40 +323,45 @@ tslu_apply_kernel(float* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int
   for (int j = 0; j < kTsW; ++j)
     x[j] = j < w ? (mi >= 0 ? staged[mi * kTsW + j] : A[p + (c0 + j) * lda]) : 0.f;
 #pragma unroll
-  for (int j = 0; j < kTsW; ++j) {
-    if (j >= w) break;
-    float sacc = x[j];
+  for (int i = 0; i < kTsW; ++i) {
+    x[i] *= rdiag[i];
+    const float4* r4 = reinterpret_cast<const float4*>(&su[i][0]);
 #pragma unroll
-    for (int i = 0; i < j; ++i) sacc = fmaf(-x[i], su[i][j], sacc);
-    x[j] = sacc * rdiag[j];
+    for (int j4 = 0; j4 < kTsW / 4; ++j4) {
+      if (4 * j4 + 3 <= i) continue;  // columns up to i are final
+      const float4 v = r4[j4];
+      if (4 * j4 > i) x[4 * j4] = fmaf(-x[i], v.x, x[4 * j4]);
+      if (4 * j4 + 1 > i) x[4 * j4 + 1] = fmaf(-x[i], v.y, x[4 * j4 + 1]);
+      if (4 * j4 + 2 > i) x[4 * j4 + 2] = fmaf(-x[i], v.z, x[4 * j4 + 2]);
+      x[4 * j4 + 3] = fmaf(-x[i], v.w, x[4 * j4 + 3]);
+    }
   }
 #pragma unroll
   for (int j = 0; j < kTsW; ++j)
     if (j < w) A[p + (c0 + j) * lda] = x[j];
 }
 
-size_t local_smem(int R) { return (size_t)R * (kTsW + 1) * sizeof(float) + (size_t)R * sizeof(int); }
-size_t tree_smem() { return (size_t)kTsMaxCand * (kTsW + 1) * sizeof(float) + kTsMaxCand * sizeof(int); }
+size_t select_smem() { return (size_t)kTsW * kTsMaxCand * sizeof(float) + kTsMaxCand * sizeof(int); }
 
 }  // namespace
 
 size_t tslu_work_bytes() {
   return align256(kTsMaxCand * sizeof(int32_t)) + align256((size_t)kTsMaxCand * kTsW * sizeof(float)) +
-         align256(kTsW * sizeof(int32_t)) + align256(kTsW * kTsW * sizeof(float)) +
+         align256(sizeof(unsigned)) + align256(kTsW * kTsW * sizeof(float)) +
          align256((1 + 4 * kTsW) * sizeof(int32_t)) + align256(2 * kTsW * kTsW * sizeof(float));
 }
 
 bool tslu_fits(int64_t rows, int w) {
-  // at most kTsMaxCand / kTsW chunks of at most 2 * kTsLocalThreads rows
-  return w <= kTsW && rows > 0 && rows <= (int64_t)(kTsMaxCand / kTsW) * 2 * kTsLocalThreads;
+  // at most kTsMaxChunks chunks of at most 2 * kTsThreads rows
+  return w <= kTsW && w > 0 && rows > 0 && rows <= (int64_t)kTsMaxChunks * 2 * kTsThreads;
 }
 
 void tslu_configure(int /*device*/) {
-  cudaFuncSetAttribute(tslu_local_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)local_smem(512));
-  cudaFuncSetAttribute(tslu_local_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)local_smem(1024));
-  cudaFuncSetAttribute(tslu_tree_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tree_smem());
+  cudaFuncSetAttribute(tslu_select_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)select_smem());
+  cudaFuncSetAttribute(tslu_select_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)select_smem());
 }
 
+// `work` (tslu_work_bytes(), zeroed when allocated: the ticket must start at 0)
 cudaError_t tslu_panel_launch(float* A, int64_t lda, int64_t m, int64_t c0, int w, int64_t* ipiv,
                               int64_t* info, void* work, DevScratch* scr, cudaStream_t s) {
   const int64_t M = m - c0;
@@ -308,44 +371,34 @@ cudaError_t tslu_panel_launch(float* A, int64_t lda, int64_t m, int64_t c0, int 
   c += align256(kTsMaxCand * sizeof(int32_t));
   float* cand_vals = reinterpret_cast<float*>(c);
   c += align256((size_t)kTsMaxCand * kTsW * sizeof(float));
-  int32_t* piv_rows = reinterpret_cast<int32_t*>(c);
-  c += align256(kTsW * sizeof(int32_t));
+  unsigned* ticket = reinterpret_cast<unsigned*>(c);
+  c += align256(sizeof(unsigned));
   float* lu11 = reinterpret_cast<float*>(c);
   c += align256(kTsW * kTsW * sizeof(float));
   int32_t* moves = reinterpret_cast<int32_t*>(c);
   c += align256((1 + 4 * kTsW) * sizeof(int32_t));
   float* staged = reinterpret_cast<float*>(c);
-  // chunks: at most kTsMaxCand / kTsW of them, of at least 512 rows
-  const int pmax = kTsMaxCand / kTsW;
-  int R = 512;
-  if ((M + R - 1) / R > pmax) R = (int)(((M + pmax - 1) / pmax + 31) / 32 * 32);
+  // chunks of 512 rows (one per thread), or of up to 1024 when more than
+  // kTsMaxChunks would be needed
+  int R = kTsThreads;
+  if ((M + R - 1) / R > kTsMaxChunks) R = 2 * kTsThreads;
   const int P = (int)((M + R - 1) / R);
   double fl = 0;
   for (int k = 0; k < w; ++k) fl += (double)(M - k - 1) * (1.0 + 2.0 * (w - k - 1));
   {
     LaunchScope ls(K_PANEL, fl, 2.0 * M * w * sizeof(float), s);
-    if (R <= 512)
-      tslu_local_kernel<1><<<P, kTsLocalThreads, local_smem(R), s>>>(A, lda, m, c0, w, R, cand_rows, cand_vals);
+    if (R == kTsThreads)
+      tslu_select_kernel<1><<<P, kTsThreads, select_smem(), s>>>(A, lda, m, c0, w, R, cand_rows, cand_vals, ticket,
+                                                                  lu11, moves, staged, ipiv, info, scr);
     else
-      tslu_local_kernel<2><<<P, kTsLocalThreads, local_smem(R), s>>>(A, lda, m, c0, w, R, cand_rows, cand_vals);
+      tslu_select_kernel<2><<<P, kTsThreads, select_smem(), s>>>(A, lda, m, c0, w, R, cand_rows, cand_vals, ticket,
+                                                                  lu11, moves, staged, ipiv, info, scr);
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  {
-    LaunchScope ls(K_PANEL, 0.0, (double)P * kTsW * kTsW * sizeof(float), s);
-    tslu_tree_kernel<<<1, kTsTreeThreads, tree_smem(), s>>>(P * kTsW, w, c0, cand_rows, cand_vals, piv_rows, lu11,
-                                                            info);
-  }
-  e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  {
-    LaunchScope ls(K_PANEL, 0.0, 0.0, s);
-    tslu_moves_kernel<<<1, 64, 0, s>>>(A, lda, c0, w, piv_rows, ipiv, moves, staged, scr);
-  }
-  e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
   LaunchScope ls(K_PANEL, (double)M * w * w, 2.0 * M * w * sizeof(float), s);
-  tslu_apply_kernel<<<(unsigned)((M + 255) / 256), 256, 0, s>>>(A, lda, m, c0, w, lu11, moves, staged);
+  tslu_apply_kernel<<<(unsigned)((M + kTsApplyThreads - 1) / kTsApplyThreads), kTsApplyThreads, 0, s>>>(
+      A, lda, m, c0, w, lu11, moves, staged);
   return cudaGetLastError();
 }
 

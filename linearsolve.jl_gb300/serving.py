@@ -75,6 +75,7 @@ class Server:
 
 
 GBLU_ENOTFACTORED = 5
+ONE_OFF_KEY = 1 << 62  # keys of resent requests: ONE_OFF_KEY + request index
 
 
 def run_stream(server: Server, requests, rate_hz: float, seed: int = 0, timeout_s: float = 300.0,
@@ -85,9 +86,12 @@ def run_stream(server: Server, requests, rate_hz: float, seed: int = 0, timeout_
 
     resubmit_missing: a solve-only request whose key's factorization was
     evicted completes with GBLU_ENOTFACTORED; the client sends it again with
-    the key's matrix (a factor + solve).  The completion then carries
-    "resubmitted": 1 and "client_latency_us", the time from the first
-    submission to the final completion."""
+    the matrix it was meant for (a factor + solve) under a one-off key
+    (ONE_OFF_KEY + its index), never under its own key: requests of that key
+    sent later may already carry a newer matrix, which the resent one must
+    not replace.  The completion then carries "resubmitted": 1 and
+    "client_latency_us", the time from the first submission to the final
+    completion."""
     rng = np.random.default_rng(seed)
     gaps = rng.exponential(1.0 / rate_hz, size=len(requests)) if rate_hz > 0 else np.zeros(len(requests))
     done = []
@@ -104,7 +108,7 @@ def run_stream(server: Server, requests, rate_hz: float, seed: int = 0, timeout_
                 if (resubmit_missing and d["status"] == GBLU_ENOTFACTORED and requests[i].get("A") is None
                         and not d.get("resubmitted")):
                     rq = requests[i]
-                    server.submit(i, rq["key"], rq["b"], rq["Aeff"])
+                    server.submit(i, ONE_OFF_KEY + i, rq["b"], rq["Aeff"])
                     with lock:
                         t_first.setdefault(("resub", i), True)
                     continue

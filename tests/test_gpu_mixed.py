@@ -228,8 +228,8 @@ def test_tensor_core_lu_reaches_fp64(ctx, oracle_mod, pkg, prec, mode, n):
     be = oracle_mod.backward_error(A, X, B)
     assert be <= 10 * n * EPS64, (be, st)
     assert st["fell_back"] == 0, st
-    # the 16-bit-operand factors (tournament pivoting for leaves taller than
-    # 512 rows) factor A: P A = L U up to the 16-bit operand rounding
+    # the 16-bit-operand factors (TRSM base blocks through cached inverses)
+    # factor A: P A = L U up to the 16-bit operand rounding
     _check_factorization(A, f.factors(), f.ipiv(), 0.05)
     f.close()
 
@@ -250,11 +250,11 @@ def _check_factorization(A, F, ipiv, tol):
     return err
 
 
-def _factor_error(ctx, monkeypatch, A, prec, panel):
-    monkeypatch.setenv("GBLU_PANEL", panel)  # read when the factor is created
+def _factor_error(ctx, monkeypatch, A, prec, panel, env="GBLU_PANEL"):
+    monkeypatch.setenv(env, panel)  # read when the factor is created
     n = A.shape[0]
     f = ctx.factor(n, n, prec)
-    monkeypatch.delenv("GBLU_PANEL")
+    monkeypatch.delenv(env)
     assert f.getrf(A) == 0
     F, ipiv = f.factors(), f.ipiv()
     f.close()
@@ -290,7 +290,9 @@ def test_tournament_panel_factors_and_refines(ctx, oracle_mod, pkg, monkeypatch,
         e_p, _, _ = _factor_error(ctx, monkeypatch, A, prec, "partial")
         assert e_t < 3 * e_p + 1e-3, (e_t, e_p)
         assert lmax_t < 16.0
-        f = ctx.factor(n, n, prec)  # the default: tournament for these precisions
+        monkeypatch.setenv("GBLU_PANEL", "tournament")
+        f = ctx.factor(n, n, prec)
+        monkeypatch.delenv("GBLU_PANEL")
         assert f.getrf(A) == 0
         X, st = f.solve_refined(B, mode="gmres_ir")
         assert oracle_mod.backward_error(A, X, B) <= 10 * n * EPS64, st
@@ -319,3 +321,20 @@ def test_tensor_core_lu_ill_conditioned_gmres(ctx, oracle_mod, pkg):
     assert f.getrf(A) == 0
     X, st = f.solve_refined(B, mode="gmres_ir")
     assert oracle_mod.backward_error(A, X, B) <= 10 * n * EPS64, st
+
+
+@pytest.mark.parametrize("n", [1000, 2048])
+def test_trsm_inverse_blocks(ctx, oracle_mod, pkg, monkeypatch, n):
+    """The 16-bit-operand factors solve TRSM base blocks of 65..128 rows
+    through cached inverses of L's diagonal blocks: factors as accurate as
+    with the substitution chain (GBLU_TRSM=exact), for power-of-two and
+    uneven recursion splits, and refinement reaches the FP64 bound."""
+    A, B = pkg.workloads.plain(n, 2, seed=90 + n)
+    e_inv, _, ipiv_inv = _factor_error(ctx, monkeypatch, A, "bf16", "default", env="GBLU_TRSM")
+    e_chain, _, ipiv_chain = _factor_error(ctx, monkeypatch, A, "bf16", "exact", env="GBLU_TRSM")
+    assert e_inv < 2 * e_chain + 1e-3, (e_inv, e_chain)
+    f = ctx.factor(n, n, "bf16")
+    assert f.getrf(A) == 0
+    X, st = f.solve_refined(B, mode="gmres_ir")
+    assert oracle_mod.backward_error(A, X, B) <= 10 * n * EPS64, st
+    f.close()

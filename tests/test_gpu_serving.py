@@ -199,3 +199,26 @@ def test_admission_waits_for_memory(ctx, pkg):
     assert all(done[i]["status"] == 0 for i in range(3))
     assert st["evictions"] >= 2 and st["admission_waits"] >= 1
     assert st["resident_bytes"] <= one + one // 2
+
+
+def test_resent_request_keeps_key_matrix(ctx, pkg, oracle_mod):
+    """A solve on an evicted key is sent again with the matrix it was meant
+    for, under a one-off key: a newer matrix of that key, already queued,
+    stays the key's matrix for the requests after it.  Budget: one n = 700
+    FP32 factorization."""
+    from importlib import import_module
+    serving = import_module(pkg.__name__ + ".serving")
+    rng = np.random.default_rng(15)
+    n = 700
+    one = 704 * n * 4 + 704 * n * 8 + 64 * n * 8 + (1 << 20)
+    A1, A2, B1 = (pkg.workloads.shifted(n, 1, seed=40 + i)[0] for i in range(3))
+    plan = [(0, A1, A1), (1, B1, B1), (0, None, A1), (0, A2, A2), (0, None, A2), (0, None, A2)]
+    reqs = [{"key": k, "A": A, "b": rng.standard_normal(n), "Aeff": Ae} for k, A, Ae in plan]
+    srv = serving.Server(ctx, workers=1, precision="fp32", hbm_budget_bytes=one + one // 2)
+    done, _ = serving.run_stream(srv, reqs, rate_hz=0.0, resubmit_missing=True, timeout_s=120)
+    srv.close()
+    assert len(done) == len(reqs)
+    for d in done:
+        assert d["status"] == 0, d
+        r = reqs[d["tag"]]
+        assert oracle_mod.backward_error(r["Aeff"], d["x"], r["b"]) <= 10 * n * EPS64, d["tag"]
