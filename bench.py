@@ -946,7 +946,7 @@ def run_serving_suite(pkg, cu, ctx, args):
            "new_A_fraction": float(np.mean([r["A"] is not None for r in reqs])),
            "precision": "fp32 factors + FP64 IR (fast inner solve); n <= 256 on the batched lane",
            "target": "p99 <= 35 ms at 400 Hz, backward error <= 10 n eps64", "rates": []}
-    runs = [(r, 120 << 30) for r in args.serve_rates] + [(400.0, args.serve_small_budget_gb << 30)]
+    runs = [(r, 120 << 30) for r in args.serve_rates] + [(400.0, int(args.serve_small_budget_gb * 2 ** 30))]
     for rate, budget in runs:
         srv = serving.Server(ctx, workers=4, precision="fp32", hbm_budget_bytes=budget)
         small = budget < (120 << 30)
@@ -976,7 +976,7 @@ def run_serving_suite(pkg, cu, ctx, args):
     return out
 
 
-KERNEL_CASES = ("gemm_bf16", "gemm_fp16", "gemm_fp32", "refine", "perm", "mixed_bf16", "step_fp64")
+KERNEL_CASES = ("gemm_bf16", "gemm_fp16", "gemm_fp32", "refine", "perm", "mixed_bf16", "step_fp64", "helpers")
 
 
 def run_kernel_case(args) -> int:
@@ -992,7 +992,14 @@ def run_kernel_case(args) -> int:
                              (upload_ipiv_check_kernel, perm_from_ipiv_kernel)
       mixed_bf16             the mixed suite's BF16 solve set, n = 16384, 4 RHS, run twice
                              (launch lists: every kernel of getrf + refined solve)
-      step_fp64              two steps of the headline workload (n = 8192, 1 getrf + 16 getrs)"""
+      step_fp64              two steps of the headline workload (n = 8192, 1 getrf + 16 getrs)
+      helpers                n = 6144: BF16 factor (trsm_inv / trsm_inv_apply, prepare and
+                             its reduction, diag_inverse of the fast solve) with a GMRES-IR
+                             solve (gmres_begin / step / scale / finish); the same factor
+                             with tournament pivoting (tslu_select / tslu_apply); an FP64
+                             factor's device residual check (sumsq_partial / final); an
+                             FP64 n = 4096 factor on the shared-memory cluster panel
+                             (panel_cluster_kernel, forced with GBLU_PANEL=cluster)"""
     pkg = load_pkg()
     _, _, local = dist_env()
     ctx = pkg.Context(local)
@@ -1029,6 +1036,30 @@ def run_kernel_case(args) -> int:
             f.getrf(dA)
             f.solve_refined(dB)
         f.close()
+    elif case == "helpers":
+        n = 6144
+        A, B = pkg.workloads.shifted(n, 4, seed=6)
+        f = ctx.factor(n, n, "bf16")
+        f.getrf(A)
+        f.solve_refined(B, mode="gmres_ir")
+        f.close()
+        os.environ["GBLU_PANEL"] = "tournament"  # read when the factor is created
+        f = ctx.factor(n, n, "bf16")
+        del os.environ["GBLU_PANEL"]
+        f.getrf(A)
+        f.close()
+        g = ctx.factor(n, n, "fp64")
+        g.keep_matrix(True)
+        g.getrf(A)
+        X = g.getrs(B)
+        g.residual_norm(X, B)
+        g.close()
+        os.environ["GBLU_PANEL"] = "cluster"  # read at each getrf
+        A2, _ = pkg.workloads.plain(4096, 1, seed=7)
+        g = ctx.factor(4096, 4096, "fp64")
+        g.getrf(A2)
+        g.close()
+        del os.environ["GBLU_PANEL"]
     elif case == "step_fp64":
         n, nrhs = args.n, args.nrhs
         A, B = pkg.workloads.plain(n, nrhs, seed=0)
@@ -1057,15 +1088,16 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--suite", default="auto",
-                    help="comma list of mixed,mixed_hard,batched,serving (or all); '' for none; "
-                         "auto = mixed,batched,serving on one GPU, none on several")
+                    help="comma list of config1,mixed,mixed_hard,batched,serving (or all); '' for none; "
+                         "auto = all of them on one GPU; none on several (the batched workload is then "
+                         "sharded across the ranks instead)")
     ap.add_argument("--batch-count", type=int, default=20000)
     ap.add_argument("--only-suite", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=1000)
     ap.add_argument("--mixed-n", type=int, default=16384)
     ap.add_argument("--serve-rates", type=float, nargs="*", default=[100.0, 400.0, 0.0])
     ap.add_argument("--serve-keys", type=int, default=300)
-    ap.add_argument("--serve-small-budget-gb", type=int, default=4)
+    ap.add_argument("--serve-small-budget-gb", type=float, default=1.0)
     ap.add_argument("--kernel-case", choices=KERNEL_CASES, default=None,
                     help="run one small case of a kernel group once (for ncu) and exit")
     args = ap.parse_args()
