@@ -199,6 +199,37 @@ __device__ __forceinline__ void div_markstein_n(T (&a)[N], T b, T y) {
   for (int i = 0; i < N; ++i) a[i] = res[i];
 }
 
+// IEEE 754 binary64 -> binary32 with round-to-nearest-even, on integer
+// operations only (the FP64 pipe of this GPU retires two lanes per cycle per
+// SM, so a conversion there costs as much as an FP64 FMA).  The standard's
+// narrowing: keep 23 of the 52 fraction bits and round on the other 29
+// (ties to even; a carry out of the fraction increments the exponent, and
+// past the largest finite value gives infinity); results below the normal
+// range are denormalised from the full 53-bit significand; NaN stays NaN
+// (quiet, upper payload bits kept).  Checked bitwise against the hardware
+// conversion by gblu_tool_cvtcheck.
+__device__ __forceinline__ float f64_to_f32_rn(double d) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(d);
+  const unsigned sign = (unsigned)(u >> 32) & 0x80000000u;
+  const int e = (int)((u >> 52) & 0x7FF);
+  const unsigned long long m = u & 0xFFFFFFFFFFFFFull;
+  if (e == 0x7FF) return __uint_as_float(sign | 0x7F800000u | (m ? 0x00400000u | (unsigned)(m >> 29) : 0u));
+  const int fe = e - 1023 + 127;
+  if (fe >= 0xFF) return __uint_as_float(sign | 0x7F800000u);
+  if (fe <= 0) {
+    const int shift = 926 - e;  // value = (2^52 + m) 2^(e - 1075) = f 2^-149
+    if (e == 0 || shift > 54) return __uint_as_float(sign);
+    const unsigned long long M = m | (1ull << 52);
+    const unsigned long long f = M >> shift, rem = M & ((1ull << shift) - 1), half = 1ull << (shift - 1);
+    const unsigned r = (unsigned)f + ((rem > half || (rem == half && (f & 1ull))) ? 1u : 0u);
+    return __uint_as_float(sign | r);
+  }
+  const unsigned long long f = m >> 29, rem = m & 0x1FFFFFFFull;
+  unsigned bits = ((unsigned)fe << 23) | (unsigned)f;
+  bits += (rem > 0x10000000ull || (rem == 0x10000000ull && (f & 1ull))) ? 1u : 0u;
+  return __uint_as_float(sign | bits);
+}
+
 template <typename T>
 __device__ __forceinline__ T ldcg(const T* p) { return __ldcg(p); }
 template <typename T>

@@ -55,7 +55,9 @@ __device__ __forceinline__ void block_max_into(double v, unsigned long long* p) 
 // chunks, j ascending), and max |A_ij| into *amax.  A CTA covers 1024
 // consecutive rows (4 per thread, 8 KB of a column per step) of one chunk,
 // so every column step is one long contiguous read; prepare_reduce_kernel
-// adds the chunks in index order.
+// adds the chunks in index order.  Only the row sums use the FP64 pipe: the
+// conversion, |a| and the maximum (over the bit patterns of |a|, which order
+// like the values, NaN above infinity) run on the integer pipe.
 constexpr int kPrepChunks = 64;
 constexpr int kPrepRows = 1024;
 
@@ -66,7 +68,8 @@ prepare_kernel(int64_t n, const double* __restrict__ A, int64_t lda, float* __re
   const int64_t cs = (n + kPrepChunks - 1) / kPrepChunks;
   const int64_t j0 = s * cs, j1 = min(n, j0 + cs);
   const int64_t i0 = (int64_t)blockIdx.x * kPrepRows + threadIdx.x;
-  double acc[4] = {0.0, 0.0, 0.0, 0.0}, mx = 0.0;
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  long long mxb = 0;  // bits of the largest |a| so far
   bool ok[4];
 #pragma unroll
   for (int r = 0; r < 4; ++r) ok[r] = i0 + 256 * r < n;
@@ -79,16 +82,16 @@ prepare_kernel(int64_t n, const double* __restrict__ A, int64_t lda, float* __re
     for (int r = 0; r < 4; ++r) v[r] = ok[r] ? a[256 * r] : 0.0;
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
-      if (ok[r]) b[256 * r] = (float)v[r];
-      const double av = fabs(v[r]);
-      acc[r] += av;
-      mx = (av > mx || isnan(av)) ? av : mx;
+      if (ok[r]) b[256 * r] = f64_to_f32_rn(v[r]);
+      const long long ab = __double_as_longlong(v[r]) & 0x7FFFFFFFFFFFFFFFll;
+      acc[r] += __longlong_as_double(ab);
+      mxb = ab > mxb ? ab : mxb;
     }
   }
 #pragma unroll
   for (int r = 0; r < 4; ++r)
     if (ok[r]) P[(size_t)s * n + i0 + 256 * r] = acc[r];
-  block_max_into(mx, amax);
+  block_max_into(__longlong_as_double(mxb), amax);
 }
 
 // ||A||_inf = max_i sum_s P[s][i] (chunks added in index order) into *anorm.
@@ -662,6 +665,26 @@ struct Solver {
     return GBLU_OK;
   }
 
+  // The first residual, x = 0: r = b exactly (b - A 0 adds only zeros), so
+  // the product with A is skipped; |r|_inf = |b|_inf, |x|_inf = 0.
+  int32_t residual_zero_x(int W, double* rnorm, double* xnorm) {
+    GBLU_CK(ctx, cudaMemsetAsync(w.colmax, 0, w.W * sizeof(unsigned long long), s), "memset");
+    GBLU_CK(ctx, cudaMemcpyAsync(w.r, w.b, (size_t)n * W * sizeof(double), cudaMemcpyDeviceToDevice, s), "r = b");
+    { LaunchScope ls_(K_REFINE, 0.0, 0.0, s);
+    colmax_kernel<<<grid_for(n), 256, 0, s>>>(n, W, w.b, n, w.colmax);
+    }
+    GBLU_CK(ctx, cudaGetLastError(), "colmax");
+    std::vector<unsigned long long> bits(w.W);
+    GBLU_CK(ctx, cudaMemcpyAsync(bits.data(), w.colmax, w.W * sizeof(unsigned long long),
+                                 cudaMemcpyDeviceToHost, s), "readback");
+    GBLU_CK(ctx, cudaStreamSynchronize(s), "residual");
+    for (int q = 0; q < W; ++q) {
+      rnorm[q] = bits_to_double(bits[q]);
+      xnorm[q] = 0.0;
+    }
+    return GBLU_OK;
+  }
+
   // GMRES(m) on op(A) d = r[:,q], left-preconditioned by the FP32 LU, for the
   // columns q < nc with run[q] set, in lockstep: each inner step does one
   // nc-column matvec, one nc-column preconditioner solve and the two
@@ -826,7 +849,7 @@ int32_t refine_solve(gblu_ctx* ctx, gblu_factor* f, char trans, int64_t nrhs, do
     } else {
       GBLU_CK(ctx, cudaMemsetAsync(w.x, 0, (size_t)n * nc * sizeof(double), s), "x0");  // x0 = 0
       for (int it = 0; it <= o.max_iter; ++it) {
-        int32_t e = S.residual(nc, rn.data(), xn.data());
+        int32_t e = it == 0 ? S.residual_zero_x(nc, rn.data(), xn.data()) : S.residual(nc, rn.data(), xn.data());
         if (e) return e;
         if (it == 0) bn = rn;  // x = 0: r = b
         bool any_active = false;

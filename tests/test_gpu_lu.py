@@ -256,6 +256,22 @@ def test_markstein_division_matches_ieee():
     assert m64.value == 0 and m32.value == 0, (m64.value, m32.value)
 
 
+def test_f64_to_f32_conversion_matches_hardware():
+    """The mixed factors convert A with an integer-pipe FP64 -> FP32 narrowing
+    (round to nearest even); it must give the hardware conversion's result
+    bit for bit (2^26 doubles: every exponent, the FP32 boundaries, rounding
+    ties; NaNs by NaN-ness)."""
+    import ctypes
+    import os
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    lib = ctypes.CDLL(os.path.join(root, "linearsolve.jl_gb300", "libgblu_tools.so"))
+    lib.gblu_tool_cvtcheck.argtypes = [ctypes.c_int64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]
+    lib.gblu_tool_cvtcheck.restype = ctypes.c_int32
+    bad = ctypes.c_uint64()
+    assert lib.gblu_tool_cvtcheck(1 << 26, 777, ctypes.byref(bad)) == 0
+    assert bad.value == 0, bad.value
+
+
 @pytest.mark.parametrize("kind", ["grid", "cluster", "reg"])
 @pytest.mark.parametrize("prec", ["fp64", "fp32"])
 def test_every_panel_kernel_bit_exact(ctx, oracle_mod, monkeypatch, kind, prec):
