@@ -36,16 +36,20 @@
 namespace gblu {
 namespace tc {
 
-// 128 x 256 output tiles: each 64-deep k slice moves 48 KB from L2 for
-// 128 x 256 x 64 MMAs (a quarter less traffic per flop than 128 x 128); two
-// 256-column FP32 accumulators fill the 512 TMEM columns.
-constexpr int BM = 128, BN = 256, BK = 64, STAGES = 4, THREADS = 192;
+// Output tiles BM x BN with BN = 256 where the tiles still cover the SMs
+// (each 64-deep k slice then moves 48 KB from L2 for 128 x 256 x 64 MMAs, a
+// quarter less traffic per flop than 128 x 128; two 256-column FP32
+// accumulators fill the 512 TMEM columns), BN = 128 otherwise.
+constexpr int BM = 128, BK = 64, THREADS = 192;
 constexpr int UMMA_K = 16;
 constexpr uint32_t A_BYTES = BM * BK * 2;
-constexpr uint32_t B_BYTES = BN * BK * 2;
-constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
-constexpr uint32_t TMEM_COLS = 2 * BN;  // two accumulators: one drains while the other fills
-constexpr size_t SMEM_BYTES = (size_t)STAGES * STAGE_BYTES + 1024 + 256;
+template <int BN> struct Tile {
+  static constexpr int STAGES = BN == 256 ? 4 : 6;
+  static constexpr uint32_t B_BYTES = BN * BK * 2;
+  static constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
+  static constexpr uint32_t TMEM_COLS = 2 * BN;  // two accumulators: one drains while the other fills
+  static constexpr size_t SMEM_BYTES = (size_t)STAGES * STAGE_BYTES + 1024 + 256;
+};
 
 __device__ __forceinline__ uint32_t saddr(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -151,6 +155,7 @@ __device__ __forceinline__ uint64_t sdesc_k128(uint32_t a) {
 
 // Instruction descriptor, kind::f16: D = F32, A/B = F16 (fmt 0) or BF16 (fmt 1),
 // both K-major, N = BN, M = BM.
+template <int BN>
 __host__ __device__ constexpr uint32_t idesc_f16(uint32_t fmt) {
   return (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(BN >> 3) << 17) |
          ((uint32_t)(BM >> 4) << 24);
@@ -163,7 +168,7 @@ __host__ __device__ constexpr uint32_t idesc_f16(uint32_t fmt) {
 // tile while the epilogue warps drain the other one.
 //   full[s] / empty[s]      smem stage s loaded / consumed (ring of STAGES)
 //   tfull[b] / tempty[b]    accumulator b complete / drained (4 epilogue warps)
-template <uint32_t FMT>
+template <uint32_t FMT, int BN>
 __global__ void __launch_bounds__(THREADS, 1)
 tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                float* __restrict__ C, int64_t ldc, int M, int N, int K,
@@ -171,6 +176,8 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  constexpr int STAGES = Tile<BN>::STAGES;
+  constexpr uint32_t STAGE_BYTES = Tile<BN>::STAGE_BYTES, TMEM_COLS = Tile<BN>::TMEM_COLS;
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);
   uint64_t* full = bars;
   uint64_t* empty = bars + STAGES;
@@ -221,7 +228,7 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
     }
   } else if (warp == 1 && lane == 0) {
     // MMA issuer
-    constexpr uint32_t idesc = idesc_f16(FMT);
+    constexpr uint32_t idesc = idesc_f16<BN>(FMT);
     int it = 0, i = 0;
     bool ok = true;
     for (int t = blockIdx.x; t < tiles && ok; t += gridDim.x, ++i) {
@@ -428,8 +435,14 @@ size_t tc_work_bytes(int64_t M, int64_t N, int64_t K) {
 }
 
 void tc_configure(int /*device*/) {
-  cudaFuncSetAttribute(tc::tc_gemm_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::SMEM_BYTES);
-  cudaFuncSetAttribute(tc::tc_gemm_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::SMEM_BYTES);
+  cudaFuncSetAttribute(tc::tc_gemm_kernel<0, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)tc::Tile<128>::SMEM_BYTES);
+  cudaFuncSetAttribute(tc::tc_gemm_kernel<1, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)tc::Tile<128>::SMEM_BYTES);
+  cudaFuncSetAttribute(tc::tc_gemm_kernel<0, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)tc::Tile<256>::SMEM_BYTES);
+  cudaFuncSetAttribute(tc::tc_gemm_kernel<1, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)tc::Tile<256>::SMEM_BYTES);
 }
 
 // C (M x N, FP32, ldc) -= round16(A) (M x K, FP32 col-major, lda) * round16(B) (K x N, ldb).
@@ -472,23 +485,38 @@ cudaError_t tc_gemm_sub(int mode, int64_t M, int64_t N, int64_t K, const float* 
   }
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  CUtensorMap ta, tb;
-  if (!tc::make_map(&ta, Ah, (uint64_t)K, (uint64_t)M, (uint64_t)Kp * 2, bf16, tc::BM) ||
-      !tc::make_map(&tb, Bh, (uint64_t)K, (uint64_t)N, (uint64_t)Kp * 2, bf16, tc::BN))
-    return cudaErrorInvalidValue;
-  // persistent: at most one CTA per SM, each walking its share of the tiles
+  // 128 x 256 tiles when they still cover the SMs, else 128 x 128
   int device = 0;
   cudaGetDevice(&device);
-  const int64_t tiles = ((M + tc::BM - 1) / tc::BM) * ((N + tc::BN - 1) / tc::BN);
+  const int sms = device_info(device).num_sms;
+  const int64_t tiles_m = (M + tc::BM - 1) / tc::BM;
+  const bool wide = tiles_m * ((N + 255) / 256) >= sms;
+  const int bn = wide ? 256 : 128;
+  CUtensorMap ta, tb;
+  if (!tc::make_map(&ta, Ah, (uint64_t)K, (uint64_t)M, (uint64_t)Kp * 2, bf16, tc::BM) ||
+      !tc::make_map(&tb, Bh, (uint64_t)K, (uint64_t)N, (uint64_t)Kp * 2, bf16, (uint32_t)bn))
+    return cudaErrorInvalidValue;
+  // persistent: at most one CTA per SM, each walking its share of the tiles
+  const int64_t tiles = tiles_m * ((N + bn - 1) / bn);
   if (tiles > INT32_MAX) return cudaErrorInvalidValue;
-  dim3 grid((unsigned)std::min<int64_t>(tiles, device_info(device).num_sms));
+  dim3 grid((unsigned)std::min<int64_t>(tiles, sms));
   LaunchScope ls(K_GEMM, 2.0 * M * N * K, (2.0 * M * N + (double)(M + N) * K / 2.0) * 4.0, s);
-  if (bf16)
-    tc::tc_gemm_kernel<1><<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(ta, tb, C, ldc, (int)M, (int)N, (int)K,
-                                                                     nullptr, err);
-  else
-    tc::tc_gemm_kernel<0><<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(ta, tb, C, ldc, (int)M, (int)N, (int)K,
-                                                                     inv_scale, err);
+  const float* isc = bf16 ? nullptr : inv_scale;
+  if (wide) {
+    if (bf16)
+      tc::tc_gemm_kernel<1, 256><<<grid, tc::THREADS, tc::Tile<256>::SMEM_BYTES, s>>>(
+          ta, tb, C, ldc, (int)M, (int)N, (int)K, isc, err);
+    else
+      tc::tc_gemm_kernel<0, 256><<<grid, tc::THREADS, tc::Tile<256>::SMEM_BYTES, s>>>(
+          ta, tb, C, ldc, (int)M, (int)N, (int)K, isc, err);
+  } else {
+    if (bf16)
+      tc::tc_gemm_kernel<1, 128><<<grid, tc::THREADS, tc::Tile<128>::SMEM_BYTES, s>>>(
+          ta, tb, C, ldc, (int)M, (int)N, (int)K, isc, err);
+    else
+      tc::tc_gemm_kernel<0, 128><<<grid, tc::THREADS, tc::Tile<128>::SMEM_BYTES, s>>>(
+          ta, tb, C, ldc, (int)M, (int)N, (int)K, isc, err);
+  }
   return cudaGetLastError();
 }
 

@@ -195,7 +195,10 @@ def _fp16_scaled(B):
 
 @pytest.mark.parametrize("prec", ["bf16", "fp16", "fp32"])
 @pytest.mark.parametrize("m,n,k", [(5, 7, 3), (128, 128, 64), (129, 130, 65), (300, 200, 100),
-                                   (1000, 513, 777), (256, 384, 1024)])
+                                   (1000, 513, 777), (256, 384, 1024),
+                                   # enough 128 x 256 tiles to cover the SMs: the wide-tile kernel,
+                                   # also with ragged edges in every dimension
+                                   (4096, 2560, 192), (4001, 2600, 100)])
 def test_gemm_update_against_rounded_operands(ctx, prec, m, n, k):
     """The trailing-update contraction: C - A B with 16-bit operands and FP32
     accumulation (tcgen05), checked against float64 products of the rounded
