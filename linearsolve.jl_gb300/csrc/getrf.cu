@@ -1492,8 +1492,13 @@ struct Driver {
     if (M <= 0 || N <= 0 || K <= 0) return;
     if constexpr (std::is_same<T, float>::value) {
       // the tensor-core path costs two conversion launches besides the GEMM:
-      // updates with fewer than 256 rows or columns stay on the SIMT kernel
-      if (p.tc_mode != 0 && M >= 256 && N >= 256 && K >= 64 &&
+      // updates with fewer than 256 rows or 128 columns stay on the SIMT
+      // kernel (GBLU_TC_MIN_N overrides the column threshold)
+      static const int64_t tc_min_n = [] {
+        const char* e = getenv("GBLU_TC_MIN_N");
+        return e ? std::max<int64_t>(1, atoll(e)) : int64_t(128);
+      }();
+      if (p.tc_mode != 0 && M >= 256 && N >= tc_min_n && K >= 64 &&
           tc_work_bytes(M, N, K) <= p.tc_work_bytes) {
         check(tc_gemm_sub(p.tc_mode, M, N, K, A, lda, B, ldb, C, ldc, p.tc_work, &p.scratch->error, s));
         return;
