@@ -646,7 +646,9 @@ def run_config1_suite(pkg, cu, ctx, args):
 def run_mixed_suite(pkg, cu, ctx, args):
     """n = 16384, A = G + 4 sqrt(n) I, 4 RHS: FP32/BF16/FP16 LU + FP64 IR vs
     plain FP64 LU; the forward error of each is taken against the plain FP64
-    solution (the reference algorithm's result, bit for bit)."""
+    solution (the reference algorithm's result, bit for bit).  Variants: the
+    exact or fast correction solve, and partial pivoting or none after a
+    random butterfly transform ("rbt")."""
     n, nrhs = args.mixed_n, 4
     A, B = pkg.workloads.shifted(n, nrhs, seed=1)
     dA = pkg.DeviceMatrix.from_host(A)
@@ -654,12 +656,16 @@ def run_mixed_suite(pkg, cu, ctx, args):
     dB = pkg.DeviceMatrix(n, nrhs)
     out = {"n": n, "nrhs": nrhs, "A": "G + 4 sqrt(n) I"}
     X64 = None
-    variants = (("fp64_plain", "fp64", "exact"), ("fp32_ir", "fp32", "exact"), ("bf16_ir", "bf16", "exact"),
-                ("fp16_ir", "fp16", "exact"), ("fp32_ir_fast_solve", "fp32", "fast"),
-                ("bf16_ir_fast_solve", "bf16", "fast"), ("fp16_ir_fast_solve", "fp16", "fast"))
-    for label, prec, solve in variants:
+    variants = (("fp64_plain", "fp64", "exact", "partial"), ("fp32_ir", "fp32", "exact", "partial"),
+                ("bf16_ir", "bf16", "exact", "partial"), ("fp16_ir", "fp16", "exact", "partial"),
+                ("fp32_ir_fast_solve", "fp32", "fast", "partial"), ("bf16_ir_fast_solve", "bf16", "fast", "partial"),
+                ("fp16_ir_fast_solve", "fp16", "fast", "partial"), ("fp32_rbt_ir_fast_solve", "fp32", "fast", "rbt"),
+                ("bf16_rbt_ir_fast_solve", "bf16", "fast", "rbt"), ("fp16_rbt_ir_fast_solve", "fp16", "fast", "rbt"))
+    for label, prec, solve, pivot in variants:
         f = ctx.factor(n, n, prec)
         f.set_solve(solve)  # the low-precision correction solve (mixed factors default to fast)
+        if pivot != "partial":
+            f.set_pivoting(pivot)
         # the FP64 solve set takes seconds: one warm-up and one timed run
         ms, st, kms = _timed_solve(pkg, cu, ctx, f, dA, dB0, dB, prec, 1 if prec == "fp64" else 3,
                                    warm=1 if prec == "fp64" else 3)
@@ -671,7 +677,7 @@ def run_mixed_suite(pkg, cu, ctx, args):
                       "forward_error_vs_fp64": _forward_error(X, X64), "stats": st, "kernel_ms": kms,
                       "getrf_roofline": getrf_phase_roofline(kms, n, prec, args)}
         f.close()
-    for label, _, _ in variants[1:]:
+    for label, _, _, _ in variants[1:]:
         out["speedup_%s_vs_fp64" % label] = out[label]["solves_per_s"] / out["fp64_plain"]["solves_per_s"]
     out["bound"] = 10 * n * EPS64
     dA.free(); dB0.free(); dB.free()
@@ -717,6 +723,9 @@ def run_mixed_hard_suite(pkg, cu, ctx, args):
         f = ctx.factor(n, n, prec)
         kw = dict(kw)
         f.set_solve(kw.pop("solve", "exact"))  # the low-precision preconditioner solve
+        pivot = kw.pop("pivot", "partial")
+        if pivot != "partial":
+            f.set_pivoting(pivot)
         ms, st, kms = _timed_solve(pkg, cu, ctx, f, dA, dB0, dB, prec, 1 if prec == "fp64" else 2,
                                    mode=mode, warm=1 if prec == "fp64" else 3, **kw)
         X = dB.to_host()
@@ -976,7 +985,8 @@ def run_serving_suite(pkg, cu, ctx, args):
     return out
 
 
-KERNEL_CASES = ("gemm_bf16", "gemm_fp16", "gemm_fp32", "refine", "perm", "mixed_bf16", "step_fp64", "helpers")
+KERNEL_CASES = ("gemm_bf16", "gemm_fp16", "gemm_fp32", "refine", "perm", "mixed_bf16", "mixed_bf16_rbt",
+                "step_fp64", "helpers")
 
 
 def run_kernel_case(args) -> int:
@@ -992,6 +1002,7 @@ def run_kernel_case(args) -> int:
                              (upload_ipiv_check_kernel, perm_from_ipiv_kernel)
       mixed_bf16             the mixed suite's BF16 solve set, n = 16384, 4 RHS, run twice
                              (launch lists: every kernel of getrf + refined solve)
+      mixed_bf16_rbt         the same with no pivoting after the random butterfly transform
       step_fp64              two steps of the headline workload (n = 8192, 1 getrf + 16 getrs)
       helpers                n = 6144: BF16 factor (trsm_inv / trsm_inv_apply, prepare and
                              its reduction, diag_inverse of the fast solve) with a GMRES-IR
@@ -1025,12 +1036,14 @@ def run_kernel_case(args) -> int:
         A, B = pkg.workloads.plain(n, 1, seed=4)
         LU, ipiv, _ = pkg.dgetrf(A)
         pkg.dgetrs(LU, ipiv, B)
-    elif case == "mixed_bf16":
+    elif case in ("mixed_bf16", "mixed_bf16_rbt"):
         n = args.mixed_n
         A, B = pkg.workloads.shifted(n, 4, seed=1)
         dA = pkg.DeviceMatrix.from_host(A)
         dB = pkg.DeviceMatrix.from_host(B)
         f = ctx.factor(n, n, "bf16")
+        if case == "mixed_bf16_rbt":
+            f.set_pivoting("rbt")
         for _ in range(2):
             dB.copy_from(pkg.DeviceMatrix.from_host(B))
             f.getrf(dA)

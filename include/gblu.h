@@ -130,6 +130,26 @@ int32_t gblu_getrf(gblu_ctx* ctx, gblu_factor* f, const double* A, int64_t lda,
 #define GBLU_SOLVE_FAST 1
 int32_t gblu_factor_set_solve(gblu_ctx* ctx, gblu_factor* f, int32_t mode);
 
+/* How a mixed-precision factor (GBLU_FP32 / BF16 / FP16) pivots its
+ * low-precision LU, from the next getrf on (gblu_factor_set_pivoting).
+ * GBLU_PIVOT_PARTIAL (default): partial pivoting, the reference's order
+ *   (blocked_lufact.jl), per 32-column leaf.
+ * GBLU_PIVOT_TOURNAMENT: tournament pivoting (CALU's tall-skinny panel) for
+ *   leaves taller than 512 rows.
+ * GBLU_PIVOT_RBT: no pivoting, after a depth-2 random butterfly transform of
+ *   both sides, Ar = U^T A V / 4 (Parker 1995; Baboulin, Dongarra, Herrmann
+ *   and Tomov 2013): the leaves need no pivot search and no interchanges.
+ *   Refinement still solves the original system (residuals against the FP64
+ *   A; corrections V (LU)^-1 U^T r); the pivot-growth check and the FP64
+ *   fallback (with partial pivoting) catch a factorization the transform
+ *   did not stabilise.  Square factors with n a multiple of 4.
+ * GBLU_EUNSUPPORTED for GBLU_FP64 factors and for RBT on other shapes.
+ * No counterpart in the reference. */
+#define GBLU_PIVOT_PARTIAL 0
+#define GBLU_PIVOT_TOURNAMENT 1
+#define GBLU_PIVOT_RBT 2
+int32_t gblu_factor_set_pivoting(gblu_ctx* ctx, gblu_factor* f, int32_t mode);
+
 /* getrs: solve op(A) X = B in place for nrhs columns of B (ldb), with
  * trans = 'N' or 'T'.  For a GBLU_FP32 factor this is the refined solve
  * (gblu_solve_refined with default options), so the result is FP64-accurate.

@@ -36,6 +36,9 @@ GBLU_REFINE_GMRES = 1
 
 GBLU_SOLVE_EXACT = 0
 GBLU_SOLVE_FAST = 1
+GBLU_PIVOT_PARTIAL = 0
+GBLU_PIVOT_TOURNAMENT = 1
+GBLU_PIVOT_RBT = 2
 
 STATUS_NAMES = {
     0: "GBLU_OK", 1: "GBLU_EINVAL", 2: "GBLU_ECUDA", 3: "GBLU_ENOMEM", 4: "GBLU_ETIMEOUT",
@@ -139,6 +142,7 @@ SIGNATURES = {
     "gblu_get_growth": (_I32, [_P, _P, ctypes.POINTER(ctypes.c_double)]),
     "gblu_factor_keep_matrix": (_I32, [_P, _P, _I32]),
     "gblu_factor_set_solve": (_I32, [_P, _P, _I32]),
+    "gblu_factor_set_pivoting": (_I32, [_P, _P, _I32]),
     "gblu_residual_norm": (_I32, [_P, _P, ctypes.c_char, _I64, _P, _I64, _P, _I64, _I32,
                                   ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     "gblu_refine_opts_default": (_I32, [ctypes.POINTER(RefineOpts)]),

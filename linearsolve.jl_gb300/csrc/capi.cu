@@ -314,6 +314,7 @@ int32_t gblu_factor_create(gblu_ctx* ctx, int64_t m, int64_t n, int32_t precisio
     }
     bytes += align256(tslu_work_bytes());
     if (m == n && n > 0) bytes += align256(getrs_inverse_bytes(n, sizeof(float)));
+    if (m == n && n > 0 && n % 4 == 0) bytes += align256((size_t)4 * n * sizeof(float));  // RBT diagonals
   }
   int32_t st = ctx_alloc(ctx, bytes, &f->arena);
   if (st) {
@@ -354,6 +355,7 @@ int32_t gblu_factor_create(gblu_ctx* ctx, int64_t m, int64_t n, int32_t precisio
     {
       const char* pe = getenv("GBLU_PANEL");
       f->rf32.tslu = pe && !strcmp(pe, "tournament");
+      if (f->rf32.tslu) f->pivoting = GBLU_PIVOT_TOURNAMENT;
       f->rf32.tslu_work = c;
       c += align256(tslu_work_bytes());
     }
@@ -365,6 +367,10 @@ int32_t gblu_factor_create(gblu_ctx* ctx, int64_t m, int64_t n, int32_t precisio
       f->rs32.fast = true;
       f->rs32.inv = reinterpret_cast<float*>(c);
       c += align256(f->inv_bytes);
+    }
+    if (m == n && n > 0 && n % 4 == 0) {
+      f->rbt = reinterpret_cast<float*>(c);
+      c += align256((size_t)4 * n * sizeof(float));
     }
   }
   cudaError_t e = cudaMemsetAsync(f->arena, 0, bytes, ctx->stream);
@@ -417,6 +423,42 @@ int32_t gblu_factor_set_solve(gblu_ctx* ctx, gblu_factor* f, int32_t mode) {
   } else {
     f->rs32.fast = fast && f->inv_arena;
     f->rs32.inv = reinterpret_cast<float*>(f->inv_arena);
+  }
+  return GBLU_OK;
+}
+
+int32_t gblu_factor_set_pivoting(gblu_ctx* ctx, gblu_factor* f, int32_t mode) {
+  if (!ctx || !f) return fail(ctx, GBLU_EINVAL, "gblu_factor_set_pivoting: NULL argument");
+  if (mode != GBLU_PIVOT_PARTIAL && mode != GBLU_PIVOT_TOURNAMENT && mode != GBLU_PIVOT_RBT)
+    return fail(ctx, GBLU_EINVAL, "gblu_factor_set_pivoting: unknown mode %d", mode);
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  DeviceGuard g(ctx->device);
+  if (f->precision == GBLU_FP64) {
+    if (mode == GBLU_PIVOT_PARTIAL) return GBLU_OK;
+    return fail(ctx, GBLU_EUNSUPPORTED, "gblu_factor_set_pivoting: FP64 factors pivot partially (the reference's LU)");
+  }
+  if (mode == GBLU_PIVOT_RBT && !f->rbt)
+    return fail(ctx, GBLU_EUNSUPPORTED,
+                "gblu_factor_set_pivoting: the butterfly transform needs a square factor with n a multiple of 4 "
+                "(%lld x %lld)", (long long)f->m, (long long)f->n);
+  if (mode == GBLU_PIVOT_RBT && !f->rbt_ready) {
+    std::vector<float> h((size_t)4 * f->n);
+    rbt_fill_host(f->n, h.data());
+    CK(ctx, cudaMemcpyAsync(f->rbt, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice, ctx->stream),
+       "uploading the butterfly diagonals");
+    CK(ctx, cudaStreamSynchronize(ctx->stream), "uploading the butterfly diagonals");
+    f->rbt_ready = true;
+  }
+  if (mode != f->pivoting) {
+    f->pivoting = mode;
+    f->rf32.tslu = mode == GBLU_PIVOT_TOURNAMENT;
+    f->rf32.nopivot = mode == GBLU_PIVOT_RBT;
+    // the captured launch sequence and the factors belong to the old mode
+    if (f->getrf_exec) cudaGraphExecDestroy(f->getrf_exec);
+    f->getrf_exec = nullptr;
+    f->getrf_runs = 0;
+    f->getrf_graph_failed = false;
+    f->factored = false;
   }
   return GBLU_OK;
 }
@@ -531,8 +573,12 @@ int32_t factor_getrf(gblu_ctx* ctx, gblu_factor* f, const double* A, int64_t lda
   } else {
     st = upload_matrix(ctx, f->lu64, f->ld, A, lda, f->m, f->n, a_loc);
     if (st) return st;
-    CK(ctx, refine_prepare(f->refine, f->n, f->lu64, f->ld, f->lu32, f->ld, ctx->stream),
+    const bool rbt = f->pivoting == GBLU_PIVOT_RBT;
+    CK(ctx, refine_prepare(f->refine, f->n, f->lu64, f->ld, f->lu32, f->ld, ctx->stream, !rbt),
        "preparing mixed-precision factorization");
+    if (rbt)  // the low-precision factors are those of U^T A V / 4
+      CK(ctx, rbt_matrix_launch(f->n, f->lu64, f->ld, f->lu32, f->ld, f->rbt, ctx->stream),
+         "butterfly transform");
     CK(ctx, run_getrf(ctx, f, [&] { return getrf_launch<float>(f->rf32, ctx->stream); }),
        "launching getrf");
     CK(ctx, refine_growth_launch(f->refine, f->n, f->lu32, f->ld, ctx->stream), "pivot growth");

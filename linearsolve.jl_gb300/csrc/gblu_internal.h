@@ -83,6 +83,10 @@ struct GetrfPlan {
   // 512 rows (tslu.cu), instead of partial pivoting
   bool tslu = false;
   void* tslu_work = nullptr; // tslu_work_bytes()
+  // FP32 working matrix only: no pivoting (the random-butterfly-transformed
+  // factors): each leaf is a no-interchange getf2 of its top block and a
+  // parallel solve below it (tslu.cu), with no laswp
+  bool nopivot = false;
   // FP32 working matrix of the 16-bit-operand factors only: TRSM base blocks
   // of 65..128 rows solved through inverses of L's diagonal blocks, each
   // computed once per getrf and kept in one of these 128 x 128 slots
@@ -100,6 +104,9 @@ bool tslu_fits(int64_t rows, int w);
 void tslu_configure(int device);
 cudaError_t tslu_panel_launch(float* A, int64_t lda, int64_t m, int64_t c0, int w, int64_t* ipiv,
                               int64_t* info, void* work, DevScratch* scr, cudaStream_t s);
+// No-pivot leaf (GetrfPlan::nopivot); work: the tslu work area (its ticket).
+cudaError_t genp_panel_launch(float* A, int64_t lda, int64_t m, int64_t c0, int w, int64_t* ipiv,
+                              int64_t* info, void* work, cudaStream_t s);
 
 // FP32 SIMT update C -= A * B in the reference's per-element order (getrf.cu).
 cudaError_t simt_gemm_sub_f32(int64_t M, int64_t N, int64_t K, const float* A, int64_t lda,

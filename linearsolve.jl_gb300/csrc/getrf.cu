@@ -1418,6 +1418,11 @@ struct Driver {
     const int64_t M = p.m - c0;
     const DeviceInfo& di = device_info(device);
     if constexpr (std::is_same<T, float>::value) {
+      // random-butterfly-transformed factors: no pivot search, no interchanges
+      if (p.nopivot && p.tslu_work) {
+        check(genp_panel_launch(p.A, p.lda, p.m, c0, w, p.ipiv, p.info, p.tslu_work, s));
+        return;
+      }
       // low-precision factors: tournament pivoting for the tall leaves
       if (p.tslu && p.tslu_work && M > 512 && tslu_fits(M, w)) {
         check(tslu_panel_launch(p.A, p.lda, p.m, c0, w, p.ipiv, p.info, p.tslu_work, p.scratch, s));

@@ -70,6 +70,12 @@ struct gblu_factor {
   gblu::LaunchCounts getrf_graph_counts;  // the captured sequence's launches
   int getrf_runs = 0;
   bool getrf_graph_failed = false;
+  // low-precision pivoting of a mixed factor (GBLU_PIVOT_*); for RBT the
+  // butterflies' random diagonals (4 n floats: left then right, each R1 S1
+  // R2 S2 of n/2), filled on the first switch to RBT
+  int32_t pivoting = 0;
+  float* rbt = nullptr;
+  bool rbt_ready = false;
 };
 
 namespace gblu {

@@ -61,6 +61,7 @@ __device__ __forceinline__ void block_max_into(double v, unsigned long long* p) 
 constexpr int kPrepChunks = 64;
 constexpr int kPrepRows = 1024;
 
+template <bool WRITE>
 __global__ void __launch_bounds__(256)
 prepare_kernel(int64_t n, const double* __restrict__ A, int64_t lda, float* __restrict__ B, int64_t ldb,
                double* __restrict__ P, unsigned long long* __restrict__ amax) {
@@ -82,7 +83,7 @@ prepare_kernel(int64_t n, const double* __restrict__ A, int64_t lda, float* __re
     for (int r = 0; r < 4; ++r) v[r] = ok[r] ? a[256 * r] : 0.0;
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
-      if (ok[r]) b[256 * r] = f64_to_f32_rn(v[r]);
+      if (WRITE && ok[r]) b[256 * r] = f64_to_f32_rn(v[r]);
       const long long ab = __double_as_longlong(v[r]) & 0x7FFFFFFFFFFFFFFFll;
       acc[r] += __longlong_as_double(ab);
       mxb = ab > mxb ? ab : mxb;
@@ -92,6 +93,89 @@ prepare_kernel(int64_t n, const double* __restrict__ A, int64_t lda, float* __re
   for (int r = 0; r < 4; ++r)
     if (ok[r]) P[(size_t)s * n + i0 + 256 * r] = acc[r];
   block_max_into(__longlong_as_double(mxb), amax);
+}
+
+// ---------------------------------------------------------------------------
+// Random butterfly transform.  A butterfly of order m is B = [R S; R -S]
+// (R, S diagonal of order m/2); the depth-2 transform of one side is
+// W = B1 diag(B2a, B2b) (B1 of order n, B2a / B2b of order n/2), with the
+// 1/sqrt(2) of each level gathered into one exact 1/2.  Rows i, i + n/4,
+// i + n/2, i + 3n/4 (i < n/4) only mix with each other: an orbit.
+//   W^T v:  level 1 then level 2 of  v_i, v_{i+h} -> R_i (v_i + v_{i+h}), S_i (v_i - v_{i+h})
+//   W v:    level 2 then level 1 of  v_i, v_{i+h} -> R_i v_i + S_i v_{i+h}, R_i v_i - S_i v_{i+h}
+// The transformed matrix only feeds the low-precision factorization, so it
+// is formed in FP32 (inputs narrowed with the integer-pipe conversion).
+
+struct RbtSide {
+  const float *R1, *S1, *R2, *S2;
+  __device__ RbtSide(const float* rbt, int64_t n, int side) {
+    const float* b = rbt + (size_t)side * 2 * n;
+    R1 = b; S1 = b + n / 2; R2 = b + n; S2 = b + 3 * n / 2;
+  }
+  // x[0..3] = the orbit of a (offsets 0, n/4, n/2, 3n/4): x := W^T x (no 1/2)
+  __device__ __forceinline__ void t_form(float (&x)[4], int64_t a, int64_t h2) const {
+    const float y0 = R1[a] * (x[0] + x[2]), y2 = S1[a] * (x[0] - x[2]);
+    const float y1 = R1[a + h2] * (x[1] + x[3]), y3 = S1[a + h2] * (x[1] - x[3]);
+    x[0] = R2[a] * (y0 + y1);
+    x[1] = S2[a] * (y0 - y1);
+    x[2] = R2[h2 + a] * (y2 + y3);
+    x[3] = S2[h2 + a] * (y2 - y3);
+  }
+  // x := W x (no 1/2)
+  __device__ __forceinline__ void n_form(float (&x)[4], int64_t a, int64_t h2) const {
+    const float y0 = R2[a] * x[0] + S2[a] * x[1], y1 = R2[a] * x[0] - S2[a] * x[1];
+    const float y2 = R2[h2 + a] * x[2] + S2[h2 + a] * x[3], y3 = R2[h2 + a] * x[2] - S2[h2 + a] * x[3];
+    x[0] = R1[a] * y0 + S1[a] * y2;
+    x[2] = R1[a] * y0 - S1[a] * y2;
+    x[1] = R1[a + h2] * y1 + S1[a + h2] * y3;
+    x[3] = R1[a + h2] * y1 - S1[a + h2] * y3;
+  }
+};
+
+// B = U^T A V / 4: thread (a, b) takes the 4 x 4 block of row orbit a and
+// column orbit b.  Consecutive threads take consecutive rows (coalesced).
+__global__ void __launch_bounds__(128)
+rbt_matrix_kernel(int64_t n, const double* __restrict__ A, int64_t lda, float* __restrict__ B, int64_t ldb,
+                  const float* __restrict__ rbt) {
+  const int64_t h2 = n / 4;
+  const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
+  if (a >= h2) return;
+  const RbtSide L(rbt, n, 0), Rt(rbt, n, 1);
+  float x[4][4];  // x[i][j]: row orbit member i, column orbit member j
+#pragma unroll
+  for (int j = 0; j < 4; ++j)
+#pragma unroll
+    for (int i = 0; i < 4; ++i) x[i][j] = f64_to_f32_rn(A[(a + i * h2) + (b + j * h2) * lda]);
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {  // rows: U^T
+    float c[4] = {x[0][j], x[1][j], x[2][j], x[3][j]};
+    L.t_form(c, a, h2);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) x[i][j] = c[i];
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) Rt.t_form(x[i], b, h2);  // columns: V (A V = (V^T A^T)^T)
+#pragma unroll
+  for (int j = 0; j < 4; ++j)
+#pragma unroll
+    for (int i = 0; i < 4; ++i) B[(a + i * h2) + (b + j * h2) * ldb] = 0.25f * x[i][j];
+}
+
+// v := W^T v / 2 or W v / 2, W columns of v.
+__global__ void __launch_bounds__(256)
+rbt_vec_kernel(int64_t n, int W, float* __restrict__ v, int64_t ldv, const float* __restrict__ rbt, int side,
+               int transposed) {
+  const int64_t h2 = n / 4;
+  const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int q = blockIdx.y;
+  if (a >= h2 || q >= W) return;
+  const RbtSide S(rbt, n, side);
+  float* c = v + (size_t)q * ldv;
+  float x[4] = {c[a], c[a + h2], c[a + 2 * h2], c[a + 3 * h2]};
+  if (transposed) S.t_form(x, a, h2);
+  else S.n_form(x, a, h2);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) c[a + i * h2] = 0.5f * x[i];
 }
 
 // ||A||_inf = max_i sum_s P[s][i] (chunks added in index order) into *anorm.
@@ -539,7 +623,7 @@ double bits_to_double(unsigned long long b) {
 }  // namespace
 
 cudaError_t refine_prepare(RefineWork& w, int64_t n, const double* A, int64_t lda, float* A32,
-                           int64_t ld32, cudaStream_t s) {
+                           int64_t ld32, cudaStream_t s, bool write_f32) {
   if (n == 0) { w.anorm = 0; w.amax = 0; return cudaSuccess; }
   cudaError_t e = cudaMemsetAsync(w.growth_bits, 0, 2 * sizeof(unsigned long long), s);
   if (e != cudaSuccess) return e;
@@ -548,9 +632,12 @@ cudaError_t refine_prepare(RefineWork& w, int64_t n, const double* A, int64_t ld
   // FP32 copy, row sums of |A| and max |A| in one pass over A; then
   // ||A||_inf = max_i sum_j |A[i,j]| from the row sums
   {
-    LaunchScope ls_(K_REFINE, (double)n * n, 12.0 * n * n, s);
+    LaunchScope ls_(K_REFINE, (double)n * n, (write_f32 ? 12.0 : 8.0) * n * n, s);
     dim3 grid((unsigned)((n + kPrepRows - 1) / kPrepRows), kPrepChunks);
-    prepare_kernel<<<grid, 256, 0, s>>>(n, A, lda, A32, ld32, w.partial, w.growth_bits);
+    if (write_f32)
+      prepare_kernel<true><<<grid, 256, 0, s>>>(n, A, lda, A32, ld32, w.partial, w.growth_bits);
+    else
+      prepare_kernel<false><<<grid, 256, 0, s>>>(n, A, lda, A32, ld32, w.partial, w.growth_bits);
   }
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
@@ -568,6 +655,41 @@ cudaError_t refine_prepare(RefineWork& w, int64_t n, const double* A, int64_t ld
   w.anorm = bits_to_double(bits[0]);
   w.amax = bits_to_double(bits[1]);
   return e;
+}
+
+cudaError_t rbt_matrix_launch(int64_t n, const double* A, int64_t lda, float* B, int64_t ldb,
+                              const float* rbt, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  if (n % 4 != 0 || n / 4 > 65535) return cudaErrorInvalidValue;
+  LaunchScope ls_(K_REFINE, 32.0 * n * n / 16.0 * 2.0, 12.0 * n * n, s);
+  dim3 grid((unsigned)((n / 4 + 127) / 128), (unsigned)(n / 4));
+  rbt_matrix_kernel<<<grid, 128, 0, s>>>(n, A, lda, B, ldb, rbt);
+  return cudaGetLastError();
+}
+
+cudaError_t rbt_vec_launch(int64_t n, int W, float* v, int64_t ldv, const float* rbt, int side,
+                           bool transposed, cudaStream_t s) {
+  if (n <= 0 || W <= 0) return cudaSuccess;
+  if (n % 4 != 0 || W > 65535) return cudaErrorInvalidValue;
+  LaunchScope ls_(K_REFINE, 12.0 * n * W, 8.0 * n * W, s);
+  dim3 grid((unsigned)((n / 4 + 255) / 256), (unsigned)W);
+  rbt_vec_kernel<<<grid, 256, 0, s>>>(n, W, v, ldv, rbt, side, transposed ? 1 : 0);
+  return cudaGetLastError();
+}
+
+void rbt_fill_host(int64_t n, float* out) {
+  // splitmix64 stream from a fixed seed: the transform (and so every
+  // result) is the same on every run
+  uint64_t x = 0x5eedb077e4f1ULL;
+  for (int64_t i = 0; i < 4 * n; ++i) {
+    x += 0x9e3779b97f4a7c15ULL;
+    uint64_t z = x;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+    z ^= z >> 31;
+    const double u = (double)(z >> 11) * (1.0 / 9007199254740992.0) - 0.5;
+    out[i] = (float)std::exp(u / 10.0);
+  }
 }
 
 cudaError_t refine_growth_launch(RefineWork& w, int64_t n, const float* LU, int64_t ld, cudaStream_t s) {
@@ -635,7 +757,13 @@ struct Solver {
       scale_to_f32_kernel<<<grid_for(n * W), 256, 0, s>>>(n, W, v, ldv, dsc, w.d32, n);
     }
     GBLU_CK(ctx, cudaGetLastError(), "scale");
+    // RBT factors: d := W1^T d / 2, LU solve, d := W2 d / 2 with (W1, W2) =
+    // (U, V) for op = N and (V, U) for op = T
+    const bool rbt = f->pivoting == GBLU_PIVOT_RBT;
+    const int side_in = trans == 'N' ? 0 : 1;
+    if (rbt) GBLU_CK(ctx, rbt_vec_launch(n, W, w.d32, n, f->rbt, side_in, true, s), "butterfly");
     GBLU_CK(ctx, getrs_launch<float>(f->rs32, trans, W, w.d32, n, nullptr, s), "FP32 getrs");
+    if (rbt) GBLU_CK(ctx, rbt_vec_launch(n, W, w.d32, n, f->rbt, 1 - side_in, false, s), "butterfly");
     {
       LaunchScope ls_(K_REFINE, 0.0, 0.0, s);
       update_from_f32_kernel<<<grid_for(n * W), 256, 0, s>>>(n, W, out, ldo, w.d32, n, dsc + kMaxW, 0.0);

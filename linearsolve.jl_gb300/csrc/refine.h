@@ -52,9 +52,23 @@ constexpr int kGmStride = kGmInv + 1;
 size_t refine_bytes(int64_t n, int64_t W);
 void refine_carve(RefineWork& w, char* base, int64_t n, int64_t W);
 
-// FP64 A (ld) -> FP32 A32 (ld32), ||A||_inf and max |A_ij|, before the FP32 getrf.
+// FP64 A (ld) -> FP32 A32 (ld32), ||A||_inf and max |A_ij|, before the FP32
+// getrf; write_f32 = false computes the norms only (the RBT path writes A32).
 cudaError_t refine_prepare(RefineWork& w, int64_t n, const double* A, int64_t lda, float* A32,
-                           int64_t ld32, cudaStream_t s);
+                           int64_t ld32, cudaStream_t s, bool write_f32 = true);
+
+// Random butterfly transform (depth 2, both sides) of the mixed factors'
+// GBLU_PIVOT_RBT mode.  rbt: 4 n floats, the left then the right butterflies'
+// random diagonals, each R1 S1 R2 S2 of n/2; n a multiple of 4.
+// B (FP32, ldb) = U^T A V / 4 for the FP64 A (lda).
+cudaError_t rbt_matrix_launch(int64_t n, const double* A, int64_t lda, float* B, int64_t ldb,
+                              const float* rbt, cudaStream_t s);
+// In place on the W columns of v (FP32, ldv): side 0 = U, 1 = V; transposed:
+// v := W^T v / 2 (before the triangular solves), else v := W v / 2 (after).
+cudaError_t rbt_vec_launch(int64_t n, int W, float* v, int64_t ldv, const float* rbt, int side,
+                           bool transposed, cudaStream_t s);
+// The random diagonals (exp(u / 10), u uniform in (-1/2, 1/2), a fixed seed).
+void rbt_fill_host(int64_t n, float* out);
 
 // max |U_ij| of the FP32 factors (upper triangle of LU) into w.growth_bits[1];
 // asynchronous, read back with refine_growth after the stream synchronises.

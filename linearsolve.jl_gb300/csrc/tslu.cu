@@ -341,7 +341,96 @@ tslu_apply_kernel(float* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int
     if (j < w) A[p + (c0 + j) * lda] = x[j];
 }
 
+// ---------------------------------------------------------------------------
+// No-pivot leaf of the random-butterfly-transformed factors: the top w x w
+// block is factored without interchanges by warp 0 of every CTA (the same
+// arithmetic everywhere, from the values before any CTA writes; lane i holds
+// row i in registers, rotating one register per column, and the finished row
+// is broadcast with shuffles), then each CTA solves l U11 = a for its 128 rows
+// below the block by right-looking substitution; the last CTA to finish
+// writes the top block back, the identity interchanges, and info for an
+// exactly zero pivot (whose column is then left unscaled, as LAPACK's getf2
+// does).
+constexpr int kGenpRows = 128;
+__global__ void __launch_bounds__(kGenpRows)
+genp_panel_kernel(float* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int w, int64_t* __restrict__ ipiv,
+                  int64_t* __restrict__ info, unsigned* __restrict__ ticket) {
+  __shared__ float U[kTsW][kTsW + 1];   // U[i][j], j >= i
+  __shared__ float Lm[kTsW][kTsW + 1];  // multipliers L[i][j], i > j
+  __shared__ float rdiag[kTsW];
+  __shared__ int zcol;
+  __shared__ bool last_s;
+  const int tid = threadIdx.x;
+  if (tid < 32) {
+    const int i = tid;
+    float r[kTsW];
+#pragma unroll
+    for (int j = 0; j < kTsW; ++j) r[j] = (i < w && j < w) ? A[(c0 + i) + (c0 + j) * lda] : 0.f;
+    int zc = -1;
+#pragma unroll 1
+    for (int k = 0; k < w; ++k) {
+      float u[kTsW];  // row k, columns k, k+1, ... (final)
+#pragma unroll
+      for (int j = 0; j < kTsW; ++j) u[j] = __shfl_sync(0xffffffffu, r[j], k);
+      if (i == k) {
+#pragma unroll
+        for (int j = 0; j < kTsW; ++j)
+          if (k + j < kTsW) U[k][k + j] = r[j];
+      }
+      if (u[0] == 0.f && zc < 0) zc = k;
+      const float rp = u[0] != 0.f ? 1.0f / u[0] : 1.0f;
+      if (i > k && i < w) {
+        const float l = r[0] * rp;
+        Lm[i][k] = l;
+#pragma unroll
+        for (int j = 0; j < kTsW - 1; ++j) r[j] = fmaf(-l, u[j + 1], r[j + 1]);
+        r[kTsW - 1] = 0.f;
+      }
+    }
+    if (i == 0) zcol = zc;
+  }
+  __syncthreads();
+  if (tid < w) rdiag[tid] = U[tid][tid] != 0.f ? 1.0f / U[tid][tid] : 1.0f;
+  __syncthreads();
+  const int64_t p = c0 + w + (int64_t)blockIdx.x * kGenpRows + tid;
+  if (p < m) {
+    float x[kTsW];
+#pragma unroll
+    for (int j = 0; j < kTsW; ++j) x[j] = j < w ? A[p + (c0 + j) * lda] : 0.f;
+#pragma unroll
+    for (int i = 0; i < kTsW; ++i) {
+      if (i >= w) break;
+      x[i] *= rdiag[i];
+#pragma unroll
+      for (int j = i + 1; j < kTsW; ++j) x[j] = fmaf(-x[i], U[i][j], x[j]);
+    }
+#pragma unroll
+    for (int j = 0; j < kTsW; ++j)
+      if (j < w) A[p + (c0 + j) * lda] = x[j];
+  }
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) last_s = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last_s) return;
+  __threadfence();
+  for (int idx = tid; idx < w * w; idx += kGenpRows) {
+    const int j = idx / w, i = idx % w;
+    A[(c0 + i) + (c0 + j) * lda] = j >= i ? U[i][j] : Lm[i][j];
+  }
+  if (tid < w) ipiv[c0 + tid] = c0 + tid + 1;
+  if (tid == 0) {
+    if (zcol >= 0) atomicCAS(reinterpret_cast<unsigned long long*>(info), 0ull, (unsigned long long)(c0 + zcol + 1));
+    *ticket = 0u;  // ready for the next leaf
+  }
+}
+
 size_t select_smem() { return (size_t)kTsW * kTsMaxCand * sizeof(float) + kTsMaxCand * sizeof(int); }
+
+unsigned* work_ticket(void* work) {
+  return reinterpret_cast<unsigned*>(reinterpret_cast<char*>(work) + align256(kTsMaxCand * sizeof(int32_t)) +
+                                     align256((size_t)kTsMaxCand * kTsW * sizeof(float)));
+}
 
 }  // namespace
 
@@ -373,6 +462,7 @@ cudaError_t tslu_panel_launch(float* A, int64_t lda, int64_t m, int64_t c0, int 
   c += align256((size_t)kTsMaxCand * kTsW * sizeof(float));
   unsigned* ticket = reinterpret_cast<unsigned*>(c);
   c += align256(sizeof(unsigned));
+  if (ticket != work_ticket(work)) return cudaErrorInvalidValue;
   float* lu11 = reinterpret_cast<float*>(c);
   c += align256(kTsW * kTsW * sizeof(float));
   int32_t* moves = reinterpret_cast<int32_t*>(c);
@@ -399,6 +489,18 @@ cudaError_t tslu_panel_launch(float* A, int64_t lda, int64_t m, int64_t c0, int 
   LaunchScope ls(K_PANEL, (double)M * w * w, 2.0 * M * w * sizeof(float), s);
   tslu_apply_kernel<<<(unsigned)((M + kTsApplyThreads - 1) / kTsApplyThreads), kTsApplyThreads, 0, s>>>(
       A, lda, m, c0, w, lu11, moves, staged);
+  return cudaGetLastError();
+}
+
+cudaError_t genp_panel_launch(float* A, int64_t lda, int64_t m, int64_t c0, int w, int64_t* ipiv,
+                              int64_t* info, void* work, cudaStream_t s) {
+  if (w <= 0 || w > kTsW || m - c0 < w) return cudaErrorInvalidValue;
+  const int64_t below = m - c0 - w;
+  const unsigned grid = (unsigned)std::max<int64_t>(1, (below + kGenpRows - 1) / kGenpRows);
+  double fl = 0;
+  for (int k = 0; k < w; ++k) fl += (double)(m - c0 - k - 1) * (1.0 + 2.0 * (w - k - 1));
+  LaunchScope ls(K_PANEL, fl, 2.0 * (m - c0) * w * sizeof(float), s);
+  genp_panel_kernel<<<grid, kGenpRows, 0, s>>>(A, lda, m, c0, w, ipiv, info, work_ticket(work));
   return cudaGetLastError();
 }
 

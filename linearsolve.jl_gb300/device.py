@@ -187,6 +187,19 @@ class Factorization:
         check(self.lib.gblu_factor_set_solve(self.ctx.handle, self.handle, modes[mode]), self.ctx.handle)
         self.solve_mode = mode
 
+    def set_pivoting(self, mode: str = "partial") -> None:
+        """Pivoting of a mixed factor's low-precision LU from the next getrf
+        on: "partial" (default, the reference's order), "tournament" (CALU's
+        tall-skinny panel for leaves over 512 rows) or "rbt" (no pivoting after
+        a depth-2 random butterfly transform of both sides; n a multiple of
+        4).  Changing it invalidates the current factors."""
+        modes = {"partial": _lib.GBLU_PIVOT_PARTIAL, "tournament": _lib.GBLU_PIVOT_TOURNAMENT,
+                 "rbt": _lib.GBLU_PIVOT_RBT}
+        if mode not in modes:
+            raise ValueError("pivoting must be 'partial', 'tournament' or 'rbt'")
+        check(self.lib.gblu_factor_set_pivoting(self.ctx.handle, self.handle, modes[mode]), self.ctx.handle)
+        self.pivoting = mode
+
     def keep_matrix(self, keep: bool = True) -> None:
         """FP64 factors: keep a device copy of A from the next getrf on, for
         residual_norm (mixed factors keep A anyway)."""

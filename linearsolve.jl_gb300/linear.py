@@ -183,6 +183,10 @@ class GB300MixedLUFactorization(AbstractDenseFactorization):
               (src/factorization.jl:127-156), run on the device.
     solve:    the low-precision correction solve, "fast" (default) or "exact"
               (see GB300LUFactorization); refinement makes either FP64-accurate.
+    pivot:    pivoting of the low-precision LU: "partial" (default), "tournament"
+              or "rbt" (no pivoting after a random butterfly transform of both
+              sides, n a multiple of 4; the growth check and FP64 fallback
+              guard it).
 
     Unlike the reference's CUDAOffload32MixedLUFactorization
     (ext/LinearSolveCUDAExt.jl:211-242) the result is FP64-accurate."""
@@ -190,14 +194,18 @@ class GB300MixedLUFactorization(AbstractDenseFactorization):
     def __init__(self, factor: str = "fp32", refine: str = "ir", maxiters: int = 30,
                  tol: Optional[float] = None, fallback: bool = True, gmres_restart: int = 30,
                  gmres_tol: float = 1e-10, growth_limit: Optional[float] = None,
-                 residualsafety: bool = False, solve: str = "fast", device: int = 0):
+                 residualsafety: bool = False, solve: str = "fast", pivot: str = "partial",
+                 device: int = 0):
         if factor not in ("fp32", "bf16", "fp16"):
             raise ValueError(f"unsupported factor precision {factor!r}")
         if refine not in ("ir", "gmres_ir"):
             raise ValueError("refine must be 'ir' or 'gmres_ir'")
         if solve not in ("exact", "fast"):
             raise ValueError("solve must be 'exact' or 'fast'")
+        if pivot not in ("partial", "tournament", "rbt"):
+            raise ValueError("pivot must be 'partial', 'tournament' or 'rbt'")
         self.solve = solve
+        self.pivot = pivot
         self.precision = factor
         self.refine = refine
         self.maxiters = int(maxiters)
@@ -375,6 +383,8 @@ def init(prob: LinearProblem, alg=None, alias: Optional[LinearAliasSpecifier] = 
     fact = ctx.factor(m, n, alg.factor_precision())
     if m == n:
         fact.set_solve(alg.solve)
+    if isinstance(alg, GB300MixedLUFactorization) and alg.pivot != "partial":
+        fact.set_pivoting(alg.pivot)
     if alg.residualsafety:
         fact.keep_matrix(True)  # the FP64 copy of A the residual check reads (A_backup)
     cache.cacheval = RFLUCacheval(fact) if isinstance(alg, GB300RFLUFactorization) else fact

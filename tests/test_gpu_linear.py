@@ -251,3 +251,20 @@ def test_default_safety_fallback_reports_failure(pkg):
     b = np.ones(n)
     sol = pkg.solve(pkg.LinearProblem(A, b))
     assert sol.retcode == pkg.ReturnCode.Failure
+
+
+def test_mixed_rbt_through_the_interface(pkg, oracle_mod):
+    """GB300MixedLUFactorization(pivot="rbt") through init / solve!: the
+    factor is created with the butterfly transform; A then b changes keep
+    the FP64 bound."""
+    n = 512
+    A, B = pkg.workloads.shifted(n, 2, seed=77)
+    alg = pkg.GB300MixedLUFactorization(factor="bf16", pivot="rbt")
+    cache = pkg.init(pkg.LinearProblem(A, B[:, 0].copy()), alg)
+    sol = pkg.solve_bang(cache)
+    assert sol.retcode == pkg.ReturnCode.Success
+    assert oracle_mod.backward_error(A, sol.u, B[:, 0]) <= 10 * n * EPS64
+    assert cache.cacheval.pivoting == "rbt"
+    cache.b = B[:, 1].copy()
+    sol = pkg.solve_bang(cache)
+    assert oracle_mod.backward_error(A, sol.u, B[:, 1]) <= 10 * n * EPS64

@@ -341,3 +341,137 @@ def test_trsm_inverse_blocks(ctx, oracle_mod, pkg, monkeypatch, n):
     X, st = f.solve_refined(B, mode="gmres_ir")
     assert oracle_mod.backward_error(A, X, B) <= 10 * n * EPS64, st
     f.close()
+
+
+def _rbt_diagonals(n):
+    """The butterflies' random diagonals as the library draws them: a
+    splitmix64 stream from a fixed seed, exp(u / 10) with u uniform in
+    (-1/2, 1/2), rounded to FP32; left then right, each R1 S1 R2 S2 of n/2."""
+    mask = (1 << 64) - 1
+    x = 0x5eedb077e4f1
+    out = np.empty(4 * n, dtype=np.float32)
+    for i in range(4 * n):
+        x = (x + 0x9e3779b97f4a7c15) & mask
+        z = x
+        z = ((z ^ (z >> 30)) * 0xbf58476d1ce4e5b9) & mask
+        z = ((z ^ (z >> 27)) * 0x94d049bb133111eb) & mask
+        z ^= z >> 31
+        u = (z >> 11) * (1.0 / 9007199254740992.0) - 0.5
+        out[i] = np.float32(np.exp(u / 10.0))
+    return out
+
+
+def _rbt_matrices(n):
+    d = _rbt_diagonals(n).astype(np.float64)
+    h1, h2 = n // 2, n // 4
+
+    def butterfly(R, S):
+        m = 2 * len(R)
+        B = np.zeros((m, m))
+        B[:m // 2, :m // 2] = np.diag(R)
+        B[:m // 2, m // 2:] = np.diag(S)
+        B[m // 2:, :m // 2] = np.diag(R)
+        B[m // 2:, m // 2:] = -np.diag(S)
+        return B
+
+    Ws = []
+    for side in (0, 1):
+        b = d[side * 2 * n:(side + 1) * 2 * n]
+        R1, S1, R2, S2 = b[:h1], b[h1:n], b[n:n + h1], b[n + h1:]
+        B2 = np.zeros((n, n))
+        B2[:h1, :h1] = butterfly(R2[:h2], S2[:h2])
+        B2[h1:, h1:] = butterfly(R2[h2:], S2[h2:])
+        Ws.append(butterfly(R1, S1) @ B2)
+    return Ws
+
+
+@pytest.mark.parametrize("prec", ["fp32", "bf16", "fp16"])
+@pytest.mark.parametrize("n", [256, 1000])
+def test_rbt_factors_the_transformed_matrix(ctx, oracle_mod, pkg, prec, n):
+    """GBLU_PIVOT_RBT: the low-precision LU is that of U^T A V / 4 (the
+    butterflies rebuilt here from the library's seeded diagonals), without
+    interchanges, and refinement reaches the FP64 bound without fallback."""
+    # A = G + 4 sqrt(n) I: the transform keeps the growth near 1 (GENP on a
+    # plain Gaussian matrix meets small pivots whatever the randomisation)
+    A, B = pkg.workloads.shifted(n, 3, seed=300 + n)
+    f = ctx.factor(n, n, prec)
+    f.set_pivoting("rbt")
+    assert f.getrf(A) == 0
+    WL, WR = _rbt_matrices(n)
+    Ar = WL.T @ A @ WR / 4
+    F = f.factors()
+    L = np.tril(F, -1) + np.eye(n)
+    U = np.triu(F)
+    assert np.array_equal(f.ipiv(), np.arange(1, n + 1))
+    err = np.abs(Ar - L @ U).max() / np.abs(Ar).max()
+    assert err < {"fp32": 1e-4, "bf16": 0.1, "fp16": 0.02}[prec], err
+    X, st = f.solve_refined(B, mode="ir")
+    assert oracle_mod.backward_error(A, X, B) <= 10 * n * EPS64, st
+    assert st["fell_back"] == 0, st
+    Xt, st = f.solve_refined(B, trans="T", mode="gmres_ir")
+    assert oracle_mod.backward_error(A.T, Xt, B) <= 10 * n * EPS64, st
+    assert st["fell_back"] == 0, st
+    f.close()
+
+
+def test_rbt_plain_gaussian_gmres(ctx, oracle_mod, pkg):
+    """A plain Gaussian matrix: no pivoting meets small pivots (growth in the
+    thousands, measured on the host for this construction); FP32 GMRES-IR
+    still reaches the FP64 bound, and the growth is reported."""
+    n = 1000
+    A, B = pkg.workloads.plain(n, 2, seed=1300)
+    f = ctx.factor(n, n, "fp32")
+    f.set_pivoting("rbt")
+    assert f.getrf(A) == 0
+    X, st = f.solve_refined(B, mode="gmres_ir")
+    assert oracle_mod.backward_error(A, X, B) <= 10 * n * EPS64, st
+    assert st["growth"] > 10, st
+    f.close()
+
+
+def test_rbt_kappa_1e6_n4096(ctx, oracle_mod, kappa_1e6_n4096):
+    """The κ = 1e6 matrix, FP32 LU without pivoting after the transform,
+    GMRES-IR: the no-pivot factors (growth in the hundreds here) are too weak
+    a preconditioner for this conditioning, refinement stalls and the FP64
+    fallback delivers the FP64 bound."""
+    A, B = kappa_1e6_n4096
+    n = A.shape[0]
+    f = ctx.factor(n, n, "fp32")
+    f.set_pivoting("rbt")
+    assert f.getrf(A) == 0
+    X, st = f.solve_refined(B, mode="gmres_ir")
+    assert oracle_mod.backward_error(A, X, B) <= 10 * n * EPS64, st
+    assert st["growth"] > 10, st
+    f.close()
+
+
+def test_rbt_mode_switches_and_graph_replay(ctx, oracle_mod, pkg):
+    """Switching the pivoting invalidates the factors (solves report
+    GBLU_ENOTFACTORED until the next getrf); repeated RBT getrfs (replayed
+    from the captured launch sequence from the third on) stay correct, and so
+    does partial pivoting after switching back."""
+    n = 768
+    f = ctx.factor(n, n, "bf16")
+    for mode in ("rbt", "partial", "rbt"):
+        f.set_pivoting(mode)
+        with pytest.raises(pkg.GBLUError):
+            f.solve_refined(np.ones((n, 1)))
+        for rep in range(4):
+            A, B = pkg.workloads.shifted(n, 2, seed=500 + rep)
+            assert f.getrf(A) == 0
+            X, st = f.solve_refined(B)
+            assert oracle_mod.backward_error(A, X, B) <= 10 * n * EPS64, (mode, rep, st)
+            assert st["fell_back"] == 0
+    f.close()
+
+
+def test_rbt_needs_multiple_of_4(ctx, pkg):
+    f = ctx.factor(1001, 1001, "bf16")
+    with pytest.raises(pkg.GBLUError):
+        f.set_pivoting("rbt")
+    f.set_pivoting("partial")
+    f.close()
+    g = ctx.factor(64, 64, "fp64")
+    with pytest.raises(pkg.GBLUError):
+        g.set_pivoting("rbt")
+    g.close()
