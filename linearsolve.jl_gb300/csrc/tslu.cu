@@ -361,6 +361,11 @@ genp_panel_kernel(float* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int
   __shared__ int zcol;
   __shared__ bool last_s;
   const int tid = threadIdx.x;
+  // this thread's row below the block, loaded while warp 0 factors the block
+  const int64_t p = c0 + w + (int64_t)blockIdx.x * kGenpRows + tid;
+  float x[kTsW];
+#pragma unroll
+  for (int j = 0; j < kTsW; ++j) x[j] = (p < m && j < w) ? A[p + (c0 + j) * lda] : 0.f;
   if (tid < 32) {
     const int i = tid;
     float r[kTsW];
@@ -392,11 +397,7 @@ genp_panel_kernel(float* __restrict__ A, int64_t lda, int64_t m, int64_t c0, int
   __syncthreads();
   if (tid < w) rdiag[tid] = U[tid][tid] != 0.f ? 1.0f / U[tid][tid] : 1.0f;
   __syncthreads();
-  const int64_t p = c0 + w + (int64_t)blockIdx.x * kGenpRows + tid;
   if (p < m) {
-    float x[kTsW];
-#pragma unroll
-    for (int j = 0; j < kTsW; ++j) x[j] = j < w ? A[p + (c0 + j) * lda] : 0.f;
 #pragma unroll
     for (int i = 0; i < kTsW; ++i) {
       if (i >= w) break;

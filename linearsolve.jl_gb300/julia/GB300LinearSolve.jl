@@ -41,6 +41,9 @@ const GBLU_FP16 = Int32(3)
 const GBLU_HOST = Int32(0)
 const GBLU_REFINE_IR = Int32(0)
 const GBLU_REFINE_GMRES = Int32(1)
+const GBLU_PIVOT_PARTIAL = Int32(0)
+const GBLU_PIVOT_TOURNAMENT = Int32(1)
+const GBLU_PIVOT_RBT = Int32(2)
 
 const libgblu_path = Ref{String}(get(ENV, "GBLU_LIBRARY",
     joinpath(@__DIR__, "..", "libgblu.so")))
@@ -52,6 +55,7 @@ function __init__()
     for s in (:gblu_create, :gblu_destroy, :gblu_last_error, :gblu_factor_create,
               :gblu_factor_destroy, :gblu_getrf, :gblu_getrs, :gblu_solve_refined,
               :gblu_refine_opts_default, :gblu_get_ipiv, :gblu_factor_keep_matrix,
+              :gblu_factor_set_pivoting,
               :gblu_residual_norm, :gblu_batch_create, :gblu_batch_solve, :gblu_batch_destroy,
               :gblu_serve_config_default, :gblu_serve_create, :gblu_serve_submit,
               :gblu_serve_poll, :gblu_serve_destroy)
@@ -132,14 +136,17 @@ GB300RFLUFactorization(; pivot = Val(true), thread = Val(true), residualsafety::
 
 """
     GB300MixedLUFactorization(; factor = :fp32, refine = :ir, maxiters = 30, tol = 0.0,
-                              fallback = true, growth_limit = 0.0, residualsafety = false)
+                              fallback = true, growth_limit = 0.0, residualsafety = false,
+                              pivot = :partial)
 
 LU in low precision on the GPU with FP64 iterative refinement (`:ir`) or
 GMRES-IR (`:gmres_ir`).  `factor = :fp32` keeps the trailing updates in FP32;
 `:bf16` / `:fp16` run them on the tensor cores with 16-bit operands.  The
 solution meets the FP64 backward-error bound: refinement that stalls, or
 factors whose pivot growth exceeds `growth_limit` (0: the library's default),
-fall back to the FP64 LU.
+fall back to the FP64 LU.  `pivot = :rbt` factors U^T A V / 4 (random
+butterflies, n a multiple of 4) without pivoting; `:tournament` uses
+tournament pivoting for tall leaves; `:partial` (default) is the reference's.
 """
 struct GB300MixedLUFactorization <: LinearSolve.AbstractDenseFactorization
     factor::Symbol
@@ -149,15 +156,19 @@ struct GB300MixedLUFactorization <: LinearSolve.AbstractDenseFactorization
     fallback::Bool
     growth_limit::Float64
     residualsafety::Bool
+    pivot::Symbol
 end
 function GB300MixedLUFactorization(; factor::Symbol = :fp32, refine::Symbol = :ir,
         maxiters::Integer = 30, tol::Real = 0.0, fallback::Bool = true,
-        growth_limit::Real = 0.0, residualsafety::Bool = false)
+        growth_limit::Real = 0.0, residualsafety::Bool = false, pivot::Symbol = :partial)
     factor in (:fp32, :bf16, :fp16) || error("factor must be :fp32, :bf16 or :fp16")
     refine in (:ir, :gmres_ir) || error("refine must be :ir or :gmres_ir")
+    pivot in (:partial, :tournament, :rbt) || error("pivot must be :partial, :tournament or :rbt")
     return GB300MixedLUFactorization(factor, refine, Int(maxiters), Float64(tol), fallback,
-                                     Float64(growth_limit), residualsafety)
+                                     Float64(growth_limit), residualsafety, pivot)
 end
+_pivot_mode(a::GB300MixedLUFactorization) =
+    a.pivot === :rbt ? GBLU_PIVOT_RBT : a.pivot === :tournament ? GBLU_PIVOT_TOURNAMENT : GBLU_PIVOT_PARTIAL
 
 const GB300Algs = Union{GB300LUFactorization, GB300RFLUFactorization, GB300MixedLUFactorization}
 
@@ -212,6 +223,10 @@ function LinearSolve.init_cacheval(alg::GB300Algs, A, b, u, Pl, Pr, maxiters::In
     if alg.residualsafety  # the FP64 copy of A the residual check reads
         _check(ccall(_syms[:gblu_factor_keep_matrix], Int32, (Ptr{Cvoid}, Ptr{Cvoid}, Int32),
                      ctx, c.factor, Int32(1)), ctx)
+    end
+    if alg isa GB300MixedLUFactorization && alg.pivot !== :partial
+        _check(ccall(_syms[:gblu_factor_set_pivoting], Int32, (Ptr{Cvoid}, Ptr{Cvoid}, Int32),
+                     ctx, c.factor, _pivot_mode(alg)), ctx)
     end
     return c
 end
