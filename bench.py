@@ -1010,7 +1010,9 @@ def run_kernel_case(args) -> int:
                              with tournament pivoting (tslu_select / tslu_apply); an FP64
                              factor's device residual check (sumsq_partial / final); an
                              FP64 n = 4096 factor on the shared-memory cluster panel
-                             (panel_cluster_kernel, forced with GBLU_PANEL=cluster)"""
+                             (panel_cluster_kernel, forced with GBLU_PANEL=cluster); a BF16
+                             factor with no pivoting after the butterfly transform
+                             (rbt_matrix, genp_panel, rbt_vec)"""
     pkg = load_pkg()
     _, _, local = dist_env()
     ctx = pkg.Context(local)
@@ -1073,6 +1075,11 @@ def run_kernel_case(args) -> int:
         g.getrf(A2)
         g.close()
         del os.environ["GBLU_PANEL"]
+        f = ctx.factor(n, n, "bf16")
+        f.set_pivoting("rbt")
+        f.getrf(A)
+        f.solve_refined(B)
+        f.close()
     elif case == "step_fp64":
         n, nrhs = args.n, args.nrhs
         A, B = pkg.workloads.plain(n, nrhs, seed=0)
