@@ -986,7 +986,7 @@ def run_serving_suite(pkg, cu, ctx, args):
 
 
 KERNEL_CASES = ("gemm_bf16", "gemm_fp16", "gemm_fp32", "refine", "perm", "mixed_bf16", "mixed_bf16_rbt",
-                "step_fp64", "helpers")
+                "step_fp64", "getrs_fast", "helpers")
 
 
 def run_kernel_case(args) -> int:
@@ -1004,6 +1004,7 @@ def run_kernel_case(args) -> int:
                              (launch lists: every kernel of getrf + refined solve)
       mixed_bf16_rbt         the same with no pivoting after the random butterfly transform
       step_fp64              two steps of the headline workload (n = 8192, 1 getrf + 16 getrs)
+      getrs_fast             the same factorization, then 8 single-RHS solves in fast mode
       helpers                n = 6144: BF16 factor (trsm_inv / trsm_inv_apply, prepare and
                              its reduction, diag_inverse of the fast solve) with a GMRES-IR
                              solve (gmres_begin / step / scale / finish); the same factor
@@ -1050,6 +1051,16 @@ def run_kernel_case(args) -> int:
             dB.copy_from(pkg.DeviceMatrix.from_host(B))
             f.getrf(dA)
             f.solve_refined(dB)
+        f.close()
+    elif case == "getrs_fast":
+        n = args.n
+        A, B = pkg.workloads.plain(n, 8, seed=0)
+        dA = pkg.DeviceMatrix.from_host(A)
+        f = ctx.factor(n, n, "fp64")
+        f.set_solve("fast")
+        f.getrf(dA)
+        for j in range(8):
+            f.getrs(pkg.DeviceMatrix.from_host(B[:, j:j + 1]))
         f.close()
     elif case == "helpers":
         n = 6144

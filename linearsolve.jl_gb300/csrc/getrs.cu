@@ -67,12 +67,33 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
+// Row stride of a staged tile: 16 bytes of padding keep every column of
+// t[c][r] 16-byte aligned (for 16-byte copies) and its reads conflict-free.
+template <typename T>
+__host__ __device__ constexpr int tile_ld() { return kTS + 16 / (int)sizeof(T); }
+
 // Issue the copies of tile element (r, c) = op(LU)[r0 + r, c0 + c] into t[c][r];
 // 'N': LU[r0+r + (c0+c)*lda] (contiguous in r), 'T': LU[c0+c + (r0+r)*lda]
-// (contiguous in c).  Elements outside nr x nc are zero-filled.
+// (contiguous in c).  Elements outside nr x nc are zero-filled.  A full 'N'
+// tile of a 16-byte-aligned matrix (vec16) moves in 16-byte copies, each
+// thread walking a fixed row slice across every (kSweepThreads / 16-byte
+// copies per column)-th column.
 template <typename T, bool TRANS>
-__device__ __forceinline__ void issue_tile(T (*t)[kTS + 1], const T* __restrict__ LU, int64_t lda,
-                                           int64_t r0, int64_t c0, int nr, int nc) {
+__device__ __forceinline__ void issue_tile(T (*t)[tile_ld<T>()], const T* __restrict__ LU, int64_t lda,
+                                           int64_t r0, int64_t c0, int nr, int nc, bool vec16) {
+  if (!TRANS && vec16 && nr == kTS && nc == kTS) {
+    constexpr int V = 16 / (int)sizeof(T);    // elements per copy
+    constexpr int CPC = kTS / V;              // copies per column
+    constexpr int CSTEP = kSweepThreads / CPC;  // columns per pass
+    const int cl = (int)threadIdx.x / CPC, rv = ((int)threadIdx.x % CPC) * V;
+    const T* src = LU + (r0 + rv) + (c0 + cl) * lda;
+#pragma unroll
+    for (int c = cl; c < kTS; c += CSTEP, src += CSTEP * lda) {
+      const unsigned d = (unsigned)__cvta_generic_to_shared(&t[c][rv]);
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+    }
+    return;
+  }
 #pragma unroll 8
   for (int idx = threadIdx.x; idx < kTS * kTS; idx += kSweepThreads) {
     const int a = idx >> 6, b = idx & 63;  // b runs along the contiguous direction
@@ -104,7 +125,9 @@ solve_sweep_kernel(int64_t n, const T* __restrict__ LU, int64_t lda, const int32
                    T* __restrict__ Out, int64_t ldo, int nrhs, int32_t* __restrict__ flags,
                    DevScratch* __restrict__ scr, const T* __restrict__ inv) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T(*tiles)[kTS][kTS + 1] = reinterpret_cast<T(*)[kTS][kTS + 1]>(smem_raw);
+  T(*tiles)[kTS][tile_ld<T>()] = reinterpret_cast<T(*)[kTS][tile_ld<T>()]>(smem_raw);
+  // 16-byte copies need a 16-byte-aligned matrix and column stride
+  const bool vec16 = ((reinterpret_cast<uintptr_t>(LU) | (uintptr_t)(lda * (int64_t)sizeof(T))) & 15) == 0;
   __shared__ T sx[kTS][NR];
   __shared__ int s_blk;
   __shared__ int s_fail;
@@ -141,13 +164,13 @@ solve_sweep_kernel(int64_t n, const T* __restrict__ LU, int64_t lda, const int32
   auto issue = [&](int t) {
     if (FAST && t == noff) {  // op(inverse of the diagonal block): tile[c][r] = op(Inv)(r, c)
       const T* ib = inv + ((int64_t)blk * 2 + (kUnit ? 0 : 1)) * (kTS * kTS);
-      issue_tile<T, TRANS>(tiles[t % kStages], ib, kTS, 0, 0, nr, nr);
+      issue_tile<T, TRANS>(tiles[t % kStages], ib, kTS, 0, 0, nr, nr, true);
       return;
     }
     const int cb = col_block(t);
     const int64_t c0 = (int64_t)cb * kTS;
     const int nc = (int)min((int64_t)kTS, n - c0);
-    issue_tile<T, TRANS>(tiles[t % kStages], LU, lda, r0, c0, nr, nc);
+    issue_tile<T, TRANS>(tiles[t % kStages], LU, lda, r0, c0, nr, nc, vec16);
   };
   // FAST: three more partial sums per right-hand side (acc is the first)
   T acc2[FAST ? 3 : 1][NR];
@@ -197,7 +220,7 @@ solve_sweep_kernel(int64_t n, const T* __restrict__ LU, int64_t lda, const int32
     cp_async_commit();
     cp_async_wait<kStages - 1>();
     __syncthreads();
-    T(*tile)[kTS + 1] = tiles[t % kStages];
+    T(*tile)[tile_ld<T>()] = tiles[t % kStages];
     if (kEarly && t == noff - 1) {
       // The tile of the block row just before this one in the sweep: its
       // rows are published one by one while that block solves its diagonal,
@@ -413,7 +436,7 @@ solve_sweep_kernel(int64_t n, const T* __restrict__ LU, int64_t lda, const int32
 }
 
 template <typename T>
-constexpr size_t sweep_smem() { return (size_t)kStages * kTS * (kTS + 1) * sizeof(T); }
+constexpr size_t sweep_smem() { return (size_t)kStages * kTS * tile_ld<T>() * sizeof(T); }
 
 // Inverses of the 64 x 64 diagonal blocks for the fast sweeps: CTA (b, 0)
 // inverts the unit-lower L_bb, CTA (b, 1) the upper U_bb; thread j computes
