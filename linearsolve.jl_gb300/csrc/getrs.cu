@@ -25,6 +25,9 @@
 namespace gblu {
 
 constexpr int kTS = kGetrsTile;  // block-row height == tile width
+// fast-solve matrices per 64-row block b, each 64 x 64 column-major:
+// InvL_bb, InvU_bb, InvL_bb L_{b,b-1}, InvU_bb U_{b,b+1}
+constexpr int kInvSlots = 4;
 
 // Wait until flags[j] != 0; returns false on timeout/abort (all threads).
 __device__ __forceinline__ bool wait_flag(const int32_t* flags, int j, DevScratch* scr) {
@@ -163,7 +166,7 @@ solve_sweep_kernel(int64_t n, const T* __restrict__ LU, int64_t lda, const int32
   auto col_block = [&](int t) -> int { return t < noff ? (FWD ? t : nblk - 1 - t) : blk; };
   auto issue = [&](int t) {
     if (FAST && t == noff) {  // op(inverse of the diagonal block): tile[c][r] = op(Inv)(r, c)
-      const T* ib = inv + ((int64_t)blk * 2 + (kUnit ? 0 : 1)) * (kTS * kTS);
+      const T* ib = inv + ((int64_t)blk * kInvSlots + (kUnit ? 0 : 1)) * (kTS * kTS);
       issue_tile<T, TRANS>(tiles[t % kStages], ib, kTS, 0, 0, nr, nr, true);
       return;
     }
@@ -435,6 +438,192 @@ solve_sweep_kernel(int64_t n, const T* __restrict__ LU, int64_t lda, const int32
   (void)flags;
 }
 
+// Fast 'N' sweeps.  Block row i's solution is x_i = d_i - M_i x_p, where x_p
+// is the block row just before it in the sweep, M_i its coupling (fold_kernel)
+// and d_i = Inv_ii (b_i - the products with every earlier block row but x_p):
+// d_i is computed while x_p is still being solved, so only the 64 x 64
+// product M_i x_p lies on the wavefront's critical path.  Two threads per
+// row, each taking half of every tile's columns with four independent
+// partial sums, combined through shared memory.  Tile order per block row:
+// the earlier off-diagonal blocks but the last (in sweep order), Inv_ii,
+// then M_i.  Backward-error accurate, not bit-exact.
+template <typename T, int NR, bool FWD>
+__global__ void __launch_bounds__(kSweepThreads)
+fast_sweep_kernel(int64_t n, const T* __restrict__ LU, int64_t lda, const int32_t* __restrict__ perm,
+                  const T* __restrict__ In, int64_t ldi, T* __restrict__ Y, int64_t ldy,
+                  T* __restrict__ Out, int64_t ldo, int nrhs, DevScratch* __restrict__ scr,
+                  const T* __restrict__ inv) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T(*tiles)[kTS][tile_ld<T>()] = reinterpret_cast<T(*)[kTS][tile_ld<T>()]>(smem_raw);
+  __shared__ T sx[kTS][NR];
+  __shared__ T part[2][kTS][NR];
+  __shared__ int s_blk;
+  const bool vec16 = ((reinterpret_cast<uintptr_t>(LU) | (uintptr_t)(lda * (int64_t)sizeof(T))) & 15) == 0;
+  const int nblk = (int)((n + kTS - 1) / kTS);
+  if (threadIdx.x == 0) {
+    const int t = (int)atomicAdd(&scr->ticket, 1u);
+    s_blk = FWD ? t : nblk - 1 - t;
+  }
+  __syncthreads();
+  const int blk = s_blk;
+  const int64_t r0 = (int64_t)blk * kTS;
+  const int nr = (int)min((int64_t)kTS, n - r0);
+  const int tid = threadIdx.x, r = tid & 63, h = tid >> 6;
+  const bool valid = r < nr;
+  const int noff = FWD ? blk : nblk - 1 - blk;  // block rows before this one in the sweep
+  const int nlead = noff > 0 ? noff - 1 : 0;    // off-diagonal tiles before the coupling
+  const int ntiles = nlead + 1 + (noff > 0 ? 1 : 0);
+  const int pcb = FWD ? blk - 1 : blk + 1;      // the coupled block row (noff > 0)
+  const int pnc = noff > 0 ? (int)min((int64_t)kTS, n - (int64_t)pcb * kTS) : 0;
+  auto col_block = [&](int t) -> int { return FWD ? t : nblk - 1 - t; };
+  auto issue = [&](int t) {
+    if (t < nlead) {
+      const int64_t c0 = (int64_t)col_block(t) * kTS;
+      issue_tile<T, false>(tiles[t % kStages], LU, lda, r0, c0, nr, (int)min((int64_t)kTS, n - c0), vec16);
+    } else {
+      const bool coupling = t > nlead;
+      const int slot = (coupling ? 2 : 0) + (FWD ? 0 : 1);
+      issue_tile<T, false>(tiles[t % kStages], inv + ((int64_t)blk * kInvSlots + slot) * (kTS * kTS), kTS, 0, 0,
+                           nr, coupling ? pnc : nr, true);
+    }
+  };
+  T a[4][NR];  // partial sums; thread h = 0 starts from the right-hand side
+#pragma unroll
+  for (int j = 0; j < 4; ++j)
+#pragma unroll
+    for (int q = 0; q < NR; ++q) a[j][q] = T(0);
+  if (h == 0 && valid)
+#pragma unroll
+    for (int q = 0; q < NR; ++q)
+      if (q < nrhs) a[0][q] = FWD ? In[(int64_t)perm[r0 + r] + q * ldi] : Y[(r0 + r) + q * ldy];
+  T d[NR];
+#pragma unroll
+  for (int q = 0; q < NR; ++q) d[q] = T(0);
+#pragma unroll
+  for (int t = 0; t < kStages - 1; ++t) {
+    if (t < ntiles) issue(t);
+    cp_async_commit();
+  }
+  // solution values of the next block needed, fetched one step ahead
+  using UB = typename SweepBits<T>::U;
+  constexpr int KP = (kTS * NR + kSweepThreads - 1) / kSweepThreads;
+  UB pre[KP];
+  auto src_of = [&](int cb, int c, int q) -> const T* {
+    const int64_t c0 = (int64_t)cb * kTS;
+    return FWD ? &Y[(c0 + c) + q * ldy] : &Out[(c0 + c) + q * ldo];
+  };
+  auto prefetch = [&](int cb) {
+    const int nc = (int)min((int64_t)kTS, n - (int64_t)cb * kTS);
+#pragma unroll
+    for (int k = 0; k < KP; ++k) {
+      const int idx = tid + k * kSweepThreads;
+      const int c = idx / NR, q = idx - c * NR;
+      pre[k] = (idx < kTS * NR && q < nrhs && c < nc) ? SweepBits<T>::load(src_of(cb, c, q)) : UB(0);
+    }
+  };
+  auto fill_sx = [&](int cb) -> int {
+    const int nc = (int)min((int64_t)kTS, n - (int64_t)cb * kTS);
+    int ok = 1;
+#pragma unroll
+    for (int k = 0; k < KP; ++k) {
+      const int idx = tid + k * kSweepThreads;
+      if (idx >= kTS * NR) continue;
+      const int c = idx / NR, q = idx - c * NR;
+      T v = T(0);
+      if (q < nrhs && c < nc) {
+        if (pre[k] != SweepBits<T>::kSentinel) v = SweepBits<T>::as_t(pre[k]);
+        else if (!poll_value(src_of(cb, c, q), scr, &v)) ok = 0;
+      }
+      sx[c][q] = v;
+    }
+    return ok;
+  };
+  // this thread's half of a tile's columns times sx, added to (sign -1) or
+  // into fresh sums (sign +1)
+  auto half_product = [&](T(*tile)[tile_ld<T>()], T(&y)[4][NR], T sign) {
+#pragma unroll 2
+    for (int c = 32 * h; c < 32 * h + 32; c += 4) {
+      const T m0 = sign * tile[c][r], m1 = sign * tile[c + 1][r], m2 = sign * tile[c + 2][r],
+              m3 = sign * tile[c + 3][r];
+#pragma unroll
+      for (int q = 0; q < NR; ++q) {
+        y[0][q] = fma(m0, sx[c][q], y[0][q]);
+        y[1][q] = fma(m1, sx[c + 1][q], y[1][q]);
+        y[2][q] = fma(m2, sx[c + 2][q], y[2][q]);
+        y[3][q] = fma(m3, sx[c + 3][q], y[3][q]);
+      }
+    }
+  };
+  if (nlead > 0) prefetch(col_block(0));
+  else if (noff > 0) prefetch(pcb);
+  for (int t = 0; t < ntiles; ++t) {
+    if (t + kStages - 1 < ntiles) issue(t + kStages - 1);
+    cp_async_commit();
+    cp_async_wait<kStages - 1>();
+    __syncthreads();
+    T(*tile)[tile_ld<T>()] = tiles[t % kStages];
+    if (t < nlead) {  // an earlier off-diagonal block: b -= L_ij x_j
+      const int ok = fill_sx(col_block(t));
+      if (!__syncthreads_and(ok)) {
+        cp_async_wait<0>();  // no copy may land after the CTA has left
+        return;
+      }
+      prefetch(t + 1 < nlead ? col_block(t + 1) : pcb);
+      half_product(tile, a, T(-1));
+      continue;
+    }
+    if (t == nlead) {  // d = Inv_ii (right-hand side so far)
+#pragma unroll
+      for (int q = 0; q < NR; ++q) part[h][r][q] = (a[0][q] + a[1][q]) + (a[2][q] + a[3][q]);
+      __syncthreads();
+      if (h == 0)
+#pragma unroll
+        for (int q = 0; q < NR; ++q) sx[r][q] = valid ? part[0][r][q] + part[1][r][q] : T(0);
+      __syncthreads();
+      T y[4][NR];
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int q = 0; q < NR; ++q) y[j][q] = T(0);
+      half_product(tile, y, T(1));
+#pragma unroll
+      for (int q = 0; q < NR; ++q) part[h][r][q] = (y[0][q] + y[1][q]) + (y[2][q] + y[3][q]);
+      __syncthreads();
+      if (h == 0)
+#pragma unroll
+        for (int q = 0; q < NR; ++q) d[q] = part[0][r][q] + part[1][r][q];
+      continue;
+    }
+    // the coupling: x = d - M_i x_p
+    const int ok = fill_sx(pcb);
+    if (!__syncthreads_and(ok)) {
+      cp_async_wait<0>();
+      return;
+    }
+    T y[4][NR];
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int q = 0; q < NR; ++q) y[j][q] = T(0);
+    half_product(tile, y, T(1));
+#pragma unroll
+    for (int q = 0; q < NR; ++q) part[h][r][q] = (y[0][q] + y[1][q]) + (y[2][q] + y[3][q]);
+    __syncthreads();
+    if (h == 0)
+#pragma unroll
+      for (int q = 0; q < NR; ++q) d[q] -= part[0][r][q] + part[1][r][q];
+  }
+  cp_async_wait<0>();
+  if (h == 0 && valid)
+#pragma unroll
+    for (int q = 0; q < NR; ++q)
+      if (q < nrhs) {
+        const T v = SweepBits<T>::canon(d[q]);
+        if (FWD) Y[(r0 + r) + q * ldy] = v;
+        else Out[(r0 + r) + q * ldo] = v;
+      }
+}
+
 template <typename T>
 constexpr size_t sweep_smem() { return (size_t)kStages * kTS * tile_ld<T>() * sizeof(T); }
 
@@ -442,7 +631,7 @@ constexpr size_t sweep_smem() { return (size_t)kStages * kTS * tile_ld<T>() * si
 // inverts the unit-lower L_bb, CTA (b, 1) the upper U_bb; thread j computes
 // column j of the inverse in registers (substitution against e_j, the block
 // in shared memory).  A ragged last block is padded with the identity.
-// Output: inv[(b * 2 + which) * 4096 + i + 64 j] = Inv(i, j).
+// Output: inv[(b * kInvSlots + which) * 4096 + i + 64 j] = Inv(i, j).
 template <typename T>
 __global__ void __launch_bounds__(kTS)
 diag_inverse_kernel(int64_t n, const T* __restrict__ LU, int64_t lda, T* __restrict__ inv) {
@@ -474,14 +663,52 @@ diag_inverse_kernel(int64_t n, const T* __restrict__ LU, int64_t lda, T* __restr
       for (int i = 0; i < k; ++i) x[i] = fma(-s[k][i], x[k], x[i]);
     }
   }
-  T* out = inv + ((int64_t)b * 2 + which) * (kTS * kTS) + (int64_t)j * kTS;
+  T* out = inv + ((int64_t)b * kInvSlots + which) * (kTS * kTS) + (int64_t)j * kTS;
 #pragma unroll
   for (int i = 0; i < kTS; ++i) out[i] = x[i];
 }
 
+// The couplings of the fast 'N' sweeps: slot 2 of block b = InvL_bb L_{b,b-1}
+// (b >= 1), slot 3 = InvU_bb U_{b,b+1} (b <= nblk - 2); zero where there is
+// no such block and outside ragged edges.  Thread (r, g): row r, columns
+// 16 g .. 16 g + 15 of the product.
+template <typename T>
+__global__ void __launch_bounds__(256)
+fold_kernel(int64_t n, const T* __restrict__ LU, int64_t lda, T* __restrict__ inv) {
+  __shared__ T sO[kTS][kTS + 1];  // sO[c][k] = O(k, c), O the off-diagonal block
+  const int b = blockIdx.x, which = blockIdx.y;
+  const int64_t nblk = (n + kTS - 1) / kTS;
+  T* out = inv + ((int64_t)b * kInvSlots + 2 + which) * (kTS * kTS);
+  const int64_t ob = which == 0 ? (int64_t)b - 1 : (int64_t)b + 1;
+  const int tid = threadIdx.x;
+  if (ob < 0 || ob >= nblk) {
+    for (int idx = tid; idx < kTS * kTS; idx += 256) out[idx] = T(0);
+    return;
+  }
+  const int64_t r0 = (int64_t)b * kTS, c0 = ob * kTS;
+  const int nb = (int)min((int64_t)kTS, n - r0), nc = (int)min((int64_t)kTS, n - c0);
+  const T* I = inv + ((int64_t)b * kInvSlots + which) * (kTS * kTS);
+  for (int idx = tid; idx < kTS * kTS; idx += 256) {
+    const int c = idx >> 6, k = idx & 63;
+    sO[c][k] = (k < nb && c < nc) ? LU[(r0 + k) + (c0 + c) * lda] : T(0);
+  }
+  __syncthreads();
+  const int r = tid & 63, g = tid >> 6;
+  T acc[16];
+#pragma unroll
+  for (int j = 0; j < 16; ++j) acc[j] = T(0);
+  for (int k = 0; k < kTS; ++k) {
+    const T a = I[r + k * kTS];  // Inv(r, k), coalesced over r
+#pragma unroll
+    for (int j = 0; j < 16; ++j) acc[j] = fma(a, sO[16 * g + j][k], acc[j]);
+  }
+#pragma unroll
+  for (int j = 0; j < 16; ++j) out[r + (int64_t)(16 * g + j) * kTS] = r < nb ? acc[j] : T(0);
+}
+
 size_t getrs_inverse_bytes(int64_t n, int elem_size) {
   const int64_t nblk = (n + kTS - 1) / kTS;
-  return (size_t)std::max<int64_t>(nblk, 1) * 2 * kTS * kTS * elem_size;
+  return (size_t)std::max<int64_t>(nblk, 1) * kInvSlots * kTS * kTS * elem_size;
 }
 
 template <typename T>
@@ -492,6 +719,10 @@ cudaError_t getrs_invert_launch(const GetrsPlan<T>& p, cudaStream_t s) {
   LaunchScope ls(K_SOLVE, (double)nblk * 2.0 * kTS * kTS * kTS / 3.0,
                  (double)nblk * 3.0 * kTS * kTS * sizeof(T), s);
   diag_inverse_kernel<T><<<dim3((unsigned)nblk, 2), kTS, 0, s>>>(p.n, p.LU, p.lda, p.inv);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  LaunchScope ls2(K_SOLVE, (double)nblk * 4.0 * kTS * kTS * kTS, (double)nblk * 6.0 * kTS * kTS * sizeof(T), s);
+  fold_kernel<T><<<dim3((unsigned)nblk, 2), 256, 0, s>>>(p.n, p.LU, p.lda, p.inv);
   return cudaGetLastError();
 }
 
@@ -534,7 +765,10 @@ cudaError_t run_chunk(const GetrsPlan<T>& p, char trans, int nr, T* B, int64_t l
   const size_t smem = sweep_smem<T>();
   {
     LaunchScope ls(K_SOLVE, sweep_flops, tri_bytes, s);
-    if (!tr)
+    if (FAST && !tr)
+      fast_sweep_kernel<T, NR, true><<<(unsigned)nblk, kSweepThreads, smem, s>>>(
+          p.n, p.LU, p.lda, p.perm, B, ldb, p.work, p.n, nullptr, 0, nr, p.scratch, p.inv);
+    else if (!tr)
       solve_sweep_kernel<T, NR, false, true, FAST><<<(unsigned)nblk, kSweepThreads, smem, s>>>(
           p.n, p.LU, p.lda, p.perm, B, ldb, p.work, p.n, nullptr, 0, nr, ffwd, p.scratch, p.inv);
     else
@@ -548,7 +782,10 @@ cudaError_t run_chunk(const GetrsPlan<T>& p, char trans, int nr, T* B, int64_t l
   e = cudaMemset2DAsync(B, ldb * sizeof(T), 0xFF, p.n * sizeof(T), nr, s);
   if (e != cudaSuccess) return e;
   LaunchScope ls(K_SOLVE, sweep_flops, tri_bytes, s);
-  if (!tr)
+  if (FAST && !tr)
+    fast_sweep_kernel<T, NR, false><<<(unsigned)nblk, kSweepThreads, smem, s>>>(
+        p.n, p.LU, p.lda, p.perm, nullptr, 0, p.work, p.n, B, ldb, nr, p.scratch, p.inv);
+  else if (!tr)
     solve_sweep_kernel<T, NR, false, false, FAST><<<(unsigned)nblk, kSweepThreads, smem, s>>>(
         p.n, p.LU, p.lda, p.perm, nullptr, 0, p.work, p.n, B, ldb, nr, fbwd, p.scratch, p.inv);
   else
@@ -571,6 +808,10 @@ void configure_nr_mode() {
   cudaFuncSetAttribute(solve_sweep_kernel<T, NR, true, true, FAST>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
   cudaFuncSetAttribute(solve_sweep_kernel<T, NR, false, false, FAST>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
   cudaFuncSetAttribute(solve_sweep_kernel<T, NR, true, false, FAST>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+  if (FAST) {
+    cudaFuncSetAttribute(fast_sweep_kernel<T, NR, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    cudaFuncSetAttribute(fast_sweep_kernel<T, NR, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+  }
 }
 
 template <typename T, int NR>
