@@ -1128,7 +1128,7 @@ def main():
     ap.add_argument("--mixed-n", type=int, default=16384)
     ap.add_argument("--serve-rates", type=float, nargs="*", default=[100.0, 400.0, 0.0])
     ap.add_argument("--serve-keys", type=int, default=300)
-    ap.add_argument("--serve-small-budget-gb", type=float, default=1.0)
+    ap.add_argument("--serve-small-budget-gb", type=float, default=0.5)
     ap.add_argument("--kernel-case", choices=KERNEL_CASES, default=None,
                     help="run one small case of a kernel group once (for ncu) and exit")
     args = ap.parse_args()
