@@ -788,15 +788,22 @@ laswp_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t m, int64_t ncols_total
   }
   const int64_t nother = ncols_total - w;
   const int warps = blockDim.x >> 5;
-  for (int64_t q = (int64_t)blockIdx.x * warps + warp; q < nother; q += (int64_t)gridDim.x * warps) {
-    const int64_t col = q < c0 ? q : q + w;
-    T* a = A + col * lda;
-    T v0 = T(0), v1 = T(0);
+  const int64_t stride = (int64_t)gridDim.x * warps;
+  // two columns per pass: all four loads in flight before the stores
+  for (int64_t q = (int64_t)blockIdx.x * warps + warp; q < nother; q += 2 * stride) {
+    const int64_t q2 = q + stride;
+    T* a = A + (q < c0 ? q : q + w) * lda;
+    T* b2 = q2 < nother ? A + (q2 < c0 ? q2 : q2 + w) * lda : nullptr;
+    T v0 = T(0), v1 = T(0), u0 = T(0), u1 = T(0);
     if (lane < nmv) v0 = a[mv_src[lane]];
     if (lane + 32 < nmv) v1 = a[mv_src[lane + 32]];
+    if (b2 && lane < nmv) u0 = b2[mv_src[lane]];
+    if (b2 && lane + 32 < nmv) u1 = b2[mv_src[lane + 32]];
     __syncwarp();
     if (lane < nmv) a[mv_dst[lane]] = v0;
     if (lane + 32 < nmv) a[mv_dst[lane + 32]] = v1;
+    if (b2 && lane < nmv) b2[mv_dst[lane]] = u0;
+    if (b2 && lane + 32 < nmv) b2[mv_dst[lane + 32]] = u1;
   }
 }
 
@@ -1486,7 +1493,14 @@ struct Driver {
   void laswp(int64_t c0, int w) {
     const DeviceInfo& di = device_info(device);
     const int64_t nother = p.n - w;
-    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((nother + 7) / 8, (int64_t)di.num_sms * 16));
+    // CTAs per SM (GBLU_LASWP_CTAS_PER_SM overrides): every CTA first turns
+    // the leaf's pivots into its row moves, so fewer CTAs walking more
+    // columns each pay that once per SM rather than once per 8 columns
+    static const int64_t per_sm = [] {
+      const char* e = getenv("GBLU_LASWP_CTAS_PER_SM");
+      return e ? std::max<int64_t>(1, atoll(e)) : int64_t(4);
+    }();
+    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((nother + 7) / 8, (int64_t)di.num_sms * per_sm));
     LaunchScope ls(K_LASWP, 0.0, 4.0 * w * std::max<int64_t>(nother, 0) * sizeof(T), s);
     laswp_leaf_kernel<T><<<blocks, 256, 0, s>>>(p.A, p.lda, p.m, p.n, c0, w, p.ipiv, p.scratch, p.perm);
     check(cudaGetLastError());
