@@ -493,9 +493,13 @@ int32_t upload_matrix(gblu_ctx* ctx, double* dst, int64_t ld_dst, const double* 
                       int64_t rows, int64_t cols, int32_t loc) {
   if (rows == 0 || cols == 0) return GBLU_OK;
   cudaMemcpyKind kind = loc == GBLU_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
-  CK(ctx, cudaMemcpy2DAsync(dst, ld_dst * sizeof(double), src, ld_src * sizeof(double),
-                            rows * sizeof(double), cols, kind, ctx->stream),
-     "copying matrix to device");
+  if (ld_dst == rows && ld_src == rows)  // both contiguous: one linear copy
+    CK(ctx, cudaMemcpyAsync(dst, src, (size_t)rows * cols * sizeof(double), kind, ctx->stream),
+       "copying matrix to device");
+  else
+    CK(ctx, cudaMemcpy2DAsync(dst, ld_dst * sizeof(double), src, ld_src * sizeof(double),
+                              rows * sizeof(double), cols, kind, ctx->stream),
+       "copying matrix to device");
   return GBLU_OK;
 }
 
