@@ -314,6 +314,11 @@ typedef struct gblu_serve_config {
   int32_t solve_mode;        /* GBLU_SOLVE_EXACT / GBLU_SOLVE_FAST for the factors
                                 the server creates                                 */
   int32_t max_small_batch;   /* systems per small-lane launch                      */
+  int32_t large_n;           /* factorizations of n >= large_n count as large ...  */
+  int32_t max_large;         /* ... and at most max_large of them run at once (0: no
+                                limit; defaults 2048 and 1): large factorizations
+                                running together slow each other down, and they
+                                are the latency tail                               */
 } gblu_serve_config;
 typedef struct gblu_request {
   uint64_t key;      /* factorization key                                        */

@@ -171,6 +171,24 @@ int32_t ensure_rhs(gblu_ctx* ctx, gblu_factor* f, int64_t cols) {
   return GBLU_OK;
 }
 
+
+// Bytes of a factor object's arena (the carve in gblu_factor_create follows
+// the same order); the serving loop admits new factorizations with it.
+size_t factor_arena_bytes(int64_t m, int64_t n, int32_t precision, int device) {
+  const int64_t ld = std::max<int64_t>(32, ((m + 31) / 32) * 32);
+  if (precision == GBLU_FP64) return set_bytes<double>(m, n, ld, device, kWorkCols);
+  size_t bytes = set_bytes<float>(m, n, ld, device, kWorkCols);
+  bytes += align256((size_t)ld * n * sizeof(double));  // FP64 copy of A
+  bytes += refine_bytes(m, kWorkCols);
+  if (precision == GBLU_BF16 || precision == GBLU_FP16) {
+    bytes += align256(tc_work_bytes(n, n / 2 + 64, n / 2 + 64));
+    bytes += align256(trsm_inv_bytes(n));
+  }
+  bytes += align256(tslu_work_bytes());
+  if (m == n && n > 0) bytes += align256(getrs_inverse_bytes(n, sizeof(float)));
+  if (m == n && n > 0 && n % 4 == 0) bytes += align256((size_t)4 * n * sizeof(float));  // RBT diagonals
+  return bytes;
+}
 }  // namespace gblu
 
 
@@ -299,23 +317,9 @@ int32_t gblu_factor_create(gblu_ctx* ctx, int64_t m, int64_t n, int32_t precisio
   f->n = n;
   f->precision = precision;
   f->ld = std::max<int64_t>(32, ((m + 31) / 32) * 32);
-  size_t bytes;
-  size_t tc_bytes = 0;
-  if (precision == GBLU_FP64) {
-    bytes = set_bytes<double>(m, n, f->ld, ctx->device, kWorkCols);
-  } else {
-    bytes = set_bytes<float>(m, n, f->ld, ctx->device, kWorkCols);
-    bytes += align256((size_t)f->ld * n * sizeof(double));  // FP64 copy of A
-    bytes += refine_bytes(m, kWorkCols);
-    if (precision == GBLU_BF16 || precision == GBLU_FP16) {
-      tc_bytes = align256(tc_work_bytes(n, n / 2 + 64, n / 2 + 64));
-      bytes += tc_bytes;
-      bytes += align256(trsm_inv_bytes(n));
-    }
-    bytes += align256(tslu_work_bytes());
-    if (m == n && n > 0) bytes += align256(getrs_inverse_bytes(n, sizeof(float)));
-    if (m == n && n > 0 && n % 4 == 0) bytes += align256((size_t)4 * n * sizeof(float));  // RBT diagonals
-  }
+  const size_t bytes = factor_arena_bytes(m, n, precision, ctx->device);
+  const size_t tc_bytes =
+      (precision == GBLU_BF16 || precision == GBLU_FP16) ? align256(tc_work_bytes(n, n / 2 + 64, n / 2 + 64)) : 0;
   int32_t st = ctx_alloc(ctx, bytes, &f->arena);
   if (st) {
     delete f;

@@ -90,6 +90,8 @@ int32_t upload_matrix(gblu_ctx* ctx, double* dst, int64_t ld_dst, const double* 
 int32_t ensure_rhs(gblu_ctx* ctx, gblu_factor* f, int64_t cols);
 // FP64 factorization of the FP64 copy of A of a mixed factor (fb_* fields).
 int32_t factor_fp64_fallback(gblu_ctx* ctx, gblu_factor* f, int64_t* info_out);
+// Bytes of the arena gblu_factor_create allocates for these arguments.
+size_t factor_arena_bytes(int64_t m, int64_t n, int32_t precision, int device);
 // Fast getrs: invert the factors' diagonal blocks if the current factors'
 // inverses are not there yet (asynchronous on the context stream).
 int32_t ensure_inverse(gblu_ctx* ctx, gblu_factor* f);

@@ -71,6 +71,7 @@ struct gblu_server {
   uint64_t seq = 0, use_clock = 0;
   bool stopping = false;
   int64_t in_flight = 0;
+  int large_running = 0;  // factorizations of n >= cfg.large_n on the workers
   gblu_serve_stats stats{};
 };
 
@@ -78,14 +79,12 @@ namespace gblu {
 namespace {
 
 uint64_t factor_bytes_estimate(gblu_server* s, gblu_ctx* c, int64_t n) {
-  (void)c;
-  // same arithmetic as gblu_factor_create: report what the object will hold
-  const int64_t ld = std::max<int64_t>(32, ((n + 31) / 32) * 32);
-  const double elem = s->cfg.precision == GBLU_FP64 ? 8.0 : 4.0;
-  double b = (double)ld * n * elem;
-  if (s->cfg.precision != GBLU_FP64) b += (double)ld * n * 8.0 + 64.0 * n * 8.0;
-  if (s->cfg.precision == GBLU_BF16 || s->cfg.precision == GBLU_FP16) b += 1.5 * (double)n * n * 2.0;
-  return (uint64_t)b + (1u << 20);
+  // what gblu_factor_create will allocate, plus the inverses of an FP64
+  // factor switched to the fast solve
+  uint64_t b = factor_arena_bytes(n, n, s->cfg.precision, c->device);
+  if (s->cfg.precision == GBLU_FP64 && s->cfg.solve_mode == GBLU_SOLVE_FAST)
+    b += getrs_inverse_bytes(n, sizeof(double));
+  return b;
 }
 
 // Evict least recently used idle factorizations until `need` more bytes fit.
@@ -139,6 +138,7 @@ void worker(gblu_server* s, int wi) {
     std::vector<Pending> batch;
     Resident* res = nullptr;
     bool need_new = false;
+    bool took_large = false;  // holds one of the max_large slots
     uint64_t need_bytes = 0;
     std::vector<std::pair<gblu_ctx*, gblu_factor*>> victims;  // destroyed outside the lock
     {
@@ -153,6 +153,8 @@ void worker(gblu_server* s, int wi) {
             if (jt->req.key == it->req.key) { earlier_same_key = true; break; }
           if (earlier_same_key) continue;  // keep per-key order
           if (s->cfg.small_n > 0 && it->req.n <= s->cfg.small_n) continue;  // the small lane's
+          const bool large = it->req.A && s->cfg.max_large > 0 && it->req.n >= s->cfg.large_n;
+          if (large && s->large_running >= s->cfg.max_large) continue;  // waits for a large slot
           auto c = s->cache.find(it->req.key);
           if (c != s->cache.end()) key_busy = c->second.busy;
           if (key_busy) continue;
@@ -180,6 +182,8 @@ void worker(gblu_server* s, int wi) {
           break;
         }
         if (pick != s->queue.end()) {
+          took_large = pick->req.A && s->cfg.max_large > 0 && pick->req.n >= s->cfg.large_n;
+          if (took_large) s->large_running++;
           batch.push_back(*pick);
           const uint64_t key = pick->req.key;
           auto next = s->queue.erase(pick);
@@ -268,6 +272,7 @@ void worker(gblu_server* s, int wi) {
       for (size_t j = 0; j < batch.size(); ++j)
         complete(s, batch[j], st, info, j == 0 ? refactored : 0, rs, t_start);
       s->in_flight -= (int64_t)batch.size();
+      if (took_large) s->large_running--;
       if (batch.size() > 1) s->stats.merged_solves += batch.size() - 1;
       if (refactored) s->stats.factorizations++;
       s->stats.solves += batch.size();
@@ -435,6 +440,8 @@ int32_t gblu_serve_config_default(gblu_serve_config* cfg) {
   cfg->small_n = 256;
   cfg->solve_mode = GBLU_SOLVE_FAST;
   cfg->max_small_batch = 1024;
+  cfg->large_n = 2048;
+  cfg->max_large = 1;
   return GBLU_OK;
 }
 

@@ -41,6 +41,8 @@ const GBLU_FP16 = Int32(3)
 const GBLU_HOST = Int32(0)
 const GBLU_REFINE_IR = Int32(0)
 const GBLU_REFINE_GMRES = Int32(1)
+const GBLU_SOLVE_EXACT = Int32(0)
+const GBLU_SOLVE_FAST = Int32(1)
 const GBLU_PIVOT_PARTIAL = Int32(0)
 const GBLU_PIVOT_TOURNAMENT = Int32(1)
 const GBLU_PIVOT_RBT = Int32(2)
@@ -344,12 +346,17 @@ end
 # ---------------------------------------------------------------------------
 # Serving loop: continuous batching over factorizations resident in HBM.
 
-struct ServeConfig
+struct ServeConfig  # gblu_serve_config, field for field
     workers::Int32
     precision::Int32
     refine_mode::Int32
     hbm_budget_bytes::UInt64
     max_rhs_batch::Int32
+    small_n::Int32
+    solve_mode::Int32
+    max_small_batch::Int32
+    large_n::Int32
+    max_large::Int32
 end
 
 struct Request
@@ -386,12 +393,19 @@ mutable struct GB300Server
 end
 
 function GB300Server(; workers::Integer = 4, precision::Symbol = :fp32, refine::Symbol = :ir,
-        hbm_budget_bytes::Integer = 0, max_rhs_batch::Integer = 8)
+        hbm_budget_bytes::Integer = 0, max_rhs_batch::Integer = 8, small_n::Integer = -1,
+        solve::Symbol = :fast, max_large::Integer = -1)
     ctx = default_context()
     prec = precision === :fp64 ? GBLU_FP64 : precision === :bf16 ? GBLU_BF16 :
            precision === :fp16 ? GBLU_FP16 : GBLU_FP32
+    d = Ref{ServeConfig}()  # the library's defaults for the fields not given here
+    _check(ccall(_syms[:gblu_serve_config_default], Int32, (Ref{ServeConfig},), d), ctx)
+    c = d[]
     cfg = ServeConfig(Int32(workers), prec, refine === :gmres_ir ? GBLU_REFINE_GMRES : GBLU_REFINE_IR,
-                      UInt64(hbm_budget_bytes), Int32(max_rhs_batch))
+                      UInt64(hbm_budget_bytes), Int32(max_rhs_batch),
+                      small_n < 0 ? c.small_n : Int32(small_n),
+                      solve === :exact ? GBLU_SOLVE_EXACT : GBLU_SOLVE_FAST, c.max_small_batch,
+                      c.large_n, max_large < 0 ? c.max_large : Int32(max_large))
     h = Ref{Ptr{Cvoid}}(C_NULL)
     _check(ccall(_syms[:gblu_serve_create], Int32, (Ptr{Cvoid}, Ref{ServeConfig}, Ref{Ptr{Cvoid}}),
                  ctx, cfg, h), ctx)

@@ -19,7 +19,8 @@ PRECISIONS = {"fp64": _lib.GBLU_FP64, "fp32": _lib.GBLU_FP32, "bf16": _lib.GBLU_
 class Server:
     def __init__(self, ctx, workers: int = 4, precision: str = "fp32", refine: str = "ir",
                  hbm_budget_bytes: int = 120 << 30, max_rhs_batch: int = 8, small_n: int = 256,
-                 solve: str = "fast", max_small_batch: int = 1024):
+                 solve: str = "fast", max_small_batch: int = 1024, max_large: int | None = None,
+                 large_n: int | None = None):
         self.ctx, self.lib = ctx, ctx.lib
         cfg = _lib.ServeConfig()
         check(self.lib.gblu_serve_config_default(ctypes.byref(cfg)), None)
@@ -31,6 +32,10 @@ class Server:
         cfg.small_n = small_n
         cfg.solve_mode = _lib.GBLU_SOLVE_FAST if solve == "fast" else _lib.GBLU_SOLVE_EXACT
         cfg.max_small_batch = max_small_batch
+        if max_large is not None:  # large factorizations running at once (0: no limit)
+            cfg.max_large = max_large
+        if large_n is not None:
+            cfg.large_n = large_n
         h = ctypes.c_void_p()
         check(self.lib.gblu_serve_create(ctx.handle, ctypes.byref(cfg), ctypes.byref(h)), ctx.handle)
         self.h = h
