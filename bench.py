@@ -957,7 +957,8 @@ def run_serving_suite(pkg, cu, ctx, args):
            "target": "p99 <= 35 ms at 400 Hz, backward error <= 10 n eps64", "rates": []}
     runs = [(r, 120 << 30) for r in args.serve_rates] + [(400.0, int(args.serve_small_budget_gb * 2 ** 30))]
     for rate, budget in runs:
-        srv = serving.Server(ctx, workers=4, precision="fp32", hbm_budget_bytes=budget)
+        srv = serving.Server(ctx, workers=4, precision="fp32", hbm_budget_bytes=budget,
+                             max_large=args.serve_max_large)
         small = budget < (120 << 30)
         wdone, wwall = serving.run_stream(srv, warm, rate_hz=0.0, seed=1)
         st0 = srv.stats()
@@ -1129,6 +1130,8 @@ def main():
     ap.add_argument("--serve-rates", type=float, nargs="*", default=[100.0, 400.0, 0.0])
     ap.add_argument("--serve-keys", type=int, default=300)
     ap.add_argument("--serve-small-budget-gb", type=float, default=0.5)
+    ap.add_argument("--serve-max-large", type=int, default=None,
+                    help="large factorizations (n >= 2048) running at once (0: no limit; default: the library's)")
     ap.add_argument("--kernel-case", choices=KERNEL_CASES, default=None,
                     help="run one small case of a kernel group once (for ncu) and exit")
     args = ap.parse_args()
