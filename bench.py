@@ -957,12 +957,15 @@ def run_serving_suite(pkg, cu, ctx, args):
            "target": "p99 <= 35 ms at 400 Hz, backward error <= 10 n eps64", "rates": []}
     runs = [(r, 120 << 30) for r in args.serve_rates] + [(400.0, int(args.serve_small_budget_gb * 2 ** 30))]
     for rate, budget in runs:
+        clocks = ClockSampler(ctx.device)  # the stream's GPU clocks (the tail varies with them)
         srv = serving.Server(ctx, workers=4, precision="fp32", hbm_budget_bytes=budget,
                              max_large=args.serve_max_large)
         small = budget < (120 << 30)
         wdone, wwall = serving.run_stream(srv, warm, rate_hz=0.0, seed=1)
         st0 = srv.stats()
+        clocks.start()
         done, wall = serving.run_stream(srv, reqs, rate_hz=rate, seed=int(rate), resubmit_missing=small)
+        clk = clocks.stop()
         st = srv.stats()
         srv.close()
         summ = serving.latency_summary(done, wall)
@@ -972,7 +975,7 @@ def run_serving_suite(pkg, cu, ctx, args):
                 i = d["tag"]
                 n = len(reqs[i]["b"])
                 worst = max(worst, pkg_backward_error(reqs[i]["Aeff"], d["x"], reqs[i]["b"]) / (n * EPS64))
-        summ.update({"offered_rate_hz": rate, "budget_gb": budget / 2 ** 30,
+        summ.update({"offered_rate_hz": rate, "budget_gb": budget / 2 ** 30, "clocks": clk,
                      "max_backward_error_over_n_eps": worst, "warm_s": wwall,
                      "warm_failed": int(sum(d["status"] != 0 for d in wdone)),
                      "merged_solves": st["merged_solves"] - st0["merged_solves"],
