@@ -147,3 +147,26 @@ def test_autotuner_finds_valid_schedule(ctx, oracle_mod, pkg, tmp_path, monkeypa
     _, Xref, _ = oracle_mod.gesv_batched(sizes, A, b)
     assert np.array_equal(X, Xref)
     bt.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_full_batch_every_system_within_bound(ctx, oracle_mod, pkg, precision):
+    """The bench's whole workload (20,000 systems, n uniform in [8, 256]):
+    every system's backward error within 10 n eps64, FP64 and FP32 + IR (the
+    bench itself samples 200 of them)."""
+    sizes, A, b, _ = pkg.workloads.batch(20000, seed=0)
+    bt = Batch(ctx, sizes, precision)
+    X, info = bt.solve(A, b)
+    assert (info == 0).all()
+    a_off, b_off = pkg.workloads.offsets(sizes)
+    worst = 0.0
+    for i, n in enumerate(sizes):
+        n = int(n)
+        Ai = A[a_off[i]:a_off[i] + n * n].reshape(n, n, order="F")
+        x = X[b_off[i]:b_off[i] + n]
+        bi = b[b_off[i]:b_off[i] + n]
+        r = bi - Ai @ x
+        be = np.abs(r).max() / (np.abs(Ai).sum(axis=1).max() * np.abs(x).max() + np.abs(bi).max())
+        worst = max(worst, be / (n * EPS64))
+    assert worst <= 10.0, worst
+    bt.close()

@@ -475,3 +475,20 @@ def test_rbt_needs_multiple_of_4(ctx, pkg):
     with pytest.raises(pkg.GBLUError):
         g.set_pivoting("rbt")
     g.close()
+
+
+@pytest.mark.parametrize("pivot", ["partial", "rbt"])
+def test_full_size_mixed_n16384(ctx, oracle_mod, pkg, pivot):
+    """The mixed configuration at its full size (n = 16384, A = G + 4 sqrt(n) I,
+    4 RHS): BF16 tcgen05 LU + FP64 IR within 10 n eps64 without fallback, for
+    partial pivoting and for no pivoting after the butterfly transform."""
+    n = 16384
+    A, B = pkg.workloads.shifted(n, 4, seed=1)
+    f = ctx.factor(n, n, "bf16")
+    f.set_pivoting(pivot)
+    assert f.getrf(A) == 0
+    X, st = f.solve_refined(B)
+    be = oracle_mod.backward_error(A, X, B)
+    assert be <= 10 * n * EPS64, (be, st)
+    assert st["fell_back"] == 0, st
+    f.close()
