@@ -953,13 +953,14 @@ def run_serving_suite(pkg, cu, ctx, args):
     out = {"keys": nkeys, "distinct_sizes": int(len(np.unique(sizes))), "warm_requests": len(warm),
            "requests": len(reqs), "n_range": [int(sizes.min()), int(sizes.max())],
            "new_A_fraction": float(np.mean([r["A"] is not None for r in reqs])),
-           "precision": "fp32 factors + FP64 IR (fast inner solve); n <= 256 on the batched lane",
+           "precision": f"{args.serve_precision} factors ({args.serve_pivot} pivoting) + FP64 IR "
+                        "(fast inner solve); n <= 256 on the batched lane",
            "target": "p99 <= 35 ms at 400 Hz, backward error <= 10 n eps64", "rates": []}
     runs = [(r, 120 << 30) for r in args.serve_rates] + [(400.0, int(args.serve_small_budget_gb * 2 ** 30))]
     for rate, budget in runs:
         clocks = ClockSampler(ctx.device)  # the stream's GPU clocks (the tail varies with them)
-        srv = serving.Server(ctx, workers=4, precision="fp32", hbm_budget_bytes=budget,
-                             max_large=args.serve_max_large)
+        srv = serving.Server(ctx, workers=4, precision=args.serve_precision, hbm_budget_bytes=budget,
+                             max_large=args.serve_max_large, pivot=args.serve_pivot)
         small = budget < (120 << 30)
         wdone, wwall = serving.run_stream(srv, warm, rate_hz=0.0, seed=1)
         st0 = srv.stats()
@@ -1135,6 +1136,10 @@ def main():
     ap.add_argument("--serve-small-budget-gb", type=float, default=0.5)
     ap.add_argument("--serve-max-large", type=int, default=None,
                     help="large factorizations (n >= 2048) running at once (0: no limit; default: the library's)")
+    ap.add_argument("--serve-precision", choices=("fp32", "bf16", "fp16"), default="fp32",
+                    help="factor precision of the serving suite's mixed factors")
+    ap.add_argument("--serve-pivot", choices=("partial", "tournament", "rbt"), default="partial",
+                    help="pivoting of the serving suite's mixed factors")
     ap.add_argument("--kernel-case", choices=KERNEL_CASES, default=None,
                     help="run one small case of a kernel group once (for ncu) and exit")
     args = ap.parse_args()

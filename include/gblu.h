@@ -142,7 +142,8 @@ int32_t gblu_factor_set_solve(gblu_ctx* ctx, gblu_factor* f, int32_t mode);
  *   Refinement still solves the original system (residuals against the FP64
  *   A; corrections V (LU)^-1 U^T r); the pivot-growth check and the FP64
  *   fallback (with partial pivoting) catch a factorization the transform
- *   did not stabilise.  Square factors with n a multiple of 4.
+ *   did not stabilise.  Square factors of order 4 or more: the butterflies
+ *   cover the leading n - n mod 4 rows and columns (U, V = diag(W, I)).
  * GBLU_EUNSUPPORTED for GBLU_FP64 factors and for RBT on other shapes.
  * No counterpart in the reference. */
 #define GBLU_PIVOT_PARTIAL 0
@@ -319,6 +320,9 @@ typedef struct gblu_serve_config {
                                 limit; defaults 2048 and 1): large factorizations
                                 running together slow each other down, and they
                                 are the latency tail                               */
+  int32_t pivoting;          /* GBLU_PIVOT_* of the mixed-precision factors the
+                                server creates (default GBLU_PIVOT_PARTIAL;
+                                GBLU_PIVOT_RBT for n >= 4, partial below)          */
 } gblu_serve_config;
 typedef struct gblu_request {
   uint64_t key;      /* factorization key                                        */

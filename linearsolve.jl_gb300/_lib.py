@@ -94,7 +94,8 @@ class ServeConfig(ctypes.Structure):
                 ("refine_mode", ctypes.c_int32), ("hbm_budget_bytes", ctypes.c_uint64),
                 ("max_rhs_batch", ctypes.c_int32), ("small_n", ctypes.c_int32),
                 ("solve_mode", ctypes.c_int32), ("max_small_batch", ctypes.c_int32),
-                ("large_n", ctypes.c_int32), ("max_large", ctypes.c_int32)]
+                ("large_n", ctypes.c_int32), ("max_large", ctypes.c_int32),
+                ("pivoting", ctypes.c_int32)]
 
 
 class Request(ctypes.Structure):

@@ -186,7 +186,7 @@ size_t factor_arena_bytes(int64_t m, int64_t n, int32_t precision, int device) {
   }
   bytes += align256(tslu_work_bytes());
   if (m == n && n > 0) bytes += align256(getrs_inverse_bytes(n, sizeof(float)));
-  if (m == n && n > 0 && n % 4 == 0) bytes += align256((size_t)4 * n * sizeof(float));  // RBT diagonals
+  if (m == n && n >= 4) bytes += align256((size_t)4 * (n - n % 4) * sizeof(float));  // RBT diagonals
   return bytes;
 }
 }  // namespace gblu
@@ -240,6 +240,9 @@ int32_t gblu_destroy(gblu_ctx* ctx) {
     DeviceGuard g(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     cudaStreamDestroy(ctx->stream);
+    for (cudaEvent_t& e : ctx->stage_ev)
+      if (e) cudaEventDestroy(e);
+    if (ctx->stage) cudaFreeHost(ctx->stage);
   }
   delete ctx;
   return GBLU_OK;
@@ -372,9 +375,9 @@ int32_t gblu_factor_create(gblu_ctx* ctx, int64_t m, int64_t n, int32_t precisio
       f->rs32.inv = reinterpret_cast<float*>(c);
       c += align256(f->inv_bytes);
     }
-    if (m == n && n > 0 && n % 4 == 0) {
+    if (m == n && n >= 4) {
       f->rbt = reinterpret_cast<float*>(c);
-      c += align256((size_t)4 * n * sizeof(float));
+      c += align256((size_t)4 * (n - n % 4) * sizeof(float));
     }
   }
   cudaError_t e = cudaMemsetAsync(f->arena, 0, bytes, ctx->stream);
@@ -443,10 +446,10 @@ int32_t gblu_factor_set_pivoting(gblu_ctx* ctx, gblu_factor* f, int32_t mode) {
   }
   if (mode == GBLU_PIVOT_RBT && !f->rbt)
     return fail(ctx, GBLU_EUNSUPPORTED,
-                "gblu_factor_set_pivoting: the butterfly transform needs a square factor with n a multiple of 4 "
+                "gblu_factor_set_pivoting: the butterfly transform needs a square factor of order 4 or more "
                 "(%lld x %lld)", (long long)f->m, (long long)f->n);
   if (mode == GBLU_PIVOT_RBT && !f->rbt_ready) {
-    std::vector<float> h((size_t)4 * f->n);
+    std::vector<float> h((size_t)4 * (f->n - f->n % 4));
     rbt_fill_host(f->n, h.data());
     CK(ctx, cudaMemcpyAsync(f->rbt, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice, ctx->stream),
        "uploading the butterfly diagonals");
@@ -492,11 +495,86 @@ int32_t gblu_factor_keep_matrix(gblu_ctx* ctx, gblu_factor* f, int32_t keep) {
 
 namespace gblu {
 
-// Copy a host or device FP64 matrix (rows x cols, ld_src) into dst (ld_dst).
-int32_t upload_matrix(gblu_ctx* ctx, double* dst, int64_t ld_dst, const double* src, int64_t ld_src,
-                      int64_t rows, int64_t cols, int32_t loc) {
-  if (rows == 0 || cols == 0) return GBLU_OK;
-  cudaMemcpyKind kind = loc == GBLU_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+namespace {
+
+// Uploads of at least kStageMin bytes from pageable host memory go through
+// pinned staging.  A cudaMemcpyAsync from pageable memory has the driver read
+// the caller's pages itself, and on GB300 the speed of that copy depends on
+// how the process's host memory happens to be mapped: about 170 GB/s in one
+// process, 5-7 GB/s for the same stream of matrices in a later one, and
+// while it is slow it also delays the other contexts' work (a serving
+// stream's p99 at 400 Hz: 13 ms in the first state, 70-110 ms in the
+// second).  Staged, the CPU copies column blocks into two pinned chunks that
+// the copy engine drains alternately (the host copy of one chunk overlaps
+// the transfer of the other): about 14 GB/s and a p99 of 24 ms in both
+// states.  GBLU_HOST_STAGING=0 copies directly.
+constexpr size_t kStageMin = size_t(4) << 20;
+constexpr size_t kStageChunk = size_t(16) << 20;
+
+bool host_staging_on() {
+  static const bool on = [] {
+    const char* e = getenv("GBLU_HOST_STAGING");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
+bool is_pageable(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return true;
+  }
+  return a.type == cudaMemoryTypeUnregistered;
+}
+
+// columns [c0, c1) of src (ld_src) packed into out (rows per column)
+void pack_columns(double* out, const double* src, int64_t ld_src, int64_t rows, int64_t c0, int64_t c1) {
+  for (int64_t c = c0; c < c1; ++c)
+    std::memcpy(out + (c - c0) * rows, src + c * ld_src, (size_t)rows * sizeof(double));
+}
+
+int32_t upload_staged(gblu_ctx* ctx, double* dst, int64_t ld_dst, const double* src, int64_t ld_src,
+                      int64_t rows, int64_t cols) {
+  const size_t col_bytes = (size_t)rows * sizeof(double);
+  const size_t chunk = std::max(kStageChunk, col_bytes);
+  if (!ctx->stage || ctx->stage_chunk < chunk) {
+    if (ctx->stage) {
+      CK(ctx, cudaStreamSynchronize(ctx->stream), "staging");
+      cudaFreeHost(ctx->stage);
+      ctx->stage = nullptr;
+    }
+    void* p = nullptr;
+    CK(ctx, cudaMallocHost(&p, 2 * chunk), "allocating pinned staging");
+    ctx->stage = static_cast<char*>(p);
+    ctx->stage_chunk = chunk;
+    for (cudaEvent_t& e : ctx->stage_ev)
+      if (!e) CK(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "staging event");
+  }
+  const int64_t per = (int64_t)(ctx->stage_chunk / col_bytes);  // columns per chunk
+  int i = 0;
+  for (int64_t c = 0; c < cols; c += per, i ^= 1) {
+    const int64_t k = std::min(per, cols - c);
+    CK(ctx, cudaEventSynchronize(ctx->stage_ev[i]), "staging");  // the chunk's last copy is done
+    double* buf = reinterpret_cast<double*>(ctx->stage + (size_t)i * ctx->stage_chunk);
+    pack_columns(buf, src + c * ld_src, ld_src, rows, 0, k);
+    if (ld_dst == rows)
+      CK(ctx, cudaMemcpyAsync(dst + c * ld_dst, buf, col_bytes * k, cudaMemcpyHostToDevice, ctx->stream),
+         "copying matrix to device");
+    else
+      CK(ctx, cudaMemcpy2DAsync(dst + c * ld_dst, ld_dst * sizeof(double), buf, col_bytes, col_bytes, k,
+                                cudaMemcpyHostToDevice, ctx->stream),
+         "copying matrix to device");
+    CK(ctx, cudaEventRecord(ctx->stage_ev[i], ctx->stream), "staging");
+  }
+  return GBLU_OK;
+}
+
+}  // namespace
+
+// One cudaMemcpyAsync / cudaMemcpy2DAsync of the matrix.
+int32_t upload_direct(gblu_ctx* ctx, double* dst, int64_t ld_dst, const double* src, int64_t ld_src,
+                      int64_t rows, int64_t cols, cudaMemcpyKind kind) {
   if (ld_dst == rows && ld_src == rows)  // both contiguous: one linear copy
     CK(ctx, cudaMemcpyAsync(dst, src, (size_t)rows * cols * sizeof(double), kind, ctx->stream),
        "copying matrix to device");
@@ -505,6 +583,17 @@ int32_t upload_matrix(gblu_ctx* ctx, double* dst, int64_t ld_dst, const double* 
                               rows * sizeof(double), cols, kind, ctx->stream),
        "copying matrix to device");
   return GBLU_OK;
+}
+
+// Copy a host or device FP64 matrix (rows x cols, ld_src) into dst (ld_dst).
+int32_t upload_matrix(gblu_ctx* ctx, double* dst, int64_t ld_dst, const double* src, int64_t ld_src,
+                      int64_t rows, int64_t cols, int32_t loc) {
+  if (rows == 0 || cols == 0) return GBLU_OK;
+  if (loc == GBLU_HOST && (size_t)rows * cols * sizeof(double) >= kStageMin && host_staging_on() &&
+      is_pageable(src))
+    return upload_staged(ctx, dst, ld_dst, src, ld_src, rows, cols);
+  return upload_direct(ctx, dst, ld_dst, src, ld_src, rows, cols,
+                       loc == GBLU_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice);
 }
 
 // Runs the factor's getrf launch sequence: directly on its first two runs

@@ -19,6 +19,11 @@ struct gblu_ctx {
   std::recursive_mutex mu;
   std::string last_error;
   gblu::Profiler prof;
+  // pinned staging for large uploads from pageable host memory: two chunks
+  // of stage_chunk bytes, each with the event of the copy that last read it
+  char* stage = nullptr;
+  size_t stage_chunk = 0;
+  cudaEvent_t stage_ev[2] = {nullptr, nullptr};
 };
 
 struct gblu_factor {

@@ -161,6 +161,44 @@ rbt_matrix_kernel(int64_t n, const double* __restrict__ A, int64_t lda, float* _
     for (int i = 0; i < 4; ++i) B[(a + i * h2) + (b + j * h2) * ldb] = 0.25f * x[i][j];
 }
 
+// The rows and columns past the butterflies' order n4 (fewer than four of
+// each): the transforms are diag(W, I), so the extra rows take the column
+// transform only, the extra columns the row transform only, and the corner
+// is copied.  blockIdx.y: extra row y (y < r), extra column y - r (y < 2r),
+// the corner (y = 2r).
+__global__ void __launch_bounds__(128)
+rbt_edge_kernel(int64_t n, int64_t n4, const double* __restrict__ A, int64_t lda, float* __restrict__ B,
+                int64_t ldb, const float* __restrict__ rbt) {
+  const int64_t h2 = n4 / 4, r = n - n4;
+  const int64_t y = blockIdx.y;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (y < r) {
+    if (t >= h2) return;
+    const RbtSide Rt(rbt, n4, 1);
+    const int64_t i = n4 + y;
+    float x[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) x[j] = f64_to_f32_rn(A[i + (t + j * h2) * lda]);
+    Rt.t_form(x, t, h2);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) B[i + (t + j * h2) * ldb] = 0.5f * x[j];
+  } else if (y < 2 * r) {
+    if (t >= h2) return;
+    const RbtSide L(rbt, n4, 0);
+    const int64_t c = n4 + (y - r);
+    float x[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) x[i] = f64_to_f32_rn(A[(t + i * h2) + c * lda]);
+    L.t_form(x, t, h2);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) B[(t + i * h2) + c * ldb] = 0.5f * x[i];
+  } else {
+    if (t >= r * r) return;
+    const int64_t i = n4 + t % r, c = n4 + t / r;
+    B[i + c * ldb] = f64_to_f32_rn(A[i + c * lda]);
+  }
+}
+
 // v := W^T v / 2 or W v / 2, W columns of v.
 __global__ void __launch_bounds__(256)
 rbt_vec_kernel(int64_t n, int W, float* __restrict__ v, int64_t ldv, const float* __restrict__ rbt, int side,
@@ -660,28 +698,38 @@ cudaError_t refine_prepare(RefineWork& w, int64_t n, const double* A, int64_t ld
 cudaError_t rbt_matrix_launch(int64_t n, const double* A, int64_t lda, float* B, int64_t ldb,
                               const float* rbt, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  if (n % 4 != 0 || n / 4 > 65535) return cudaErrorInvalidValue;
-  LaunchScope ls_(K_REFINE, 32.0 * n * n / 16.0 * 2.0, 12.0 * n * n, s);
-  dim3 grid((unsigned)((n / 4 + 127) / 128), (unsigned)(n / 4));
-  rbt_matrix_kernel<<<grid, 128, 0, s>>>(n, A, lda, B, ldb, rbt);
+  const int64_t n4 = n - n % 4;
+  if (n4 < 4 || n4 / 4 > 65535) return cudaErrorInvalidValue;
+  {
+    LaunchScope ls_(K_REFINE, 32.0 * n4 * n4 / 16.0 * 2.0, 12.0 * n4 * n4, s);
+    dim3 grid((unsigned)((n4 / 4 + 127) / 128), (unsigned)(n4 / 4));
+    rbt_matrix_kernel<<<grid, 128, 0, s>>>(n4, A, lda, B, ldb, rbt);
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || n4 == n) return e;
+  LaunchScope ls_(K_REFINE, 0.0, 12.0 * 2.0 * (n - n4) * n, s);
+  dim3 grid((unsigned)((n4 / 4 + 127) / 128), (unsigned)(2 * (n - n4) + 1));
+  rbt_edge_kernel<<<grid, 128, 0, s>>>(n, n4, A, lda, B, ldb, rbt);
   return cudaGetLastError();
 }
 
 cudaError_t rbt_vec_launch(int64_t n, int W, float* v, int64_t ldv, const float* rbt, int side,
                            bool transposed, cudaStream_t s) {
   if (n <= 0 || W <= 0) return cudaSuccess;
-  if (n % 4 != 0 || W > 65535) return cudaErrorInvalidValue;
-  LaunchScope ls_(K_REFINE, 12.0 * n * W, 8.0 * n * W, s);
-  dim3 grid((unsigned)((n / 4 + 255) / 256), (unsigned)W);
-  rbt_vec_kernel<<<grid, 256, 0, s>>>(n, W, v, ldv, rbt, side, transposed ? 1 : 0);
+  const int64_t n4 = n - n % 4;  // entries past n4 are left as they are (identity)
+  if (n4 < 4 || W > 65535) return cudaErrorInvalidValue;
+  LaunchScope ls_(K_REFINE, 12.0 * n4 * W, 8.0 * n4 * W, s);
+  dim3 grid((unsigned)((n4 / 4 + 255) / 256), (unsigned)W);
+  rbt_vec_kernel<<<grid, 256, 0, s>>>(n4, W, v, ldv, rbt, side, transposed ? 1 : 0);
   return cudaGetLastError();
 }
 
 void rbt_fill_host(int64_t n, float* out) {
   // splitmix64 stream from a fixed seed: the transform (and so every
-  // result) is the same on every run
+  // result) is the same on every run; 4 n4 values, n4 = n - n mod 4
+  const int64_t n4 = n - n % 4;
   uint64_t x = 0x5eedb077e4f1ULL;
-  for (int64_t i = 0; i < 4 * n; ++i) {
+  for (int64_t i = 0; i < 4 * n4; ++i) {
     x += 0x9e3779b97f4a7c15ULL;
     uint64_t z = x;
     z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;

@@ -58,13 +58,16 @@ cudaError_t refine_prepare(RefineWork& w, int64_t n, const double* A, int64_t ld
                            int64_t ld32, cudaStream_t s, bool write_f32 = true);
 
 // Random butterfly transform (depth 2, both sides) of the mixed factors'
-// GBLU_PIVOT_RBT mode.  rbt: 4 n floats, the left then the right butterflies'
-// random diagonals, each R1 S1 R2 S2 of n/2; n a multiple of 4.
-// B (FP32, ldb) = U^T A V / 4 for the FP64 A (lda).
+// GBLU_PIVOT_RBT mode, over the leading n4 = n - n mod 4 rows and columns
+// (the transforms are diag(W, I)).  rbt: 4 n4 floats, the left then the
+// right butterflies' random diagonals, each R1 S1 R2 S2 of n4/2; n >= 4.
+// B (FP32, ldb) = U^T A V for the FP64 A (lda), U = diag(W_L / 2, I),
+// V = diag(W_R / 2, I).
 cudaError_t rbt_matrix_launch(int64_t n, const double* A, int64_t lda, float* B, int64_t ldb,
                               const float* rbt, cudaStream_t s);
 // In place on the W columns of v (FP32, ldv): side 0 = U, 1 = V; transposed:
-// v := W^T v / 2 (before the triangular solves), else v := W v / 2 (after).
+// v := U^T v (before the triangular solves), else v := V v (after); entries
+// past n4 are unchanged.
 cudaError_t rbt_vec_launch(int64_t n, int W, float* v, int64_t ldv, const float* rbt, int side,
                            bool transposed, cudaStream_t s);
 // The random diagonals (exp(u / 10), u uniform in (-1/2, 1/2), a fixed seed).

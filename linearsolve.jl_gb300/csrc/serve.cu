@@ -228,6 +228,9 @@ void worker(gblu_server* s, int wi) {
       gblu_factor* f = nullptr;
       st = gblu_factor_create(ctx, n, n, s->cfg.precision, &f);
       if (st == GBLU_OK) st = gblu_factor_set_solve(ctx, f, s->cfg.solve_mode);
+      if (st == GBLU_OK && s->cfg.precision != GBLU_FP64 && s->cfg.pivoting != GBLU_PIVOT_PARTIAL &&
+          !(s->cfg.pivoting == GBLU_PIVOT_RBT && n < 4))
+        st = gblu_factor_set_pivoting(ctx, f, s->cfg.pivoting);
       res->f = f;
       if (f) res->owner = ctx;
     }
@@ -442,6 +445,7 @@ int32_t gblu_serve_config_default(gblu_serve_config* cfg) {
   cfg->max_small_batch = 1024;
   cfg->large_n = 2048;
   cfg->max_large = 1;
+  cfg->pivoting = GBLU_PIVOT_PARTIAL;
   return GBLU_OK;
 }
 
@@ -461,6 +465,8 @@ int32_t gblu_serve_create(gblu_ctx* ctx, const gblu_serve_config* cfg, gblu_serv
     return fail(ctx, GBLU_EINVAL, "gblu_serve_create: bad solve mode");
   if (c.small_n > 0 && c.max_small_batch < 1)
     return fail(ctx, GBLU_EINVAL, "gblu_serve_create: max_small_batch < 1");
+  if (c.pivoting != GBLU_PIVOT_PARTIAL && c.pivoting != GBLU_PIVOT_TOURNAMENT && c.pivoting != GBLU_PIVOT_RBT)
+    return fail(ctx, GBLU_EINVAL, "gblu_serve_create: bad pivoting mode");
   gblu_server* s = new gblu_server();
   s->parent = ctx;
   s->cfg = c;

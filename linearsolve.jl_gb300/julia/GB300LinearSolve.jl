@@ -147,7 +147,7 @@ GMRES-IR (`:gmres_ir`).  `factor = :fp32` keeps the trailing updates in FP32;
 solution meets the FP64 backward-error bound: refinement that stalls, or
 factors whose pivot growth exceeds `growth_limit` (0: the library's default),
 fall back to the FP64 LU.  `pivot = :rbt` factors U^T A V / 4 (random
-butterflies, n a multiple of 4) without pivoting; `:tournament` uses
+butterflies over the leading n - n mod 4 rows and columns) without pivoting; `:tournament` uses
 tournament pivoting for tall leaves; `:partial` (default) is the reference's.
 """
 struct GB300MixedLUFactorization <: LinearSolve.AbstractDenseFactorization
@@ -357,6 +357,7 @@ struct ServeConfig  # gblu_serve_config, field for field
     max_small_batch::Int32
     large_n::Int32
     max_large::Int32
+    pivoting::Int32
 end
 
 struct Request
@@ -381,7 +382,8 @@ struct Completion
 end
 
 """
-    GB300Server(; workers = 4, precision = :fp32, refine = :ir, hbm_budget_bytes = 0, max_rhs_batch = 8)
+    GB300Server(; workers = 4, precision = :fp32, refine = :ir, hbm_budget_bytes = 0, max_rhs_batch = 8,
+                  small_n = -1, solve = :fast, max_large = -1, pivot = :partial)
 
 A `gblu_serve_*` server: `submit!(srv, key, A, b, x, tag)` (A = nothing: solve
 with the resident factors of `key`), `poll(srv)` returns the completions.
@@ -394,7 +396,7 @@ end
 
 function GB300Server(; workers::Integer = 4, precision::Symbol = :fp32, refine::Symbol = :ir,
         hbm_budget_bytes::Integer = 0, max_rhs_batch::Integer = 8, small_n::Integer = -1,
-        solve::Symbol = :fast, max_large::Integer = -1)
+        solve::Symbol = :fast, max_large::Integer = -1, pivot::Symbol = :partial)
     ctx = default_context()
     prec = precision === :fp64 ? GBLU_FP64 : precision === :bf16 ? GBLU_BF16 :
            precision === :fp16 ? GBLU_FP16 : GBLU_FP32
@@ -405,7 +407,9 @@ function GB300Server(; workers::Integer = 4, precision::Symbol = :fp32, refine::
                       UInt64(hbm_budget_bytes), Int32(max_rhs_batch),
                       small_n < 0 ? c.small_n : Int32(small_n),
                       solve === :exact ? GBLU_SOLVE_EXACT : GBLU_SOLVE_FAST, c.max_small_batch,
-                      c.large_n, max_large < 0 ? c.max_large : Int32(max_large))
+                      c.large_n, max_large < 0 ? c.max_large : Int32(max_large),
+                      pivot === :rbt ? GBLU_PIVOT_RBT : pivot === :tournament ? GBLU_PIVOT_TOURNAMENT :
+                      GBLU_PIVOT_PARTIAL)
     h = Ref{Ptr{Cvoid}}(C_NULL)
     _check(ccall(_syms[:gblu_serve_create], Int32, (Ptr{Cvoid}, Ref{ServeConfig}, Ref{Ptr{Cvoid}}),
                  ctx, cfg, h), ctx)

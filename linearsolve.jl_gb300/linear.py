@@ -185,8 +185,7 @@ class GB300MixedLUFactorization(AbstractDenseFactorization):
               (see GB300LUFactorization); refinement makes either FP64-accurate.
     pivot:    pivoting of the low-precision LU: "partial" (default), "tournament"
               or "rbt" (no pivoting after a random butterfly transform of both
-              sides, n a multiple of 4; the growth check and FP64 fallback
-              guard it).
+              sides, n >= 4; the growth check and FP64 fallback guard it).
 
     Unlike the reference's CUDAOffload32MixedLUFactorization
     (ext/LinearSolveCUDAExt.jl:211-242) the result is FP64-accurate."""

@@ -20,7 +20,7 @@ class Server:
     def __init__(self, ctx, workers: int = 4, precision: str = "fp32", refine: str = "ir",
                  hbm_budget_bytes: int = 120 << 30, max_rhs_batch: int = 8, small_n: int = 256,
                  solve: str = "fast", max_small_batch: int = 1024, max_large: int | None = None,
-                 large_n: int | None = None):
+                 large_n: int | None = None, pivot: str = "partial"):
         self.ctx, self.lib = ctx, ctx.lib
         cfg = _lib.ServeConfig()
         check(self.lib.gblu_serve_config_default(ctypes.byref(cfg)), None)
@@ -36,6 +36,9 @@ class Server:
             cfg.max_large = max_large
         if large_n is not None:
             cfg.large_n = large_n
+        # pivoting of the mixed-precision factors: partial, tournament or rbt
+        cfg.pivoting = {"partial": _lib.GBLU_PIVOT_PARTIAL, "tournament": _lib.GBLU_PIVOT_TOURNAMENT,
+                        "rbt": _lib.GBLU_PIVOT_RBT}[pivot]
         h = ctypes.c_void_p()
         check(self.lib.gblu_serve_create(ctx.handle, ctypes.byref(cfg), ctypes.byref(h)), ctx.handle)
         self.h = h

@@ -81,3 +81,43 @@ def test_lapack_shaped_argument_errors(pkg):
     m0 = ctypes.c_int64(0)
     lib.gblu_dgetrf_(ctypes.byref(m0), ctypes.byref(n), None, ctypes.byref(lda), None, ctypes.byref(info))
     assert info.value == 0  # empty matrix: nothing to do, no device touched
+
+
+def _header_struct_fields(name):
+    src = open(os.path.join(ROOT, "include", "gblu.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    body = re.search(r"typedef struct %s \{(.*?)\}" % name, src, flags=re.S).group(1)
+    return re.findall(r"([A-Za-z_][A-Za-z0-9_]*)\s*;", body)
+
+
+@pytest.mark.parametrize("c_name,py_name,jl_name", [
+    ("gblu_serve_config", "ServeConfig", "ServeConfig"),
+    ("gblu_request", "Request", "Request"),
+    ("gblu_completion", "Completion", "Completion"),
+])
+def test_struct_layouts_match_header(pkg, c_name, py_name, jl_name):
+    """The Python ctypes and Julia mirrors of the C structs list the header's
+    fields in the header's order (a missing trailing field would let the
+    library write past the caller's struct)."""
+    from importlib import import_module
+    lib_mod = import_module(pkg.__name__ + "._lib")
+    fields = _header_struct_fields(c_name)
+    assert fields
+    assert [f[0] for f in getattr(lib_mod, py_name)._fields_] == fields
+    src = open(os.path.join(ROOT, "linearsolve.jl_gb300", "julia", "GB300LinearSolve.jl")).read()
+    body = re.search(r"struct %s\b[^\n]*\n(.*?)\nend" % jl_name, src, flags=re.S).group(1)
+    assert re.findall(r"^\s*([A-Za-z0-9_]+)::", body, flags=re.M) == fields
+
+
+def test_serve_config_default_fills_every_field(pkg):
+    """gblu_serve_config_default writes the whole struct (no GPU needed)."""
+    import ctypes
+    from importlib import import_module
+    lib_mod = import_module(pkg.__name__ + "._lib")
+    lib = pkg.load_library()
+    cfg = lib_mod.ServeConfig()
+    ctypes.memset(ctypes.byref(cfg), 0x7f, ctypes.sizeof(cfg))
+    assert lib.gblu_serve_config_default(ctypes.byref(cfg)) == 0
+    vals = {f[0]: getattr(cfg, f[0]) for f in cfg._fields_}
+    assert all(v != 0x7f7f7f7f and v != 0x7f7f7f7f7f7f7f7f for v in vals.values()), vals
+    assert vals["pivoting"] == lib_mod.GBLU_PIVOT_PARTIAL and vals["max_large"] == 1

@@ -395,3 +395,39 @@ def test_fast_getrs_through_the_interface(pkg, oracle_mod):
     cache.b = rng.standard_normal(n)
     sol = pkg.solve_bang(cache)
     assert oracle_mod.backward_error(A, sol.u, cache.b) <= 10 * n * EPS64
+
+
+@pytest.mark.parametrize("pad", [0, 37])
+def test_host_upload_staging_identical(pkg, pad):
+    """Host matrices of 4 MB and more in pageable memory are copied through
+    pinned staging chunks (here four 16 MB chunks, and a leading dimension
+    above n); pinned host memory and device memory go straight to the copy
+    engine.  All give identical factors, and a second staged upload in the
+    same context (the chunks reused) too."""
+    import ctypes
+    import torch
+    from importlib import import_module
+    _lib = import_module(pkg.__name__ + "._lib")
+    ctx = pkg.Context(0)
+    n = 2600  # 54 MB
+    rng = np.random.default_rng(2600 + pad)
+    Ap = np.asfortranarray(rng.standard_normal((n + pad, n)))  # pageable, lda = n + pad
+    pinned = torch.empty((n, n + pad), dtype=torch.float64, pin_memory=True)
+    pinned.numpy()[:] = Ap.T  # the same column-major matrix in pinned memory
+    results = []
+    for ptr in (Ap.ctypes.data, Ap.ctypes.data, pinned.data_ptr()):
+        f = ctx.factor(n, n)
+        info = ctypes.c_int64()
+        st = ctx.lib.gblu_getrf(ctx.handle, f.handle, ptr, n + pad, _lib.GBLU_HOST, ctypes.byref(info))
+        assert st == 0 and info.value == 0
+        results.append((f.factors(), f.ipiv()))
+        f.close()
+    f = ctx.factor(n, n)
+    dA = pkg.DeviceMatrix.from_host(np.asfortranarray(Ap[:n]))
+    assert f.getrf(dA) == 0
+    results.append((f.factors(), f.ipiv()))
+    dA.free()
+    f.close()
+    ctx.close()
+    for LU, ipiv in results[1:]:
+        assert np.array_equal(LU, results[0][0]) and np.array_equal(ipiv, results[0][1])

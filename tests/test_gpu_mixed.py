@@ -346,11 +346,13 @@ def test_trsm_inverse_blocks(ctx, oracle_mod, pkg, monkeypatch, n):
 def _rbt_diagonals(n):
     """The butterflies' random diagonals as the library draws them: a
     splitmix64 stream from a fixed seed, exp(u / 10) with u uniform in
-    (-1/2, 1/2), rounded to FP32; left then right, each R1 S1 R2 S2 of n/2."""
+    (-1/2, 1/2), rounded to FP32; left then right, each R1 S1 R2 S2 of n4/2
+    (n4 = n - n mod 4, the order the butterflies cover)."""
+    n4 = n - n % 4
     mask = (1 << 64) - 1
     x = 0x5eedb077e4f1
-    out = np.empty(4 * n, dtype=np.float32)
-    for i in range(4 * n):
+    out = np.empty(4 * n4, dtype=np.float32)
+    for i in range(4 * n4):
         x = (x + 0x9e3779b97f4a7c15) & mask
         z = x
         z = ((z ^ (z >> 30)) * 0xbf58476d1ce4e5b9) & mask
@@ -362,8 +364,11 @@ def _rbt_diagonals(n):
 
 
 def _rbt_matrices(n):
+    """U = diag(W_L / 2, I) and V = diag(W_R / 2, I): the factors are those of
+    U^T A V."""
     d = _rbt_diagonals(n).astype(np.float64)
-    h1, h2 = n // 2, n // 4
+    n4 = n - n % 4
+    h1, h2 = n4 // 2, n4 // 4
 
     def butterfly(R, S):
         m = 2 * len(R)
@@ -374,31 +379,35 @@ def _rbt_matrices(n):
         B[m // 2:, m // 2:] = -np.diag(S)
         return B
 
-    Ws = []
+    Ts = []
     for side in (0, 1):
-        b = d[side * 2 * n:(side + 1) * 2 * n]
-        R1, S1, R2, S2 = b[:h1], b[h1:n], b[n:n + h1], b[n + h1:]
-        B2 = np.zeros((n, n))
+        b = d[side * 2 * n4:(side + 1) * 2 * n4]
+        R1, S1, R2, S2 = b[:h1], b[h1:n4], b[n4:n4 + h1], b[n4 + h1:]
+        B2 = np.zeros((n4, n4))
         B2[:h1, :h1] = butterfly(R2[:h2], S2[:h2])
         B2[h1:, h1:] = butterfly(R2[h2:], S2[h2:])
-        Ws.append(butterfly(R1, S1) @ B2)
-    return Ws
+        T = np.eye(n)
+        T[:n4, :n4] = butterfly(R1, S1) @ B2 / 2
+        Ts.append(T)
+    return Ts
 
 
 @pytest.mark.parametrize("prec", ["fp32", "bf16", "fp16"])
-@pytest.mark.parametrize("n", [256, 1000])
+@pytest.mark.parametrize("n", [256, 1000, 1001, 1002, 1003, 7])
 def test_rbt_factors_the_transformed_matrix(ctx, oracle_mod, pkg, prec, n):
-    """GBLU_PIVOT_RBT: the low-precision LU is that of U^T A V / 4 (the
-    butterflies rebuilt here from the library's seeded diagonals), without
-    interchanges, and refinement reaches the FP64 bound without fallback."""
+    """GBLU_PIVOT_RBT: the low-precision LU is that of U^T A V (the
+    butterflies rebuilt here from the library's seeded diagonals; for n not a
+    multiple of 4 the last n mod 4 rows and columns are left out of them),
+    without interchanges, and refinement reaches the FP64 bound without
+    fallback."""
     # A = G + 4 sqrt(n) I: the transform keeps the growth near 1 (GENP on a
     # plain Gaussian matrix meets small pivots whatever the randomisation)
     A, B = pkg.workloads.shifted(n, 3, seed=300 + n)
     f = ctx.factor(n, n, prec)
     f.set_pivoting("rbt")
     assert f.getrf(A) == 0
-    WL, WR = _rbt_matrices(n)
-    Ar = WL.T @ A @ WR / 4
+    U_, V_ = _rbt_matrices(n)
+    Ar = U_.T @ A @ V_
     F = f.factors()
     L = np.tril(F, -1) + np.eye(n)
     U = np.triu(F)
@@ -465,16 +474,16 @@ def test_rbt_mode_switches_and_graph_replay(ctx, oracle_mod, pkg):
     f.close()
 
 
-def test_rbt_needs_multiple_of_4(ctx, pkg):
-    f = ctx.factor(1001, 1001, "bf16")
-    with pytest.raises(pkg.GBLUError):
-        f.set_pivoting("rbt")
-    f.set_pivoting("partial")
-    f.close()
-    g = ctx.factor(64, 64, "fp64")
-    with pytest.raises(pkg.GBLUError):
-        g.set_pivoting("rbt")
-    g.close()
+def test_rbt_needs_a_square_mixed_factor(ctx, pkg):
+    """RBT takes mixed factors (square by construction) of order 4 or more,
+    not FP64 ones."""
+    for m, n, prec in ((3, 3, "bf16"), (2, 2, "fp32"), (64, 64, "fp64")):
+        f = ctx.factor(m, n, prec)
+        with pytest.raises(pkg.GBLUError):
+            f.set_pivoting("rbt")
+        if prec != "fp64":
+            f.set_pivoting("partial")
+        f.close()
 
 
 @pytest.mark.parametrize("pivot", ["partial", "rbt"])

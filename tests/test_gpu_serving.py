@@ -27,10 +27,10 @@ def _requests(pkg, seed=0, nkeys=6, nreq=60, nmin=64, nmax=600):
     return reqs
 
 
-def _run(pkg, ctx, reqs, workers, precision, rate=0.0):
+def _run(pkg, ctx, reqs, workers, precision, rate=0.0, pivot="partial"):
     from importlib import import_module
     serving = import_module(pkg.__name__ + ".serving")
-    srv = serving.Server(ctx, workers=workers, precision=precision)
+    srv = serving.Server(ctx, workers=workers, precision=precision, pivot=pivot)
     if rate == 0.0 and workers == 1:
         done = []
         for i, r in enumerate(reqs):  # strictly one at a time
@@ -46,11 +46,14 @@ def _run(pkg, ctx, reqs, workers, precision, rate=0.0):
     return {d["tag"]: d for d in done}, stats
 
 
-@pytest.mark.parametrize("precision", ["fp64", "fp32", "bf16"])
-def test_serving_results_accurate_and_mix_independent(ctx, oracle_mod, pkg, precision):
+@pytest.mark.parametrize("precision,pivot", [("fp64", "partial"), ("fp32", "partial"), ("bf16", "partial"),
+                                             ("fp32", "rbt"), ("bf16", "rbt")])
+def test_serving_results_accurate_and_mix_independent(ctx, oracle_mod, pkg, precision, pivot):
+    """pivot = rbt: the server's mixed factors pivot no rows after the random
+    butterfly transform (orders 257..600 here, most not multiples of 4)."""
     reqs = _requests(pkg, seed=3)
-    alone, _ = _run(pkg, ctx, reqs, workers=1, precision=precision)
-    mixed, stats = _run(pkg, ctx, reqs, workers=4, precision=precision)
+    alone, _ = _run(pkg, ctx, reqs, workers=1, precision=precision, pivot=pivot)
+    mixed, stats = _run(pkg, ctx, reqs, workers=4, precision=precision, pivot=pivot)
     assert stats["completed"] == len(reqs)
     for i, r in enumerate(reqs):
         a, m = alone[i], mixed[i]
