@@ -945,7 +945,9 @@ def run_serving_suite(pkg, cu, ctx, args):
     kernels.  Budget 120 GB at the swept rates, and one rate with a budget
     small enough that the warm phase already evicts: admission waits and
     evictions happen, and a solve on an evicted key is sent again with its
-    matrix (its client latency counts both trips)."""
+    matrix (its client latency counts both trips).  Then the 400 Hz stream
+    once more with --serve-variant's factors (default BF16 with no pivoting
+    after the butterfly transform)."""
     from importlib import import_module
     serving = import_module(pkg.__name__ + ".serving")
     nkeys = args.serve_keys
@@ -956,11 +958,15 @@ def run_serving_suite(pkg, cu, ctx, args):
            "precision": f"{args.serve_precision} factors ({args.serve_pivot} pivoting) + FP64 IR "
                         "(fast inner solve); n <= 256 on the batched lane",
            "target": "p99 <= 35 ms at 400 Hz, backward error <= 10 n eps64", "rates": []}
-    runs = [(r, 120 << 30) for r in args.serve_rates] + [(400.0, int(args.serve_small_budget_gb * 2 ** 30))]
-    for rate, budget in runs:
+    base = (args.serve_precision, args.serve_pivot)
+    runs = [(r, 120 << 30, base) for r in args.serve_rates] + [
+        (400.0, int(args.serve_small_budget_gb * 2 ** 30), base)]
+    if args.serve_variant[0] and tuple(args.serve_variant) != base:  # the same stream, other factors
+        runs.append((400.0, 120 << 30, tuple(args.serve_variant)))
+    for rate, budget, (precision, pivot) in runs:
         clocks = ClockSampler(ctx.device)  # the stream's GPU clocks (the tail varies with them)
-        srv = serving.Server(ctx, workers=4, precision=args.serve_precision, hbm_budget_bytes=budget,
-                             max_large=args.serve_max_large, pivot=args.serve_pivot)
+        srv = serving.Server(ctx, workers=4, precision=precision, hbm_budget_bytes=budget,
+                             max_large=args.serve_max_large, pivot=pivot)
         small = budget < (120 << 30)
         wdone, wwall = serving.run_stream(srv, warm, rate_hz=0.0, seed=1)
         st0 = srv.stats()
@@ -977,6 +983,7 @@ def run_serving_suite(pkg, cu, ctx, args):
                 n = len(reqs[i]["b"])
                 worst = max(worst, pkg_backward_error(reqs[i]["Aeff"], d["x"], reqs[i]["b"]) / (n * EPS64))
         summ.update({"offered_rate_hz": rate, "budget_gb": budget / 2 ** 30, "clocks": clk,
+                     "factors": f"{precision}, {pivot} pivoting",
                      "max_backward_error_over_n_eps": worst, "warm_s": wwall,
                      "warm_failed": int(sum(d["status"] != 0 for d in wdone)),
                      "merged_solves": st["merged_solves"] - st0["merged_solves"],
@@ -1140,6 +1147,8 @@ def main():
                     help="factor precision of the serving suite's mixed factors")
     ap.add_argument("--serve-pivot", choices=("partial", "tournament", "rbt"), default="partial",
                     help="pivoting of the serving suite's mixed factors")
+    ap.add_argument("--serve-variant", nargs=2, default=["bf16", "rbt"], metavar=("PRECISION", "PIVOT"),
+                    help="one more 400 Hz stream with these factors ('' '' for none)")
     ap.add_argument("--kernel-case", choices=KERNEL_CASES, default=None,
                     help="run one small case of a kernel group once (for ncu) and exit")
     args = ap.parse_args()
