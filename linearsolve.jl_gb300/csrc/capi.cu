@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdarg>
 #include <cstdlib>
 #include <cstdio>
@@ -497,19 +498,23 @@ namespace gblu {
 
 namespace {
 
-// Uploads of at least kStageMin bytes from pageable host memory go through
-// pinned staging.  A cudaMemcpyAsync from pageable memory has the driver read
-// the caller's pages itself, and on GB300 the speed of that copy depends on
-// how the process's host memory happens to be mapped: about 170 GB/s in one
-// process, 5-7 GB/s for the same stream of matrices in a later one, and
-// while it is slow it also delays the other contexts' work (a serving
-// stream's p99 at 400 Hz: 13 ms in the first state, 70-110 ms in the
-// second).  Staged, the CPU copies column blocks into two pinned chunks that
-// the copy engine drains alternately (the host copy of one chunk overlaps
-// the transfer of the other): about 14 GB/s and a p99 of 24 ms in both
-// states.  GBLU_HOST_STAGING=0 copies directly.
+// Uploads from pageable host memory of kStageAlways bytes or more, and of
+// kStageMin or more while another such upload is in progress in the
+// process, go through pinned staging.  A cudaMemcpyAsync from pageable
+// memory has the driver read the caller's pages itself; on GB300 one such
+// copy at a time ran at ~170 GB/s in every process measured, but with
+// several worker threads copying at once the speed depended on the process:
+// fine in the first serving process of a box, 3-8x slower factorization
+// service in every later one (a serving stream's p99 at 400 Hz: 13 ms, then
+// 70-200 ms).  Staged, the CPU copies column blocks into two pinned chunks
+// that the copy engine drains alternately (the host copy of one chunk
+// overlaps the transfer of the other): about 14 GB/s per thread and a p99 of
+// 24 ms in every process.  A lone mid-size upload keeps the direct copy,
+// which is faster than the host copy.  GBLU_HOST_STAGING=0 copies directly.
 constexpr size_t kStageMin = size_t(4) << 20;
+constexpr size_t kStageAlways = size_t(32) << 20;
 constexpr size_t kStageChunk = size_t(16) << 20;
+std::atomic<int> g_pageable_uploads{0};  // pageable uploads of kStageMin or more in progress
 
 bool host_staging_on() {
   static const bool on = [] {
@@ -589,9 +594,15 @@ int32_t upload_direct(gblu_ctx* ctx, double* dst, int64_t ld_dst, const double* 
 int32_t upload_matrix(gblu_ctx* ctx, double* dst, int64_t ld_dst, const double* src, int64_t ld_src,
                       int64_t rows, int64_t cols, int32_t loc) {
   if (rows == 0 || cols == 0) return GBLU_OK;
-  if (loc == GBLU_HOST && (size_t)rows * cols * sizeof(double) >= kStageMin && host_staging_on() &&
-      is_pageable(src))
-    return upload_staged(ctx, dst, ld_dst, src, ld_src, rows, cols);
+  const size_t bytes = (size_t)rows * cols * sizeof(double);
+  if (loc == GBLU_HOST && bytes >= kStageMin && host_staging_on() && is_pageable(src)) {
+    const int others = g_pageable_uploads.fetch_add(1);
+    const int32_t st = bytes >= kStageAlways || others > 0
+                           ? upload_staged(ctx, dst, ld_dst, src, ld_src, rows, cols)
+                           : upload_direct(ctx, dst, ld_dst, src, ld_src, rows, cols, cudaMemcpyHostToDevice);
+    g_pageable_uploads.fetch_sub(1);
+    return st;
+  }
   return upload_direct(ctx, dst, ld_dst, src, ld_src, rows, cols,
                        loc == GBLU_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice);
 }

@@ -409,7 +409,7 @@ def test_host_upload_staging_identical(pkg, pad):
     from importlib import import_module
     _lib = import_module(pkg.__name__ + "._lib")
     ctx = pkg.Context(0)
-    n = 2600  # 54 MB
+    n = 2600  # 54 MB: staged whatever else is in progress
     rng = np.random.default_rng(2600 + pad)
     Ap = np.asfortranarray(rng.standard_normal((n + pad, n)))  # pageable, lda = n + pad
     pinned = torch.empty((n, n + pad), dtype=torch.float64, pin_memory=True)
