@@ -107,7 +107,10 @@ int32_t gblu_factor_create(gblu_ctx* ctx, int64_t m, int64_t n, int32_t precisio
 int32_t gblu_factor_destroy(gblu_ctx* ctx, gblu_factor* f);
 
 /* getrf: factor A (m x n, leading dimension lda) into f.  A is read, never
- * written; a_loc = GBLU_HOST copies it to the device first.
+ * written; a_loc = GBLU_HOST copies it to the device first (a pageable A of
+ * 32 MB or more, or of 4 MB or more while another such copy is running in the
+ * process, goes through the context's pinned staging chunks; pinned memory
+ * is copied directly; GBLU_HOST_STAGING=0 copies every A directly).
  * Replaces: LAPACK.getrf! reached from solve!(cache, ::LUFactorization)
  * (src/factorization.jl:643-736, do_factorization :738-751) and the
  * dgetrf_ ccall of src/openblas.jl:131-154. */
