@@ -187,14 +187,14 @@ void worker(gblu_server* s, int wi) {
           batch.push_back(*pick);
           const uint64_t key = pick->req.key;
           auto next = s->queue.erase(pick);
-          // merge following solve-only requests on the same key (until a refactor of it)
-          if (!batch[0].req.A || true) {
-            for (auto it = next; it != s->queue.end() && (int)batch.size() < std::max(1, s->cfg.max_rhs_batch);) {
-              if (it->req.key != key) { ++it; continue; }
-              if (it->req.A || it->req.n != batch[0].req.n) break;
-              batch.push_back(*it);
-              it = s->queue.erase(it);
-            }
+          // merge the following solve-only requests on the same key, up to the
+          // next refactor of it (a factoring head request is merged with the
+          // solves queued behind it: they use the matrix it factors)
+          for (auto it = next; it != s->queue.end() && (int)batch.size() < std::max(1, s->cfg.max_rhs_batch);) {
+            if (it->req.key != key) { ++it; continue; }
+            if (it->req.A || it->req.n != batch[0].req.n) break;
+            batch.push_back(*it);
+            it = s->queue.erase(it);
           }
           if (need_new) {
             Resident r;
