@@ -553,9 +553,9 @@ int32_t upload_staged(gblu_ctx* ctx, double* dst, int64_t ld_dst, const double* 
     CK(ctx, cudaMallocHost(&p, 2 * chunk), "allocating pinned staging");
     ctx->stage = static_cast<char*>(p);
     ctx->stage_chunk = chunk;
-    for (cudaEvent_t& e : ctx->stage_ev)
-      if (!e) CK(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "staging event");
   }
+  for (cudaEvent_t& e : ctx->stage_ev)
+    if (!e) CK(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "staging event");
   const int64_t per = (int64_t)(ctx->stage_chunk / col_bytes);  // columns per chunk
   int i = 0;
   for (int64_t c = 0; c < cols; c += per, i ^= 1) {
