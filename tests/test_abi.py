@@ -121,3 +121,21 @@ def test_serve_config_default_fills_every_field(pkg):
     vals = {f[0]: getattr(cfg, f[0]) for f in cfg._fields_}
     assert all(v != 0x7f7f7f7f and v != 0x7f7f7f7f7f7f7f7f for v in vals.values()), vals
     assert vals["pivoting"] == lib_mod.GBLU_PIVOT_PARTIAL and vals["max_large"] == 1
+
+
+def test_constants_match_header(pkg):
+    """Every GBLU_* constant the Python and Julia bindings define has the
+    header's value; the Python binding defines all of the header's status,
+    precision, location, mode and fallback codes."""
+    from importlib import import_module
+    lib_mod = import_module(pkg.__name__ + "._lib")
+    src = open(os.path.join(ROOT, "include", "gblu.h")).read()
+    header = {k: int(v) for k, v in re.findall(r"^#define (GBLU_[A-Z0-9_]+) (-?\d+)", src, flags=re.M)}
+    assert len(header) > 25
+    py = {k: getattr(lib_mod, k) for k in dir(lib_mod) if k.startswith("GBLU_") and isinstance(getattr(lib_mod, k), int)}
+    missing = sorted(k for k in header if k not in py and k != "GBLU_PROFILE_KINDS")
+    assert not missing, missing
+    assert {k: v for k, v in py.items() if k in header} == {k: header[k] for k in py if k in header}
+    jl = open(os.path.join(ROOT, "linearsolve.jl_gb300", "julia", "GB300LinearSolve.jl")).read()
+    for k, v in re.findall(r"^const (GBLU_[A-Z0-9_]+) = Int32\((-?\d+)\)", jl, flags=re.M):
+        assert header[k] == int(v), k
